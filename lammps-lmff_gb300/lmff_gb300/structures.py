@@ -1,0 +1,331 @@
+"""Seeded generators for the layered systems the engine is measured and tested on.
+
+Atom types follow one fixed convention everywhere in this package: 1 = C, 2 = B, 3 = N,
+matching ``pair_coeff * * tersoff BNC.tersoff C B N`` and
+``pair_coeff * * ilp/graphene/hbn BNCH.ILP C B N``.  Molecule ids mark layers, as the
+ILP style requires (``pair_ilp_graphene_hbn.cpp:504,597`` interacts only
+``molecule[i] != molecule[j]``; ``:732`` builds the intralayer list from
+``molecule[i] == molecule[j]``).
+
+Honeycomb layers are built on the rectangular 4-atom cell a = sqrt(3)*d, b = 3*d with
+basis (0,0), (a/2, d/2), (a/2, 3d/2), (0, 2d), d the bond length.  Twisted layers are made
+commensurate with the rectangular periodic box by a small homogeneous strain, which every
+generator reports in ``meta`` (no exactly commensurate cell exists for an arbitrary twist
+or for the 2% graphene/hBN lattice mismatch).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Dict, List, Optional
+
+import numpy as np
+
+A_CC_GRAPHENE = 1.42
+A_CC_HBN = 1.45
+MASSES = {1: 12.011, 2: 10.811, 3: 14.0067}
+BOLTZ_METAL = 8.617343e-5          # eV/K        (LAMMPS update.cpp, units metal)
+MVV2E_METAL = 1.0364269e-4         # amu*A^2/ps^2 -> eV
+
+
+@dataclasses.dataclass
+class System:
+    x: np.ndarray                  # (N,3) float64, Angstrom
+    type: np.ndarray               # (N,)  int32, 1=C 2=B 3=N
+    mol: np.ndarray                # (N,)  int64 layer id
+    tag: np.ndarray                # (N,)  int64, 1..N
+    box_lo: np.ndarray             # (3,)
+    box_hi: np.ndarray             # (3,)
+    periodic: np.ndarray           # (3,) bool
+    v: Optional[np.ndarray] = None  # (N,3) Angstrom/ps
+    meta: Dict = dataclasses.field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return int(self.x.shape[0])
+
+    def masses(self) -> np.ndarray:
+        return np.array([MASSES[int(t)] for t in range(1, 4)])[self.type - 1]
+
+    def copy(self) -> "System":
+        return System(self.x.copy(), self.type.copy(), self.mol.copy(), self.tag.copy(),
+                      self.box_lo.copy(), self.box_hi.copy(), self.periodic.copy(),
+                      None if self.v is None else self.v.copy(), dict(self.meta))
+
+
+# --------------------------------------------------------------------------- layers
+
+def _rect_layer(nx: int, ny: int, a_cc: float, species=(1, 1)) -> np.ndarray:
+    """Unrotated honeycomb layer on nx x ny rectangular cells; returns (N,4) [x,y,0,type]."""
+    a = math.sqrt(3.0) * a_cc
+    d = a_cc
+    basis = [(0.0, 0.0, species[0]), (a / 2, d / 2, species[1]),
+             (a / 2, 1.5 * d, species[0]), (0.0, 2.0 * d, species[1])]
+    out = []
+    for iy in range(ny):
+        for ix in range(nx):
+            for bx, by, t in basis:
+                out.append((ix * a + bx, iy * 3 * d + by, 0.0, t))
+    return np.array(out, dtype=np.float64)
+
+
+def _commensurate_layer(lx: float, ly: float, a_cc: float, theta_deg: float,
+                        species=(1, 1), shift=(0.0, 0.0)):
+    """Honeycomb layer rotated by theta, strained to tile the box [0,lx) x [0,ly).
+
+    Returns (atoms (N,4), strain_max) where strain_max is the largest principal
+    strain of the homogeneous deformation that makes the layer commensurate.
+    """
+    a = math.sqrt(3.0) * a_cc
+    th = math.radians(theta_deg)
+    rot = np.array([[math.cos(th), -math.sin(th)], [math.sin(th), math.cos(th)]])
+    a1 = rot @ np.array([a, 0.0])
+    a2 = rot @ np.array([a / 2, a * math.sqrt(3.0) / 2])
+    lat = np.stack([a1, a2], axis=1)
+    s1 = np.rint(np.linalg.solve(lat, [lx, 0.0])).astype(np.int64)
+    s2 = np.rint(np.linalg.solve(lat, [0.0, ly])).astype(np.int64)
+    t1 = lat @ s1
+    t2 = lat @ s2
+    fdef = np.array([[lx, 0.0], [0.0, ly]]) @ np.linalg.inv(np.stack([t1, t2], axis=1))
+    strain = 0.5 * (fdef.T @ fdef - np.eye(2))
+    strain_max = float(np.max(np.abs(np.linalg.eigvalsh(strain))))
+    p1, q1 = int(s1[0]), int(s1[1])
+    p2, q2 = int(s2[0]), int(s2[1])
+    det = p1 * q2 - q1 * p2
+    if det == 0:
+        raise ValueError("degenerate commensurate cell")
+    corners = np.array([[0, 0], [p1, q1], [p2, q2], [p1 + p2, q1 + q2]])
+    mlo, nlo = corners.min(axis=0) - 1
+    mhi, nhi = corners.max(axis=0) + 1
+    mm, nn = np.meshgrid(np.arange(mlo, mhi + 1), np.arange(nlo, nhi + 1), indexing="ij")
+    mm = mm.ravel()
+    nn = nn.ravel()
+    # fractional coordinates in the supercell basis, exact in integers: f = S^-1 (m,n)
+    f1n = mm * q2 - nn * p2
+    f2n = -mm * q1 + nn * p1
+    if det < 0:
+        f1n, f2n, det = -f1n, -f2n, -det
+    keep = (f1n >= 0) & (f1n < det) & (f2n >= 0) & (f2n < det)
+    f1 = f1n[keep] / det
+    f2 = f2n[keep] / det
+    base = np.stack([f1 * lx, f2 * ly], axis=1)
+    delta = fdef @ (rot @ np.array([a / 2, a_cc / 2]))
+    sh = np.asarray(shift, dtype=np.float64)
+    pts = []
+    for off, t in ((np.zeros(2), species[0]), (delta, species[1])):
+        p = base + off + sh
+        p[:, 0] = np.mod(p[:, 0], lx)
+        p[:, 1] = np.mod(p[:, 1], ly)
+        pts.append(np.column_stack([p, np.zeros(len(p)), np.full(len(p), t)]))
+    atoms = np.concatenate(pts, axis=0)
+    return atoms, strain_max
+
+
+def _assemble(layers: List[np.ndarray], zs: List[float], mols: List[int], lx: float, ly: float,
+              vacuum: float, periodic_z: bool = False, meta: Optional[Dict] = None) -> System:
+    xs, ts, ms = [], [], []
+    for atoms, z, m in zip(layers, zs, mols):
+        p = atoms[:, :3].copy()
+        p[:, 2] = z
+        xs.append(p)
+        ts.append(atoms[:, 3].astype(np.int32))
+        ms.append(np.full(len(atoms), m, dtype=np.int64))
+    x = np.concatenate(xs)
+    t = np.concatenate(ts)
+    mol = np.concatenate(ms)
+    zlo = min(zs) - vacuum / 2
+    zhi = max(zs) + vacuum / 2
+    box_lo = np.array([0.0, 0.0, zlo])
+    box_hi = np.array([lx, ly, zhi])
+    per = np.array([True, True, periodic_z])
+    tag = np.arange(1, len(x) + 1, dtype=np.int64)
+    return System(x, t, mol, tag, box_lo, box_hi, per, None, dict(meta or {}))
+
+
+def ab_bilayer_graphene(nx: int = 30, ny: int = 30, spacing: float = 3.4,
+                        vacuum: float = 30.0) -> System:
+    """AB-stacked bilayer graphene, C-C 1.42 A, on nx x ny rectangular 4-atom cells.
+
+    nx = ny = 30 gives the 7,200-atom plain-FP64 parity workload (box 73.79 x 127.80 A,
+    layers at z = 0 and 3.4, 30 A of z vacuum, periodic x/y)."""
+    a = math.sqrt(3.0) * A_CC_GRAPHENE
+    lx, ly = nx * a, ny * 3 * A_CC_GRAPHENE
+    l1 = _rect_layer(nx, ny, A_CC_GRAPHENE)
+    l2 = l1.copy()
+    l2[:, 1] = np.mod(l2[:, 1] + A_CC_GRAPHENE, ly)
+    return _assemble([l1, l2], [0.0, spacing], [1, 2], lx, ly, vacuum,
+                     meta={"kind": "ab_bilayer_graphene", "nx": nx, "ny": ny, "spacing": spacing})
+
+
+def graphite_slab(nlayers: int = 10, nx: int = 342, ny: int = 197, spacing: float = 3.35,
+                  mol_mode: str = "alternate", vacuum: float = 30.0) -> System:
+    """AB-stacked graphite slab, periodic x/y.
+
+    Defaults give the 10-layer, 2.7M-atom slab (269,496 atoms per layer, box
+    841.2 x 839.2 A, 3.35 A spacing).  mol_mode "alternate" gives layers molecule ids
+    1,2,1,2,... (only odd layer separations interact through ILP); "unique" gives each
+    layer its own id."""
+    a = math.sqrt(3.0) * A_CC_GRAPHENE
+    lx, ly = nx * a, ny * 3 * A_CC_GRAPHENE
+    base = _rect_layer(nx, ny, A_CC_GRAPHENE)
+    layers, zs, mols = [], [], []
+    for k in range(nlayers):
+        l = base.copy()
+        if k % 2 == 1:
+            l[:, 1] = np.mod(l[:, 1] + A_CC_GRAPHENE, ly)
+        layers.append(l)
+        zs.append(k * spacing)
+        mols.append(1 + (k % 2) if mol_mode == "alternate" else k + 1)
+    return _assemble(layers, zs, mols, lx, ly, vacuum,
+                     meta={"kind": "graphite_slab", "nlayers": nlayers, "nx": nx, "ny": ny,
+                           "spacing": spacing, "mol_mode": mol_mode})
+
+
+def twisted_bilayer(nx: int, ny: int, theta_deg: float, top: str = "hbn", spacing: float = 3.4,
+                    shift=(0.0, 0.0), vacuum: float = 30.0) -> System:
+    """Graphene (bottom, unstrained, nx x ny rectangular cells) under a top layer
+    ("graphene" or "hbn") twisted by theta and strained to be commensurate with the box.
+    meta["strain_max"] is the top layer's largest principal strain."""
+    a = math.sqrt(3.0) * A_CC_GRAPHENE
+    lx, ly = nx * a, ny * 3 * A_CC_GRAPHENE
+    bottom = _rect_layer(nx, ny, A_CC_GRAPHENE)
+    if top == "hbn":
+        upper, strain = _commensurate_layer(lx, ly, A_CC_HBN, theta_deg, species=(2, 3), shift=shift)
+    else:
+        upper, strain = _commensurate_layer(lx, ly, A_CC_GRAPHENE, theta_deg, species=(1, 1),
+                                            shift=shift)
+    return _assemble([bottom, upper], [0.0, spacing], [1, 2], lx, ly, vacuum,
+                     meta={"kind": "twisted_bilayer", "top": top, "theta_deg": theta_deg,
+                           "strain_max": strain, "nx": nx, "ny": ny, "spacing": spacing})
+
+
+def twisted_graphene_hbn_500k(seed: int = 2, theta_deg: float = 0.6) -> System:
+    """Twisted graphene/hBN, 0.6 degrees, about 500k atoms over two layers, with the
+    per-atom N(0, 0.02 A) displacement applied from ``seed``."""
+    s = twisted_bilayer(329, 190, theta_deg, top="hbn", spacing=3.4)
+    rng = np.random.default_rng(seed)
+    s.x += rng.normal(0.0, 0.02, size=s.x.shape)
+    s.meta["displacement_sigma"] = 0.02
+    return s
+
+
+def flake_edges(nx: int = 4, ny: int = 3) -> System:
+    """Bilayer ribbon periodic in x only, plus one isolated and one dangling atom in each
+    layer: exercises atoms with 0, 1, 2 and 3 intralayer neighbours (normal cases
+    nilp <= 1, 2, 3)."""
+    a = math.sqrt(3.0) * A_CC_GRAPHENE
+    lx = nx * a
+    l1 = _rect_layer(nx, ny, A_CC_GRAPHENE)
+    l2 = l1.copy()
+    l2[:, 1] += A_CC_GRAPHENE
+    ly_span = ny * 3 * A_CC_GRAPHENE
+    iso1 = np.array([[lx / 2, ly_span + 4.0, 0.0, 1.0],          # no neighbour
+                     [0.0, -A_CC_GRAPHENE, 0.0, 1.0]])            # dangling: one neighbour
+    iso2 = np.array([[lx / 2, ly_span + 4.0 + A_CC_GRAPHENE, 0.0, 1.0],
+                     [0.0, 0.0, 0.0, 1.0]])
+    l1 = np.concatenate([l1, iso1])
+    l2 = np.concatenate([l2, iso2])
+    s = _assemble([l1, l2], [0.0, 3.4], [1, 2], lx, 1.0, 30.0)
+    s.box_lo[1] = -10.0
+    s.box_hi[1] = ly_span + 16.0
+    s.periodic = np.array([True, False, False])
+    s.meta = {"kind": "flake_edges", "nx": nx, "ny": ny}
+    return s
+
+
+# ------------------------------------------------------------------ perturbations
+
+def displace(s: System, sigma: float, seed: int) -> System:
+    out = s.copy()
+    rng = np.random.default_rng(seed)
+    out.x = out.x + rng.normal(0.0, sigma, size=out.x.shape)
+    out.meta["displacement_sigma"] = sigma
+    return out
+
+
+def thermalize(s: System, temp: float, seed: int) -> System:
+    """Gaussian velocities at ``temp`` (K): zero total momentum, then scaled so the
+    kinetic temperature (3N-3 degrees of freedom) is exactly ``temp``."""
+    out = s.copy()
+    rng = np.random.default_rng(seed)
+    m = out.masses()
+    v = rng.normal(0.0, 1.0, size=out.x.shape) / np.sqrt(m)[:, None]
+    v -= (m[:, None] * v).sum(axis=0) / m.sum()
+    ke = 0.5 * MVV2E_METAL * float((m[:, None] * v * v).sum())
+    dof = 3 * out.n - 3
+    t_now = 2.0 * ke / (dof * BOLTZ_METAL)
+    out.v = v * math.sqrt(temp / t_now)
+    out.meta["temperature"] = temp
+    return out
+
+
+def wrap(s: System) -> System:
+    out = s.copy()
+    L = out.box_hi - out.box_lo
+    for c in range(3):
+        if out.periodic[c]:
+            out.x[:, c] = out.box_lo[c] + np.mod(out.x[:, c] - out.box_lo[c], L[c])
+    return out
+
+
+# -------------------------------------------------------------------- replica sets
+
+def _rect_for_count(n_layer: int, a_cc: float = A_CC_GRAPHENE):
+    a = math.sqrt(3.0) * a_cc
+    b = 3 * a_cc
+    cells = max(1, round(n_layer / 4))
+    nx = max(1, round(math.sqrt(cells * b / a)))
+    ny = max(1, round(cells / nx))
+    return nx, ny
+
+
+def replica_set(count: int = 256, nmin: int = 500, nmax: int = 20000, seed: int = 4) -> List[System]:
+    """Independent bilayer replicas: 50/50 graphene/graphene and graphene/hBN, total atom
+    counts log-uniform in [nmin, nmax], twist U[0,5] degrees, lateral shift uniform in one
+    unit cell, interlayer spacing U[3.2,3.6] A.  Every periodic side is at least 20 A."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(count):
+        ntot = math.exp(rng.uniform(math.log(nmin), math.log(nmax)))
+        top = "graphene" if r % 2 == 0 else "hbn"
+        theta = float(rng.uniform(0.0, 5.0))
+        spacing = float(rng.uniform(3.2, 3.6))
+        a = math.sqrt(3.0) * A_CC_GRAPHENE
+        shift = (float(rng.uniform(0, a)), float(rng.uniform(0, 3 * A_CC_GRAPHENE)))
+        nx, ny = _rect_for_count(int(ntot / 2))
+        nx = max(nx, math.ceil(20.0 / a))
+        ny = max(ny, math.ceil(20.0 / (3 * A_CC_GRAPHENE)))
+        best = None
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                cx, cy = nx + dx, ny + dy
+                if cx * a < 20.0 or cy * 3 * A_CC_GRAPHENE < 20.0:
+                    continue
+                s = twisted_bilayer(cx, cy, theta, top=top, spacing=spacing, shift=shift)
+                if best is None or s.meta["strain_max"] < best.meta["strain_max"]:
+                    best = s
+        best.meta["replica"] = r
+        out.append(best)
+    return out
+
+
+# ------------------------------------------------------------------------- output
+
+def write_lammps_data(s: System, path: str, ntypes: int = 3) -> None:
+    """LAMMPS data file, atom_style full (id mol type q x y z), with Velocities if set."""
+    with open(path, "w") as fh:
+        fh.write("LAMMPS data file written by lmff_gb300.structures\n\n")
+        fh.write(f"{s.n} atoms\n{ntypes} atom types\n\n")
+        for c, nm in enumerate("xyz"):
+            fh.write(f"{s.box_lo[c]:.17g} {s.box_hi[c]:.17g} {nm}lo {nm}hi\n")
+        fh.write("\nMasses\n\n")
+        for t in range(1, ntypes + 1):
+            fh.write(f"{t} {MASSES[t]}\n")
+        fh.write("\nAtoms # full\n\n")
+        for i in range(s.n):
+            fh.write(f"{int(s.tag[i])} {int(s.mol[i])} {int(s.type[i])} 0.0 "
+                     f"{s.x[i,0]:.17g} {s.x[i,1]:.17g} {s.x[i,2]:.17g}\n")
+        if s.v is not None:
+            fh.write("\nVelocities\n\n")
+            for i in range(s.n):
+                fh.write(f"{int(s.tag[i])} {s.v[i,0]:.17g} {s.v[i,1]:.17g} {s.v[i,2]:.17g}\n")

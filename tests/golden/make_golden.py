@@ -1,0 +1,150 @@
+"""Generate the golden fixtures in tests/golden/ by running the REFERENCE implementation.
+
+The reference snapshot ships no tests and no reference outputs, so the fixtures are made
+here: each case's structure comes from lmff_gb300.structures (seeded), is written as a
+LAMMPS data file, and is run through the reference's own pair styles
+(pair_style hybrid/overlay tersoff ilp/graphene/hbn, unchanged BNC.tersoff / BNCH.ILP)
+by the harness that oracle/ref.mk builds from the reference sources
+(oracle/_ref/lmff_ref).  Needs the reference checkout, so it runs only in a container
+that has it:
+
+    make -f oracle/ref.mk REF=/root/reference -j8
+    python tests/golden/make_golden.py
+
+Every fixture stores the inputs (x, v, type, mol, tag, box, periodicity, potential
+settings) and the reference outputs (forces, per-style energies, ILP pvector, fdotr
+virial, per-atom energy; for list cases the full Verlet list and the ILP intralayer list
+as (tag_i, tag_j, image) triples with image = sum_c ((s_c+8)&15) << 4c).
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(ROOT, "lammps-lmff_gb300"))
+from lmff_gb300 import structures as S  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "lmff_ref")
+POT = os.path.join(ROOT, "lammps-lmff_gb300", "potentials")
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def read_records(path):
+    out = {}
+    data = open(path, "rb").read()
+    off = 0
+    while off < len(data):
+        name = data[off:off + 16].split(b"\0")[0].decode()
+        off += 16
+        kind = chr(data[off])
+        off += 1
+        n = int(np.frombuffer(data[off:off + 8], dtype=np.int64)[0])
+        off += 8
+        dt = np.float64 if kind == "d" else np.int64
+        out[name] = np.frombuffer(data[off:off + 8 * n], dtype=dt).copy()
+        off += 8 * n
+    return out
+
+
+def run_reference(s: S.System, tap_flag=1, nsteps=0, dt=0.001, lists=False, cut=16.0):
+    with tempfile.TemporaryDirectory() as td:
+        data = os.path.join(td, "data.lmp")
+        S.write_lammps_data(s, data)
+        bnd = " ".join("p" if p else "f" for p in s.periodic)
+        script = f"""units metal
+atom_style full
+boundary {bnd}
+atom_modify map array
+read_data {data}
+pair_style hybrid/overlay tersoff ilp/graphene/hbn {cut} {tap_flag}
+pair_coeff * * tersoff {POT}/BNC.tersoff C B N
+pair_coeff * * ilp/graphene/hbn {POT}/BNCH.ILP C B N
+neighbor 2.0 bin
+neigh_modify every 1 delay 0 check yes one 10000 page 200000
+compute peatom all pe/atom pair
+compute pesum all reduce sum c_peatom
+thermo_style custom step pe c_pesum press
+thermo {max(nsteps, 1)}
+timestep {dt}
+"""
+        if nsteps:
+            script += "fix 1 all nve\n"
+        script += f"run {nsteps}\n"
+        inp = os.path.join(td, "in.lmp")
+        open(inp, "w").write(script)
+        out = os.path.join(td, "out.bin")
+        args = [HARNESS, inp, out] + (["lists"] if lists else [])
+        subprocess.check_call(args)
+        return read_records(out)
+
+
+def pack(s: S.System, r, tap_flag, extra=None):
+    n = s.n
+    d = {
+        "x": r["x"].reshape(n, 3), "v": r["v"].reshape(n, 3), "f": r["f"].reshape(n, 3),
+        "type": r["type"].astype(np.int32), "mol": r["mol"], "tag": r["tag"],
+        "box_lo": r["box"][:3], "box_hi": r["box"][3:], "periodic": s.periodic.astype(np.int32),
+        "e_tersoff": r["e_tersoff"][0], "e_ilp": r["e_ilp"][0], "pvector": r["pvector"],
+        "virial": r["virial"], "eatom": r["eatom"], "tap_flag": tap_flag, "cut_global": 16.0,
+        "skin": 2.0, "step": r["step"][0],
+    }
+    if "nlist" in r:
+        nl = r["nlist"].reshape(-1, 3)
+        nl = nl[np.lexsort((nl[:, 2], nl[:, 1], nl[:, 0]))]
+        d["nlist"] = nl.astype(np.int32)
+        il = r["ilplist"].reshape(-1, 3)
+        il = il[np.lexsort((il[:, 2], il[:, 1], il[:, 0]))]
+        d["ilplist"] = il.astype(np.int32)
+    if extra:
+        d.update(extra)
+    return d
+
+
+def save(name, d):
+    path = os.path.join(OUT, f"{name}.npz")
+    np.savez_compressed(path, **d)
+    print(f"{name}: {len(d['tag'])} atoms, {os.path.getsize(path) / 1024:.0f} KiB")
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        sys.exit("reference harness missing: make -f oracle/ref.mk REF=<reference> -j8")
+
+    # 1. small AB bilayer graphene, displaced, thermal velocities; lists
+    s = S.thermalize(S.displace(S.ab_bilayer_graphene(8, 5), 0.05, seed=11), 300.0, seed=12)
+    save("bilayer_small", pack(s, run_reference(s, lists=True), 1))
+    # 2. same structure with the taper off
+    save("bilayer_small_notaper", pack(s, run_reference(s, tap_flag=0), 0))
+    # 3. twisted graphene/hBN bilayer (B, N, C parameters); lists
+    s = S.displace(S.twisted_bilayer(8, 5, 3.0, top="hbn", spacing=3.3, shift=(0.4, 0.7)), 0.03, seed=21)
+    save("hetero_small", pack(s, run_reference(s, lists=True), 1, {"strain_max": s.meta["strain_max"]}))
+    # 4. box shorter than the 18 A neighbour cutoff: several images of each atom; lists
+    s = S.displace(S.ab_bilayer_graphene(6, 4), 0.04, seed=31)
+    save("tiny_images", pack(s, run_reference(s, lists=True), 1))
+    # 5. ribbon with free edges + isolated atoms: 0/1/2/3 intralayer neighbours; lists
+    s = S.displace(S.flake_edges(4, 3), 0.03, seed=41)
+    save("edges", pack(s, run_reference(s, lists=True), 1))
+    # 6. three-layer graphite, alternating molecule ids (layers 1 and 3 share an id); lists
+    s = S.displace(S.graphite_slab(3, 8, 5, spacing=3.35, mol_mode="alternate"), 0.04, seed=51)
+    save("trilayer_alt", pack(s, run_reference(s, lists=True), 1))
+    # 7. the 7,200-atom plain-FP64 workload at t=0 and after 100 NVE steps (dt = 1 fs)
+    c1 = S.thermalize(S.ab_bilayer_graphene(30, 30), 300.0, seed=1)
+    r0 = run_reference(c1)
+    save("c1_t0", pack(c1, r0, 1))
+    r100 = run_reference(c1, nsteps=100)
+    save("c1_t100", pack(c1, r100, 1, {"x0": r0["x"].reshape(-1, 3), "v0": r0["v"].reshape(-1, 3)}))
+    # 8. short NVE on the hetero cell (exercises B/N masses and parameters)
+    h = S.thermalize(S.twisted_bilayer(8, 5, 3.0, top="hbn", spacing=3.3, shift=(0.4, 0.7)), 300.0, seed=61)
+    r0 = run_reference(h)
+    r20 = run_reference(h, nsteps=20)
+    save("hetero_t20", pack(h, r20, 1, {"x0": r0["x"].reshape(-1, 3), "v0": r0["v"].reshape(-1, 3),
+                                        "f0": r0["f"].reshape(-1, 3)}))
+
+
+if __name__ == "__main__":
+    main()

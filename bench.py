@@ -1,0 +1,342 @@
+"""Benchmark: atom-steps/s of the Tersoff + ILP path on the 2.7M-atom graphite slab.
+
+Workload (default): 10-layer AB graphite, 342 x 197 rectangular cells per layer
+(269,496 atoms/layer, 2,694,960 atoms, 841 x 839 A, 3.35 A spacing, periodic x/y),
+alternating molecule ids, 300 K Gaussian velocities from a seed; velocity-Verlet NVE
+with dt = 1 fs, device resident, mixed precision (FP32 pair arithmetic, FP64
+integration and accumulation).  One step = integrate + [neighbour check/rebuild] +
+Tersoff + ILP forces.  Synthetic inputs generated here (the reference's own large data
+files are not available).
+
+Timing: W untimed warm-up steps, then exactly K steps timed on the device with CUDA
+events on the engine's stream (lmff_stats.ms_last_run), bracketed by
+torch.cuda.synchronize() (and a barrier with N > 1).  Inputs are far larger than L2
+(the pair list alone is ~15 GB), so no L2 flush is needed.
+
+Multi-GPU: the path is run as independent replicas (one system per GPU, no data-path
+collective): value = total atom-steps of all ranks / max rank time, scaling "weak".
+
+--impl reference: the CPU arm (the oracle restatement of the reference's CPU algorithm,
+OpenMP over all host cores) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "lammps-lmff_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "atom-steps/s at 2.7M-atom graphite"
+UNIT = "atom-steps/s"
+TERSOFF_FILE = os.path.join(ROOT, "lammps-lmff_gb300", "potentials", "BNC.tersoff")
+ILP_FILE = os.path.join(ROOT, "lammps-lmff_gb300", "potentials", "BNCH.ILP")
+
+# Arithmetic of the pair kernel per interlayer pair inside the cutoff, counted from the
+# kernel source (lammps-lmff_gb300/csrc/forces_impl.cuh, k_ilp pair body, no energy or
+# virial): add/sub/mul = 1, FMA = 2, each exp2/rsqrt/rcp = 1.  A candidate outside the
+# cutoff costs the displacement and r^2 only.
+FLOPS_PER_PAIR = 155
+FLOPS_PER_REJECTED = 26
+
+
+def workload(name: str):
+    from lmff_gb300 import structures as S
+    if name == "graphite_2p7m":
+        s = S.graphite_slab(10, 342, 197, spacing=3.35, mol_mode="alternate")
+    elif name == "bilayer_7200":
+        s = S.ab_bilayer_graphene(30, 30)
+    elif name == "graphite_small":
+        s = S.graphite_slab(10, 40, 23, spacing=3.35, mol_mode="alternate")
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return S.thermalize(s, 300.0, seed=3)
+
+
+def cpu_sample():
+    """Bounded CPU sample of the same workload: a 98 x 98 A periodic patch of the same
+    10-layer graphite slab (36,800 atoms), same density and per-atom neighbour counts."""
+    from lmff_gb300 import structures as S
+    return S.thermalize(S.graphite_slab(10, 40, 23, spacing=3.35, mol_mode="alternate"), 300.0, seed=3)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [v for v in sm if v > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        try:
+            return json.load(open(path))
+        except ValueError:
+            return {}
+    return {}
+
+
+def fp_peak_tflops(dtype_name: str) -> float:
+    """SIMT peak measured here: cuBLAS GEMM at 8192^3 in FP32 (TF32 off) or FP64, best of 5
+    after warm-up (MEASURED_PEAKS.json carries HBM and bf16 tensor peaks only)."""
+    import torch
+    torch.backends.cuda.matmul.allow_tf32 = False
+    dt = torch.float32 if dtype_name == "fp32" else torch.float64
+    n = 8192 if dt == torch.float32 else 4096
+    a = torch.randn(n, n, device="cuda", dtype=dt)
+    b = torch.randn(n, n, device="cuda", dtype=dt)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def time_cpu_baseline(nsteps: int, warm: int, nthreads: int):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+    s = cpu_sample()
+    o = Oracle(TERSOFF_FILE, ILP_FILE, nthreads=nthreads)
+    x = s.x.copy()
+    v = s.v.copy()
+    o.set_atoms(x, s.type, s.mol, s.tag, s.box_lo, s.box_hi, s.periodic)
+    f = o.forces()["f"]
+    masses = [12.011, 10.811, 14.0067]
+    if warm:
+        o.nve(warm, 0.001, masses, x, v, f)
+    t0 = time.perf_counter()
+    o.nve(nsteps, 0.001, masses, x, v, f)
+    dt = time.perf_counter() - t0
+    return s.n * nsteps / dt, s.n, dt
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    steps = max(1, args.steps)
+    value, natoms, dt = time_cpu_baseline(steps, args.warmup, nthreads)
+    sample = (f"{natoms}-atom 98x98 A periodic patch of the same 10-layer graphite, {steps} NVE steps "
+              f"(+{args.warmup} warm-up), oracle restatement of the reference CPU algorithm")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "10-layer AB graphite, 2.7M atoms (CPU runs a 36.8k-atom patch of it)",
+                       "precision": "fp64", "sample_atoms": natoms},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="graphite_2p7m")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--tpa", type=int, default=16)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo" if args.impl == "reference" else "nccl")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    from lmff_gb300 import build, capi
+    if rank == 0:
+        build.build()
+    if dist:
+        dist.barrier()
+    if rank != 0:
+        build.build()
+
+    s = workload(args.workload)
+    prec = capi.MIXED if args.precision == "mixed" else capi.FP64
+    eng = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=prec)
+    eng.set_option("tpa", args.tpa)
+    eng.upload(s)
+    eng.run_nve(args.warmup, 0.001)
+    eng.set_option("count_pairs", 1)
+    eng.set_option("kernel_timing", 1)
+    eng.set_option("reset_timing", 1)
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    eng.run_nve(args.steps, 0.001)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    st = eng.stats()
+    dev_s = st["ms_last_run"] / 1e3
+    tmax = dev_s
+    if dist:
+        t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tmax = float(t.item())
+    value = world * s.n * args.steps / tmax
+    ms_per_step = tmax / args.steps * 1e3
+
+    # dominant kernel: the ILP pair kernel; live per-launch device time
+    k_ms = st["kernel_ms"]["pair_ilp"]
+    k_n = max(1, st["kernel_launches"]["pair_ilp"])
+    k_avg = k_ms / k_n / 1e3
+    pairs = st["pairs_in_cutoff"]
+    cands = st["list_entries"]
+    flops = pairs * FLOPS_PER_PAIR + (cands - pairs) * FLOPS_PER_REJECTED
+    launches_total = sum(st["kernel_launches"].values())
+
+    # e2e through the drop-in call (lmff_compute) with pinned host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        xa = torch.empty((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        xb = torch.empty((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        fb = torch.empty((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        xa[:] = s.x
+        xb[:] = s.x + np.random.default_rng(1).normal(0.0, 0.01, s.x.shape)
+        eng2 = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=prec)
+        eng2.set_option("tpa", args.tpa)
+        eng2.set_box(s.box_lo, s.box_hi, s.periodic)
+        eng2.compute(xa, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb, overwrite=True)
+        eng2.compute(xb, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb, overwrite=True, same_atoms=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.e2e_steps):
+            eng2.compute(xa if k % 2 == 0 else xb, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb,
+                         overwrite=True, same_atoms=True)
+        torch.cuda.synchronize()
+        te = time.perf_counter() - t0
+        e2e = {"value": world * s.n * args.e2e_steps / te, "unit": UNIT, "h2d_bytes_per_step": int(xa.nbytes),
+               "d2h_bytes_per_step": int(fb.nbytes),
+               "path": "lmff_compute: pinned host x in, host f out, per force evaluation"}
+        del eng2
+
+    peaks = measured_peaks()
+    peak_name = "fp32" if prec == capi.MIXED else "fp64"
+    peak = fp_peak_tflops(peak_name) if rank == 0 else 0.0
+    achieved = flops / k_avg / 1e12
+    roofline = {"bound": peak_name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if peak else None, "traffic": None,
+                "kernel": "k_ilp (pair kernel)", "kernel_ms_avg": k_avg * 1e3,
+                "peak_source": f"cuBLAS {peak_name.upper()} GEMM measured in this run (SIMT; MEASURED_PEAKS.json has "
+                               f"HBM {peaks.get('hbm_gbs')} GB/s and bf16 tensor only)",
+                "pairs_in_cutoff": pairs, "list_entries": cands,
+                "flops_per_pair": FLOPS_PER_PAIR, "flops_per_rejected": FLOPS_PER_REJECTED,
+                "hbm_gbs_of_list_stream": cands * 4 / k_avg / 1e9, "hbm_peak_gbs": peaks.get("hbm_gbs")}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        cv, cn, cdt = time_cpu_baseline(args.cpu_steps, 1, nthreads)
+        cpu = {"value": cv, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"{cn}-atom 98x98 A patch of the same slab, {args.cpu_steps} NVE steps, "
+                         f"oracle restatement, {cdt:.1f} s"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32" if prec == capi.MIXED else "f64", "data": "synthetic",
+                "config": {"workload": "10-layer AB graphite slab, 2,694,960 atoms, 300 K NVE dt 1 fs"
+                           if args.workload == "graphite_2p7m" else args.workload,
+                           "natoms": s.n, "precision": args.precision, "tpa": args.tpa,
+                           "l2": "inputs larger than L2 (pair list ~15 GB), no flush",
+                           "parallelism": f"replicas x{world}", "wall_s": wall},
+                "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches_total,
+                "kernel_ms": st["kernel_ms"], "kernel_launches": st["kernel_launches"],
+                "rebuilds": st["rebuilds"], "list_per_atom": st["list_per_atom"]}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,216 @@
+/*
+ * lmff_gb300 -- GB300 (sm_103a) force engine for the layered-materials path of
+ * LAMMPS-LMFF: Tersoff intralayer three-body forces + the ILP interlayer potential
+ * (per-atom normals and their derivatives) + the neighbour build that feeds both.
+ *
+ * C ABI: plain pointers and sizes, no C++ or CUDA types.  One engine handle drives one
+ * GPU through one CUDA stream; calls on one handle are not reentrant.
+ *
+ * What each entry point replaces in the reference (paths relative to the reference
+ * snapshot's source trees):
+ *   lmff_create / lmff_create_from_files
+ *       PairTersoff::coeff + read_file + setup_params (MANYBODY/pair_tersoff.cpp:293-580)
+ *       PairILPGrapheneHBN::settings + coeff + read_file + init_one
+ *       (USER-MISC/pair_ilp_graphene_hbn.cpp:132-240, :246-387)
+ *   lmff_set_box           Domain box + periodicity consumed by the neighbour build
+ *                          (neighbor.cpp:240-317, nbin_standard.cpp:53-192)
+ *   lmff_compute           PairHybrid::compute over {tersoff, ilp/graphene/hbn}
+ *                          (pair_hybrid.cpp:93-137) = PairTersoff::compute
+ *                          (pair_tersoff.cpp:86-265) + PairILPGrapheneHBN::compute
+ *                          (pair_ilp_graphene_hbn.cpp:428-443: ILP_neigh, calc_normal,
+ *                          calc_FvdW, calc_FRep) + the neighbour build
+ *                          (npair_full_bin_ghost.cpp:36-140) + virial_fdotr_compute
+ *                          (pair.cpp:1554) + per-atom energy tallies (pair.cpp:913,1060)
+ *   lmff_upload / lmff_run_nve / lmff_download
+ *                          Verlet::run (verlet.cpp:220-339) with FixNVE
+ *                          (fix_nve.cpp:64-111) and Neighbor::decide / check_distance
+ *                          (neighbor.cpp:1947-1976), device resident
+ *   lmff_batch_*           no counterpart: many independent systems per launch
+ *   lmff_last_error        error->one / error->all messages of both pair styles
+ */
+#ifndef LMFF_GB300_H
+#define LMFF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (0 = success) ------------------------------------------------ */
+#define LMFF_OK 0
+#define LMFF_EINVAL (-1)              /* bad argument */
+#define LMFF_ECUDA (-2)               /* CUDA runtime error (message in lmff_last_error) */
+#define LMFF_EOVERFLOW (-3)           /* a neighbour list outgrew its capacity */
+#define LMFF_ETOO_MANY_ILP_NEIGH (-4) /* > 3 intralayer neighbours (pair_ilp_graphene_hbn.cpp:739) */
+#define LMFF_EZERO_NORMAL (-5)        /* zero normal (pair_ilp_graphene_hbn.cpp:887,1030) */
+#define LMFF_EBADPARAM (-6)           /* potential file / parameter error */
+#define LMFF_ETIMEDOUT (-7)           /* a bounded device wait gave up */
+#define LMFF_EUNSUPPORTED (-8)        /* request outside what the engine implements */
+#define LMFF_ENOMEM (-9)              /* device or host allocation failed */
+#define LMFF_ENODEV (-10)             /* no usable CUDA device */
+
+/* ---- precision modes ------------------------------------------------------------ */
+#define LMFF_FP64 0   /* all-FP64 drop-in */
+#define LMFF_MIXED 1  /* FP32 pair / three-body arithmetic on FP64 displacements;
+                         FP64 integration, per-atom accumulation, reductions and
+                         normal-derivative assembly */
+
+/* ---- compute flags (the `which` argument) ----------------------------------------- */
+#define LMFF_TERSOFF 1     /* evaluate pair_style tersoff */
+#define LMFF_ILP 2         /* evaluate pair_style ilp/graphene/hbn */
+#define LMFF_SAME_ATOMS 4  /* caller promises type/mol/tag unchanged since the last call
+                              (LAMMPS: no reneighbouring this step); skips their upload */
+#define LMFF_OVERWRITE 8   /* store forces / per-atom energies instead of adding to them */
+
+typedef struct lmff_engine lmff_engine;
+
+/* One Tersoff entry; same fields and meaning as PairTersoff::Param
+ * (pair_tersoff.h:38-53), derived values (cut, cutsq, c1..c4) filled as setup_params
+ * does (pair_tersoff.cpp:565-573). */
+typedef struct lmff_tersoff_param {
+  double lam1, lam2, lam3, c, d, h, gamma, powerm, powern, beta;
+  double biga, bigb, bigd, bigr, cut, cutsq, c1, c2, c3, c4;
+  int ielement, jelement, kelement, powermint;
+} lmff_tersoff_param;
+
+/* One ILP entry; PairILPGrapheneHBN::Param (pair_ilp_graphene_hbn.h:53-57) after
+ * read_file's unit scaling and derived values (pair_ilp_graphene_hbn.cpp:354-364). */
+typedef struct lmff_ilp_param {
+  double z0, alpha, epsilon, C, delta, d, sR, reff, C6, S;
+  double delta2inv, seff, lambda, rcut;
+  int ielement, jelement;
+} lmff_ilp_param;
+
+/* Everything the two pair styles hold after coeff().  Arrays are copied. */
+typedef struct lmff_params {
+  int ntypes;                                 /* LAMMPS atom types 1..ntypes (<= 16) */
+  /* tersoff; tersoff_nparams == 0 disables the style */
+  int tersoff_nelements, tersoff_nparams;
+  const lmff_tersoff_param *tersoff_params;
+  const int *tersoff_elem2param;              /* [ne*ne*ne], (i*ne+j)*ne+k */
+  const int *tersoff_map;                     /* [ntypes+1], entry 0 unused, -1 = NULL */
+  double tersoff_cutmax;
+  /* ilp/graphene/hbn; ilp_nparams == 0 disables the style */
+  int ilp_nelements, ilp_nparams;
+  const lmff_ilp_param *ilp_params;
+  const int *ilp_elem2param;                  /* [ne*ne] */
+  const int *ilp_map;                         /* [ntypes+1] */
+  const double *ilp_cutILPsq;                 /* [ne*ne] */
+  double ilp_cut_global;                      /* pair_style ... ilp/graphene/hbn <cut> */
+  int ilp_tap_flag;                           /* pair_style ... <tap_flag> */
+  double skin;                                /* neighbor <skin> bin */
+} lmff_params;
+
+/* Energies and virials of one evaluation.  The virial is the global fdotr virial
+ * (xx, yy, zz, xy, xz, yz) of each style; pvector as PairILPGrapheneHBN (vdW, rep). */
+typedef struct lmff_result {
+  double e_tersoff, e_ilp;
+  double pvector[2];
+  double virial_tersoff[6], virial_ilp[6];
+} lmff_result;
+
+/* Per-step thermo sample of the device-resident NVE loop. */
+typedef struct lmff_thermo {
+  int64_t step;
+  double pe, ke, etotal, temp;
+  double virial[6];
+} lmff_thermo;
+
+typedef struct lmff_stats {
+  int64_t natoms, list_entries, short_entries, list_capacity, rebuilds, steps;
+  double list_per_atom, bytes_device;
+  double ms_last_build, ms_last_forces;
+  int precision, tpa, block;
+  /* device time of the last lmff_run_nve (CUDA events on the engine's stream) */
+  double ms_last_run;
+  /* with option "kernel_timing" = 1: summed device time and launch count per kernel
+   * since the last "reset_timing": [0] pair (ILP) kernel, [1] Tersoff, [2] intralayer
+   * lists, normals and normal-derivative assembly, [3] gather, [4] integrator,
+   * [5] neighbour build */
+  double kernel_ms[6];
+  int64_t kernel_launches[6];
+  /* interlayer pairs within the ILP cutoff in the current configuration (option
+   * "count_pairs" = 1 counts them once, outside any timed region) */
+  int64_t pairs_in_cutoff;
+} lmff_stats;
+
+/* ---- lifecycle ------------------------------------------------------------------- */
+int lmff_device_count(void);
+int lmff_create(lmff_engine **out, const lmff_params *p, int device);
+/* Parses the potential files as the reference does (17-word Tersoff entries,
+ * 13-word ILP entries, '#' comments, continuation lines, element filtering,
+ * duplicate / missing entry errors).  elements[t-1] names the element of type t or
+ * "NULL"; either file may be NULL to disable that style. */
+int lmff_create_from_files(lmff_engine **out, const char *tersoff_file, const char *ilp_file,
+                           int ntypes, const char *const *elements, double cut_global,
+                           int tap_flag, double skin, int device);
+void lmff_destroy(lmff_engine *e);
+
+/* ---- configuration ---------------------------------------------------------------- */
+int lmff_set_precision(lmff_engine *e, int mode);
+/* Orthogonal box only (xy = xz = yz = 0); periodic[d] != 0 marks periodic dims. */
+int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double xy, double xz,
+                 double yz, const int periodic[3]);
+/* Tunables: "tpa" threads per atom in the ILP kernel (4,8,16,32), "block" threads per
+ * block, "list_full" 1 = keep same-molecule pairs in the pair list (the reference's
+ * full list, for set comparisons), "skin" neighbour skin in Angstrom,
+ * "kernel_timing" 1 = record per-kernel device time, "reset_timing" clears it,
+ * "count_pairs" counts interlayer pairs within the cutoff now (see lmff_stats). */
+int lmff_set_option(lmff_engine *e, const char *key, double value);
+
+/* ---- one-shot evaluation on host buffers (the pair-style drop-in) ------------------ */
+/* x[natoms*3] positions; type[natoms] 1..ntypes; mol[natoms] molecule ids; tag[natoms]
+ * atom ids (NULL: 1..natoms).  which = LMFF_TERSOFF | LMFF_ILP.  f[natoms*3] is
+ * accumulated (+=); eatom[natoms] accumulated if not NULL.  res may be NULL. */
+int lmff_compute(lmff_engine *e, int natoms, const double *x, const int *type, const int64_t *mol,
+                 const int64_t *tag, int which, int eflag, int vflag, double *f, double *eatom,
+                 lmff_result *res);
+
+/* Same on device pointers (d_x[natoms*3] double, d_type int32, d_mol int64, d_tag int64
+ * or NULL, d_f double accumulated), ordered on the engine's stream. */
+int lmff_compute_device(lmff_engine *e, int natoms, const double *d_x, const int *d_type,
+                        const int64_t *d_mol, const int64_t *d_tag, int which, int eflag,
+                        int vflag, double *d_f, lmff_result *res);
+
+/* ---- device-resident system (standalone MD) ---------------------------------------- */
+/* mass[t-1] is the mass of type t (amu); v may be NULL (zero). */
+int lmff_upload(lmff_engine *e, int natoms, const double *x, const double *v, const int *type,
+                const int64_t *mol, const int64_t *tag, const double *mass);
+int lmff_compute_resident(lmff_engine *e, int which, int eflag, int vflag, lmff_result *res);
+/* nsteps of velocity Verlet (metal units, dt in ps); a thermo sample every
+ * thermo_every steps (0: none) into thermo[nsteps/thermo_every + 1] (may be NULL). */
+int lmff_run_nve(lmff_engine *e, int nsteps, double dt, int thermo_every, lmff_thermo *thermo);
+/* Copies back in the upload order; any pointer may be NULL. */
+int lmff_download(lmff_engine *e, double *x, double *v, double *f);
+
+/* ---- batched independent systems --------------------------------------------------- */
+/* A batch holds many independent periodic systems in one flattened device layout and
+ * evaluates them in one launch per kernel.  Box per system: lo[3], hi[3], periodic[3]. */
+typedef struct lmff_system_desc {
+  int natoms;
+  const double *x;          /* [natoms*3] */
+  const int *type;
+  const int64_t *mol;
+  double lo[3], hi[3];
+  int periodic[3];
+} lmff_system_desc;
+int lmff_batch_set(lmff_engine *e, int nsys, const lmff_system_desc *sys);
+/* Energies/forces/virials of every system: f_out[sum natoms * 3] in batch order
+ * (overwritten), res[nsys]. */
+int lmff_batch_compute(lmff_engine *e, double *f_out, lmff_result *res);
+
+/* ---- diagnostics ------------------------------------------------------------------- */
+int lmff_get_stats(lmff_engine *e, lmff_stats *out);
+/* Neighbour lists of the last build as (tag_i, tag_j, image) triples with
+ * image = sum_d ((s_d + 8) & 15) << (4 d): which = 0 pair list, 1 ILP intralayer list
+ * (current step).  Returns the entry count; out may be NULL to query. */
+int64_t lmff_export_list(lmff_engine *e, int which, int64_t *out, int64_t cap);
+const char *lmff_last_error(const lmff_engine *e);
+const char *lmff_strerror(int code);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

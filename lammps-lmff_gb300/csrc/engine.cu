@@ -1,0 +1,1577 @@
+// Engine orchestration and the C ABI (include/lmff_gb300.h).
+//
+// One engine = one device + one stream.  Atoms live on the device in bin-sorted order;
+// perm maps sorted positions back to the caller's order.  A call runs, in order:
+//   [rebuild when atoms moved > skin/2 since the last build, or identity/box changed]
+//     k_wrap_bin -> radix sort by bin -> k_permute -> k_bin_ranges -> k_hilo
+//     -> k_list (count + short lists) -> exclusive scan -> k_list (fill)
+//   k_short (intralayer ILP list, Tersoff short list, normals)
+//   k_tersoff (bonds centred at each atom)   k_ilp (interlayer pairs, normal derivatives)
+//   k_finish (gather) -> [k_reduce energies/virials]
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "engine.cuh"
+#include "forces.cuh"
+#include "lmff_gb300.h"
+#include "neighbor.cuh"
+#include "potentials.h"
+
+namespace lmff {
+
+#define LMFF_FORCE_API(NS, R)                                                                              \
+  namespace NS {                                                                                           \
+  void upload_pot(const PotConst<R> &p, cudaStream_t s);                                                   \
+  void launch_short(const ForceArgs<R> &a, const double *cutILPsq64, double tcutmaxsq64, cudaStream_t s); \
+  void launch_tersoff(const ForceArgs<R> &a, bool ev, bool eatom, cudaStream_t s);                        \
+  void launch_ilp(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, cudaStream_t s);         \
+  void launch_nderiv(const ForceArgs<R> &a, bool ev, cudaStream_t s);                                      \
+  void launch_finish(const ForceArgs<R> &a, bool eatom, cudaStream_t s);                                   \
+  }
+LMFF_FORCE_API(f64, double)
+LMFF_FORCE_API(f32, float)
+
+static const double LOG2E = 1.4426950408889634;
+static const double FTM2V = 1.0 / 1.0364269e-4;  // units metal (update.cpp)
+static const double MVV2E = 1.0364269e-4;
+static const double BOLTZ = 8.617343e-5;
+
+// ------------------------------------------------------------------ small kernels
+
+__global__ void k_load(int n, const double *x, const int *type, const int64_t *mol, const int64_t *tag, const double *v,
+                       const double *mass_t, const int *sysid_in, d4 *xq, int64_t *tag_s, int *perm, int *sysid,
+                       double *vs, double *mass) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  long long info = ((long long)mol[p] << 8) | (long long)type[p];
+  xq[p] = make_d4(x[3 * p], x[3 * p + 1], x[3 * p + 2], __longlong_as_double(info));
+  tag_s[p] = tag ? tag[p] : (int64_t)(p + 1);
+  perm[p] = p;
+  sysid[p] = sysid_in ? sysid_in[p] : 0;
+  vs[p] = v ? v[3 * p] : 0.0;
+  vs[n + p] = v ? v[3 * p + 1] : 0.0;
+  vs[2 * n + p] = v ? v[3 * p + 2] : 0.0;
+  mass[p] = mass_t ? mass_t[type[p] - 1] : 1.0;
+}
+
+// identity check of the caller's arrays against the resident state
+__global__ void k_check_ident(int n, const int *perm, const int *type, const int64_t *mol, const int64_t *tag,
+                              const d4 *xq, const int64_t *tag_s, int *flag) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int o = perm[q];
+  long long info = ((long long)mol[o] << 8) | (long long)type[o];
+  bool bad = info != __double_as_longlong(xq[q].w);
+  if (tag && tag[o] != tag_s[q]) bad = true;
+  if (bad) atomicOr(flag, 1);
+}
+
+// new caller positions into sorted order + max squared displacement since the build
+__global__ void k_update_x(int n, const int *perm, const double *x, d4 *xq, const double *xhold,
+                           unsigned long long *maxdisp) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  double d2 = 0.0;
+  if (q < n) {
+    int o = perm[q];
+    d4 w = xq[q];
+    double a = x[3 * o], b = x[3 * o + 1], c = x[3 * o + 2];
+    xq[q] = make_d4(a, b, c, w.w);
+    double dx = a - xhold[3 * q], dy = b - xhold[3 * q + 1], dz = c - xhold[3 * q + 2];
+    d2 = dx * dx + dy * dy + dz * dz;
+  }
+  for (int o = 16; o > 0; o >>= 1) d2 = fmax(d2, __shfl_xor_sync(0xffffffff, d2, o));
+  if ((threadIdx.x & 31) == 0 && d2 > 0.0) atomicMax(maxdisp, (unsigned long long)__double_as_longlong(d2));
+}
+
+__global__ void k_scatter_add(int n, const int *perm, const double *fs, double *fin, int overwrite) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int o = perm[q];
+  for (int c = 0; c < 3; c++) {
+    double v = fs[(size_t)c * n + q];
+    fin[3 * o + c] = overwrite ? v : fin[3 * o + c] + v;
+  }
+}
+
+__global__ void k_scatter_add1(int n, const int *perm, const double *es, double *ein, int overwrite) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int o = perm[q];
+  ein[o] = overwrite ? es[q] : ein[o] + es[q];
+}
+
+__global__ void k_unpermute_state(int n, const int *perm, const d4 *xq, const double *v, const double *f, double *xo,
+                                  double *vo, double *fo) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int o = perm[q];
+  d4 w = xq[q];
+  xo[3 * o] = w.x; xo[3 * o + 1] = w.y; xo[3 * o + 2] = w.z;
+  for (int c = 0; c < 3; c++) {
+    vo[3 * o + c] = v[(size_t)c * n + q];
+    fo[3 * o + c] = f[(size_t)c * n + q];
+  }
+}
+
+// deterministic per-system reduction of the per-atom stat arrays: block (s, q) sums
+// quantity q of system s in a fixed order
+__global__ void k_reduce(int n, int nq, const double *const *arrs, const SysDesc *sys, double *out) {
+  int s = blockIdx.x / nq, q = blockIdx.x % nq;
+  const double *a = arrs[q / 8] + (size_t)(q % 8) * n;
+  int b = sys[s].atom_begin, e = sys[s].atom_end;
+  double acc = 0.0;
+  for (int p = b + threadIdx.x; p < e; p += blockDim.x) acc += a[p];
+  __shared__ double sh[256];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+}
+
+// interlayer pairs of the list within the ILP cutoff (same test as the pair kernel)
+__global__ void k_count_pairs(int n, const d4 *xq, const SysDesc *sys, const int *sysid, const int64_t *off,
+                              const uint32_t *list, ListCode lc, double cutsq, unsigned long long *out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long c = 0;
+  if (i < n) {
+    const SysDesc &sd = sys[sysid[i]];
+    d4 a = xq[i];
+    long long mi = __double_as_longlong(a.w) >> 8;
+    for (int64_t k = off[i]; k < off[i + 1]; k++) {
+      int j, sx, sy, sz;
+      decode_entry(list[k], lc, j, sx, sy, sz);
+      d4 b = xq[j];
+      if ((__double_as_longlong(b.w) >> 8) == mi) continue;
+      double dx = a.x - (b.x + sx * sd.L[0]), dy = a.y - (b.y + sy * sd.L[1]), dz = a.z - (b.z + sz * sd.L[2]);
+      if (dx * dx + dy * dy + dz * dz < cutsq) c++;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffff, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// velocity Verlet halves (fix_nve.cpp:64-111); the first also moves x, refreshes the
+// double-float split and tracks the displacement since the last build
+__global__ void k_nve1(int n, d4 *xq, double *v, const double *f, const double *mass, double dtf, double dtv,
+                       const double *xhold, unsigned long long *maxdisp, const SysDesc *sys, const int *sysid,
+                       float4 *xh, float4 *xl, int do_hilo) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  double d2 = 0.0;
+  if (q < n) {
+    double dtfm = dtf / mass[q];
+    d4 w = xq[q];
+    double vx = v[q] + dtfm * f[q];
+    double vy = v[n + q] + dtfm * f[n + q];
+    double vz = v[2 * n + q] + dtfm * f[2 * n + q];
+    v[q] = vx; v[n + q] = vy; v[2 * n + q] = vz;
+    double x = w.x + dtv * vx, y = w.y + dtv * vy, z = w.z + dtv * vz;
+    xq[q] = make_d4(x, y, z, w.w);
+    double dx = x - xhold[3 * q], dy = y - xhold[3 * q + 1], dz = z - xhold[3 * q + 2];
+    d2 = dx * dx + dy * dy + dz * dz;
+    if (do_hilo) {
+      const SysDesc &sd = sys[sysid[q]];
+      double X = x - sd.lo[0] + 32.0 + sd.base;
+      double Y = y - sd.lo[1] + 32.0 + sd.base;
+      double Z = z - sd.lo[2] + 32.0 + sd.base;
+      float hx = (float)X, hy = (float)Y, hz = (float)Z;
+      float4 h = xh[q];
+      xh[q] = make_float4(hx, hy, hz, h.w);
+      xl[q] = make_float4((float)(X - (double)hx), (float)(Y - (double)hy), (float)(Z - (double)hz), 0.f);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) d2 = fmax(d2, __shfl_xor_sync(0xffffffff, d2, o));
+  if ((threadIdx.x & 31) == 0 && d2 > 0.0) atomicMax(maxdisp, (unsigned long long)__double_as_longlong(d2));
+}
+
+__global__ void k_nve2(int n, double *v, const double *f, const double *mass, double dtf, double *ke) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  double dtfm = dtf / mass[q];
+  double vx = v[q] + dtfm * f[q];
+  double vy = v[n + q] + dtfm * f[n + q];
+  double vz = v[2 * n + q] + dtfm * f[2 * n + q];
+  v[q] = vx; v[n + q] = vy; v[2 * n + q] = vz;
+  if (ke) ke[q] = 0.5 * MVV2E * mass[q] * (vx * vx + vy * vy + vz * vz);
+}
+
+// ------------------------------------------------------------------ engine
+
+template <class T>
+static cudaError_t dalloc(T *&p, size_t count) {
+  if (p) cudaFree(p);
+  p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void **)&p, count * sizeof(T));
+}
+
+struct Engine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int precision = LMFF_FP64;
+  int tpa = 16, block = 128;
+  int list_full = 0;
+  double skin = 2.0;
+  int ntypes = 0;
+  HostTersoff ht;
+  HostIlp hi;
+  bool t_on = false, i_on = false;
+  double cut_global = 16.0;
+  int tap = 1;
+  PotConst<double> pot64;
+  PotConst<float> pot32;
+  NbConst nbc;
+  double *d_cutILPsq = nullptr;
+  double rshort = 0.0, cutneigh_max = 0.0;
+  bool pot_dirty = true;
+  // geometry
+  double blo[3] = {0, 0, 0}, bhi[3] = {0, 0, 0};
+  int bper[3] = {0, 0, 0};
+  bool have_box = false;
+  // state
+  DevState d;
+  std::vector<SysDesc> hsys;
+  ListCode lc{};
+  bool loaded = false, built = false, forces_valid = false;
+  int n = 0;
+  // staging (caller order)
+  double *d_xin = nullptr, *d_fin = nullptr, *d_vin = nullptr, *d_ein = nullptr;
+  int *d_tin = nullptr, *d_sysin = nullptr;
+  int64_t *d_min = nullptr, *d_gin = nullptr;
+  double *d_massT = nullptr;
+  // spares for permutation
+  d4 *xq2 = nullptr;
+  double *v2 = nullptr, *mass2 = nullptr;
+  int64_t *tag2 = nullptr;
+  int *perm2 = nullptr, *sysid2 = nullptr;
+  double *stat_ilp = nullptr, *stat_ters = nullptr, *eatom_ilp = nullptr, *eatom_ters = nullptr, *ke = nullptr;
+  double **d_arrs = nullptr;
+  double **d_karrs = nullptr;
+  double *d_kout = nullptr;
+  double *h_pinned = nullptr;
+  size_t h_pinned_bytes = 0;
+  std::vector<double> mass_type;
+  // stats
+  int64_t rebuilds = 0, steps = 0, list_total = 0, short_total = 0;
+  double ms_build = 0, ms_forces = 0, ms_run = 0;
+  int64_t pairs_in_cut = 0;
+  // per-kernel device timing (option "kernel_timing"): events around each launch
+  bool ktiming = false;
+  double kms[6] = {0, 0, 0, 0, 0, 0};
+  int64_t klaunch[6] = {0, 0, 0, 0, 0, 0};
+  struct Pend {
+    cudaEvent_t a, b;
+    int k;
+  };
+  std::vector<Pend> pend;
+  std::vector<cudaEvent_t> evpool;
+  cudaEvent_t ev_get() {
+    if (evpool.empty()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      return e;
+    }
+    cudaEvent_t e = evpool.back();
+    evpool.pop_back();
+    return e;
+  }
+  template <class F>
+  void timed(int k, F &&f) {
+    if (!ktiming) {
+      f();
+      return;
+    }
+    Pend p{ev_get(), ev_get(), k};
+    cudaEventRecord(p.a, stream);
+    f();
+    cudaEventRecord(p.b, stream);
+    pend.push_back(p);
+  }
+  // after a stream synchronisation: fold finished events into the per-kernel sums
+  void harvest() {
+    for (auto &p : pend) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+        kms[p.k] += ms;
+        klaunch[p.k]++;
+      }
+      evpool.push_back(p.a);
+      evpool.push_back(p.b);
+    }
+    pend.clear();
+  }
+  std::string err;
+  int64_t nbit_bins = 1;
+
+  int fail(int code, const std::string &m) {
+    err = m;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char *where) {
+    err = std::string(where) + ": " + cudaGetErrorString(e);
+    return LMFF_ECUDA;
+  }
+#define CK(expr)                                    \
+  do {                                              \
+    cudaError_t _e = (expr);                        \
+    if (_e != cudaSuccess) return cuda_fail(_e, #expr); \
+  } while (0)
+
+  ~Engine() { release(); }
+
+  void release() {
+    if (device >= 0) cudaSetDevice(device);
+    void *ptrs[] = {d.xq, d.xh, d.xl, d.v, d.f, d.xhold, d.tag, d.perm, d.sysid, d.mass, d.nrm64, d.nrm32, d.ilp_cnt,
+                    d.ilp_nb, d.ters_cnt, d.ters_nb, d.ters_g, d.ters_f, d.ilp_f, d.ilp_c, d.ilp_g, d.list_off, d.list,
+                    d.short_cnt, d.short_nb, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.cub_tmp,
+                    d.cnt_tmp, d.sys, d.red_out, d.status, d.maxdisp, d_xin, d_fin, d_vin, d_ein, d_tin, d_sysin,
+                    d_min, d_gin, d_massT, xq2, v2, mass2, tag2, perm2, sysid2, stat_ilp, stat_ters, eatom_ilp,
+                    eatom_ters, ke, d_arrs, d_karrs, d_kout, d_cutILPsq};
+    for (void *p : ptrs)
+      if (p) cudaFree(p);
+    d = DevState();
+    d_xin = d_fin = d_vin = d_ein = nullptr;
+    d_tin = d_sysin = nullptr;
+    d_min = d_gin = nullptr;
+    d_massT = nullptr;
+    xq2 = nullptr;
+    v2 = mass2 = nullptr;
+    tag2 = nullptr;
+    perm2 = sysid2 = nullptr;
+    stat_ilp = stat_ters = eatom_ilp = eatom_ters = ke = nullptr;
+    d_arrs = nullptr;
+    d_karrs = nullptr;
+    d_kout = nullptr;
+    d_cutILPsq = nullptr;
+    if (h_pinned) cudaFreeHost(h_pinned);
+    h_pinned = nullptr;
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+  }
+
+  // ---------------------------------------------------------------- parameters
+  int set_params(const lmff_params *p) {
+    if (!p || p->ntypes < 1 || p->ntypes > MAXTYPE) return fail(LMFF_EINVAL, "ntypes must be in 1..16");
+    ntypes = p->ntypes;
+    t_on = p->tersoff_nparams > 0;
+    i_on = p->ilp_nparams > 0;
+    if (!t_on && !i_on) return fail(LMFF_EINVAL, "neither tersoff nor ilp/graphene/hbn parameters given");
+    ht = HostTersoff();
+    hi = HostIlp();
+    if (t_on) {
+      int ne = p->tersoff_nelements;
+      if (ne < 1 || ne > MAXELEM) return fail(LMFF_EUNSUPPORTED, "tersoff: at most 4 elements are supported");
+      ht.params.assign(p->tersoff_params, p->tersoff_params + p->tersoff_nparams);
+      ht.elem2param.assign(p->tersoff_elem2param, p->tersoff_elem2param + ne * ne * ne);
+      ht.map.assign(p->tersoff_map, p->tersoff_map + ntypes + 1);
+      ht.elements.resize(ne);
+      ht.cutmax = p->tersoff_cutmax;
+    }
+    if (i_on) {
+      int ne = p->ilp_nelements;
+      if (ne < 1 || ne > MAXELEM) return fail(LMFF_EUNSUPPORTED, "ilp: at most 4 elements are supported");
+      hi.params.assign(p->ilp_params, p->ilp_params + p->ilp_nparams);
+      hi.elem2param.assign(p->ilp_elem2param, p->ilp_elem2param + ne * ne);
+      hi.map.assign(p->ilp_map, p->ilp_map + ntypes + 1);
+      hi.cutILPsq.assign(p->ilp_cutILPsq, p->ilp_cutILPsq + ne * ne);
+      hi.elements.resize(ne);
+    }
+    cut_global = p->ilp_cut_global;
+    tap = p->ilp_tap_flag;
+    skin = p->skin;
+    return build_consts();
+  }
+
+  template <class R>
+  void fill_pot(PotConst<R> &P) {
+    memset(&P, 0, sizeof P);
+    P.ntypes = ntypes;
+    P.t_enabled = t_on;
+    P.i_enabled = i_on;
+    P.t_ne = t_on ? (int)ht.elements.size() : 0;
+    P.i_ne = i_on ? (int)hi.elements.size() : 0;
+    for (int t = 0; t <= MAXTYPE; t++) {
+      P.t_map[t] = (t_on && t >= 1 && t <= ntypes) ? ht.map[t] : -1;
+      P.i_map[t] = (i_on && t >= 1 && t <= ntypes) ? hi.map[t] : -1;
+    }
+    P.tap = tap;
+    P.vdw_sym = 1;
+    P.rep_sym = 1;
+    P.t_cutmaxsq = (R)(ht.cutmax * ht.cutmax);
+    P.i_cutsq = (R)(cut_global * cut_global);
+    P.i_inv_rcut = (R)(1.0 / cut_global);
+    if (i_on) {
+      int ne = P.i_ne;
+      for (int a = 0; a < ne; a++)
+        for (int b = 0; b < ne; b++) {
+          const lmff_ilp_param &q = hi.params[hi.elem2param[a * ne + b]];
+          const lmff_ilp_param &s = hi.params[hi.elem2param[b * ne + a]];
+          IlpP<R> &o = P.ilp[a * MAXELEM + b];
+          o.z0 = (R)q.z0;
+          o.lambda = (R)q.lambda;
+          o.eps_half = (R)(0.5 * q.epsilon);
+          o.C = (R)q.C;
+          o.delta2inv = (R)q.delta2inv;
+          o.d = (R)q.d;
+          o.seff = (R)q.seff;
+          o.C6 = (R)q.C6;
+          o.d_over_seff = (R)(q.d / q.seff);
+          o.lam_l2e = (R)(q.lambda * LOG2E);
+          o.lamz0_l2e = (R)(q.lambda * q.z0 * LOG2E);
+          o.nd2_l2e = (R)(-q.delta2inv * LOG2E);
+          o.ts_a = (R)(q.d / q.seff * LOG2E);
+          o.ts_b = (R)(q.d * LOG2E);
+          o.same_as_swapped = (q.z0 == s.z0 && q.lambda == s.lambda && q.epsilon == s.epsilon && q.C == s.C &&
+                               q.delta2inv == s.delta2inv);
+          if (!(q.C6 == s.C6 && q.d == s.d && q.seff == s.seff)) P.vdw_sym = 0;
+          P.i_cutILPsq[a * MAXELEM + b] = (R)hi.cutILPsq[a * ne + b];
+        }
+    }
+    if (t_on) {
+      int ne = P.t_ne;
+      for (int a = 0; a < ne; a++)
+        for (int b = 0; b < ne; b++)
+          for (int c = 0; c < ne; c++) {
+            const lmff_tersoff_param &q = ht.params[ht.elem2param[(a * ne + b) * ne + c]];
+            TersP<R> &o = P.ters[(a * MAXELEM + b) * MAXELEM + c];
+            o.lam1 = (R)q.lam1;
+            o.lam2 = (R)q.lam2;
+            o.lam3 = (R)q.lam3;
+            o.c2 = (R)(q.c * q.c);
+            o.d2 = (R)(q.d * q.d);
+            o.h = (R)q.h;
+            o.gamma = (R)q.gamma;
+            o.powern = (R)q.powern;
+            o.beta = (R)q.beta;
+            o.biga = (R)q.biga;
+            o.bigb = (R)q.bigb;
+            o.bigr = (R)q.bigr;
+            o.bigd = (R)q.bigd;
+            o.cutsq = (R)q.cutsq;
+            o.c1 = (R)q.c1;
+            o.c2t = (R)q.c2;
+            o.c3 = (R)q.c3;
+            o.c4 = (R)q.c4;
+            o.cd2 = (R)((q.c * q.c) / (q.d * q.d));
+            o.inv2n = (R)(1.0 / (2.0 * q.powern));
+            o.pi2_over_D = (R)(1.57079632679489661923 / q.bigd);
+            o.pi4_over_D = (R)(0.78539816339744830962 / q.bigd);
+            o.rlo = (R)(q.bigr - q.bigd);
+            o.rhi = (R)(q.bigr + q.bigd);
+            o.A64 = q.biga;
+            o.B64 = q.bigb;
+            o.lam1_64 = q.lam1;
+            o.lam2_64 = q.lam2;
+            o.R64 = q.bigr;
+            o.D64 = q.bigd;
+            o.rlo64 = q.bigr - q.bigd;
+            o.rhi64 = q.bigr + q.bigd;
+            o.pi4D64 = 0.78539816339744830962 / q.bigd;
+            o.cutsq64 = q.cutsq;
+            o.powermint = q.powermint;
+          }
+      for (int a = 0; a < ne; a++)
+        for (int b = 0; b < ne; b++) {
+          const lmff_tersoff_param &q = ht.params[ht.elem2param[(a * ne + b) * ne + b]];
+          const lmff_tersoff_param &s = ht.params[ht.elem2param[(b * ne + a) * ne + a]];
+          if (!(q.lam1 == s.lam1 && q.biga == s.biga && q.bigr == s.bigr && q.bigd == s.bigd)) P.rep_sym = 0;
+        }
+    }
+  }
+
+  int build_consts() {
+    fill_pot(pot64);
+    fill_pot(pot32);
+    memset(&nbc, 0, sizeof nbc);
+    cutneigh_max = 0.0;
+    double rmaxilp = 0.0;
+    for (int a = 0; a <= MAXTYPE; a++) nbc.ilp_mapped[a] = (i_on && a >= 1 && a <= ntypes && hi.map[a] >= 0) ? 1 : 0;
+    for (int a = 0; a <= MAXTYPE; a++)
+      for (int b = 0; b <= MAXTYPE; b++) {
+        double cut = 0.0;
+        if (a >= 1 && b >= 1 && a <= ntypes && b <= ntypes) {
+          if (i_on && hi.map[a] >= 0 && hi.map[b] >= 0) cut = std::max(cut, cut_global);
+          if (t_on && ht.map[a] >= 0 && ht.map[b] >= 0) cut = std::max(cut, ht.cutmax);
+        }
+        double cn = cut > 0.0 ? cut + skin : -1.0;
+        nbc.cutnsq_d[a * (MAXTYPE + 1) + b] = cn > 0 ? cn * cn : -1.0;
+        nbc.cutnsq_f[a * (MAXTYPE + 1) + b] = cn > 0 ? (float)(cn * cn) : -1.0f;
+        cutneigh_max = std::max(cutneigh_max, cn);
+      }
+    if (i_on)
+      for (double c : hi.cutILPsq) rmaxilp = std::max(rmaxilp, std::sqrt(c));
+    rshort = std::max(rmaxilp, t_on ? ht.cutmax : 0.0) + skin;
+    nbc.rshortsq_d = rshort * rshort;
+    nbc.rshortsq_f = (float)(rshort * rshort);
+    pot_dirty = true;
+    built = false;
+    return LMFF_OK;
+  }
+
+  int init_device(int dev) {
+    int cnt = 0;
+    if (cudaGetDeviceCount(&cnt) != cudaSuccess || cnt == 0) return fail(LMFF_ENODEV, "no CUDA device");
+    if (dev < 0 || dev >= cnt) return fail(LMFF_EINVAL, "device index out of range");
+    device = dev;
+    CK(cudaSetDevice(dev));
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaMalloc(&d.status, sizeof(int)));
+    CK(cudaMalloc(&d.maxdisp, sizeof(unsigned long long)));
+    CK(cudaMalloc(&d_cutILPsq, sizeof(double) * MAXELEM * MAXELEM));
+    CK(cudaMalloc(&d_arrs, sizeof(double *) * 2));
+    CK(cudaMalloc(&d_karrs, sizeof(double *) * 2));
+    CK(cudaMalloc(&d_kout, sizeof(double)));
+    CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
+    return LMFF_OK;
+  }
+
+  int push_consts() {
+    if (!pot_dirty) return LMFF_OK;
+    f64::upload_pot(pot64, stream);
+    f32::upload_pot(pot32, stream);
+    nb_upload_const(nbc, stream);
+    double c[MAXELEM * MAXELEM] = {0};
+    if (i_on) {
+      int ne = (int)hi.elements.size();
+      for (int a = 0; a < ne; a++)
+        for (int b = 0; b < ne; b++) c[a * MAXELEM + b] = hi.cutILPsq[a * ne + b];
+    }
+    CK(cudaMemcpyAsync(d_cutILPsq, c, sizeof c, cudaMemcpyHostToDevice, stream));
+    CK(cudaGetLastError());
+    pot_dirty = false;
+    return LMFF_OK;
+  }
+
+  // ---------------------------------------------------------------- capacity
+  int cap_n = 0, cap_sys = 0;
+
+  int ensure_atoms(int nn) {
+    if (nn <= cap_n) return LMFF_OK;
+    int c = nn + nn / 8 + 64;
+    CK(cudaStreamSynchronize(stream));
+    CK(dalloc(d.xq, c)); CK(dalloc(xq2, c)); CK(dalloc(d.xh, c)); CK(dalloc(d.xl, c));
+    CK(dalloc(d.v, 3 * (size_t)c)); CK(dalloc(v2, 3 * (size_t)c)); CK(dalloc(d.f, 3 * (size_t)c));
+    CK(dalloc(d.xhold, 3 * (size_t)c));
+    CK(dalloc(d.tag, c)); CK(dalloc(tag2, c)); CK(dalloc(d.perm, c)); CK(dalloc(perm2, c));
+    CK(dalloc(d.sysid, c)); CK(dalloc(sysid2, c)); CK(dalloc(d.mass, c)); CK(dalloc(mass2, c));
+    CK(dalloc(d.nrm64, c)); CK(dalloc(d.nrm32, c));
+    CK(dalloc(d.ilp_cnt, c)); CK(dalloc(d.ilp_nb, (size_t)c * MAXILP));
+    CK(dalloc(d.ters_cnt, c)); CK(dalloc(d.ters_nb, (size_t)c * MAXTERS));
+    CK(dalloc(d.ters_g, (size_t)c * MAXTERS)); CK(dalloc(d.ters_f, 3 * (size_t)c));
+    CK(dalloc(d.ilp_f, 3 * (size_t)c)); CK(dalloc(d.ilp_c, (size_t)c * MAXILP)); CK(dalloc(d.ilp_g, c));
+    CK(dalloc(stat_ilp, 8 * (size_t)c)); CK(dalloc(stat_ters, 8 * (size_t)c));
+    CK(dalloc(eatom_ilp, c)); CK(dalloc(eatom_ters, c)); CK(dalloc(ke, c));
+    CK(dalloc(d.list_off, (size_t)c + 1)); CK(dalloc(d.short_cnt, c)); CK(dalloc(d.short_nb, (size_t)c * MAXSHORT));
+    CK(dalloc(d.bin_key, c)); CK(dalloc(d.bin_key2, c)); CK(dalloc(d.idx, c)); CK(dalloc(d.idx2, c));
+    CK(dalloc(d.cnt_tmp, (size_t)c + 1));
+    CK(dalloc(d_xin, 3 * (size_t)c)); CK(dalloc(d_fin, 3 * (size_t)c)); CK(dalloc(d_vin, 3 * (size_t)c));
+    CK(dalloc(d_ein, c)); CK(dalloc(d_tin, c)); CK(dalloc(d_sysin, c)); CK(dalloc(d_min, c)); CK(dalloc(d_gin, c));
+    // CUB temporary storage for the sort (32 key bits) and the scan
+    size_t tb = nb_sort_tmp_bytes(c, 32);
+    if (d.cub_tmp) cudaFree(d.cub_tmp);
+    d.cub_tmp = nullptr;
+    CK(cudaMalloc(&d.cub_tmp, tb));
+    d.cub_tmp_bytes = tb;
+    cap_n = c;
+    const double *arrs[2] = {stat_ilp, stat_ters};
+    CK(cudaMemcpy(d_arrs, arrs, sizeof arrs, cudaMemcpyHostToDevice));
+    const double *karrs[2] = {ke, ke};
+    CK(cudaMemcpy(d_karrs, karrs, sizeof karrs, cudaMemcpyHostToDevice));
+    return LMFF_OK;
+  }
+
+  int ensure_pinned(size_t bytes) {
+    if (bytes <= h_pinned_bytes) return LMFF_OK;
+    if (h_pinned) cudaFreeHost(h_pinned);
+    h_pinned = nullptr;
+    CK(cudaMallocHost(&h_pinned, bytes));
+    h_pinned_bytes = bytes;
+    return LMFF_OK;
+  }
+
+  // ---------------------------------------------------------------- geometry
+  // One SysDesc per system: bins of at least (cutneigh/2)*1.0001 so that any pair
+  // within cutneigh is at most `reach` bins apart whatever the rounding of the bin index.
+  int make_sys(std::vector<SysDesc> &out, const std::vector<std::array<double, 9>> &boxes) {
+    out.clear();
+    int bin_begin = 0;
+    double target = 0.5 * cutneigh_max * 1.0001;
+    int R = 0;
+    for (size_t s = 0; s < boxes.size(); s++) {
+      const auto &b = boxes[s];
+      SysDesc sd;
+      memset(&sd, 0, sizeof sd);
+      double maxL = 0.0;
+      for (int k = 0; k < 3; k++) {
+        sd.lo[k] = b[k];
+        sd.L[k] = b[3 + k] - b[k];
+        sd.per[k] = b[6 + k] != 0.0;
+        if (!(sd.L[k] > 0.0)) return fail(LMFF_EINVAL, "box length must be positive");
+        int nb = std::max(1, (int)std::floor(sd.L[k] / target));
+        if (nb > 4096) nb = 4096;
+        double bs = sd.L[k] / nb;
+        sd.nb[k] = nb;
+        sd.binv[k] = 1.0 / bs;
+        sd.reach[k] = (int)std::ceil(cutneigh_max / bs * (1.0 + 1e-12));
+        // images needed: |s| <= ceil(reach / nb) for a stencil of +-reach bins
+        if (sd.per[k]) R = std::max(R, (sd.reach[k] + nb - 1) / nb);
+        sd.Lhi[k] = (float)sd.L[k];
+        sd.Llo[k] = (float)(sd.L[k] - (double)sd.Lhi[k]);
+        maxL = std::max(maxL, sd.L[k]);
+      }
+      sd.base = std::ldexp(1.0, (int)std::ceil(std::log2(maxL + 64.0)));
+      sd.bin_begin = bin_begin;
+      long long nbins = (long long)sd.nb[0] * sd.nb[1] * sd.nb[2];
+      if (bin_begin + nbins > (1LL << 30)) return fail(LMFF_EOVERFLOW, "too many bins");
+      bin_begin += (int)nbins;
+      out.push_back(sd);
+    }
+    d.nbins = bin_begin;
+    int w = 1;
+    while ((1 << w) < 2 * R + 1) w++;
+    lc.R = R;
+    lc.w = w;
+    lc.ibits = 32 - 3 * w;
+    lc.imask = (lc.ibits >= 32) ? 0xffffffffu : ((1u << lc.ibits) - 1u);
+    lc.wmask = (1u << w) - 1u;
+    nbit_bins = 1;
+    while ((1LL << nbit_bins) < d.nbins) nbit_bins++;
+    return LMFF_OK;
+  }
+
+  int upload_sys() {
+    if ((int)hsys.size() > cap_sys) {
+      CK(dalloc(d.sys, hsys.size()));
+      CK(dalloc(d.red_out, hsys.size() * 16));
+      cap_sys = (int)hsys.size();
+    }
+    CK(cudaMemcpyAsync(d.sys, hsys.data(), sizeof(SysDesc) * hsys.size(), cudaMemcpyHostToDevice, stream));
+    if (d.nbins > d.nbins_cap) {
+      CK(dalloc(d.bin_start, d.nbins));
+      CK(dalloc(d.bin_end, d.nbins));
+      d.nbins_cap = d.nbins;
+    }
+    d.nsys = (int)hsys.size();
+    return LMFF_OK;
+  }
+
+  // ---------------------------------------------------------------- load / rebuild
+  int load_from_staging(int nn, bool have_v, bool have_sysid) {
+    n = nn;
+    d.n = nn;
+    if ((int64_t)n >= (1LL << lc.ibits))
+      return fail(LMFF_EOVERFLOW, "too many atoms for the 32-bit neighbour-list code of this box");
+    int g = (n + 255) / 256;
+    if (n) {
+      k_load<<<g, 256, 0, stream>>>(n, d_xin, d_tin, d_min, d_gin, have_v ? d_vin : nullptr, d_massT,
+                                    have_sysid ? d_sysin : nullptr, d.xq, d.tag, d.perm, d.sysid, d.v, d.mass);
+      CK(cudaGetLastError());
+    }
+    loaded = true;
+    built = false;
+    forces_valid = false;
+    return rebuild();
+  }
+
+  int rebuild() {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, stream);
+    int rc = push_consts();
+    if (rc) return rc;
+    if (n == 0) {
+      built = true;
+      return LMFF_OK;
+    }
+    int g = (n + 255) / 256;
+    nb_wrap_bin(n, d.xq, d.sys, d.sysid, d.bin_key, d.idx, stream);
+    CK(nb_sort(d.cub_tmp, d.cub_tmp_bytes, d.bin_key, d.bin_key2, d.idx, d.idx2, n, (int)nbit_bins, stream));
+    nb_permute(n, d.idx2, d.xq, xq2, d.v, v2, d.tag, tag2, d.perm, perm2, d.sysid, sysid2, d.mass, mass2, stream);
+    std::swap(d.xq, xq2);
+    std::swap(d.v, v2);
+    std::swap(d.tag, tag2);
+    std::swap(d.perm, perm2);
+    std::swap(d.sysid, sysid2);
+    std::swap(d.mass, mass2);
+    CK(cudaMemsetAsync(d.bin_start, 0, sizeof(int) * d.nbins, stream));
+    CK(cudaMemsetAsync(d.bin_end, 0, sizeof(int) * d.nbins, stream));
+    nb_bin_ranges(n, d.bin_key2, d.bin_start, d.bin_end, stream);
+    // atoms' systems are contiguous after the sort: atom ranges per system
+    CK(cudaGetLastError());
+    hilo_all();
+    NbArgs a;
+    memset(&a, 0, sizeof a);
+    a.n = n;
+    a.xq = d.xq;
+    a.xh = d.xh;
+    a.xl = d.xl;
+    a.sys = d.sys;
+    a.sysid = d.sysid;
+    a.bin_start = d.bin_start;
+    a.bin_end = d.bin_end;
+    a.list_off = d.list_off;
+    a.list = d.list;
+    a.list_cap = d.list_cap;
+    a.cnt = d.cnt_tmp;
+    a.short_cnt = d.short_cnt;
+    a.short_nb = d.short_nb;
+    a.lc = lc;
+    a.full = list_full;
+    a.status = d.status;
+    CK(cudaMemsetAsync(d.cnt_tmp + n, 0, sizeof(int64_t), stream));
+    nb_list(a, false, stream);
+    CK(nb_scan(d.cub_tmp, d.cub_tmp_bytes, d.cnt_tmp, d.list_off, n, stream));
+    int64_t total = 0;
+    CK(cudaMemcpyAsync(&total, d.list_off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (total < 0 || total > (int64_t)n * 65536)
+      return fail(LMFF_EOVERFLOW, "pair-list count out of range (" + std::to_string(total) + ")");
+    if (total > d.list_cap) {
+      int64_t cap = total + total / 8 + 1024;
+      if (d.list) cudaFree(d.list);
+      d.list = nullptr;
+      cudaError_t e = cudaMalloc(&d.list, sizeof(uint32_t) * cap);
+      if (e != cudaSuccess) {
+        d.list_cap = 0;
+        return fail(LMFF_ENOMEM, "pair list of " + std::to_string(total) + " entries does not fit on the device");
+      }
+      d.list_cap = cap;
+    }
+    a.list = d.list;
+    a.list_cap = d.list_cap;
+    nb_list(a, true, stream);
+    nb_copy_hold(n, d.xq, d.xhold, stream);
+    CK(cudaGetLastError());
+    // atoms of one system stay contiguous after the sort (bins of system s precede
+    // those of s+1), so the ranges follow from the per-system atom counts
+    if (batch_offsets.size() == hsys.size() + 1) {
+      for (size_t s = 0; s < hsys.size(); s++) {
+        hsys[s].atom_begin = batch_offsets[s];
+        hsys[s].atom_end = batch_offsets[s + 1];
+      }
+    } else {
+      hsys[0].atom_begin = 0;
+      hsys[0].atom_end = n;
+    }
+    CK(cudaMemcpyAsync(d.sys, hsys.data(), sizeof(SysDesc) * hsys.size(), cudaMemcpyHostToDevice, stream));
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemsetAsync(d.maxdisp, 0, sizeof(unsigned long long), stream));
+    cudaEventRecord(e1, stream);
+    CK(cudaStreamSynchronize(stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ms_build = ms;
+    if (ktiming) {
+      kms[5] += ms;
+      klaunch[5]++;
+    }
+    list_total = total;
+    if (st) return status_error(st);
+    built = true;
+    forces_valid = false;
+    rebuilds++;
+    return LMFF_OK;
+  }
+
+  void hilo_all() { nb_hilo(n, d.xq, d.sys, d.sysid, d.xh, d.xl, stream); }
+
+  int status_error(int st) {
+    CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
+    if (st & ST_TOO_MANY_ILP)
+      return fail(LMFF_ETOO_MANY_ILP_NEIGH,
+                  "There are too many neighbors for some atoms, please check your configuration");
+    if (st & ST_ZERO_NORMAL) return fail(LMFF_EZERO_NORMAL, "The magnitude of the normal vector is zero");
+    if (st & ST_TERS_OVERFLOW) return fail(LMFF_EOVERFLOW, "more than 12 Tersoff neighbours within cutmax for an atom");
+    if (st & ST_SHORT_OVERFLOW) return fail(LMFF_EOVERFLOW, "more than 64 short-range candidates for an atom");
+    if (st & ST_LIST_OVERFLOW) return fail(LMFF_EOVERFLOW, "Neighbor list overflow");
+    return fail(LMFF_ECUDA, "kernel status " + std::to_string(st));
+  }
+
+  // rebuild when any atom moved more than skin/2 since the last build
+  int maybe_rebuild() {
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, d.maxdisp, sizeof bits, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    double d2;
+    memcpy(&d2, &bits, sizeof d2);
+    if (!built || d2 > 0.25 * skin * skin) return rebuild();
+    return LMFF_OK;
+  }
+
+  // ---------------------------------------------------------------- forces
+  template <class R>
+  ForceArgs<R> args() {
+    ForceArgs<R> a;
+    memset(&a, 0, sizeof a);
+    a.A.xq = d.xq;
+    a.A.xh = d.xh;
+    a.A.xl = d.xl;
+    a.A.sys = d.sys;
+    a.A.sysid = d.sysid;
+    a.lc = lc;
+    a.n = n;
+    a.tag = d.tag;
+    a.list_off = d.list_off;
+    a.list = d.list;
+    a.short_cnt = d.short_cnt;
+    a.short_nb = d.short_nb;
+    a.ilp_cnt = d.ilp_cnt;
+    a.ilp_nb = d.ilp_nb;
+    a.ters_cnt = d.ters_cnt;
+    a.ters_nb = d.ters_nb;
+    a.nrm64 = d.nrm64;
+    a.nrm32 = d.nrm32;
+    a.ters_g = d.ters_g;
+    a.ters_f = d.ters_f;
+    a.ilp_f = d.ilp_f;
+    a.ilp_c = d.ilp_c;
+    a.ilp_g = d.ilp_g;
+    a.stat_ilp = stat_ilp;
+    a.stat_ters = stat_ters;
+    a.eatom_ilp = eatom_ilp;
+    a.eatom_ters = eatom_ters;
+    a.f_out = d.f;
+    a.status = d.status;
+    return a;
+  }
+
+  template <class R, class NS_SHORT, class NS_TERS, class NS_ILP, class NS_ND, class NS_FIN>
+  void run_kernels(ForceArgs<R> a, int which, bool ev, bool eatom, NS_SHORT fs, NS_TERS ft, NS_ILP fi, NS_ND fn,
+                   NS_FIN ff) {
+    a.do_ters = t_on && (which & LMFF_TERSOFF);
+    a.do_ilp = i_on && (which & LMFF_ILP);
+    timed(2, [&] { fs(a, d_cutILPsq, ht.cutmax * ht.cutmax, stream); });
+    if (a.do_ters) timed(1, [&] { ft(a, ev, eatom, stream); });
+    else if (ev) cudaMemsetAsync(stat_ters, 0, sizeof(double) * 8 * (size_t)n, stream);
+    if (a.do_ilp) {
+      timed(0, [&] { fi(a, ev, eatom, tpa, block, stream); });
+      timed(2, [&] { fn(a, ev, stream); });
+    }
+    else if (ev) cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)n, stream);
+    if (eatom && !a.do_ters) cudaMemsetAsync(eatom_ters, 0, sizeof(double) * (size_t)n, stream);
+    timed(3, [&] { ff(a, eatom, stream); });
+  }
+
+  // forces (+ energies/virials per system into hres when ev) on the resident state
+  int forces(int which, bool ev, bool eatom, std::vector<lmff_result> *hres) {
+    int rc = push_consts();
+    if (rc) return rc;
+    if (!built) {
+      rc = rebuild();
+      if (rc) return rc;
+    }
+    if (eatom) ev = true;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, stream);
+    if (n > 0) {
+      if (precision == LMFF_FP64) {
+        run_kernels(args<double>(), which, ev, eatom, f64::launch_short, f64::launch_tersoff, f64::launch_ilp,
+                    f64::launch_nderiv, f64::launch_finish);
+      } else {
+        if (!hilo_fresh) hilo_all();
+        run_kernels(args<float>(), which, ev, eatom, f32::launch_short, f32::launch_tersoff, f32::launch_ilp,
+                    f32::launch_nderiv, f32::launch_finish);
+      }
+      CK(cudaGetLastError());
+      if (ev) {
+        k_reduce<<<(int)hsys.size() * 16, 256, 0, stream>>>(n, 16, (const double *const *)d_arrs, d.sys, d.red_out);
+        CK(cudaGetLastError());
+      }
+    }
+    cudaEventRecord(e1, stream);
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    std::vector<double> red;
+    if (ev && n > 0) {
+      red.resize(hsys.size() * 16);
+      CK(cudaMemcpyAsync(red.data(), d.red_out, sizeof(double) * red.size(), cudaMemcpyDeviceToHost, stream));
+    }
+    CK(cudaStreamSynchronize(stream));
+    harvest();
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ms_forces = ms;
+    if (st) return status_error(st);
+    forces_valid = true;
+    if (hres) {
+      hres->assign(hsys.size(), lmff_result());
+      for (size_t s = 0; s < hsys.size(); s++) {
+        lmff_result &r = (*hres)[s];
+        memset(&r, 0, sizeof r);
+        if (!ev || n == 0) continue;
+        const double *q = &red[s * 16];
+        r.pvector[0] = q[0];
+        r.pvector[1] = q[1];
+        r.e_ilp = q[0] + q[1];
+        for (int k = 0; k < 6; k++) r.virial_ilp[k] = q[2 + k];
+        r.e_tersoff = q[8];
+        for (int k = 0; k < 6; k++) r.virial_tersoff[k] = q[10 + k];
+      }
+    }
+    return LMFF_OK;
+  }
+  bool hilo_fresh = false;
+
+  // ---------------------------------------------------------------- API paths
+  int set_single_box() {
+    if (!have_box) return fail(LMFF_EINVAL, "lmff_set_box must be called first");
+    std::vector<std::array<double, 9>> boxes(1);
+    for (int k = 0; k < 3; k++) {
+      boxes[0][k] = blo[k];
+      boxes[0][3 + k] = bhi[k];
+      boxes[0][6 + k] = bper[k];
+    }
+    int rc = make_sys(hsys, boxes);
+    if (rc) return rc;
+    return upload_sys();
+  }
+
+  int check_mol(int nn, const int64_t *mol, const int *type) {
+    for (int p = 0; p < nn; p++) {
+      if (mol && (mol[p] < 0 || mol[p] >= (1LL << 23)))
+        return fail(LMFF_EUNSUPPORTED, "molecule ids must lie in [0, 2^23)");
+      if (type[p] < 1 || type[p] > ntypes) return fail(LMFF_EINVAL, "atom type out of range");
+    }
+    return LMFF_OK;
+  }
+
+  // stage caller host arrays; returns whether the identity must be (re)loaded
+  int stage_host(int nn, const double *x, const int *type, const int64_t *mol, const int64_t *tag, bool same_atoms,
+                 bool &reload) {
+    int rc = ensure_atoms(nn);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(d_xin, x, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, stream));
+    reload = !loaded || nn != n || !built;
+    if (!same_atoms || reload) {
+      rc = check_mol(nn, mol, type);
+      if (rc) return rc;
+      CK(cudaMemcpyAsync(d_tin, type, sizeof(int) * nn, cudaMemcpyHostToDevice, stream));
+      if (mol) CK(cudaMemcpyAsync(d_min, mol, sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
+      else CK(cudaMemsetAsync(d_min, 0, sizeof(int64_t) * nn, stream));
+      if (tag) CK(cudaMemcpyAsync(d_gin, tag, sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
+      if (!reload && nn > 0) {
+        CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
+        k_check_ident<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, d_tin, d_min, tag ? d_gin : nullptr, d.xq, d.tag,
+                                                            d.status);
+        int flag = 0;
+        CK(cudaMemcpyAsync(&flag, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
+        CK(cudaStreamSynchronize(stream));
+        if (flag) reload = true;
+      }
+      if (!tag && reload) {
+        // default tags 1..n
+        std::vector<int64_t> t(nn);
+        for (int p = 0; p < nn; p++) t[p] = p + 1;
+        CK(cudaMemcpyAsync(d_gin, t.data(), sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
+      }
+    }
+    return LMFF_OK;
+  }
+
+  int apply_positions(int nn, bool reload) {
+    if (reload) {
+      if (!mass_type.empty()) {
+        if (!d_massT) CK(cudaMalloc(&d_massT, sizeof(double) * (MAXTYPE + 1)));
+        CK(cudaMemcpyAsync(d_massT, mass_type.data(), sizeof(double) * mass_type.size(), cudaMemcpyHostToDevice, stream));
+      }
+      batch_offsets.clear();
+      int rc = set_single_box();
+      if (rc) return rc;
+      return load_from_staging(nn, false, false);
+    }
+    if (nn > 0) {
+      k_update_x<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, d_xin, d.xq, d.xhold, d.maxdisp);
+      CK(cudaGetLastError());
+    }
+    hilo_fresh = false;
+    if (precision == LMFF_MIXED) {
+      hilo_all();
+      hilo_fresh = true;
+    }
+    return maybe_rebuild();
+  }
+
+  int compute_host(int nn, const double *x, const int *type, const int64_t *mol, const int64_t *tag, int which,
+                   int eflag, int vflag, double *f, double *eatom, lmff_result *res) {
+    bool reload = false;
+    int rc = stage_host(nn, x, type, mol, tag, (which & LMFF_SAME_ATOMS) != 0, reload);
+    if (rc) return rc;
+    rc = apply_positions(nn, reload);
+    if (rc) return rc;
+    std::vector<lmff_result> hr;
+    bool ev = eflag || vflag || eatom;
+    rc = forces(which, ev, eatom != nullptr, &hr);
+    if (rc) return rc;
+    if (res) *res = hr.empty() ? lmff_result() : hr[0];
+    bool overwrite = (which & LMFF_OVERWRITE) != 0;
+    if (nn > 0 && f) {
+      if (!overwrite) CK(cudaMemcpyAsync(d_fin, f, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, stream));
+      k_scatter_add<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, d.f, d_fin, overwrite);
+      CK(cudaMemcpyAsync(f, d_fin, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost, stream));
+    }
+    if (nn > 0 && eatom) {
+      if (!overwrite) CK(cudaMemcpyAsync(d_ein, eatom, sizeof(double) * nn, cudaMemcpyHostToDevice, stream));
+      k_scatter_add1<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, eatom_ters, d_ein, overwrite);
+      CK(cudaMemcpyAsync(eatom, d_ein, sizeof(double) * nn, cudaMemcpyDeviceToHost, stream));
+    }
+    CK(cudaStreamSynchronize(stream));
+    return LMFF_OK;
+  }
+
+  int compute_device(int nn, const double *dx, const int *dtype, const int64_t *dmol, const int64_t *dtag, int which,
+                     int eflag, int vflag, double *df, lmff_result *res) {
+    int rc = ensure_atoms(nn);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(d_xin, dx, sizeof(double) * 3 * nn, cudaMemcpyDeviceToDevice, stream));
+    bool reload = !loaded || nn != n || !built;
+    if (!(which & LMFF_SAME_ATOMS) || reload) {
+      CK(cudaMemcpyAsync(d_tin, dtype, sizeof(int) * nn, cudaMemcpyDeviceToDevice, stream));
+      if (dmol) CK(cudaMemcpyAsync(d_min, dmol, sizeof(int64_t) * nn, cudaMemcpyDeviceToDevice, stream));
+      else CK(cudaMemsetAsync(d_min, 0, sizeof(int64_t) * nn, stream));
+      if (dtag) CK(cudaMemcpyAsync(d_gin, dtag, sizeof(int64_t) * nn, cudaMemcpyDeviceToDevice, stream));
+      else {
+        std::vector<int64_t> t(nn);
+        for (int p = 0; p < nn; p++) t[p] = p + 1;
+        CK(cudaMemcpyAsync(d_gin, t.data(), sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
+      }
+      if (!reload && nn > 0) {
+        k_check_ident<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, d_tin, d_min, d_gin, d.xq, d.tag, d.status);
+        int flag = 0;
+        CK(cudaMemcpyAsync(&flag, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
+        CK(cudaStreamSynchronize(stream));
+        if (flag) reload = true;
+      }
+    }
+    rc = apply_positions(nn, reload);
+    if (rc) return rc;
+    std::vector<lmff_result> hr;
+    rc = forces(which, eflag || vflag, false, &hr);
+    if (rc) return rc;
+    if (res) *res = hr.empty() ? lmff_result() : hr[0];
+    if (nn > 0 && df) {
+      k_scatter_add<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, d.f, df, (which & LMFF_OVERWRITE) != 0);
+      CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(stream));
+    return LMFF_OK;
+  }
+
+  int upload(int nn, const double *x, const double *v, const int *type, const int64_t *mol, const int64_t *tag,
+             const double *mass) {
+    int rc = ensure_atoms(nn);
+    if (rc) return rc;
+    rc = check_mol(nn, mol, type);
+    if (rc) return rc;
+    mass_type.assign(MAXTYPE + 1, 1.0);
+    if (mass)
+      for (int t = 0; t < ntypes; t++) mass_type[t] = mass[t];
+    if (!d_massT) CK(cudaMalloc(&d_massT, sizeof(double) * (MAXTYPE + 1)));
+    CK(cudaMemcpyAsync(d_massT, mass_type.data(), sizeof(double) * (MAXTYPE + 1), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_xin, x, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, stream));
+    if (v) CK(cudaMemcpyAsync(d_vin, v, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_tin, type, sizeof(int) * nn, cudaMemcpyHostToDevice, stream));
+    if (mol) CK(cudaMemcpyAsync(d_min, mol, sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
+    else CK(cudaMemsetAsync(d_min, 0, sizeof(int64_t) * nn, stream));
+    std::vector<int64_t> t;
+    if (!tag) {
+      t.resize(nn);
+      for (int p = 0; p < nn; p++) t[p] = p + 1;
+      tag = t.data();
+    }
+    CK(cudaMemcpyAsync(d_gin, tag, sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    batch_offsets.clear();
+    rc = set_single_box();
+    if (rc) return rc;
+    return load_from_staging(nn, v != nullptr, false);
+  }
+
+  int run_nve(int nsteps, double dt, int thermo_every, lmff_thermo *thermo) {
+    if (!loaded) return fail(LMFF_EINVAL, "no resident system: call lmff_upload first");
+    double dtf = 0.5 * dt * FTM2V, dtv = dt;
+    int rc;
+    std::vector<lmff_result> hr;
+    int nth = 0;
+    auto sample = [&](int64_t step, const std::vector<lmff_result> &r) -> int {
+      double kes = 0.0;
+      if (n > 0) {
+        k_reduce<<<1, 256, 0, stream>>>(n, 1, (const double *const *)d_karrs, d.sys, d_kout);
+        CK(cudaMemcpyAsync(&kes, d_kout, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+      }
+      if (thermo) {
+        lmff_thermo &t = thermo[nth];
+        memset(&t, 0, sizeof t);
+        t.step = step;
+        t.ke = kes;
+        t.pe = r.empty() ? 0.0 : r[0].e_tersoff + r[0].e_ilp;
+        t.etotal = t.pe + t.ke;
+        int dof = 3 * n - 3;
+        t.temp = dof > 0 ? 2.0 * kes / (dof * BOLTZ) : 0.0;
+        if (!r.empty())
+          for (int k = 0; k < 6; k++) t.virial[k] = r[0].virial_tersoff[k] + r[0].virial_ilp[k];
+      }
+      nth++;
+      return LMFF_OK;
+    };
+    if (!forces_valid) {
+      rc = forces(LMFF_TERSOFF | LMFF_ILP, thermo_every > 0, false, &hr);
+      if (rc) return rc;
+      if (thermo_every > 0) {
+        k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, 0.0, ke);
+        rc = sample(steps, hr);
+        if (rc) return rc;
+      }
+    } else if (thermo_every > 0) {
+      rc = forces(LMFF_TERSOFF | LMFF_ILP, true, false, &hr);
+      if (rc) return rc;
+      k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, 0.0, ke);
+      rc = sample(steps, hr);
+      if (rc) return rc;
+    }
+    cudaEvent_t r0, r1;
+    cudaEventCreate(&r0);
+    cudaEventCreate(&r1);
+    cudaEventRecord(r0, stream);
+    for (int s = 1; s <= nsteps; s++) {
+      bool mixed = precision == LMFF_MIXED;
+      timed(4, [&] {
+        k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, d.mass, dtf, dtv, d.xhold, d.maxdisp, d.sys,
+                                                    d.sysid, d.xh, d.xl, mixed ? 1 : 0);
+      });
+      CK(cudaGetLastError());
+      hilo_fresh = mixed;
+      rc = maybe_rebuild();
+      if (rc) return rc;
+      bool th = thermo_every > 0 && (s % thermo_every == 0);
+      rc = forces(LMFF_TERSOFF | LMFF_ILP, th, false, th ? &hr : nullptr);
+      if (rc) return rc;
+      timed(4, [&] { k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, dtf, th ? ke : nullptr); });
+      CK(cudaGetLastError());
+      steps++;
+      if (th) {
+        rc = sample(steps, hr);
+        if (rc) return rc;
+      }
+    }
+    cudaEventRecord(r1, stream);
+    CK(cudaStreamSynchronize(stream));
+    harvest();
+    float ms = 0;
+    cudaEventElapsedTime(&ms, r0, r1);
+    cudaEventDestroy(r0);
+    cudaEventDestroy(r1);
+    ms_run = ms;
+    return LMFF_OK;
+  }
+
+  int count_pairs() {
+    if (!built || n == 0) {
+      pairs_in_cut = 0;
+      return LMFF_OK;
+    }
+    unsigned long long *dc = nullptr;
+    CK(cudaMalloc(&dc, sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(dc, 0, sizeof(unsigned long long), stream));
+    k_count_pairs<<<(n + 127) / 128, 128, 0, stream>>>(n, d.xq, d.sys, d.sysid, d.list_off, d.list, lc,
+                                                       cut_global * cut_global, dc);
+    unsigned long long h = 0;
+    CK(cudaMemcpyAsync(&h, dc, sizeof h, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    cudaFree(dc);
+    pairs_in_cut = (int64_t)h;
+    return LMFF_OK;
+  }
+
+  int download(double *x, double *v, double *f) {
+    if (!loaded) return fail(LMFF_EINVAL, "no resident system");
+    if (n == 0) return LMFF_OK;
+    double *xo = d_xin, *vo = d_vin, *fo = d_fin;
+    k_unpermute_state<<<(n + 255) / 256, 256, 0, stream>>>(n, d.perm, d.xq, d.v, d.f, xo, vo, fo);
+    CK(cudaGetLastError());
+    if (x) CK(cudaMemcpyAsync(x, xo, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, stream));
+    if (v) CK(cudaMemcpyAsync(v, vo, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, stream));
+    if (f) CK(cudaMemcpyAsync(f, fo, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    return LMFF_OK;
+  }
+
+  // ---------------------------------------------------------------- batch
+  std::vector<int> batch_offsets;
+
+  int batch_set(int nsys, const lmff_system_desc *sys) {
+    if (nsys < 1) return fail(LMFF_EINVAL, "empty batch");
+    std::vector<std::array<double, 9>> boxes(nsys);
+    int64_t total = 0;
+    batch_offsets.assign(nsys + 1, 0);
+    for (int s = 0; s < nsys; s++) {
+      for (int k = 0; k < 3; k++) {
+        boxes[s][k] = sys[s].lo[k];
+        boxes[s][3 + k] = sys[s].hi[k];
+        boxes[s][6 + k] = sys[s].periodic[k];
+      }
+      batch_offsets[s] = (int)total;
+      total += sys[s].natoms;
+    }
+    batch_offsets[nsys] = (int)total;
+    if (total > (1LL << 30)) return fail(LMFF_EINVAL, "batch too large");
+    int nn = (int)total;
+    int rc = make_sys(hsys, boxes);
+    if (rc) return rc;
+    rc = upload_sys();
+    if (rc) return rc;
+    rc = ensure_atoms(nn);
+    if (rc) return rc;
+    std::vector<double> x(3 * (size_t)nn);
+    std::vector<int> t(nn), sid(nn);
+    std::vector<int64_t> m(nn), g(nn);
+    for (int s = 0; s < nsys; s++) {
+      int o = batch_offsets[s];
+      rc = check_mol(sys[s].natoms, sys[s].mol, sys[s].type);
+      if (rc) return rc;
+      memcpy(&x[3 * (size_t)o], sys[s].x, sizeof(double) * 3 * sys[s].natoms);
+      for (int p = 0; p < sys[s].natoms; p++) {
+        t[o + p] = sys[s].type[p];
+        m[o + p] = sys[s].mol ? sys[s].mol[p] : 0;
+        g[o + p] = p + 1;
+        sid[o + p] = s;
+      }
+    }
+    CK(cudaMemcpyAsync(d_xin, x.data(), sizeof(double) * x.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_tin, t.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_min, m.data(), sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_gin, g.data(), sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_sysin, sid.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    return load_from_staging(nn, false, true);
+  }
+
+  int batch_compute(double *f_out, lmff_result *res) {
+    if (!loaded) return fail(LMFF_EINVAL, "no batch loaded");
+    std::vector<lmff_result> hr;
+    int rc = forces(LMFF_TERSOFF | LMFF_ILP, true, false, &hr);
+    if (rc) return rc;
+    for (size_t s = 0; s < hr.size() && res; s++) res[s] = hr[s];
+    if (f_out && n > 0) {
+      k_scatter_add<<<(n + 255) / 256, 256, 0, stream>>>(n, d.perm, d.f, d_fin, 1);
+      CK(cudaMemcpyAsync(f_out, d_fin, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, stream));
+    }
+    CK(cudaStreamSynchronize(stream));
+    return LMFF_OK;
+  }
+
+  // ---------------------------------------------------------------- lists export
+  int64_t export_list(int which, int64_t *out, int64_t cap) {
+    if (!built) return fail(LMFF_EINVAL, "no neighbour list built");
+    std::vector<int64_t> tag(n);
+    std::vector<int> perm(n);
+    cudaMemcpyAsync(tag.data(), d.tag, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, stream);
+    std::vector<int64_t> off(n + 1);
+    std::vector<uint32_t> ent;
+    std::vector<int> cnt;
+    if (which == 0) {
+      cudaMemcpyAsync(off.data(), d.list_off, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, stream);
+      cudaStreamSynchronize(stream);
+      ent.resize(off[n]);
+      cudaMemcpyAsync(ent.data(), d.list, sizeof(uint32_t) * off[n], cudaMemcpyDeviceToHost, stream);
+    } else {
+      cnt.resize(n);
+      ent.resize((size_t)n * MAXILP);
+      cudaMemcpyAsync(cnt.data(), d.ilp_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost, stream);
+      cudaMemcpyAsync(ent.data(), d.ilp_nb, sizeof(uint32_t) * n * MAXILP, cudaMemcpyDeviceToHost, stream);
+    }
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return fail(LMFF_ECUDA, "list export failed");
+    int64_t m = 0;
+    for (int i = 0; i < n; i++) {
+      int64_t b = which == 0 ? off[i] : (int64_t)i * MAXILP;
+      int64_t e = which == 0 ? off[i + 1] : b + cnt[i];
+      for (int64_t k = b; k < e; k++) {
+        int j, sx, sy, sz;
+        decode_entry(ent[k], lc, j, sx, sy, sz);
+        if (out && m < cap) {
+          out[3 * m] = tag[i];
+          out[3 * m + 1] = tag[j];
+          out[3 * m + 2] = ((int64_t)((sx + 8) & 15)) | ((int64_t)((sy + 8) & 15) << 4) | ((int64_t)((sz + 8) & 15) << 8);
+        }
+        m++;
+      }
+    }
+    return m;
+  }
+};
+
+}  // namespace lmff
+
+using lmff::Engine;
+
+// ====================================================================== C ABI
+
+struct lmff_engine {
+  Engine e;
+};
+
+static thread_local std::string g_create_error;
+
+extern "C" {
+
+int lmff_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+  return n;
+}
+
+int lmff_create(lmff_engine **out, const lmff_params *p, int device) {
+  if (!out) return LMFF_EINVAL;
+  *out = nullptr;
+  lmff_engine *h = new (std::nothrow) lmff_engine;
+  if (!h) return LMFF_ENOMEM;
+  int rc = h->e.set_params(p);
+  if (rc == LMFF_OK) rc = h->e.init_device(device);
+  if (rc != LMFF_OK) {
+    g_create_error = h->e.err;
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return LMFF_OK;
+}
+
+int lmff_create_from_files(lmff_engine **out, const char *tersoff_file, const char *ilp_file, int ntypes,
+                           const char *const *elements, double cut_global, int tap_flag, double skin, int device) {
+  if (!out || !elements || ntypes < 1 || ntypes > lmff::MAXTYPE) return LMFF_EINVAL;
+  *out = nullptr;
+  lmff::HostTersoff ht;
+  lmff::HostIlp hi;
+  std::string err;
+  if (tersoff_file && !lmff::parse_tersoff(tersoff_file, ntypes, elements, ht, err)) {
+    g_create_error = err;
+    return LMFF_EBADPARAM;
+  }
+  if (ilp_file && !lmff::parse_ilp(ilp_file, ntypes, elements, hi, err)) {
+    g_create_error = err;
+    return LMFF_EBADPARAM;
+  }
+  lmff_params p;
+  memset(&p, 0, sizeof p);
+  p.ntypes = ntypes;
+  if (tersoff_file) {
+    p.tersoff_nelements = (int)ht.elements.size();
+    p.tersoff_nparams = (int)ht.params.size();
+    p.tersoff_params = ht.params.data();
+    p.tersoff_elem2param = ht.elem2param.data();
+    p.tersoff_map = ht.map.data();
+    p.tersoff_cutmax = ht.cutmax;
+  }
+  if (ilp_file) {
+    p.ilp_nelements = (int)hi.elements.size();
+    p.ilp_nparams = (int)hi.params.size();
+    p.ilp_params = hi.params.data();
+    p.ilp_elem2param = hi.elem2param.data();
+    p.ilp_map = hi.map.data();
+    p.ilp_cutILPsq = hi.cutILPsq.data();
+  }
+  p.ilp_cut_global = cut_global;
+  p.ilp_tap_flag = tap_flag;
+  p.skin = skin;
+  return lmff_create(out, &p, device);
+}
+
+void lmff_destroy(lmff_engine *e) { delete e; }
+
+int lmff_set_precision(lmff_engine *e, int mode) {
+  if (!e || (mode != LMFF_FP64 && mode != LMFF_MIXED)) return LMFF_EINVAL;
+  e->e.precision = mode;
+  e->e.hilo_fresh = false;
+  return LMFF_OK;
+}
+
+int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double xy, double xz, double yz,
+                 const int periodic[3]) {
+  if (!e || !lo || !hi || !periodic) return LMFF_EINVAL;
+  if (xy != 0.0 || xz != 0.0 || yz != 0.0) return e->e.fail(LMFF_EUNSUPPORTED, "triclinic boxes are not supported");
+  bool changed = false;
+  for (int k = 0; k < 3; k++) {
+    if (!(hi[k] > lo[k])) return e->e.fail(LMFF_EINVAL, "box hi must exceed lo");
+    changed |= e->e.blo[k] != lo[k] || e->e.bhi[k] != hi[k] || e->e.bper[k] != (periodic[k] != 0);
+    e->e.blo[k] = lo[k];
+    e->e.bhi[k] = hi[k];
+    e->e.bper[k] = periodic[k] != 0;
+  }
+  e->e.have_box = true;
+  if (changed) {
+    e->e.built = false;
+    e->e.loaded = false;
+  }
+  return LMFF_OK;
+}
+
+int lmff_set_option(lmff_engine *e, const char *key, double value) {
+  if (!e || !key) return LMFF_EINVAL;
+  std::string k(key);
+  if (k == "tpa") {
+    int v = (int)value;
+    if (v != 4 && v != 8 && v != 16 && v != 32) return e->e.fail(LMFF_EINVAL, "tpa must be 4, 8, 16 or 32");
+    e->e.tpa = v;
+  } else if (k == "block") {
+    int v = (int)value;
+    if (v < 32 || v > 256 || (v & 31)) return e->e.fail(LMFF_EINVAL, "block must be a multiple of 32 in 32..256");
+    e->e.block = v;
+  } else if (k == "list_full") {
+    e->e.list_full = value != 0.0;
+    e->e.built = false;
+  } else if (k == "skin") {
+    if (!(value >= 0.0)) return e->e.fail(LMFF_EINVAL, "skin must be >= 0");
+    e->e.skin = value;
+    e->e.build_consts();
+    e->e.loaded = false;
+  } else if (k == "kernel_timing") {
+    e->e.ktiming = value != 0.0;
+  } else if (k == "reset_timing") {
+    for (int q = 0; q < 6; q++) {
+      e->e.kms[q] = 0.0;
+      e->e.klaunch[q] = 0;
+    }
+  } else if (k == "count_pairs") {
+    cudaSetDevice(e->e.device);
+    return e->e.count_pairs();
+  } else {
+    return e->e.fail(LMFF_EINVAL, "unknown option " + k);
+  }
+  return LMFF_OK;
+}
+
+int lmff_compute(lmff_engine *e, int natoms, const double *x, const int *type, const int64_t *mol, const int64_t *tag,
+                 int which, int eflag, int vflag, double *f, double *eatom, lmff_result *res) {
+  if (!e || natoms < 0 || (natoms > 0 && (!x || !type))) return LMFF_EINVAL;
+  cudaSetDevice(e->e.device);
+  return e->e.compute_host(natoms, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
+}
+
+int lmff_compute_device(lmff_engine *e, int natoms, const double *d_x, const int *d_type, const int64_t *d_mol,
+                        const int64_t *d_tag, int which, int eflag, int vflag, double *d_f, lmff_result *res) {
+  if (!e || natoms < 0 || (natoms > 0 && (!d_x || !d_type))) return LMFF_EINVAL;
+  cudaSetDevice(e->e.device);
+  return e->e.compute_device(natoms, d_x, d_type, d_mol, d_tag, which, eflag, vflag, d_f, res);
+}
+
+int lmff_upload(lmff_engine *e, int natoms, const double *x, const double *v, const int *type, const int64_t *mol,
+                const int64_t *tag, const double *mass) {
+  if (!e || natoms < 0 || (natoms > 0 && (!x || !type))) return LMFF_EINVAL;
+  cudaSetDevice(e->e.device);
+  return e->e.upload(natoms, x, v, type, mol, tag, mass);
+}
+
+int lmff_compute_resident(lmff_engine *e, int which, int eflag, int vflag, lmff_result *res) {
+  if (!e) return LMFF_EINVAL;
+  if (!e->e.loaded) return e->e.fail(LMFF_EINVAL, "no resident system");
+  cudaSetDevice(e->e.device);
+  int rc = e->e.maybe_rebuild();
+  if (rc) return rc;
+  std::vector<lmff_result> hr;
+  rc = e->e.forces(which, eflag || vflag, false, &hr);
+  if (rc) return rc;
+  if (res) *res = hr.empty() ? lmff_result() : hr[0];
+  return LMFF_OK;
+}
+
+int lmff_run_nve(lmff_engine *e, int nsteps, double dt, int thermo_every, lmff_thermo *thermo) {
+  if (!e || nsteps < 0 || thermo_every < 0) return LMFF_EINVAL;
+  cudaSetDevice(e->e.device);
+  return e->e.run_nve(nsteps, dt, thermo_every, thermo);
+}
+
+int lmff_download(lmff_engine *e, double *x, double *v, double *f) {
+  if (!e) return LMFF_EINVAL;
+  cudaSetDevice(e->e.device);
+  return e->e.download(x, v, f);
+}
+
+int lmff_batch_set(lmff_engine *e, int nsys, const lmff_system_desc *sys) {
+  if (!e || !sys) return LMFF_EINVAL;
+  cudaSetDevice(e->e.device);
+  return e->e.batch_set(nsys, sys);
+}
+
+int lmff_batch_compute(lmff_engine *e, double *f_out, lmff_result *res) {
+  if (!e) return LMFF_EINVAL;
+  cudaSetDevice(e->e.device);
+  return e->e.batch_compute(f_out, res);
+}
+
+int lmff_get_stats(lmff_engine *e, lmff_stats *out) {
+  if (!e || !out) return LMFF_EINVAL;
+  memset(out, 0, sizeof *out);
+  Engine &g = e->e;
+  out->natoms = g.n;
+  out->list_entries = g.list_total;
+  out->list_capacity = g.d.list_cap;
+  out->rebuilds = g.rebuilds;
+  out->steps = g.steps;
+  out->list_per_atom = g.n ? (double)g.list_total / g.n : 0.0;
+  out->ms_last_build = g.ms_build;
+  out->ms_last_forces = g.ms_forces;
+  out->precision = g.precision;
+  out->tpa = g.tpa;
+  out->block = g.block;
+  out->ms_last_run = g.ms_run;
+  for (int q = 0; q < 6; q++) {
+    out->kernel_ms[q] = g.kms[q];
+    out->kernel_launches[q] = g.klaunch[q];
+  }
+  out->pairs_in_cutoff = g.pairs_in_cut;
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) out->bytes_device = (double)(tot - fr);
+  return LMFF_OK;
+}
+
+int64_t lmff_export_list(lmff_engine *e, int which, int64_t *out, int64_t cap) {
+  if (!e) return LMFF_EINVAL;
+  cudaSetDevice(e->e.device);
+  return e->e.export_list(which, out, cap);
+}
+
+const char *lmff_last_error(const lmff_engine *e) {
+  if (!e) return g_create_error.c_str();
+  return e->e.err.c_str();
+}
+
+const char *lmff_strerror(int code) {
+  switch (code) {
+    case LMFF_OK: return "success";
+    case LMFF_EINVAL: return "invalid argument";
+    case LMFF_ECUDA: return "CUDA error";
+    case LMFF_EOVERFLOW: return "neighbour list overflow";
+    case LMFF_ETOO_MANY_ILP_NEIGH: return "There are too many neighbors for some atoms, please check your configuration";
+    case LMFF_EZERO_NORMAL: return "The magnitude of the normal vector is zero";
+    case LMFF_EBADPARAM: return "potential file or parameter error";
+    case LMFF_ETIMEDOUT: return "device wait timed out";
+    case LMFF_EUNSUPPORTED: return "unsupported request";
+    case LMFF_ENOMEM: return "out of memory";
+    case LMFF_ENODEV: return "no CUDA device";
+    default: return "unknown error";
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,178 @@
+// Force kernels of the Tersoff + ILP engine, templated on the arithmetic type R
+// (double: all-FP64 drop-in; float: mixed precision, FP32 pair/three-body arithmetic on
+// displacements formed from double-float positions, FP64 per-atom accumulation,
+// reductions and normal-derivative assembly).
+//
+// Formulation: a deterministic gather, no force atomics.  Every owned atom sums every
+// force on itself:
+//   * ILP (pair_ilp_graphene_hbn.cpp:449-675): for each interlayer neighbour j the vdW
+//     force, the repulsion of the term that uses i's normal (calc_FRep with i as owner)
+//     and the repulsion of the term that uses j's normal (i plays calc_FRep's "j").
+//     The normal-derivative forces of the terms owned by i are reverse-accumulated: the
+//     pair loop sums g_i = sum_j Tap*prod*fpair1*del, then (dn_i/dx_m)^T g_i is applied
+//     once per intralayer neighbour m (the LMFF dprodni idea, LMFF/pair_lmff.cpp:916-1025).
+//     Those per-neighbour forces are left in ilp_c slots and gathered by their targets.
+//   * Tersoff (pair_tersoff.cpp:117-262): each atom evaluates the bonds it centres (zeta,
+//     force_zeta, attractive over k) and leaves the forces on its bond partners in
+//     ters_g slots; repulsion is evaluated from both ends.
+//   * k_finish gathers the slots of the neighbours (slot of a in N(j) found by matching
+//     the reversed image code), so every force sum has a fixed order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "engine.cuh"
+
+namespace lmff {
+
+// ------------------------------------------------------------------ precision policy
+
+template <class R>
+struct Math;
+
+template <>
+struct Math<double> {
+  static __device__ __forceinline__ double ex(double a) { return exp(a); }
+  // exp(-lambda (r - z0)) and friends in the reference's own form
+  static __device__ __forceinline__ double exp_rep0(const IlpP<double> &p, double r) { return exp(-p.lambda * (r - p.z0)); }
+  static __device__ __forceinline__ double exp_rep1(const IlpP<double> &p, double rhosq) { return exp(-(rhosq * p.delta2inv)); }
+  static __device__ __forceinline__ double exp_ts(const IlpP<double> &p, double r) { return exp(-p.d * (r / p.seff - 1.0)); }
+  static __device__ __forceinline__ double rcp(double a) { return 1.0 / a; }
+  static __device__ __forceinline__ double sqrt_(double a) { return sqrt(a); }
+  static __device__ __forceinline__ double pow_(double a, double b) { return pow(a, b); }
+  static __device__ __forceinline__ void sincospi_(double a, double *s, double *c) { sincospi(a, s, c); }
+};
+
+template <>
+struct Math<float> {
+  static __device__ __forceinline__ float ex(float a) { return expf(a); }
+  // lambda log2e (z0 - r): the constant's rounding scales a small argument instead of
+  // shifting every pair's exponent by the same absolute amount
+  static __device__ __forceinline__ float exp_rep0(const IlpP<float> &p, float r) { return exp2f(p.lam_l2e * (p.z0 - r)); }
+  static __device__ __forceinline__ float exp_rep1(const IlpP<float> &p, float rhosq) { return exp2f(p.nd2_l2e * rhosq); }
+  // exp(-d (r/seff - 1)) = exp2((d/seff) log2e (seff - r))
+  static __device__ __forceinline__ float exp_ts(const IlpP<float> &p, float r) { return exp2f(p.ts_a * (p.seff - r)); }
+  static __device__ __forceinline__ float rcp(float a) { return __fdividef(1.0f, a); }
+  static __device__ __forceinline__ float sqrt_(float a) { return sqrtf(a); }
+  static __device__ __forceinline__ float pow_(float a, float b) { return powf(a, b); }
+  static __device__ __forceinline__ void sincospi_(float a, float *s, float *c) { sincospif(a, s, c); }
+};
+
+// atom info packed next to the position: (mol_dense << 8) | type
+__device__ __forceinline__ int info_type(long long w) { return (int)(w & 255); }
+__device__ __forceinline__ long long info_mol(long long w) { return w >> 8; }
+
+// --------------------------------------------------------------- position access
+
+struct AtomArrays {
+  const d4 *xq;
+  const float4 *xh;
+  const float4 *xl;
+  const SysDesc *sys;
+  const int *sysid;
+};
+
+template <class R>
+struct AtomI;
+
+template <>
+struct AtomI<double> {
+  double x, y, z;
+  long long info;
+  __device__ __forceinline__ void load(const AtomArrays &A, int i) {
+    d4 q = A.xq[i];
+    x = q.x; y = q.y; z = q.z;
+    info = __double_as_longlong(q.w);
+  }
+  // del = x_i - (x_j + s L): the reference's delx = xtmp - x[j][0] on a ghost x[j] = x + prd
+  __device__ __forceinline__ void disp(const AtomArrays &A, const SysDesc &sd, int j, int sx, int sy, int sz,
+                                       double &dx, double &dy, double &dz, long long &jinfo) const {
+    d4 q = A.xq[j];
+    double xj = sx ? __dadd_rn(q.x, sx * sd.L[0]) : q.x;
+    double yj = sy ? __dadd_rn(q.y, sy * sd.L[1]) : q.y;
+    double zj = sz ? __dadd_rn(q.z, sz * sd.L[2]) : q.z;
+    dx = __dsub_rn(x, xj);
+    dy = __dsub_rn(y, yj);
+    dz = __dsub_rn(z, zj);
+    jinfo = __double_as_longlong(q.w);
+  }
+};
+
+template <>
+struct AtomI<float> {
+  float hx, hy, hz, lx, ly, lz;
+  long long info;
+  __device__ __forceinline__ void load(const AtomArrays &A, int i) {
+    float4 h = A.xh[i];
+    float4 l = A.xl[i];
+    hx = h.x; hy = h.y; hz = h.z;
+    lx = l.x; ly = l.y; lz = l.z;
+    info = (long long)__float_as_int(h.w);
+  }
+  // del = x_i - x_j(image) from double-float parts: the hi difference is exact (both
+  // hi parts share one binade), the lo parts carry the remaining 24 bits.
+  __device__ __forceinline__ void disp(const AtomArrays &A, const SysDesc &sd, int j, int sx, int sy, int sz,
+                                       float &dx, float &dy, float &dz, long long &jinfo) const {
+    float4 h = __ldg(&A.xh[j]);
+    float4 l = __ldg(&A.xl[j]);
+    float sxh = (float)sx * sd.Lhi[0], syh = (float)sy * sd.Lhi[1], szh = (float)sz * sd.Lhi[2];
+    float sxl = (float)sx * sd.Llo[0], syl = (float)sy * sd.Llo[1], szl = (float)sz * sd.Llo[2];
+    dx = ((hx - h.x) - sxh) + ((lx - l.x) - sxl);
+    dy = ((hy - h.y) - syh) + ((ly - l.y) - syl);
+    dz = ((hz - h.z) - szh) + ((lz - l.z) - szl);
+    jinfo = (long long)__float_as_int(h.w);
+  }
+};
+
+// exact FP64 squared distance in the reference's evaluation order (no contraction)
+__device__ __forceinline__ double rsq_rn(double dx, double dy, double dz) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// FP64 displacement x_i - x_j(image) used for set decisions and FP64 assembly
+__device__ __forceinline__ void disp64(const d4 *xq, const SysDesc &sd, int i, int j, int sx, int sy, int sz,
+                                       double &dx, double &dy, double &dz) {
+  d4 a = xq[i];
+  d4 b = xq[j];
+  double xj = sx ? __dadd_rn(b.x, sx * sd.L[0]) : b.x;
+  double yj = sy ? __dadd_rn(b.y, sy * sd.L[1]) : b.y;
+  double zj = sz ? __dadd_rn(b.z, sz * sd.L[2]) : b.z;
+  dx = __dsub_rn(a.x, xj);
+  dy = __dsub_rn(a.y, yj);
+  dz = __dsub_rn(a.z, zj);
+}
+
+// --------------------------------------------------------------- kernel arguments
+
+template <class R>
+struct ForceArgs {
+  AtomArrays A;
+  ListCode lc;
+  int n;
+  const int64_t *tag;
+  const int64_t *list_off;
+  const uint32_t *list;
+  const int *short_cnt;
+  const uint32_t *short_nb;
+  int *ilp_cnt;
+  uint32_t *ilp_nb;
+  int *ters_cnt;
+  uint32_t *ters_nb;
+  d4 *nrm64;
+  float4 *nrm32;
+  d4 *ters_g;
+  double *ters_f;
+  double *ilp_f;
+  d4 *ilp_c;
+  d4 *ilp_g;           // reverse-accumulated dE/dn_i of the terms owned by i (k_ilp -> k_nderiv)
+  double *stat_ilp;    // 8 * n SoA: e_vdw/2, e_rep/2, virial[6]    (EV only)
+  double *stat_ters;   // 8 * n SoA: e, 0, virial[6]
+  double *eatom_ilp;   // n (EATOM only)
+  double *eatom_ters;  // n
+  double *f_out;       // 3*n SoA (k_finish)
+  int *status;
+  int do_ters, do_ilp;
+};
+
+}  // namespace lmff

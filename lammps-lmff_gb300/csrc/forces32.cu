@@ -1,0 +1,5 @@
+// Mixed-precision instantiation of the force kernels (FP32 pair and three-body
+// arithmetic; FP64 accumulation, reductions and normal-derivative assembly).
+#define LMFF_REAL float
+#define LMFF_NS f32
+#include "forces_impl.cuh"

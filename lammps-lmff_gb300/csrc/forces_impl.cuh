@@ -1,0 +1,781 @@
+// Kernel bodies; included by forces64.cu (LMFF_REAL = double) and forces32.cu
+// (LMFF_REAL = float), each of which owns one __constant__ copy of the potential.
+#pragma once
+
+#include "forces.cuh"
+
+namespace lmff {
+namespace LMFF_NS {
+
+using R = LMFF_REAL;
+__constant__ PotConst<R> c_pot;
+
+__device__ __forceinline__ R cR(double v) { return (R)v; }
+
+__device__ __forceinline__ void raise_status(int *status, int bit) { atomicOr(status, bit); }
+
+// squared distance in R; for FP64 in the reference's rounding
+__device__ __forceinline__ R rsqR(R dx, R dy, R dz) {
+  if constexpr (sizeof(R) == 8) return rsq_rn(dx, dy, dz);
+  else return dx * dx + dy * dy + dz * dz;
+}
+
+// rsq < thr decided exactly as FP64 would (mixed: FP32 first, FP64 when within 1e-5)
+__device__ __forceinline__ bool lt_exact(R rsq, R thr, const d4 *xq, const SysDesc &sd, int i, int j, int sx,
+                                         int sy, int sz, double thr64) {
+  if constexpr (sizeof(R) == 8) {
+    return rsq < thr;
+  } else {
+    float m = 1e-5f * thr;
+    if (rsq < thr - m) return true;
+    if (rsq > thr + m) return false;
+    double dx, dy, dz;
+    disp64(xq, sd, i, j, sx, sy, sz, dx, dy, dz);
+    return rsq_rn(dx, dy, dz) < thr64;
+  }
+}
+
+// ============================================================== k_short ==========
+// Per atom: the current-step ILP intralayer list (ILP_neigh, pair_ilp_graphene_hbn.cpp:
+// 723-743: same molecule, rsq != 0, rsq < cutILPsq) and the Tersoff short list
+// (pair_tersoff.cpp:132-147: rsq < cutmax^2), both taken in candidate order from the
+// short candidate list built with skin; then the unit normal (calc_normal :776-1074).
+__global__ void k_short(ForceArgs<R> a, const double *cutILPsq64, double tcutmaxsq64) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const SysDesc &sd = a.A.sys[a.A.sysid[i]];
+  AtomI<R> ai;
+  ai.load(a.A, i);
+  int ti = info_type(ai.info);
+  long long mi = info_mol(ai.info);
+  int ie = c_pot.i_enabled ? c_pot.i_map[ti] : -1;
+  int te = c_pot.t_enabled ? c_pot.t_map[ti] : -1;
+  int nilp = 0, nters = 0;
+  R vx[MAXILP], vy[MAXILP], vz[MAXILP];
+  int cnt = a.short_cnt[i];
+  for (int c = 0; c < cnt; c++) {
+    uint32_t e = a.short_nb[(size_t)i * MAXSHORT + c];
+    int j, sx, sy, sz;
+    decode_entry(e, a.lc, j, sx, sy, sz);
+    R dx, dy, dz;
+    long long jinfo;
+    ai.disp(a.A, sd, j, sx, sy, sz, dx, dy, dz, jinfo);
+    R rsq = rsqR(dx, dy, dz);
+    int tj = info_type(jinfo);
+    if (ie >= 0 && info_mol(jinfo) == mi) {
+      int je = c_pot.i_map[tj];
+      if (je >= 0 && rsq != R(0)) {
+        int pe = ie * MAXELEM + je;
+        if (lt_exact(rsq, c_pot.i_cutILPsq[pe], a.A.xq, sd, i, j, sx, sy, sz, cutILPsq64[pe])) {
+          if (nilp < MAXILP) {
+            a.ilp_nb[(size_t)i * MAXILP + nilp] = e;
+            vx[nilp] = -dx; vy[nilp] = -dy; vz[nilp] = -dz;
+          }
+          nilp++;
+        }
+      }
+    }
+    if (te >= 0 && c_pot.t_map[tj] >= 0) {
+      if (lt_exact(rsq, c_pot.t_cutmaxsq, a.A.xq, sd, i, j, sx, sy, sz, tcutmaxsq64)) {
+        if (nters < MAXTERS) a.ters_nb[(size_t)i * MAXTERS + nters] = e;
+        nters++;
+      }
+    }
+  }
+  if (nilp > MAXILP) {
+    raise_status(a.status, ST_TOO_MANY_ILP);
+    nilp = MAXILP;
+  }
+  if (nters > MAXTERS) {
+    raise_status(a.status, ST_TERS_OVERFLOW);
+    nters = MAXTERS;
+  }
+  a.ilp_cnt[i] = nilp;
+  a.ters_cnt[i] = nters;
+  // unit normal
+  R nx = 0, ny = 0, nz = 1;
+  if (nilp >= 2) {
+    R n1x = vy[0] * vz[1] - vy[1] * vz[0];
+    R n1y = vz[0] * vx[1] - vz[1] * vx[0];
+    R n1z = vx[0] * vy[1] - vx[1] * vy[0];
+    if (nilp == 3) {
+      // (v1 x v2 + v3 x v1 + v2 x v3) / 3
+      n1x += vy[2] * vz[0] - vy[0] * vz[2];
+      n1y += vz[2] * vx[0] - vz[0] * vx[2];
+      n1z += vx[2] * vy[0] - vx[0] * vy[2];
+      n1x += vy[1] * vz[2] - vy[2] * vz[1];
+      n1y += vz[1] * vx[2] - vz[2] * vx[1];
+      n1z += vx[1] * vy[2] - vx[2] * vy[1];
+      n1x /= R(3); n1y /= R(3); n1z /= R(3);
+    }
+    R nn = Math<R>::sqrt_(n1x * n1x + n1y * n1y + n1z * n1z);
+    if (nn == R(0)) {
+      raise_status(a.status, ST_ZERO_NORMAL);
+    } else {
+      nx = n1x / nn; ny = n1y / nn; nz = n1z / nn;
+    }
+  }
+  if constexpr (sizeof(R) == 8) a.nrm64[i] = make_d4(nx, ny, nz, 0.0);
+  else a.nrm32[i] = make_float4(nx, ny, nz, 0.f);
+}
+
+// ============================================================ Tersoff math ========
+// pair_tersoff.cpp:663-734 and pair_tersoff.h:90-107, in R
+__device__ __forceinline__ void ters_fc_both(R r, const TersP<R> &p, R &fc, R &fcd) {
+  if (r < p.rlo) { fc = R(1); fcd = R(0); return; }
+  if (r > p.rhi) { fc = R(0); fcd = R(0); return; }
+  R s, c;
+  Math<R>::sincospi_(R(0.5) * (r - p.bigr) / p.bigd, &s, &c);
+  fc = R(0.5) * (R(1) - s);
+  fcd = -p.pi4_over_D * c;
+}
+
+__device__ __forceinline__ R ters_fc(R r, const TersP<R> &p) {
+  R fc, fcd;
+  ters_fc_both(r, p, fc, fcd);
+  return fc;
+}
+
+__device__ __forceinline__ R ters_gijk(R costheta, const TersP<R> &p) {
+  R hcth = p.h - costheta;
+  if constexpr (sizeof(R) == 8) {
+    return p.gamma * (R(1) + p.cd2 - p.c2 / (p.d2 + hcth * hcth));
+  } else {
+    // c^2/d^2 - c^2/(d^2 + u^2) = c^2 u^2 / (d^2 (d^2 + u^2)): the same value without the
+    // cancellation of two ~1e8 terms (BNC.tersoff carbon) that FP32 cannot afford
+    R u2 = hcth * hcth;
+    return p.gamma * (R(1) + p.c2 * u2 / (p.d2 * (p.d2 + u2)));
+  }
+}
+
+__device__ __forceinline__ R ters_gijk_d(R costheta, const TersP<R> &p) {
+  R hcth = p.h - costheta;
+  R numerator = R(-2) * p.c2 * hcth;
+  R den = R(1) / (p.d2 + hcth * hcth);
+  return p.gamma * numerator * den * den;
+}
+
+__device__ __forceinline__ R ters_exdelr(R rij, R rik, const TersP<R> &p) {
+  R arg = p.powermint == 3 ? (p.lam3 * (rij - rik)) * (p.lam3 * (rij - rik)) * (p.lam3 * (rij - rik))
+                           : p.lam3 * (rij - rik);
+  if (arg > R(69.0776)) return R(1.e30);
+  if (arg < R(-69.0776)) return R(0);
+  return Math<R>::ex(arg);
+}
+
+__device__ __forceinline__ R ters_bij(R zeta, const TersP<R> &p) {
+  R tmp = p.beta * zeta;
+  if (tmp > p.c1) return R(1) / Math<R>::sqrt_(tmp);
+  if (tmp > p.c2t) return (R(1) - Math<R>::pow_(tmp, -p.powern) * p.inv2n) / Math<R>::sqrt_(tmp);
+  if (tmp < p.c4) return R(1);
+  if (tmp < p.c3) return R(1) - Math<R>::pow_(tmp, p.powern) * p.inv2n;
+  return Math<R>::pow_(R(1) + Math<R>::pow_(tmp, p.powern), -p.inv2n);
+}
+
+__device__ __forceinline__ R ters_bij_d(R zeta, const TersP<R> &p) {
+  R tmp = p.beta * zeta;
+  if (tmp > p.c1) return p.beta * R(-0.5) * Math<R>::pow_(tmp, R(-1.5));
+  if (tmp > p.c2t)
+    return p.beta * (R(-0.5) * Math<R>::pow_(tmp, R(-1.5)) *
+                     (R(1) - (R(1) + p.inv2n) * Math<R>::pow_(tmp, -p.powern)));
+  if (tmp < p.c4) return R(0);
+  if (tmp < p.c3) return R(-0.5) * p.beta * Math<R>::pow_(tmp, p.powern - R(1));
+  R tmp_n = Math<R>::pow_(tmp, p.powern);
+  return R(-0.5) * Math<R>::pow_(R(1) + tmp_n, R(-1) - p.inv2n) * tmp_n / zeta;
+}
+
+// tag-parity half selection of a full list (pair_tersoff.cpp:150-158,
+// pair_ilp_graphene_hbn.cpp:488-496); with periodic images the coordinate tie-break of
+// equal tags compares the image shift lexicographically on (z, y, x)
+__device__ __forceinline__ bool keep_half(long long itag, long long jtag, int sx, int sy, int sz) {
+  if (itag > jtag) return ((itag + jtag) & 1) != 0;
+  if (itag < jtag) return ((itag + jtag) & 1) == 0;
+  if (sz != 0) return sz > 0;
+  if (sy != 0) return sy > 0;
+  return sx > 0;
+}
+
+// ============================================================ k_tersoff ==========
+// One thread per centre atom i: the bonds i-j it centres (zeta over k, force_zeta,
+// attractive over k, pair_tersoff.cpp:181-258) and the repulsion of every bond from i's
+// end (:132-175).  Forces on bond partners go to ters_g slots (gathered in k_finish).
+//
+// Precision: the radial bond terms (repulsion A e^{-lam1 r} and the attraction
+// b_ij f_A(r), which nearly cancel at the equilibrium bond length) are evaluated in
+// FP64 in both modes, from FP64 displacements; b_ij enters as 1 + delta with delta
+// computed as expm1(-log1p((beta zeta)^n)/(2n)), which keeps its full relative accuracy
+// in FP32.  zeta, g(theta) and the three-body derivatives are evaluated in R.
+__device__ __forceinline__ void ters_fc_both64(double r, const TersP<R> &p, double &fc, double &fcd) {
+  if (r < p.rlo64) { fc = 1.0; fcd = 0.0; return; }
+  if (r > p.rhi64) { fc = 0.0; fcd = 0.0; return; }
+  double s, c;
+  sincospi(0.5 * (r - p.R64) / p.D64, &s, &c);
+  fc = 0.5 * (1.0 - s);
+  fcd = -p.pi4D64 * c;
+}
+
+// b_ij - 1 and db_ij/dzeta (ters_bij, ters_bij_d, pair_tersoff.cpp:704-734)
+__device__ __forceinline__ void ters_bij_delta(R zeta, const TersP<R> &p, double &bm1, R &bd) {
+  R tmp = p.beta * zeta;
+  if (tmp > p.c1) {
+    bm1 = (double)(R(1) / Math<R>::sqrt_(tmp)) - 1.0;
+    bd = p.beta * R(-0.5) * Math<R>::pow_(tmp, R(-1.5));
+    return;
+  }
+  if (tmp > p.c2t) {
+    bm1 = (double)((R(1) - Math<R>::pow_(tmp, -p.powern) * p.inv2n) / Math<R>::sqrt_(tmp)) - 1.0;
+    bd = p.beta * (R(-0.5) * Math<R>::pow_(tmp, R(-1.5)) * (R(1) - (R(1) + p.inv2n) * Math<R>::pow_(tmp, -p.powern)));
+    return;
+  }
+  if (tmp < p.c4) {
+    bm1 = 0.0;
+    bd = R(0);
+    return;
+  }
+  if (tmp < p.c3) {
+    R tn = Math<R>::pow_(tmp, p.powern);
+    bm1 = -(double)(tn * p.inv2n);
+    bd = R(-0.5) * p.beta * Math<R>::pow_(tmp, p.powern - R(1));
+    return;
+  }
+  R tmp_n = Math<R>::pow_(tmp, p.powern);
+  if constexpr (sizeof(R) == 8) {
+    bm1 = pow(1.0 + tmp_n, -p.inv2n) - 1.0;
+  } else {
+    bm1 = (double)expm1f(-log1pf(tmp_n) * p.inv2n);
+  }
+  bd = R(-0.5) * Math<R>::pow_(R(1) + tmp_n, R(-1) - p.inv2n) * tmp_n / zeta;
+}
+
+template <bool EV, bool EATOM>
+__global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const SysDesc &sd = a.A.sys[a.A.sysid[i]];
+  const long long iinfo = __double_as_longlong(a.A.xq[i].w);
+  int ie = c_pot.t_map[info_type(iinfo)];
+  int cnt = a.ters_cnt[i];
+  if (ie < 0) cnt = 0;
+  double dxd[MAXTERS], dyd[MAXTERS], dzd[MAXTERS], r64[MAXTERS], rs64[MAXTERS];
+  R dx[MAXTERS], dy[MAXTERS], dz[MAXTERS], rr[MAXTERS];
+  int el[MAXTERS];
+  double gx[MAXTERS], gy[MAXTERS], gz[MAXTERS], ge[MAXTERS];
+  int sxv[MAXTERS], syv[MAXTERS], szv[MAXTERS], jv[MAXTERS];
+  double fx = 0, fy = 0, fz = 0, eng = 0;
+  double v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
+  for (int s = 0; s < cnt; s++) {
+    uint32_t e = a.ters_nb[(size_t)i * MAXTERS + s];
+    int j, sx, sy, sz;
+    decode_entry(e, a.lc, j, sx, sy, sz);
+    double ddx, ddy, ddz;
+    disp64(a.A.xq, sd, i, j, sx, sy, sz, ddx, ddy, ddz);
+    dxd[s] = -ddx; dyd[s] = -ddy; dzd[s] = -ddz;  // delr = x_j - x_i
+    double rs = rsq_rn(ddx, ddy, ddz);
+    rs64[s] = rs;
+    r64[s] = sqrt(rs);
+    dx[s] = (R)dxd[s]; dy[s] = (R)dyd[s]; dz[s] = (R)dzd[s];
+    rr[s] = (R)rs;
+    el[s] = c_pot.t_map[info_type(__double_as_longlong(a.A.xq[j].w))];
+    jv[s] = j; sxv[s] = sx; syv[s] = sy; szv[s] = sz;
+    gx[s] = gy[s] = gz[s] = ge[s] = 0.0;
+  }
+  long long itag = c_pot.rep_sym ? 0 : a.tag[i];
+  for (int s = 0; s < cnt; s++) {
+    int je = el[s];
+    const TersP<R> &pij = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + je];
+    const double r = r64[s];
+    const R rR = (R)r;
+    // ---- repulsion (:584-595) in FP64, from both ends of the bond, with the parameters
+    // of the end the reference's half list keeps
+    {
+      const TersP<R> *pr = &pij;
+      if (!c_pot.rep_sym && !keep_half(itag, a.tag[jv[s]], sxv[s], syv[s], szv[s]))
+        pr = &c_pot.ters[(je * MAXELEM + ie) * MAXELEM + ie];
+      if (rs64[s] < pr->cutsq64) {
+        double fc, fcd;
+        ters_fc_both64(r, *pr, fc, fcd);
+        double tmp_exp = exp(-pr->lam1_64 * r);
+        double fpair = -pr->A64 * tmp_exp * (fcd - fc * pr->lam1_64) / r;
+        fx -= dxd[s] * fpair; fy -= dyd[s] * fpair; fz -= dzd[s] * fpair;
+        if (EV) {
+          eng += 0.5 * fc * pr->A64 * tmp_exp;
+          double h = 0.5 * fpair;
+          v0 += h * dxd[s] * dxd[s]; v1 += h * dyd[s] * dyd[s]; v2 += h * dzd[s] * dzd[s];
+          v3 += h * dxd[s] * dyd[s]; v4 += h * dxd[s] * dzd[s]; v5 += h * dyd[s] * dzd[s];
+        }
+      }
+    }
+    if (!(rs64[s] < pij.cutsq64)) continue;
+    // ---- zeta_ij over k (:197-210), in R
+    R zeta = 0;
+    for (int k = 0; k < cnt; k++) {
+      if (k == s) continue;
+      const TersP<R> &pk = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + el[k]];
+      if (!(rs64[k] < pk.cutsq64)) continue;
+      R rik = (R)r64[k];
+      R cost = (dx[s] * dx[k] + dy[s] * dy[k] + dz[s] * dz[k]) / (rR * rik);
+      R ex = pk.lam3 == R(0) ? R(1) : ters_exdelr(rR, rik, pk);
+      zeta += ters_fc(rik, pk) * ters_gijk(cost, pk) * ex;
+    }
+    // ---- force_zeta (:621-634): radial part in FP64
+    double fa = 0.0, fa_d = 0.0;
+    {
+      double fc, fcd;
+      ters_fc_both64(r, pij, fc, fcd);
+      if (!(r > pij.rhi64)) {
+        double ex2 = exp(-pij.lam2_64 * r);
+        fa = -pij.B64 * ex2 * fc;
+        fa_d = pij.B64 * ex2 * (pij.lam2_64 * fc - fcd);
+      }
+    }
+    double bm1;
+    R bd;
+    ters_bij_delta(zeta, pij, bm1, bd);
+    const double bij = 1.0 + bm1;
+    const double fpair = 0.5 * bij * fa_d / r;
+    const R prefactor = (R)(-0.5 * fa) * bd;
+    fx += dxd[s] * fpair; fy += dyd[s] * fpair; fz += dzd[s] * fpair;
+    double fjx = -dxd[s] * fpair, fjy = -dyd[s] * fpair, fjz = -dzd[s] * fpair;
+    if (EV) {
+      double eb = 0.5 * bij * fa;
+      eng += eb;
+      ge[s] += eb;
+      v0 += dxd[s] * fjx; v1 += dyd[s] * fjy; v2 += dzd[s] * fjz;
+      v3 += dxd[s] * fjy; v4 += dxd[s] * fjz; v5 += dyd[s] * fjz;
+    }
+    // ---- attractive over k (:228-254) -> ters_zetaterm_d (:738-793), in R
+    if (prefactor != R(0)) {
+      R rinv = R(1) / rR;
+      R rhx = dx[s] * rinv, rhy = dy[s] * rinv, rhz = dz[s] * rinv;
+      R ajx = 0, ajy = 0, ajz = 0;
+      for (int k = 0; k < cnt; k++) {
+        if (k == s) continue;
+        const TersP<R> &pk = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + el[k]];
+        if (!(rs64[k] < pk.cutsq64)) continue;
+        R rik = (R)r64[k];
+        R rikinv = R(1) / rik;
+        R khx = dx[k] * rikinv, khy = dy[k] * rikinv, khz = dz[k] * rikinv;
+        R fck, dfck;
+        ters_fc_both(rik, pk, fck, dfck);
+        R exd, exd_d;
+        if (pk.lam3 == R(0)) {
+          exd = R(1);
+          exd_d = R(0);
+        } else {
+          exd = ters_exdelr(rR, rik, pk);
+          exd_d = pk.powermint == 3 ? R(3) * pk.lam3 * pk.lam3 * pk.lam3 * (rR - rik) * (rR - rik) * exd
+                                    : pk.lam3 * exd;
+        }
+        R cs = rhx * khx + rhy * khy + rhz * khz;
+        R g = ters_gijk(cs, pk), gd = ters_gijk_d(cs, pk);
+        // costheta_d (:797-811)
+        R djx = (-cs * rhx + khx) * rinv, djy = (-cs * rhy + khy) * rinv, djz = (-cs * rhz + khz) * rinv;
+        R dkx = (-cs * khx + rhx) * rikinv, dky = (-cs * khy + rhy) * rikinv, dkz = (-cs * khz + rhz) * rikinv;
+        R A1 = fck * gd * exd, A2 = fck * g * exd_d, A3 = dfck * g * exd;
+        R fjx_ = prefactor * (A1 * djx + A2 * rhx);
+        R fjy_ = prefactor * (A1 * djy + A2 * rhy);
+        R fjz_ = prefactor * (A1 * djz + A2 * rhz);
+        R fkx_ = prefactor * (A3 * khx + A1 * dkx - A2 * khx);
+        R fky_ = prefactor * (A3 * khy + A1 * dky - A2 * khy);
+        R fkz_ = prefactor * (A3 * khz + A1 * dkz - A2 * khz);
+        // fi = -(fj + fk) (:766-774)
+        fx -= (double)(fjx_ + fkx_); fy -= (double)(fjy_ + fky_); fz -= (double)(fjz_ + fkz_);
+        ajx += fjx_; ajy += fjy_; ajz += fjz_;
+        gx[k] += (double)fkx_; gy[k] += (double)fky_; gz[k] += (double)fkz_;
+        if (EV) {
+          v0 += (double)(dx[k] * fkx_); v1 += (double)(dy[k] * fky_); v2 += (double)(dz[k] * fkz_);
+          v3 += (double)(dx[k] * fky_); v4 += (double)(dx[k] * fkz_); v5 += (double)(dy[k] * fkz_);
+        }
+      }
+      fjx += (double)ajx; fjy += (double)ajy; fjz += (double)ajz;
+      if (EV) {
+        v0 += (double)(dx[s] * ajx); v1 += (double)(dy[s] * ajy); v2 += (double)(dz[s] * ajz);
+        v3 += (double)(dx[s] * ajy); v4 += (double)(dx[s] * ajz); v5 += (double)(dy[s] * ajz);
+      }
+    }
+    gx[s] += fjx; gy[s] += fjy; gz[s] += fjz;
+  }
+  for (int s = 0; s < cnt; s++) a.ters_g[(size_t)i * MAXTERS + s] = make_d4(gx[s], gy[s], gz[s], ge[s]);
+  a.ters_f[i] = fx;
+  a.ters_f[a.n + i] = fy;
+  a.ters_f[2 * a.n + i] = fz;
+  if (EV) {
+    double *st = a.stat_ters;
+    st[i] = eng;
+    st[(size_t)a.n + i] = 0.0;
+    st[(size_t)2 * a.n + i] = v0; st[(size_t)3 * a.n + i] = v1; st[(size_t)4 * a.n + i] = v2;
+    st[(size_t)5 * a.n + i] = v3; st[(size_t)6 * a.n + i] = v4; st[(size_t)7 * a.n + i] = v5;
+  }
+}
+
+// ============================================================== k_ilp ============
+// TPA lanes per atom i stride over i's interlayer list.  Per pair (del = x_i - x_j):
+//   vdW (calc_FvdW :509-533) from both ends; repulsion of term (i,j) with n_i and of
+//   term (j,i) with n_j (calc_FRep :602-647); g_i += Tap*prod*fpair1*del.
+// Lane 0 of the group then applies the normal derivatives of i (calc_normal's dnormdri
+// and dnormal, :893-926 / :1043-1067) to g_i in FP64: the force on i itself and the
+// force on each intralayer neighbour (ilp_c slots).
+template <int TPA, bool EV, bool EATOM>
+__global__ void __launch_bounds__(256) k_ilp(ForceArgs<R> a) {
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gtid / TPA;
+  const int lane = threadIdx.x & (TPA - 1);
+  const bool valid = i < a.n;
+  const int ii = valid ? i : a.n - 1;
+  const SysDesc &sd = a.A.sys[a.A.sysid[ii]];
+  AtomI<R> ai;
+  ai.load(a.A, ii);
+  const int ti = info_type(ai.info);
+  const long long mi = info_mol(ai.info);
+  const int ie = c_pot.i_map[ti];
+  R nix, niy, niz;
+  if constexpr (sizeof(R) == 8) { d4 q = a.nrm64[ii]; nix = q.x; niy = q.y; niz = q.z; }
+  else { float4 q = a.nrm32[ii]; nix = q.x; niy = q.y; niz = q.z; }
+  const long long itag = c_pot.vdw_sym ? 0 : a.tag[ii];
+  R fx = 0, fy = 0, fz = 0, gxa = 0, gya = 0, gza = 0;
+  R evdw = 0, erep = 0, w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
+  const R cutsq = c_pot.i_cutsq;
+  if (valid && ie >= 0) {
+    const int64_t b = a.list_off[i], end = a.list_off[i + 1];
+    for (int64_t k = b + lane; k < end; k += TPA) {
+      uint32_t e = __ldg(&a.list[k]);
+      int j, sx, sy, sz;
+      decode_entry(e, a.lc, j, sx, sy, sz);
+      R dx, dy, dz;
+      long long jinfo;
+      ai.disp(a.A, sd, j, sx, sy, sz, dx, dy, dz, jinfo);
+      R rsq = dx * dx + dy * dy + dz * dz;
+      if (!(rsq < cutsq)) continue;
+      if (info_mol(jinfo) == mi) continue;
+      const int je = c_pot.i_map[info_type(jinfo)];
+      if (je < 0) continue;
+      const IlpP<R> &pij = c_pot.ilp[ie * MAXELEM + je];
+      const IlpP<R> &pji = c_pot.ilp[je * MAXELEM + ie];
+      R njx, njy, njz;
+      if constexpr (sizeof(R) == 8) { d4 q = a.nrm64[j]; njx = q.x; njy = q.y; njz = q.z; }
+      else { float4 q = __ldg(&a.nrm32[j]); njx = q.x; njy = q.y; njz = q.z; }
+      R r, rinv;
+      if constexpr (sizeof(R) == 8) { r = sqrt(rsq); rinv = R(1) / r; }
+      else { rinv = rsqrtf(rsq); r = rsq * rinv; }
+      // taper (pair_ilp_graphene_hbn.h:80-115), Tap and dTap in one pass
+      R Tap = 1, dTap = 0;
+      if (c_pot.tap) {
+        R x = r * c_pot.i_inv_rcut;
+        Tap = R(20) * x + R(-70);
+        Tap = Tap * x + R(84);
+        Tap = Tap * x + R(-35);
+        Tap = Tap * x;
+        Tap = Tap * x;
+        Tap = Tap * x;
+        Tap = Tap * x + R(1);
+        R dT = R(140) * x + R(-420);
+        dT = dT * x + R(420);
+        dT = dT * x + R(-140);
+        dT = dT * x;
+        dT = dT * x;
+        dT = dT * x;
+        dTap = dT * c_pot.i_inv_rcut;
+      }
+      // ---- vdW (both ends evaluate the pair force; energy halved)
+      const IlpP<R> &pv = (c_pot.vdw_sym || keep_half(itag, a.tag[j], sx, sy, sz)) ? pij : pji;
+      R r2inv = rinv * rinv;
+      R r6inv = r2inv * r2inv * r2inv;
+      R r8inv = r6inv * r2inv;
+      R TSvdw = R(1) + Math<R>::exp_ts(pv, r);
+      R TSinv = Math<R>::rcp(TSvdw);
+      R Vvdw = -pv.C6 * r6inv * TSinv;
+      R fpv = R(-6) * pv.C6 * r8inv * TSinv + pv.C6 * pv.d_over_seff * (TSvdw - R(1)) * TSinv * TSinv * r8inv * r;
+      R fsum_v = fpv * Tap - Vvdw * dTap * rinv;
+      // ---- repulsion of term (i,j) with n_i
+      R p = nix * dx + niy * dy + niz * dz;
+      R rhosq = rsq - p * p;
+      R exp0 = Math<R>::exp_rep0(pij, r);
+      R exp1 = Math<R>::exp_rep1(pij, rhosq);
+      R frho = exp1 * pij.C;
+      R Erep = pij.eps_half + frho;
+      R V = exp0 * Erep;
+      R fpair1 = R(2) * exp0 * frho * pij.delta2inv;
+      R fsum = pij.lambda * exp0 * rinv * Erep + fpair1;
+      // ---- repulsion of term (j,i) with n_j (del' = -del, prod' = -q)
+      R q = njx * dx + njy * dy + njz * dz;
+      R rhosq2 = rsq - q * q;
+      R exp0b = pji.same_as_swapped ? exp0 : Math<R>::exp_rep0(pji, r);
+      R exp1b = Math<R>::exp_rep1(pji, rhosq2);
+      R frho2 = exp1b * pji.C;
+      R Erep2 = pji.eps_half + frho2;
+      R V2 = exp0b * Erep2;
+      R fpair1b = R(2) * exp0b * frho2 * pji.delta2inv;
+      R fsum2 = pji.lambda * exp0b * rinv * Erep2 + fpair1b;
+      // ---- force on i
+      R tp1 = Tap * p * fpair1;
+      R tq1 = Tap * q * fpair1b;
+      R crad = fsum_v + (fsum + fsum2) * Tap - (V + V2) * dTap * rinv;
+      fx += crad * dx - tp1 * nix - tq1 * njx;
+      fy += crad * dy - tp1 * niy - tq1 * njy;
+      fz += crad * dz - tp1 * niz - tq1 * njz;
+      gxa += tp1 * dx; gya += tp1 * dy; gza += tp1 * dz;
+      if (EV) {
+        evdw += R(0.5) * Vvdw * Tap;
+        erep += R(0.5) * (V + V2) * Tap;
+        // term (i,j): del (x) fkc_ij;  vdW: half of del (x) fsum_v del
+        R cr1 = fsum * Tap - V * dTap * rinv + R(0.5) * fsum_v;
+        R kx = cr1 * dx - tp1 * nix, ky = cr1 * dy - tp1 * niy, kz = cr1 * dz - tp1 * niz;
+        w0 += dx * kx; w1 += dy * ky; w2 += dz * kz;
+        w3 += dx * ky; w4 += dx * kz; w5 += dy * kz;
+      }
+    }
+  }
+  // ---- reduce over the TPA lanes of atom i in R; one conversion to FP64 per atom
+#pragma unroll
+  for (int o = TPA / 2; o > 0; o >>= 1) {
+    fx += __shfl_xor_sync(0xffffffff, fx, o);
+    fy += __shfl_xor_sync(0xffffffff, fy, o);
+    fz += __shfl_xor_sync(0xffffffff, fz, o);
+    gxa += __shfl_xor_sync(0xffffffff, gxa, o);
+    gya += __shfl_xor_sync(0xffffffff, gya, o);
+    gza += __shfl_xor_sync(0xffffffff, gza, o);
+    if (EV) {
+      evdw += __shfl_xor_sync(0xffffffff, evdw, o);
+      erep += __shfl_xor_sync(0xffffffff, erep, o);
+      w0 += __shfl_xor_sync(0xffffffff, w0, o);
+      w1 += __shfl_xor_sync(0xffffffff, w1, o);
+      w2 += __shfl_xor_sync(0xffffffff, w2, o);
+      w3 += __shfl_xor_sync(0xffffffff, w3, o);
+      w4 += __shfl_xor_sync(0xffffffff, w4, o);
+      w5 += __shfl_xor_sync(0xffffffff, w5, o);
+    }
+  }
+  if (!valid || lane != 0) return;
+  a.ilp_f[i] = (double)fx;
+  a.ilp_f[a.n + i] = (double)fy;
+  a.ilp_f[2 * a.n + i] = (double)fz;
+  a.ilp_g[i] = make_d4((double)gxa, (double)gya, (double)gza, 0.0);
+  if (EV) {
+    double *st = a.stat_ilp;
+    st[i] = (double)evdw;
+    st[(size_t)a.n + i] = (double)erep;
+    st[(size_t)2 * a.n + i] = (double)w0; st[(size_t)3 * a.n + i] = (double)w1; st[(size_t)4 * a.n + i] = (double)w2;
+    st[(size_t)5 * a.n + i] = (double)w3; st[(size_t)6 * a.n + i] = (double)w4; st[(size_t)7 * a.n + i] = (double)w5;
+    if (EATOM) a.eatom_ilp[i] = (double)evdw + (double)erep;
+  }
+}
+
+// ============================================================== k_nderiv =========
+// Normal-derivative assembly in FP64, one thread per atom i (calc_normal's dnormdri and
+// dnormal, pair_ilp_graphene_hbn.cpp:893-926 / :1043-1067, applied to the reverse-
+// accumulated g_i of the pair kernel).  With h = (I - n n^T) g / |n1| the force on
+// intralayer neighbour m is -(dn1/dv_m)^T h and on i -(dn1/dx_i)^T h; dn1/dv of a cross
+// product is a skew matrix, so each term is one cross product with h.  The neighbour
+// forces go to ilp_c slots, gathered by k_finish.
+template <bool EV>
+__global__ void k_nderiv(ForceArgs<R> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const SysDesc &sd = a.A.sys[a.A.sysid[i]];
+  const int ie = c_pot.i_map[info_type(__double_as_longlong(a.A.xq[i].w))];
+  const int cont = ie >= 0 ? a.ilp_cnt[i] : 0;
+  const d4 g = a.ilp_g[i];
+  const double Gx = g.x, Gy = g.y, Gz = g.z;
+  double Fx = 0, Fy = 0, Fz = 0;
+  double W0 = 0, W1 = 0, W2 = 0, W3 = 0, W4 = 0, W5 = 0;
+  double c0x = 0, c0y = 0, c0z = 0, c1x = 0, c1y = 0, c1z = 0, c2x = 0, c2y = 0, c2z = 0;
+  double v[MAXILP][3];
+  if (cont >= 2) {
+    for (int m = 0; m < cont; m++) {
+      int j, sx, sy, sz;
+      decode_entry(a.ilp_nb[(size_t)i * MAXILP + m], a.lc, j, sx, sy, sz);
+      double ddx, ddy, ddz;
+      disp64(a.A.xq, sd, i, j, sx, sy, sz, ddx, ddy, ddz);
+      v[m][0] = -ddx; v[m][1] = -ddy; v[m][2] = -ddz;
+    }
+    double n1x = v[0][1] * v[1][2] - v[1][1] * v[0][2];
+    double n1y = v[0][2] * v[1][0] - v[1][2] * v[0][0];
+    double n1z = v[0][0] * v[1][1] - v[1][0] * v[0][1];
+    if (cont == 3) {
+      n1x += v[2][1] * v[0][2] - v[0][1] * v[2][2];
+      n1y += v[2][2] * v[0][0] - v[0][2] * v[2][0];
+      n1z += v[2][0] * v[0][1] - v[0][0] * v[2][1];
+      n1x += v[1][1] * v[2][2] - v[2][1] * v[1][2];
+      n1y += v[1][2] * v[2][0] - v[2][2] * v[1][0];
+      n1z += v[1][0] * v[2][1] - v[2][0] * v[1][1];
+      n1x /= 3.0; n1y /= 3.0; n1z /= 3.0;
+    }
+    double nn = sqrt(n1x * n1x + n1y * n1y + n1z * n1z);
+    if (nn > 0.0) {
+      double inn = 1.0 / nn;
+      double nx = n1x * inn, ny = n1y * inn, nz = n1z * inn;
+      double ng = nx * Gx + ny * Gy + nz * Gz;
+      double hx = (Gx - nx * ng) * inn, hy = (Gy - ny * ng) * inn, hz = (Gz - nz * ng) * inn;
+      auto crs = [](double ax, double ay, double az, double bx, double by, double bz, double &ox, double &oy, double &oz) {
+        ox = ay * bz - az * by; oy = az * bx - ax * bz; oz = ax * by - ay * bx;
+      };
+      if (cont == 2) {
+        // -(dn1/dv1)^T h = -(v2 x h); -(dn1/dv2)^T h = v1 x h; on i: (v2 - v1) x h
+        crs(v[1][0], v[1][1], v[1][2], hx, hy, hz, c0x, c0y, c0z);
+        c0x = -c0x; c0y = -c0y; c0z = -c0z;
+        crs(v[0][0], v[0][1], v[0][2], hx, hy, hz, c1x, c1y, c1z);
+        Fx = -(c0x + c1x); Fy = -(c0y + c1y); Fz = -(c0z + c1z);
+      } else {
+        const double t = 1.0 / 3.0;
+        crs(v[2][0] - v[1][0], v[2][1] - v[1][1], v[2][2] - v[1][2], hx, hy, hz, c0x, c0y, c0z);
+        crs(v[0][0] - v[2][0], v[0][1] - v[2][1], v[0][2] - v[2][2], hx, hy, hz, c1x, c1y, c1z);
+        crs(v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2], hx, hy, hz, c2x, c2y, c2z);
+        c0x *= t; c0y *= t; c0z *= t;
+        c1x *= t; c1y *= t; c1z *= t;
+        c2x *= t; c2y *= t; c2z *= t;
+      }
+      if (EV) {
+        // virial of the neighbour forces relative to i (the term's forces sum to zero)
+        W0 = v[0][0] * c0x + v[1][0] * c1x; W1 = v[0][1] * c0y + v[1][1] * c1y; W2 = v[0][2] * c0z + v[1][2] * c1z;
+        W3 = v[0][0] * c0y + v[1][0] * c1y; W4 = v[0][0] * c0z + v[1][0] * c1z; W5 = v[0][1] * c0z + v[1][1] * c1z;
+        if (cont == 3) {
+          W0 += v[2][0] * c2x; W1 += v[2][1] * c2y; W2 += v[2][2] * c2z;
+          W3 += v[2][0] * c2y; W4 += v[2][0] * c2z; W5 += v[2][1] * c2z;
+        }
+      }
+    }
+  }
+  d4 *cs = a.ilp_c + (size_t)i * MAXILP;
+  cs[0] = make_d4(c0x, c0y, c0z, 0.0);
+  cs[1] = make_d4(c1x, c1y, c1z, 0.0);
+  cs[2] = make_d4(c2x, c2y, c2z, 0.0);
+  a.ilp_f[i] += Fx;
+  a.ilp_f[a.n + i] += Fy;
+  a.ilp_f[2 * a.n + i] += Fz;
+  if (EV) {
+    double *st = a.stat_ilp;
+    st[(size_t)2 * a.n + i] += W0; st[(size_t)3 * a.n + i] += W1; st[(size_t)4 * a.n + i] += W2;
+    st[(size_t)5 * a.n + i] += W3; st[(size_t)6 * a.n + i] += W4; st[(size_t)7 * a.n + i] += W5;
+  }
+}
+
+// ============================================================== k_finish =========
+// Per atom a: its own ILP and Tersoff forces + the slots its neighbours left for it:
+// Tersoff bond/three-body forces from every j with a in N_ters(j) and ILP normal-
+// derivative forces from every j with a in N_ilp(j).  Fixed summation order.
+template <bool EATOM>
+__global__ void k_finish(ForceArgs<R> a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  double Fx = 0, Fy = 0, Fz = 0, ea = 0;
+  if (a.do_ilp) {
+    Fx += a.ilp_f[i]; Fy += a.ilp_f[a.n + i]; Fz += a.ilp_f[2 * a.n + i];
+  }
+  if (a.do_ters) {
+    Fx += a.ters_f[i]; Fy += a.ters_f[a.n + i]; Fz += a.ters_f[2 * a.n + i];
+    int cnt = a.ters_cnt[i];
+    for (int s = 0; s < cnt; s++) {
+      int j, sx, sy, sz;
+      decode_entry(a.ters_nb[(size_t)i * MAXTERS + s], a.lc, j, sx, sy, sz);
+      uint32_t want = encode_entry(i, -sx, -sy, -sz, a.lc);
+      int cj = a.ters_cnt[j];
+      for (int t = 0; t < cj; t++) {
+        if (a.ters_nb[(size_t)j * MAXTERS + t] == want) {
+          d4 g = a.ters_g[(size_t)j * MAXTERS + t];
+          Fx += g.x; Fy += g.y; Fz += g.z;
+          if (EATOM) ea += 0.5 * g.w;
+          break;
+        }
+      }
+    }
+  }
+  if (a.do_ilp) {
+    const d4 q = a.A.xq[i];
+    const long long mi = info_mol(__double_as_longlong(q.w));
+    int cnt = a.short_cnt[i];
+    for (int c = 0; c < cnt; c++) {
+      int j, sx, sy, sz;
+      decode_entry(a.short_nb[(size_t)i * MAXSHORT + c], a.lc, j, sx, sy, sz);
+      int cj = a.ilp_cnt[j];
+      if (cj == 0) continue;
+      if (info_mol(__double_as_longlong(a.A.xq[j].w)) != mi) continue;
+      uint32_t want = encode_entry(i, -sx, -sy, -sz, a.lc);
+      for (int t = 0; t < cj; t++) {
+        if (a.ilp_nb[(size_t)j * MAXILP + t] == want) {
+          d4 g = a.ilp_c[(size_t)j * MAXILP + t];
+          Fx += g.x; Fy += g.y; Fz += g.z;
+          break;
+        }
+      }
+    }
+  }
+  a.f_out[i] = Fx;
+  a.f_out[a.n + i] = Fy;
+  a.f_out[2 * a.n + i] = Fz;
+  if (EATOM) {
+    // per-atom energy as the reference's ev_tally splits it: the Tersoff own share was
+    // written by k_ters_eatom_own, the partners' halves are gathered above
+    double e = a.do_ters ? a.eatom_ters[i] + ea : 0.0;
+    if (a.do_ilp) e += a.eatom_ilp[i];
+    a.eatom_ters[i] = e;
+  }
+}
+
+// Tersoff per-atom energy, own share (half of each bond energy centred here and half of
+// each repulsion from this end), written before k_finish adds the partners' halves.
+__global__ void k_ters_eatom_own(ForceArgs<R> a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  double e = 0.0;
+  int cnt = a.ters_cnt[i];
+  for (int s = 0; s < cnt; s++) e += 0.5 * a.ters_g[(size_t)i * MAXTERS + s].w;
+  // stat_ters[i] = sum of bond energies centred at i + half repulsions from this end
+  double bonds = 0.0;
+  for (int s = 0; s < cnt; s++) bonds += a.ters_g[(size_t)i * MAXTERS + s].w;
+  a.eatom_ters[i] = (a.stat_ters[i] - bonds) + e;
+}
+
+// ============================================================ host launchers ======
+
+void upload_pot(const PotConst<R> &p, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(c_pot, &p, sizeof(p), 0, cudaMemcpyHostToDevice, s);
+}
+
+void launch_short(const ForceArgs<R> &a, const double *cutILPsq64, double tcutmaxsq64, cudaStream_t s) {
+  if (a.n == 0) return;
+  k_short<<<(a.n + 127) / 128, 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
+}
+
+void launch_tersoff(const ForceArgs<R> &a, bool ev, bool eatom, cudaStream_t s) {
+  if (a.n == 0) return;
+  int g = (a.n + 127) / 128;
+  if (ev) k_tersoff<true, false><<<g, 128, 0, s>>>(a);
+  else k_tersoff<false, false><<<g, 128, 0, s>>>(a);
+  if (ev && eatom) k_ters_eatom_own<<<g, 128, 0, s>>>(a);
+}
+
+template <int TPA>
+static void launch_ilp_t(const ForceArgs<R> &a, bool ev, bool eatom, int block, cudaStream_t s) {
+  long long threads = (long long)a.n * TPA;
+  int g = (int)((threads + block - 1) / block);
+  if (ev && eatom) k_ilp<TPA, true, true><<<g, block, 0, s>>>(a);
+  else if (ev) k_ilp<TPA, true, false><<<g, block, 0, s>>>(a);
+  else k_ilp<TPA, false, false><<<g, block, 0, s>>>(a);
+}
+
+void launch_ilp(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, cudaStream_t s) {
+  if (a.n == 0) return;
+  switch (tpa) {
+    case 4: launch_ilp_t<4>(a, ev, eatom, block, s); break;
+    case 8: launch_ilp_t<8>(a, ev, eatom, block, s); break;
+    case 16: launch_ilp_t<16>(a, ev, eatom, block, s); break;
+    default: launch_ilp_t<32>(a, ev, eatom, block, s); break;
+  }
+}
+
+void launch_nderiv(const ForceArgs<R> &a, bool ev, cudaStream_t s) {
+  if (a.n == 0) return;
+  int g = (a.n + 127) / 128;
+  if (ev) k_nderiv<true><<<g, 128, 0, s>>>(a);
+  else k_nderiv<false><<<g, 128, 0, s>>>(a);
+}
+
+void launch_finish(const ForceArgs<R> &a, bool eatom, cudaStream_t s) {
+  if (a.n == 0) return;
+  int g = (a.n + 127) / 128;
+  if (eatom) k_finish<true><<<g, 128, 0, s>>>(a);
+  else k_finish<false><<<g, 128, 0, s>>>(a);
+}
+
+}  // namespace LMFF_NS
+}  // namespace lmff

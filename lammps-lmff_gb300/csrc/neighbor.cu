@@ -1,0 +1,263 @@
+// GPU neighbour build: cell binning, stable sort of atoms by bin, and the two lists
+// the force kernels consume, built with skin like LAMMPS's binned full list
+// (npair_full_bin_ghost.cpp:75-117, accept rsq <= cutneighsq; cutneigh = cutforce + skin,
+// neighbor.cpp:294-317):
+//   * the pair list: for the ILP pair kernel, every j within cutneigh with a different
+//     molecule id (or, with list_full, every j: the reference's full list), stored as
+//     32-bit (index, periodic image) codes in CSR form;
+//   * the short candidate list: every j within max(ILP intralayer rcut, Tersoff
+//     cutmax) + skin, from which each step picks the ILP intralayer and Tersoff lists.
+// Periodic images are explicit image codes, never minimum image, so boxes shorter than
+// the cutoff (several images of one atom, self images) are exact.
+#include <cub/cub.cuh>
+
+#include "engine.cuh"
+#include "neighbor.cuh"
+
+namespace lmff {
+
+__constant__ NbConst c_nb;
+
+__device__ __forceinline__ int bin_coord(double x, double lo, double binv, int nb) {
+  int b = (int)floor((x - lo) * binv);
+  return b < 0 ? 0 : (b >= nb ? nb - 1 : b);
+}
+
+// Wrap periodic coordinates into the box (LAMMPS Domain::pbc at reneighbouring) and
+// compute each atom's global bin.
+__global__ void k_wrap_bin(int n, d4 *xq, const SysDesc *sys, const int *sysid, uint32_t *key, int *idx) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const SysDesc &sd = sys[sysid[p]];
+  d4 q = xq[p];
+  double c[3] = {q.x, q.y, q.z};
+  int b[3];
+  for (int d = 0; d < 3; d++) {
+    if (sd.per[d]) {
+      double hi = sd.lo[d] + sd.L[d];
+      if (c[d] < sd.lo[d]) c[d] += sd.L[d] * ceil((sd.lo[d] - c[d]) / sd.L[d]);
+      if (c[d] >= hi) c[d] -= sd.L[d] * floor((c[d] - sd.lo[d]) / sd.L[d]);
+      if (c[d] < sd.lo[d] || c[d] >= hi) c[d] = sd.lo[d];
+    }
+    b[d] = bin_coord(c[d], sd.lo[d], sd.binv[d], sd.nb[d]);
+  }
+  xq[p] = make_d4(c[0], c[1], c[2], q.w);
+  key[p] = (uint32_t)(sd.bin_begin + (b[2] * sd.nb[1] + b[1]) * sd.nb[0] + b[0]);
+  idx[p] = p;
+}
+
+__global__ void k_permute(int n, const int *idx2, const d4 *xq, d4 *xq2, const double *v, double *v2,
+                          const int64_t *tag, int64_t *tag2, const int *perm, int *perm2, const int *sysid,
+                          int *sysid2, const double *mass, double *mass2) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int o = idx2[q];
+  xq2[q] = xq[o];
+  v2[q] = v[o];
+  v2[n + q] = v[n + o];
+  v2[2 * n + q] = v[2 * n + o];
+  tag2[q] = tag[o];
+  perm2[q] = perm[o];
+  sysid2[q] = sysid[o];
+  mass2[q] = mass[o];
+}
+
+__global__ void k_bin_ranges(int n, const uint32_t *key, int *bin_start, int *bin_end) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  uint32_t k = key[q];
+  if (q == 0 || key[q - 1] != k) bin_start[k] = q;
+  if (q == n - 1 || key[q + 1] != k) bin_end[k] = q + 1;
+}
+
+// double-float split of each position: X = x - lo + 32 + base lies in [base, 2 base) for
+// every position within 32 A of the box (base = 2^ceil(log2(Lmax + 64))), so
+// the hi parts of any two atoms of a system share one binade and their difference is
+// exact in FP32; lo = X - hi carries the remaining bits.
+__global__ void k_hilo(int n, const d4 *xq, const SysDesc *sys, const int *sysid, float4 *xh, float4 *xl) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const SysDesc &sd = sys[sysid[p]];
+  d4 q = xq[p];
+  double X = q.x - sd.lo[0] + 32.0 + sd.base;
+  double Y = q.y - sd.lo[1] + 32.0 + sd.base;
+  double Z = q.z - sd.lo[2] + 32.0 + sd.base;
+  float hx = (float)X, hy = (float)Y, hz = (float)Z;
+  int info = (int)__double_as_longlong(q.w);
+  xh[p] = make_float4(hx, hy, hz, __int_as_float(info));
+  xl[p] = make_float4((float)(X - (double)hx), (float)(Y - (double)hy), (float)(Z - (double)hz), 0.f);
+}
+
+__device__ __forceinline__ bool le_exact(float rsq, float thr, double thr64, const d4 *xq, const SysDesc &sd,
+                                         int i, int j, int sx, int sy, int sz) {
+  float m = 1e-5f * thr;
+  if (rsq < thr - m) return true;
+  if (rsq > thr + m) return false;
+  d4 a = xq[i];
+  d4 b = xq[j];
+  double xj = sx ? __dadd_rn(b.x, sx * sd.L[0]) : b.x;
+  double yj = sy ? __dadd_rn(b.y, sy * sd.L[1]) : b.y;
+  double zj = sz ? __dadd_rn(b.z, sz * sd.L[2]) : b.z;
+  double dx = __dsub_rn(a.x, xj), dy = __dsub_rn(a.y, yj), dz = __dsub_rn(a.z, zj);
+  double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  return r2 <= thr64;
+}
+
+// One warp per atom i, scanning the bins of its stencil (with periodic images).
+// FILL = false: counts pair-list entries into cnt[i] and writes the short list.
+// FILL = true: writes the pair list at list_off[i] in the same deterministic order.
+template <bool FILL>
+__global__ void __launch_bounds__(256) k_list(NbArgs a) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= a.n) return;
+  const int i = warp;
+  const SysDesc &sd = a.sys[a.sysid[i]];
+  const d4 qi = a.xq[i];
+  const float4 hi = a.xh[i];
+  const float4 li = a.xl[i];
+  const int infoi = __float_as_int(hi.w);
+  const int ti = infoi & 255;
+  const int mi = infoi >> 8;
+  const int ilp_i = c_nb.ilp_mapped[ti];
+  int b[3];
+  b[0] = bin_coord(qi.x, sd.lo[0], sd.binv[0], sd.nb[0]);
+  b[1] = bin_coord(qi.y, sd.lo[1], sd.binv[1], sd.nb[1]);
+  b[2] = bin_coord(qi.z, sd.lo[2], sd.binv[2], sd.nb[2]);
+  int64_t nlong = 0;
+  int nshort = 0;
+  const int64_t base = FILL ? a.list_off[i] : 0;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int dz = -sd.reach[2]; dz <= sd.reach[2]; dz++) {
+    int bz = b[2] + dz, sz = 0;
+    if (sd.per[2]) {
+      sz = bz >= 0 ? bz / sd.nb[2] : -((-bz + sd.nb[2] - 1) / sd.nb[2]);
+      bz -= sz * sd.nb[2];
+    } else if (bz < 0 || bz >= sd.nb[2]) continue;
+    for (int dy = -sd.reach[1]; dy <= sd.reach[1]; dy++) {
+      int by = b[1] + dy, sy = 0;
+      if (sd.per[1]) {
+        sy = by >= 0 ? by / sd.nb[1] : -((-by + sd.nb[1] - 1) / sd.nb[1]);
+        by -= sy * sd.nb[1];
+      } else if (by < 0 || by >= sd.nb[1]) continue;
+      for (int dx = -sd.reach[0]; dx <= sd.reach[0]; dx++) {
+        int bx = b[0] + dx, sx = 0;
+        if (sd.per[0]) {
+          sx = bx >= 0 ? bx / sd.nb[0] : -((-bx + sd.nb[0] - 1) / sd.nb[0]);
+          bx -= sx * sd.nb[0];
+        } else if (bx < 0 || bx >= sd.nb[0]) continue;
+        const int gb = sd.bin_begin + (bz * sd.nb[1] + by) * sd.nb[0] + bx;
+        const int start = a.bin_start[gb], end = a.bin_end[gb];
+        const float shx = (float)sx * sd.Lhi[0], shy = (float)sy * sd.Lhi[1], shz = (float)sz * sd.Lhi[2];
+        const float slx = (float)sx * sd.Llo[0], sly = (float)sy * sd.Llo[1], slz = (float)sz * sd.Llo[2];
+        const bool self_image = (sx | sy | sz) == 0;
+        for (int j0 = start; j0 < end; j0 += 32) {
+          const int j = j0 + lane;
+          bool take_long = false, take_short = false;
+          if (j < end && !(self_image && j == i)) {
+            const float4 hj = __ldg(&a.xh[j]);
+            const float4 lj = __ldg(&a.xl[j]);
+            float ddx = ((hi.x - hj.x) - shx) + ((li.x - lj.x) - slx);
+            float ddy = ((hi.y - hj.y) - shy) + ((li.y - lj.y) - sly);
+            float ddz = ((hi.z - hj.z) - shz) + ((li.z - lj.z) - slz);
+            float rsq = ddx * ddx + ddy * ddy + ddz * ddz;
+            const int infoj = __float_as_int(hj.w);
+            const int tj = infoj & 255;
+            const int mj = infoj >> 8;
+            const int tt = ti * (MAXTYPE + 1) + tj;
+            if (a.full || (mj != mi && ilp_i && c_nb.ilp_mapped[tj]))
+              take_long = le_exact(rsq, c_nb.cutnsq_f[tt], c_nb.cutnsq_d[tt], a.xq, sd, i, j, sx, sy, sz);
+            if (!FILL) take_short = le_exact(rsq, c_nb.rshortsq_f, c_nb.rshortsq_d, a.xq, sd, i, j, sx, sy, sz);
+          }
+          const unsigned ml = __ballot_sync(0xffffffff, take_long);
+          if (FILL && take_long) {
+            int64_t pos = base + nlong + __popc(ml & lt);
+            if (pos < a.list_cap) a.list[pos] = encode_entry(j, sx, sy, sz, a.lc);
+          }
+          nlong += __popc(ml);
+          if (!FILL) {
+            const unsigned ms = __ballot_sync(0xffffffff, take_short);
+            if (take_short) {
+              int pos = nshort + __popc(ms & lt);
+              if (pos < MAXSHORT) a.short_nb[(size_t)i * MAXSHORT + pos] = encode_entry(j, sx, sy, sz, a.lc);
+            }
+            nshort += __popc(ms);
+          }
+        }
+      }
+    }
+  }
+  if (lane == 0) {
+    if (!FILL) {
+      a.cnt[i] = nlong;
+      a.short_cnt[i] = nshort < MAXSHORT ? nshort : MAXSHORT;
+      if (nshort > MAXSHORT) atomicOr(a.status, ST_SHORT_OVERFLOW);
+    } else if (base + nlong > a.list_cap) {
+      atomicOr(a.status, ST_LIST_OVERFLOW);
+    }
+  }
+}
+
+__global__ void k_copy_hold(int n, const d4 *xq, double *xhold) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  d4 q = xq[p];
+  xhold[3 * p] = q.x;
+  xhold[3 * p + 1] = q.y;
+  xhold[3 * p + 2] = q.z;
+}
+
+// ---------------------------------------------------------------- host side
+
+void nb_upload_const(const NbConst &c, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(c_nb, &c, sizeof(c), 0, cudaMemcpyHostToDevice, s);
+}
+
+void nb_wrap_bin(int n, d4 *xq, const SysDesc *sys, const int *sysid, uint32_t *key, int *idx, cudaStream_t s) {
+  if (n) k_wrap_bin<<<(n + 255) / 256, 256, 0, s>>>(n, xq, sys, sysid, key, idx);
+}
+
+size_t nb_sort_tmp_bytes(int n, int nbits) {
+  size_t a = 0, b = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, a, (uint32_t *)nullptr, (uint32_t *)nullptr, (int *)nullptr, (int *)nullptr, n, 0,
+                                  nbits);
+  cub::DeviceScan::ExclusiveSum(nullptr, b, (int64_t *)nullptr, (int64_t *)nullptr, n + 1);
+  return a > b ? a : b;
+}
+
+cudaError_t nb_sort(void *tmp, size_t tmp_bytes, const uint32_t *k, uint32_t *k2, const int *v, int *v2, int n, int nbits,
+                    cudaStream_t s) {
+  return cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, k, k2, v, v2, n, 0, nbits, s);
+}
+
+cudaError_t nb_scan(void *tmp, size_t tmp_bytes, const int64_t *cnt, int64_t *off, int n, cudaStream_t s) {
+  return cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, cnt, off, n + 1, s);
+}
+
+void nb_permute(int n, const int *idx2, const d4 *xq, d4 *xq2, const double *v, double *v2, const int64_t *tag,
+                int64_t *tag2, const int *perm, int *perm2, const int *sysid, int *sysid2, const double *mass,
+                double *mass2, cudaStream_t s) {
+  if (n) k_permute<<<(n + 255) / 256, 256, 0, s>>>(n, idx2, xq, xq2, v, v2, tag, tag2, perm, perm2, sysid, sysid2, mass, mass2);
+}
+
+void nb_bin_ranges(int n, const uint32_t *key, int *bs, int *be, cudaStream_t s) {
+  if (n) k_bin_ranges<<<(n + 255) / 256, 256, 0, s>>>(n, key, bs, be);
+}
+
+void nb_hilo(int n, const d4 *xq, const SysDesc *sys, const int *sysid, float4 *xh, float4 *xl, cudaStream_t s) {
+  if (n) k_hilo<<<(n + 255) / 256, 256, 0, s>>>(n, xq, sys, sysid, xh, xl);
+}
+
+void nb_list(const NbArgs &a, bool fill, cudaStream_t s) {
+  if (!a.n) return;
+  long long threads = (long long)a.n * 32;
+  int g = (int)((threads + 255) / 256);
+  if (fill) k_list<true><<<g, 256, 0, s>>>(a);
+  else k_list<false><<<g, 256, 0, s>>>(a);
+}
+
+void nb_copy_hold(int n, const d4 *xq, double *xhold, cudaStream_t s) {
+  if (n) k_copy_hold<<<(n + 255) / 256, 256, 0, s>>>(n, xq, xhold);
+}
+
+}  // namespace lmff

@@ -1,0 +1,51 @@
+// Neighbour-build interface between neighbor.cu and the engine.
+#pragma once
+
+#include "engine.cuh"
+
+namespace lmff {
+
+// per type-pair cutoffs of the pair list and the short-candidate cutoff
+struct NbConst {
+  float cutnsq_f[(MAXTYPE + 1) * (MAXTYPE + 1)];
+  double cutnsq_d[(MAXTYPE + 1) * (MAXTYPE + 1)];
+  int ilp_mapped[MAXTYPE + 1];
+  float rshortsq_f;
+  double rshortsq_d;
+};
+
+struct NbArgs {
+  int n;
+  const d4 *xq;
+  const float4 *xh;
+  const float4 *xl;
+  const SysDesc *sys;
+  const int *sysid;
+  const int *bin_start;
+  const int *bin_end;
+  const int64_t *list_off;
+  uint32_t *list;
+  int64_t list_cap;
+  int64_t *cnt;       // per-atom pair-list counts (int64: totals exceed 2^31)
+  int *short_cnt;
+  uint32_t *short_nb;
+  ListCode lc;
+  int full;
+  int *status;
+};
+
+void nb_upload_const(const NbConst &c, cudaStream_t s);
+void nb_wrap_bin(int n, d4 *xq, const SysDesc *sys, const int *sysid, uint32_t *key, int *idx, cudaStream_t s);
+size_t nb_sort_tmp_bytes(int n, int nbits);
+cudaError_t nb_sort(void *tmp, size_t tmp_bytes, const uint32_t *k, uint32_t *k2, const int *v, int *v2, int n, int nbits,
+                    cudaStream_t s);
+cudaError_t nb_scan(void *tmp, size_t tmp_bytes, const int64_t *cnt, int64_t *off, int n, cudaStream_t s);
+void nb_permute(int n, const int *idx2, const d4 *xq, d4 *xq2, const double *v, double *v2, const int64_t *tag,
+                int64_t *tag2, const int *perm, int *perm2, const int *sysid, int *sysid2, const double *mass,
+                double *mass2, cudaStream_t s);
+void nb_bin_ranges(int n, const uint32_t *key, int *bs, int *be, cudaStream_t s);
+void nb_hilo(int n, const d4 *xq, const SysDesc *sys, const int *sysid, float4 *xh, float4 *xl, cudaStream_t s);
+void nb_list(const NbArgs &a, bool fill, cudaStream_t s);
+void nb_copy_hold(int n, const d4 *xq, double *xhold, cudaStream_t s);
+
+}  // namespace lmff

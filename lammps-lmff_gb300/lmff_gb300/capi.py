@@ -1,0 +1,290 @@
+"""ctypes binding of the engine's C ABI (include/lmff_gb300.h).
+
+This is plumbing for the tests, the benchmark and the serving loop; the compute path is
+the CUDA library itself.  There is no CPU fallback: loading fails loudly when
+liblmff_gb300.so is missing or cannot be loaded, and every non-zero status code raises
+``LmffError`` with the engine's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "liblmff_gb300.so")
+POTENTIALS = os.path.join(os.path.dirname(PKG), "potentials")
+
+LMFF_OK = 0
+CODES = {-1: "LMFF_EINVAL", -2: "LMFF_ECUDA", -3: "LMFF_EOVERFLOW", -4: "LMFF_ETOO_MANY_ILP_NEIGH",
+         -5: "LMFF_EZERO_NORMAL", -6: "LMFF_EBADPARAM", -7: "LMFF_ETIMEDOUT", -8: "LMFF_EUNSUPPORTED",
+         -9: "LMFF_ENOMEM", -10: "LMFF_ENODEV"}
+FP64 = 0
+MIXED = 1
+TERSOFF = 1
+ILP = 2
+SAME_ATOMS = 4
+OVERWRITE = 8
+
+
+class LmffError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{CODES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Result(C.Structure):
+    _fields_ = [("e_tersoff", C.c_double), ("e_ilp", C.c_double), ("pvector", C.c_double * 2),
+                ("virial_tersoff", C.c_double * 6), ("virial_ilp", C.c_double * 6)]
+
+    def to_dict(self) -> Dict:
+        vt = np.array(self.virial_tersoff[:])
+        vi = np.array(self.virial_ilp[:])
+        return {"e_tersoff": self.e_tersoff, "e_ilp": self.e_ilp, "pvector": np.array(self.pvector[:]),
+                "virial_tersoff": vt, "virial_ilp": vi, "virial": vt + vi,
+                "e_pair": self.e_tersoff + self.e_ilp}
+
+
+class Thermo(C.Structure):
+    _fields_ = [("step", C.c_int64), ("pe", C.c_double), ("ke", C.c_double), ("etotal", C.c_double),
+                ("temp", C.c_double), ("virial", C.c_double * 6)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("natoms", C.c_int64), ("list_entries", C.c_int64), ("short_entries", C.c_int64),
+                ("list_capacity", C.c_int64), ("rebuilds", C.c_int64), ("steps", C.c_int64),
+                ("list_per_atom", C.c_double), ("bytes_device", C.c_double), ("ms_last_build", C.c_double),
+                ("ms_last_forces", C.c_double), ("precision", C.c_int), ("tpa", C.c_int), ("block", C.c_int),
+                ("ms_last_run", C.c_double), ("kernel_ms", C.c_double * 6), ("kernel_launches", C.c_int64 * 6),
+                ("pairs_in_cutoff", C.c_int64)]
+KERNELS = ["pair_ilp", "tersoff", "intralayer_normals", "gather", "integrate", "neighbor_build"]
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [("natoms", C.c_int), ("x", C.c_void_p), ("type", C.c_void_p), ("mol", C.c_void_p),
+                ("lo", C.c_double * 3), ("hi", C.c_double * 3), ("periodic", C.c_int * 3)]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load liblmff_gb300.so (built by lmff_gb300.build); raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"{path} not found: build it with lmff_gb300.build.build()")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    I = C.c_int
+    D = C.c_double
+    sig = {
+        "lmff_device_count": ([], I),
+        "lmff_create": ([C.POINTER(P), P, I], I),
+        "lmff_create_from_files": ([C.POINTER(P), C.c_char_p, C.c_char_p, I, C.POINTER(C.c_char_p), D, I, D, I], I),
+        "lmff_destroy": ([P], None),
+        "lmff_set_precision": ([P, I], I),
+        "lmff_set_box": ([P, P, P, D, D, D, P], I),
+        "lmff_set_option": ([P, C.c_char_p, D], I),
+        "lmff_compute": ([P, I, P, P, P, P, I, I, I, P, P, C.POINTER(Result)], I),
+        "lmff_compute_device": ([P, I, P, P, P, P, I, I, I, P, C.POINTER(Result)], I),
+        "lmff_upload": ([P, I, P, P, P, P, P, P], I),
+        "lmff_compute_resident": ([P, I, I, I, C.POINTER(Result)], I),
+        "lmff_run_nve": ([P, I, D, I, P], I),
+        "lmff_download": ([P, P, P, P], I),
+        "lmff_batch_set": ([P, I, P], I),
+        "lmff_batch_compute": ([P, P, P], I),
+        "lmff_get_stats": ([P, C.POINTER(Stats)], I),
+        "lmff_export_list": ([P, I, P, C.c_int64], C.c_int64),
+        "lmff_last_error": ([P], C.c_char_p),
+        "lmff_strerror": ([I], C.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+class Engine:
+    """One engine handle: one GPU, one stream, one resident system or batch."""
+
+    def __init__(self, tersoff_file: Optional[str] = None, ilp_file: Optional[str] = None,
+                 elements: Sequence[str] = ("C", "B", "N"), cut_global: float = 16.0, tap_flag: int = 1,
+                 skin: float = 2.0, device: int = 0, precision: int = FP64):
+        lib = load_library()
+        if tersoff_file is None and ilp_file is None:
+            tersoff_file = os.path.join(POTENTIALS, "BNC.tersoff")
+            ilp_file = os.path.join(POTENTIALS, "BNCH.ILP")
+        self._h = C.c_void_p()
+        arr = (C.c_char_p * len(elements))(*[e.encode() for e in elements])
+        rc = lib.lmff_create_from_files(C.byref(self._h), tersoff_file.encode() if tersoff_file else None,
+                                        ilp_file.encode() if ilp_file else None, len(elements), arr, cut_global,
+                                        tap_flag, skin, device)
+        if rc != 0:
+            raise LmffError(rc, lib.lmff_last_error(None).decode())
+        self.ntypes = len(elements)
+        self.set_precision(precision)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value and _lib is not None:
+            _lib.lmff_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+    def _ck(self, rc: int):
+        if rc != 0:
+            raise LmffError(rc, _lib.lmff_last_error(self._h).decode())
+
+    # -------------------------------------------------------------- configuration
+    def set_precision(self, mode: int):
+        self._ck(_lib.lmff_set_precision(self._h, mode))
+
+    def set_box(self, lo, hi, periodic):
+        lo = _f64(lo)
+        hi = _f64(hi)
+        per = np.ascontiguousarray(np.asarray(periodic, dtype=bool).astype(np.int32))
+        self._ck(_lib.lmff_set_box(self._h, _p(lo), _p(hi), 0.0, 0.0, 0.0, _p(per)))
+
+    def set_option(self, key: str, value: float):
+        self._ck(_lib.lmff_set_option(self._h, key.encode(), float(value)))
+
+    # -------------------------------------------------------------- one-shot compute
+    def compute(self, x, type_, mol=None, tag=None, which: int = TERSOFF | ILP, eflag: bool = True,
+                vflag: bool = True, eatom: bool = False, same_atoms: bool = False, f=None,
+                overwrite: bool = False) -> Dict:
+        x = _f64(x)
+        n = x.shape[0]
+        t = np.ascontiguousarray(type_, dtype=np.int32)
+        m = None if mol is None else np.ascontiguousarray(mol, dtype=np.int64)
+        g = None if tag is None else np.ascontiguousarray(tag, dtype=np.int64)
+        out_f = np.zeros((n, 3)) if f is None else f
+        ea = np.zeros(n) if eatom else None
+        r = Result()
+        flags = which | (SAME_ATOMS if same_atoms else 0) | (OVERWRITE if overwrite else 0)
+        self._ck(_lib.lmff_compute(self._h, n, _p(x), _p(t), _p(m), _p(g), flags, int(eflag), int(vflag),
+                                   _p(out_f), _p(ea), C.byref(r)))
+        out = r.to_dict()
+        out["f"] = out_f
+        if eatom:
+            out["eatom"] = ea
+        return out
+
+    def compute_system(self, s, **kw) -> Dict:
+        self.set_box(s.box_lo, s.box_hi, s.periodic)
+        return self.compute(s.x, s.type, s.mol, s.tag, **kw)
+
+    def compute_device(self, x, type_, mol, tag, f, which: int = TERSOFF | ILP, eflag=True, vflag=True,
+                       same_atoms=False, overwrite=True) -> Dict:
+        """Device-pointer variant: x, type, mol, tag, f are torch CUDA tensors
+        (float64 [n,3], int32 [n], int64 [n], int64 [n] or None, float64 [n,3])."""
+        r = Result()
+        flags = which | (SAME_ATOMS if same_atoms else 0) | (OVERWRITE if overwrite else 0)
+        self._ck(_lib.lmff_compute_device(self._h, int(x.shape[0]), x.data_ptr(), type_.data_ptr(),
+                                          mol.data_ptr() if mol is not None else None,
+                                          tag.data_ptr() if tag is not None else None, flags, int(eflag),
+                                          int(vflag), f.data_ptr(), C.byref(r)))
+        return r.to_dict()
+
+    # -------------------------------------------------------------- resident MD
+    def upload(self, s, masses=(12.011, 10.811, 14.0067)):
+        self.set_box(s.box_lo, s.box_hi, s.periodic)
+        x = _f64(s.x)
+        v = None if s.v is None else _f64(s.v)
+        t = np.ascontiguousarray(s.type, dtype=np.int32)
+        m = np.ascontiguousarray(s.mol, dtype=np.int64)
+        g = np.ascontiguousarray(s.tag, dtype=np.int64)
+        ms = _f64(list(masses) + [1.0] * (self.ntypes - len(masses)))
+        self._n = x.shape[0]
+        self._ck(_lib.lmff_upload(self._h, self._n, _p(x), _p(v), _p(t), _p(m), _p(g), _p(ms)))
+
+    def compute_resident(self, which: int = TERSOFF | ILP, eflag=True, vflag=True) -> Dict:
+        r = Result()
+        self._ck(_lib.lmff_compute_resident(self._h, which, int(eflag), int(vflag), C.byref(r)))
+        return r.to_dict()
+
+    def run_nve(self, nsteps: int, dt: float = 0.001, thermo_every: int = 0) -> List[Dict]:
+        nth = (nsteps // thermo_every + 1) if thermo_every > 0 else 0
+        th = (Thermo * max(nth, 1))()
+        self._ck(_lib.lmff_run_nve(self._h, nsteps, dt, thermo_every, C.cast(th, C.c_void_p) if nth else None))
+        return [{"step": t.step, "pe": t.pe, "ke": t.ke, "etotal": t.etotal, "temp": t.temp,
+                 "virial": np.array(t.virial[:])} for t in th[:nth]]
+
+    def download(self):
+        x = np.zeros((self._n, 3))
+        v = np.zeros((self._n, 3))
+        f = np.zeros((self._n, 3))
+        self._ck(_lib.lmff_download(self._h, _p(x), _p(v), _p(f)))
+        return x, v, f
+
+    # -------------------------------------------------------------- batch
+    def batch_set(self, systems) -> None:
+        self._batch_keep = []
+        descs = (SystemDesc * len(systems))()
+        for k, s in enumerate(systems):
+            x = _f64(s.x)
+            t = np.ascontiguousarray(s.type, dtype=np.int32)
+            m = np.ascontiguousarray(s.mol, dtype=np.int64)
+            self._batch_keep += [x, t, m]
+            descs[k].natoms = s.n
+            descs[k].x = x.ctypes.data
+            descs[k].type = t.ctypes.data
+            descs[k].mol = m.ctypes.data
+            for c in range(3):
+                descs[k].lo[c] = float(s.box_lo[c])
+                descs[k].hi[c] = float(s.box_hi[c])
+                descs[k].periodic[c] = int(bool(s.periodic[c]))
+        self._batch_n = [s.n for s in systems]
+        self._ck(_lib.lmff_batch_set(self._h, len(systems), C.cast(descs, C.c_void_p)))
+
+    def batch_compute(self):
+        ntot = sum(self._batch_n)
+        f = np.zeros((ntot, 3))
+        res = (Result * len(self._batch_n))()
+        self._ck(_lib.lmff_batch_compute(self._h, _p(f), C.cast(res, C.c_void_p)))
+        out = []
+        o = 0
+        for k, n in enumerate(self._batch_n):
+            d = res[k].to_dict()
+            d["f"] = f[o:o + n]
+            o += n
+            out.append(d)
+        return out
+
+    # -------------------------------------------------------------- diagnostics
+    def stats(self) -> Dict:
+        s = Stats()
+        self._ck(_lib.lmff_get_stats(self._h, C.byref(s)))
+        out = {k: getattr(s, k) for k, _ in Stats._fields_}
+        out["kernel_ms"] = dict(zip(KERNELS, s.kernel_ms[:]))
+        out["kernel_launches"] = dict(zip(KERNELS, s.kernel_launches[:]))
+        return out
+
+    def export_list(self, which: int = 0) -> np.ndarray:
+        n = _lib.lmff_export_list(self._h, which, None, 0)
+        if n < 0:
+            self._ck(int(n))
+        out = np.zeros((n, 3), dtype=np.int64)
+        _lib.lmff_export_list(self._h, which, _p(out), n)
+        return out
+
+
+def device_count() -> int:
+    return int(load_library().lmff_device_count())

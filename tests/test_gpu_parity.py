@@ -1,0 +1,232 @@
+"""Parity of the CUDA engine (through the C ABI) with the reference and the oracle.
+
+Bars (max-norm relative unless stated):
+  FP64 drop-in   forces max and RMS <= 1e-10, per-style energies and pvector <= 1e-10,
+                 fdotr virial <= 1e-10, per-atom energy <= 1e-10 (of max |eatom|)
+  mixed          forces: max |dF| <= 1e-5 eV/A absolute; energies <= 1e-6 relative;
+                 virial <= 1e-5 relative
+  lists          bit-exact as sets (tag_i, tag_j, periodic image)
+"""
+import numpy as np
+import pytest
+from conftest import (GOLDEN_LISTS, GOLDEN_SINGLE, ILP, TERSOFF, load_golden, min_image, rel_max,
+                      rel_rms)
+
+from lmff_gb300 import build, capi
+from lmff_gb300 import structures as S
+
+pytestmark = pytest.mark.gpu
+
+F64_TOL = 1e-10
+MIX_F_ABS = 1e-5
+MIX_E_REL = 1e-6
+MIX_W_REL = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    build.build()
+
+
+def engine_for(g, precision=capi.FP64, **kw):
+    eng = capi.Engine(TERSOFF, ILP, cut_global=float(g["cut_global"]), tap_flag=int(g["tap_flag"]),
+                      skin=float(g["skin"]), precision=precision)
+    for k, v in kw.items():
+        eng.set_option(k, v)
+    eng.set_box(g["box_lo"], g["box_hi"], g["periodic"])
+    return eng
+
+
+def compute_golden(eng, g, **kw):
+    return eng.compute(g["x"], g["type"], g["mol"], g["tag"], eatom=True, **kw)
+
+
+@pytest.mark.parametrize("name", GOLDEN_SINGLE)
+def test_fp64_matches_reference(name):
+    g = load_golden(name)
+    r = compute_golden(engine_for(g), g)
+    assert rel_max(r["f"], g["f"]) <= F64_TOL
+    assert rel_rms(r["f"], g["f"]) <= F64_TOL
+    assert abs(r["e_tersoff"] - g["e_tersoff"]) <= F64_TOL * abs(g["e_tersoff"])
+    assert abs(r["e_ilp"] - g["e_ilp"]) <= F64_TOL * abs(g["e_ilp"])
+    assert rel_max(r["pvector"], g["pvector"]) <= F64_TOL
+    assert rel_max(r["virial"], g["virial"]) <= F64_TOL
+    assert rel_max(r["eatom"], g["eatom"]) <= F64_TOL
+
+
+@pytest.mark.parametrize("tpa", [4, 8, 32])
+def test_fp64_threads_per_atom_variants(tpa):
+    g = load_golden("hetero_small")
+    r = compute_golden(engine_for(g, tpa=tpa), g)
+    assert rel_max(r["f"], g["f"]) <= F64_TOL
+    assert rel_max(r["virial"], g["virial"]) <= F64_TOL
+
+
+def _set(a):
+    return set(map(tuple, np.asarray(a).reshape(-1, 3).tolist()))
+
+
+@pytest.mark.parametrize("name", GOLDEN_LISTS)
+def test_lists_match_reference(name):
+    g = load_golden(name)
+    eng = engine_for(g, list_full=1)
+    compute_golden(eng, g)
+    assert _set(eng.export_list(0)) == _set(g["nlist"])
+    assert _set(eng.export_list(1)) == _set(g["ilplist"])
+    # default (interlayer) pair list = the reference list restricted to mol_i != mol_j
+    eng2 = engine_for(g)
+    compute_golden(eng2, g)
+    mol = dict(zip(g["tag"].tolist(), g["mol"].tolist()))
+    ref = {t for t in _set(g["nlist"]) if mol[t[0]] != mol[t[1]]}
+    assert _set(eng2.export_list(0)) == ref
+
+
+@pytest.mark.parametrize("name", ["c1_t0", "hetero_small", "trilayer_alt", "edges", "tiny_images"])
+def test_mixed_precision_accuracy(name):
+    g = load_golden(name)
+    r = compute_golden(engine_for(g, precision=capi.MIXED), g)
+    assert np.abs(r["f"] - g["f"]).max() <= MIX_F_ABS
+    assert abs(r["e_tersoff"] - g["e_tersoff"]) <= MIX_E_REL * abs(g["e_tersoff"])
+    assert abs(r["e_ilp"] - g["e_ilp"]) <= MIX_E_REL * abs(g["e_ilp"])
+    assert rel_max(r["virial"], g["virial"]) <= MIX_W_REL
+
+
+def test_nve_trajectory_matches_reference():
+    """100 velocity-Verlet steps of the 7,200-atom bilayer, device resident, vs the
+    reference's own trajectory from the same start."""
+    g = load_golden("c1_t100")
+    eng = engine_for(g)
+    s = S.System(g["x0"], g["type"], g["mol"], g["tag"], g["box_lo"], g["box_hi"], g["periodic"].astype(bool),
+                 g["v0"])
+    eng.upload(s)
+    eng.run_nve(100, 0.001)
+    x, v, f = eng.download()
+    dx = min_image(x - g["x"], g["box_lo"], g["box_hi"], g["periodic"])
+    assert np.abs(dx).max() < 1e-9
+    assert rel_max(v, g["v"]) < 1e-8
+    assert rel_max(f, g["f"]) < 1e-8
+
+
+def test_nve_hetero_matches_reference():
+    g = load_golden("hetero_t20")
+    eng = engine_for(g)
+    s = S.System(g["x0"], g["type"], g["mol"], g["tag"], g["box_lo"], g["box_hi"], g["periodic"].astype(bool),
+                 g["v0"])
+    eng.upload(s)
+    eng.run_nve(20, 0.001)
+    x, v, f = eng.download()
+    dx = min_image(x - g["x"], g["box_lo"], g["box_hi"], g["periodic"])
+    assert np.abs(dx).max() < 1e-9
+    assert rel_max(f, g["f"]) < 1e-8
+
+
+def test_deterministic_bitwise():
+    g = load_golden("hetero_small")
+    e1 = compute_golden(engine_for(g), g)
+    e2 = compute_golden(engine_for(g), g)
+    assert np.array_equal(e1["f"], e2["f"])
+    assert e1["e_ilp"] == e2["e_ilp"] and np.array_equal(e1["virial"], e2["virial"])
+
+
+def test_same_atoms_fast_path_and_identity_change():
+    g = load_golden("bilayer_small")
+    eng = engine_for(g)
+    r0 = compute_golden(eng, g)
+    r1 = eng.compute(g["x"], g["type"], g["mol"], g["tag"], same_atoms=True, eatom=True)
+    assert np.array_equal(r0["f"], r1["f"])
+    # permuted atom order: identity check notices and reloads
+    p = np.random.default_rng(0).permutation(len(g["tag"]))
+    r2 = eng.compute(g["x"][p], g["type"][p], g["mol"][p], g["tag"][p])
+    assert rel_max(r2["f"], g["f"][p]) <= F64_TOL
+
+
+def test_force_accumulates():
+    g = load_golden("bilayer_small")
+    eng = engine_for(g)
+    f = np.ones((len(g["tag"]), 3))
+    r = eng.compute(g["x"], g["type"], g["mol"], g["tag"], f=f)
+    assert rel_max(r["f"] - 1.0, g["f"]) <= F64_TOL
+
+
+def test_batch_equals_single():
+    systems = S.replica_set(count=4, nmin=500, nmax=3000, seed=9)
+    systems = [S.displace(s, 0.03, seed=k) for k, s in enumerate(systems)]
+    eng = capi.Engine(TERSOFF, ILP)
+    eng.batch_set(systems)
+    out = eng.batch_compute()
+    for s, b in zip(systems, out):
+        single = capi.Engine(TERSOFF, ILP).compute_system(s)
+        assert np.array_equal(b["f"], single["f"])
+        assert b["e_ilp"] == single["e_ilp"] and b["e_tersoff"] == single["e_tersoff"]
+
+
+def _oracle_vs_engine(s, precision=capi.FP64, tap=1):
+    from oracle import Oracle
+    o = Oracle(TERSOFF, ILP, tap_flag=tap, nthreads=8)
+    o.set_system(s)
+    ref = o.forces(eatom=True)
+    eng = capi.Engine(TERSOFF, ILP, tap_flag=tap, precision=precision)
+    got = eng.compute_system(s, eatom=True)
+    return ref, got
+
+
+@pytest.mark.parametrize("seed", [101, 102, 103])
+def test_fp64_vs_oracle_random_heterostructures(seed):
+    rng = np.random.default_rng(seed)
+    top = ["hbn", "graphene"][seed % 2]
+    s = S.twisted_bilayer(int(rng.integers(8, 14)), int(rng.integers(5, 9)), float(rng.uniform(0, 5)), top=top,
+                          spacing=float(rng.uniform(3.2, 3.6)), shift=tuple(rng.uniform(0, 2, 2)))
+    s = S.displace(s, 0.05, seed=seed)
+    ref, got = _oracle_vs_engine(s)
+    assert rel_max(got["f"], ref["f"]) <= F64_TOL
+    assert abs(got["e_ilp"] - ref["e_ilp"]) <= F64_TOL * abs(ref["e_ilp"])
+    assert abs(got["e_tersoff"] - ref["e_tersoff"]) <= F64_TOL * abs(ref["e_tersoff"])
+    assert rel_max(got["virial"], ref["virial"]) <= F64_TOL
+    assert rel_max(got["eatom"], ref["eatom"]) <= F64_TOL
+
+
+def test_fp64_vs_oracle_graphite_unique_mols():
+    s = S.displace(S.graphite_slab(5, 10, 6, mol_mode="unique"), 0.04, seed=7)
+    ref, got = _oracle_vs_engine(s)
+    assert rel_max(got["f"], ref["f"]) <= F64_TOL
+    assert rel_max(got["virial"], ref["virial"]) <= F64_TOL
+
+
+def test_too_many_ilp_neighbours_is_reported():
+    s = S.ab_bilayer_graphene(8, 5)
+    # a fourth intralayer neighbour within 2 A of atom 0
+    x = np.vstack([s.x, s.x[0] + np.array([0.0, -1.3, 0.0])])
+    s2 = S.System(x, np.append(s.type, 1), np.append(s.mol, 1), np.arange(1, len(x) + 1), s.box_lo, s.box_hi,
+                  s.periodic)
+    eng = capi.Engine(TERSOFF, ILP)
+    with pytest.raises(capi.LmffError) as ei:
+        eng.compute_system(s2)
+    assert ei.value.code == -4 and "too many neighbors" in str(ei.value)
+
+
+def test_newton_third_law_and_translation_invariance_large():
+    """Size-independent properties on a 97k-atom graphite slab (FP64 and mixed)."""
+    s = S.displace(S.graphite_slab(6, 60, 34, mol_mode="alternate"), 0.03, seed=3)
+    for prec in (capi.FP64, capi.MIXED):
+        eng = capi.Engine(TERSOFF, ILP, precision=prec)
+        r = eng.compute_system(s)
+        ftot = r["f"].sum(0)
+        if prec == capi.FP64:
+            assert np.abs(ftot).max() <= 1e-9 * np.abs(r["f"]).sum(0).max()
+        else:   # per-atom FP32 rounding does not cancel between the two ends of a pair
+            assert np.abs(ftot).max() <= MIX_F_ABS * np.sqrt(s.n)
+        s2 = s.copy()
+        s2.x = s2.x + np.array([0.37, -1.1, 0.25])
+        s2.box_lo = s2.box_lo + np.array([0.37, -1.1, 0.25])
+        s2.box_hi = s2.box_hi + np.array([0.37, -1.1, 0.25])
+        r2 = capi.Engine(TERSOFF, ILP, precision=prec).compute_system(s2)
+        tol = 1e-10 if prec == capi.FP64 else 1e-5
+        assert np.abs(r2["f"] - r["f"]).max() <= tol * max(1.0, np.abs(r["f"]).max())
+
+
+def test_mixed_vs_fp64_large():
+    s = S.displace(S.graphite_slab(4, 60, 34, mol_mode="unique"), 0.03, seed=4)
+    r64 = capi.Engine(TERSOFF, ILP).compute_system(s)
+    r32 = capi.Engine(TERSOFF, ILP, precision=capi.MIXED).compute_system(s)
+    assert np.abs(r32["f"] - r64["f"]).max() <= MIX_F_ABS
+    assert abs(r32["e_ilp"] - r64["e_ilp"]) <= MIX_E_REL * abs(r64["e_ilp"])

@@ -174,6 +174,27 @@ int lmff_compute_device(lmff_engine *e, int natoms, const double *d_x, const int
                         const int64_t *d_mol, const int64_t *d_tag, int which, int eflag,
                         int vflag, double *d_f, lmff_result *res);
 
+/* Allocation-free variant of lmff_compute_device for one small system.  No counterpart
+ * in the reference: it exists for callers that must not allocate device memory once
+ * they run -- an application that hands all GPU memory to its own pool at start-up,
+ * or code on a path where cudaMalloc would synchronise the device or is not allowed.
+ * The caller passes device inputs (d_x[natoms*3], d_type, d_mol, all required) and the
+ * output d_f[natoms*3], which is overwritten; energies and virials go to res.  Nothing
+ * is allocated: every buffer the kernels need (sorted atoms, bins, neighbour lists,
+ * normals, force slots, reductions, sort workspace) lives in one 16 MiB static device
+ * array that every GPU loading this library holds until the process exits.  Limits:
+ * natoms <= 2048, at most 8192 neighbour bins, and the pair list must fit the space
+ * left in the array (about 1,600 entries per atom at 2048 atoms); larger requests are
+ * rejected with LMFF_EINVAL or LMFF_EOVERFLOW and a message, never truncated.  The
+ * engine handle supplies parameters, box, precision and stream.  The first call on a
+ * device looks the array's device address up (cudaGetSymbolAddress), so make that
+ * first call before capturing any stream.  All calls share the one array and it keeps
+ * the previous call's contents: calls that can overlap on the GPU (several streams,
+ * threads or handles) race and must be serialised by the caller. */
+int lmff_compute_device_noalloc(lmff_engine *e, int natoms, const double *d_x, const int *d_type,
+                                const int64_t *d_mol, int which, int eflag, int vflag, double *d_f,
+                                lmff_result *res);
+
 /* ---- device-resident system (standalone MD) ---------------------------------------- */
 /* mass[t-1] is the mass of type t (amu); v may be NULL (zero). */
 int lmff_upload(lmff_engine *e, int natoms, const double *x, const double *v, const int *type,

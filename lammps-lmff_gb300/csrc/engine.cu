@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <array>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -321,6 +322,11 @@ struct Engine {
     err = std::string(where) + ": " + cudaGetErrorString(e);
     return LMFF_ECUDA;
   }
+#define CK2(expr)                                                  \
+  do {                                                             \
+    cudaError_t _e = (expr);                                       \
+    if (_e != cudaSuccess) return g.cuda_fail(_e, #expr);          \
+  } while (0)
 #define CK(expr)                                    \
   do {                                              \
     cudaError_t _e = (expr);                        \
@@ -1322,6 +1328,268 @@ struct Engine {
   }
 };
 
+// =========================================================== allocation-free call
+// lmff_compute_device_noalloc: the force evaluation of one small system for callers
+// that may not allocate device memory once they are running -- for example an
+// application that reserves all GPU memory up front for its own pool, or code that
+// must not call cudaMalloc where an allocation would synchronise the device or is
+// forbidden.  Every buffer the kernels need beyond the caller's inputs and outputs
+// comes from one file-scope device array, g_noalloc_scratch, of NOALLOC_BYTES.  The
+// array is part of the module image: every GPU that loads this library holds it until
+// the process exits.  All calls share it and it keeps the last call's contents, so
+// calls that overlap on the GPU (two streams, two host threads, two engine handles)
+// race and must be serialised by the caller.
+
+constexpr size_t NOALLOC_BYTES = (size_t)16 << 20;   // 16 MiB
+constexpr int NOALLOC_MAX_ATOMS = 2048;
+constexpr int NOALLOC_MAX_BINS = 8192;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+// Device address of g_noalloc_scratch, looked up once per device with that device
+// current (in host code the symbol name is only a stand-in, never a device address).
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_base[64] = {nullptr};
+
+static int noalloc_base(int device, void **base, std::string &err) {
+  if (device < 0 || device >= 64) {
+    err = "device ordinal out of range";
+    return LMFF_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_base[device]) {
+    void *ptr = nullptr;
+    cudaError_t rc = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (rc != cudaSuccess || !ptr) {
+      err = std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(rc);
+      return LMFF_ECUDA;
+    }
+    g_noalloc_base[device] = ptr;
+  }
+  *base = g_noalloc_base[device];
+  return LMFF_OK;
+}
+
+// bump carving of the scratch array, 256-byte aligned pieces
+struct Carve {
+  unsigned char *p, *end;
+  template <class T>
+  T *take(size_t count) {
+    size_t bytes = (count * sizeof(T) + 255) & ~(size_t)255;
+    if (p + bytes > end) return nullptr;
+    T *r = (T *)p;
+    p += bytes;
+    return r;
+  }
+};
+
+int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const int64_t *dmol, int which, int eflag,
+                    int vflag, double *df, lmff_result *res) {
+  if (nn < 1 || nn > NOALLOC_MAX_ATOMS)
+    return g.fail(LMFF_EINVAL, "lmff_compute_device_noalloc: natoms must be in 1.." +
+                                   std::to_string(NOALLOC_MAX_ATOMS) + " (got " + std::to_string(nn) + ")");
+  if (!g.have_box) return g.fail(LMFF_EINVAL, "lmff_set_box must be called first");
+  void *basev = nullptr;
+  int rc = noalloc_base(g.device, &basev, g.err);
+  if (rc) return rc;
+  rc = g.push_consts();
+  if (rc) return rc;
+  cudaStream_t st = g.stream;
+  // geometry of the one system (same binning rules as the resident path)
+  SysDesc sd;
+  memset(&sd, 0, sizeof sd);
+  double target = 0.5 * g.cutneigh_max * 1.0001, maxL = 0.0;
+  int R = 0;
+  for (int k = 0; k < 3; k++) {
+    sd.lo[k] = g.blo[k];
+    sd.L[k] = g.bhi[k] - g.blo[k];
+    sd.per[k] = g.bper[k];
+    int nb = std::max(1, (int)std::floor(sd.L[k] / target));
+    if (nb > 4096) nb = 4096;
+    double bs = sd.L[k] / nb;
+    sd.nb[k] = nb;
+    sd.binv[k] = 1.0 / bs;
+    sd.reach[k] = (int)std::ceil(g.cutneigh_max / bs * (1.0 + 1e-12));
+    if (sd.per[k]) R = std::max(R, (sd.reach[k] + nb - 1) / nb);
+    sd.Lhi[k] = (float)sd.L[k];
+    sd.Llo[k] = (float)(sd.L[k] - (double)sd.Lhi[k]);
+    maxL = std::max(maxL, sd.L[k]);
+  }
+  sd.base = std::ldexp(1.0, (int)std::ceil(std::log2(maxL + 64.0)));
+  sd.atom_begin = 0;
+  sd.atom_end = nn;
+  long long nbins = (long long)sd.nb[0] * sd.nb[1] * sd.nb[2];
+  if (nbins > NOALLOC_MAX_BINS)
+    return g.fail(LMFF_EINVAL, "lmff_compute_device_noalloc: box needs " + std::to_string(nbins) +
+                                   " bins, more than the limit of " + std::to_string(NOALLOC_MAX_BINS));
+  ListCode lc;
+  lc.R = R;
+  lc.w = 1;
+  while ((1 << lc.w) < 2 * R + 1) lc.w++;
+  lc.ibits = 32 - 3 * lc.w;
+  lc.imask = (1u << lc.ibits) - 1u;
+  lc.wmask = (1u << lc.w) - 1u;
+  int nbits = 1;
+  while ((1LL << nbits) < nbins) nbits++;
+  // carve the scratch array
+  const int c = NOALLOC_MAX_ATOMS;
+  Carve cv{(unsigned char *)basev, (unsigned char *)basev + NOALLOC_BYTES};
+  d4 *xq = cv.take<d4>(c), *xq2 = cv.take<d4>(c), *nrm64 = cv.take<d4>(c), *ilp_g = cv.take<d4>(c);
+  float4 *xh = cv.take<float4>(c), *xl = cv.take<float4>(c), *nrm32 = cv.take<float4>(c);
+  double *v = cv.take<double>(3 * c), *v2 = cv.take<double>(3 * c), *mass = cv.take<double>(c),
+         *mass2 = cv.take<double>(c);
+  int64_t *tag = cv.take<int64_t>(c), *tag2 = cv.take<int64_t>(c);
+  int *perm = cv.take<int>(c), *perm2 = cv.take<int>(c), *sysid = cv.take<int>(c), *sysid2 = cv.take<int>(c);
+  int *ilp_cnt = cv.take<int>(c), *ters_cnt = cv.take<int>(c), *short_cnt = cv.take<int>(c);
+  uint32_t *ilp_nb = cv.take<uint32_t>((size_t)c * MAXILP), *ters_nb = cv.take<uint32_t>((size_t)c * MAXTERS);
+  uint32_t *short_nb = cv.take<uint32_t>((size_t)c * MAXSHORT);
+  d4 *ters_g = cv.take<d4>((size_t)c * MAXTERS), *ilp_c = cv.take<d4>((size_t)c * MAXILP);
+  double *ters_f = cv.take<double>(3 * c), *ilp_f = cv.take<double>(3 * c), *fs = cv.take<double>(3 * c);
+  double *stat_ilp = cv.take<double>(8 * c), *stat_ters = cv.take<double>(8 * c);
+  double *eat_i = cv.take<double>(c), *eat_t = cv.take<double>(c);
+  int64_t *list_off = cv.take<int64_t>(c + 1), *cnt = cv.take<int64_t>(c + 1);
+  uint32_t *key = cv.take<uint32_t>(c), *key2 = cv.take<uint32_t>(c);
+  int *idx = cv.take<int>(c), *idx2 = cv.take<int>(c);
+  int *bin_start = cv.take<int>(NOALLOC_MAX_BINS), *bin_end = cv.take<int>(NOALLOC_MAX_BINS);
+  SysDesc *dsys = cv.take<SysDesc>(1);
+  double *red = cv.take<double>(16);
+  double **arrs = cv.take<double *>(2);
+  int *status = cv.take<int>(1);
+  size_t tmp_bytes = nb_sort_tmp_bytes(c, 32);
+  void *tmp = cv.take<unsigned char>(tmp_bytes);
+  if (!tmp) return g.fail(LMFF_EOVERFLOW, "lmff_compute_device_noalloc: scratch layout does not fit");
+  size_t list_cap = (size_t)(cv.end - cv.p) / sizeof(uint32_t);
+  uint32_t *list = cv.take<uint32_t>(list_cap);
+  // what must start at zero: status word, bin ranges, the count past the last atom
+  const double *host_arrs[2] = {stat_ilp, stat_ters};
+  CK2(cudaMemsetAsync(status, 0, sizeof(int), st));
+  CK2(cudaMemsetAsync(bin_start, 0, sizeof(int) * nbins, st));
+  CK2(cudaMemsetAsync(bin_end, 0, sizeof(int) * nbins, st));
+  CK2(cudaMemsetAsync(cnt + nn, 0, sizeof(int64_t), st));
+  CK2(cudaMemcpyAsync(dsys, &sd, sizeof sd, cudaMemcpyHostToDevice, st));
+  CK2(cudaMemcpyAsync(arrs, host_arrs, sizeof host_arrs, cudaMemcpyHostToDevice, st));
+  int gb = (nn + 255) / 256;
+  k_load<<<gb, 256, 0, st>>>(nn, dx, dtype, dmol, nullptr, nullptr, nullptr, nullptr, xq, tag, perm, sysid, v, mass);
+  nb_wrap_bin(nn, xq, dsys, sysid, key, idx, st);
+  CK2(nb_sort(tmp, tmp_bytes, key, key2, idx, idx2, nn, nbits, st));
+  nb_permute(nn, idx2, xq, xq2, v, v2, tag, tag2, perm, perm2, sysid, sysid2, mass, mass2, st);
+  nb_bin_ranges(nn, key2, bin_start, bin_end, st);
+  nb_hilo(nn, xq2, dsys, sysid2, xh, xl, st);
+  NbArgs na;
+  memset(&na, 0, sizeof na);
+  na.n = nn;
+  na.xq = xq2;
+  na.xh = xh;
+  na.xl = xl;
+  na.sys = dsys;
+  na.sysid = sysid2;
+  na.bin_start = bin_start;
+  na.bin_end = bin_end;
+  na.list_off = list_off;
+  na.list = list;
+  na.list_cap = (int64_t)list_cap;
+  na.cnt = cnt;
+  na.short_cnt = short_cnt;
+  na.short_nb = short_nb;
+  na.lc = lc;
+  na.full = g.list_full;
+  na.status = status;
+  nb_list(na, false, st);
+  CK2(nb_scan(tmp, tmp_bytes, cnt, list_off, nn, st));
+  int64_t total = 0;
+  CK2(cudaMemcpyAsync(&total, list_off + nn, sizeof total, cudaMemcpyDeviceToHost, st));
+  CK2(cudaStreamSynchronize(st));
+  if (total < 0 || (size_t)total > list_cap)
+    return g.fail(LMFF_EOVERFLOW, "lmff_compute_device_noalloc: pair list of " + std::to_string(total) +
+                                      " entries exceeds the scratch capacity of " + std::to_string(list_cap));
+  nb_list(na, true, st);
+  auto fill = [&](auto &a) {
+    memset(&a, 0, sizeof a);
+    a.A.xq = xq2;
+    a.A.xh = xh;
+    a.A.xl = xl;
+    a.A.sys = dsys;
+    a.A.sysid = sysid2;
+    a.lc = lc;
+    a.n = nn;
+    a.tag = tag2;
+    a.list_off = list_off;
+    a.list = list;
+    a.short_cnt = short_cnt;
+    a.short_nb = short_nb;
+    a.ilp_cnt = ilp_cnt;
+    a.ilp_nb = ilp_nb;
+    a.ters_cnt = ters_cnt;
+    a.ters_nb = ters_nb;
+    a.nrm64 = nrm64;
+    a.nrm32 = nrm32;
+    a.ters_g = ters_g;
+    a.ters_f = ters_f;
+    a.ilp_f = ilp_f;
+    a.ilp_c = ilp_c;
+    a.ilp_g = ilp_g;
+    a.stat_ilp = stat_ilp;
+    a.stat_ters = stat_ters;
+    a.eatom_ilp = eat_i;
+    a.eatom_ters = eat_t;
+    a.f_out = fs;
+    a.status = status;
+    a.do_ters = g.t_on && (which & LMFF_TERSOFF);
+    a.do_ilp = g.i_on && (which & LMFF_ILP);
+  };
+  const bool ev = true;
+  if (g.precision == LMFF_FP64) {
+    ForceArgs<double> a;
+    fill(a);
+    f64::launch_short(a, g.d_cutILPsq, g.ht.cutmax * g.ht.cutmax, st);
+    if (a.do_ters) f64::launch_tersoff(a, ev, false, st);
+    else CK2(cudaMemsetAsync(stat_ters, 0, sizeof(double) * 8 * (size_t)nn, st));
+    if (a.do_ilp) {
+      f64::launch_ilp(a, ev, false, g.tpa, g.block, st);
+      f64::launch_nderiv(a, ev, st);
+    } else {
+      CK2(cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)nn, st));
+    }
+    f64::launch_finish(a, false, st);
+  } else {
+    ForceArgs<float> a;
+    fill(a);
+    f32::launch_short(a, g.d_cutILPsq, g.ht.cutmax * g.ht.cutmax, st);
+    if (a.do_ters) f32::launch_tersoff(a, ev, false, st);
+    else CK2(cudaMemsetAsync(stat_ters, 0, sizeof(double) * 8 * (size_t)nn, st));
+    if (a.do_ilp) {
+      f32::launch_ilp(a, ev, false, g.tpa, g.block, st);
+      f32::launch_nderiv(a, ev, st);
+    } else {
+      CK2(cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)nn, st));
+    }
+    f32::launch_finish(a, false, st);
+  }
+  k_reduce<<<16, 256, 0, st>>>(nn, 16, (const double *const *)arrs, dsys, red);
+  k_scatter_add<<<gb, 256, 0, st>>>(nn, perm2, fs, df, 1);
+  CK2(cudaGetLastError());
+  double hred[16];
+  int hst = 0;
+  CK2(cudaMemcpyAsync(hred, red, sizeof hred, cudaMemcpyDeviceToHost, st));
+  CK2(cudaMemcpyAsync(&hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
+  CK2(cudaStreamSynchronize(st));
+  if (hst & ST_TOO_MANY_ILP)
+    return g.fail(LMFF_ETOO_MANY_ILP_NEIGH, "There are too many neighbors for some atoms, please check your configuration");
+  if (hst & ST_ZERO_NORMAL) return g.fail(LMFF_EZERO_NORMAL, "The magnitude of the normal vector is zero");
+  if (hst) return g.fail(LMFF_EOVERFLOW, "lmff_compute_device_noalloc: neighbour capacity exceeded");
+  if (res) {
+    memset(res, 0, sizeof *res);
+    if (eflag || vflag) {
+      res->pvector[0] = hred[0];
+      res->pvector[1] = hred[1];
+      res->e_ilp = hred[0] + hred[1];
+      for (int k = 0; k < 6; k++) res->virial_ilp[k] = hred[2 + k];
+      res->e_tersoff = hred[8];
+      for (int k = 0; k < 6; k++) res->virial_tersoff[k] = hred[10 + k];
+    }
+  }
+  return LMFF_OK;
+}
+
 }  // namespace lmff
 
 using lmff::Engine;
@@ -1474,6 +1742,15 @@ int lmff_compute_device(lmff_engine *e, int natoms, const double *d_x, const int
   if (!e || natoms < 0 || (natoms > 0 && (!d_x || !d_type))) return LMFF_EINVAL;
   cudaSetDevice(e->e.device);
   return e->e.compute_device(natoms, d_x, d_type, d_mol, d_tag, which, eflag, vflag, d_f, res);
+}
+
+int lmff_compute_device_noalloc(lmff_engine *e, int natoms, const double *d_x, const int *d_type,
+                                const int64_t *d_mol, int which, int eflag, int vflag, double *d_f, lmff_result *res) {
+  if (!e || !d_x || !d_type || !d_f) return LMFF_EINVAL;
+  if (!d_mol) return e->e.fail(LMFF_EINVAL, "lmff_compute_device_noalloc: d_mol is required");
+  cudaError_t rc = cudaSetDevice(e->e.device);
+  if (rc != cudaSuccess) return e->e.cuda_fail(rc, "cudaSetDevice");
+  return lmff::noalloc_compute(e->e, natoms, d_x, d_type, d_mol, which, eflag, vflag, d_f, res);
 }
 
 int lmff_upload(lmff_engine *e, int natoms, const double *x, const double *v, const int *type, const int64_t *mol,

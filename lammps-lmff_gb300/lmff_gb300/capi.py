@@ -91,6 +91,7 @@ def load_library(path: str = LIB_PATH):
         "lmff_set_option": ([P, C.c_char_p, D], I),
         "lmff_compute": ([P, I, P, P, P, P, I, I, I, P, P, C.POINTER(Result)], I),
         "lmff_compute_device": ([P, I, P, P, P, P, I, I, I, P, C.POINTER(Result)], I),
+        "lmff_compute_device_noalloc": ([P, I, P, P, P, I, I, I, P, C.POINTER(Result)], I),
         "lmff_upload": ([P, I, P, P, P, P, P, P], I),
         "lmff_compute_resident": ([P, I, I, I, C.POINTER(Result)], I),
         "lmff_run_nve": ([P, I, D, I, P], I),
@@ -201,6 +202,15 @@ class Engine:
                                           mol.data_ptr() if mol is not None else None,
                                           tag.data_ptr() if tag is not None else None, flags, int(eflag),
                                           int(vflag), f.data_ptr(), C.byref(r)))
+        return r.to_dict()
+
+    def compute_device_noalloc(self, x, type_, mol, f, which: int = TERSOFF | ILP, eflag=True, vflag=True) -> Dict:
+        """Allocation-free evaluation (lmff_compute_device_noalloc) on torch CUDA tensors:
+        x float64 [n,3], type int32 [n], mol int64 [n], f float64 [n,3] (overwritten)."""
+        r = Result()
+        self._ck(_lib.lmff_compute_device_noalloc(self._h, int(x.shape[0]), x.data_ptr(), type_.data_ptr(),
+                                                  mol.data_ptr(), which, int(eflag), int(vflag), f.data_ptr(),
+                                                  C.byref(r)))
         return r.to_dict()
 
     # -------------------------------------------------------------- resident MD

@@ -57,6 +57,8 @@ def workload(name: str):
         s = S.ab_bilayer_graphene(30, 30)
     elif name == "graphite_small":
         s = S.graphite_slab(10, 40, 23, spacing=3.35, mol_mode="alternate")
+    elif name == "graphite_330k":
+        s = S.graphite_slab(10, 120, 69, spacing=3.35, mol_mode="alternate")
     else:
         raise SystemExit(f"unknown workload {name}")
     return S.thermalize(s, 300.0, seed=3)
@@ -202,10 +204,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="graphite_2p7m")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--tpa", type=int, default=16)
+    ap.add_argument("--tpa", type=int, default=0, help="threads per atom (0: autotune)")
+    ap.add_argument("--block", type=int, default=0, help="threads per block (0: autotune)")
+    ap.add_argument("--skin", type=float, default=0.0, help="neighbour skin in A (0: autotune)")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-peak", action="store_true", help="skip the cuBLAS peak measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -235,8 +240,21 @@ def main():
 
     s = workload(args.workload)
     prec = capi.MIXED if args.precision == "mixed" else capi.FP64
-    eng = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=prec)
+    # pure carbon: one atom type mapped to C (pair_coeff * * <style> <file> C)
+    elements = ("C",) if set(np.unique(s.type)) == {1} else ("C", "B", "N")
+    tuned = None
+    if not (args.tpa and args.block and args.skin):
+        from lmff_gb300 import tune
+        probe = workload("graphite_330k") if args.workload == "graphite_2p7m" else s
+        tuned = tune.tune(probe, TERSOFF_FILE, ILP_FILE, elements=elements, precision=prec, device=local,
+                          tpas=(8, 16, 32), blocks=(128, 256), skins=(1.0, 2.0), use_cache=False, n_full=s.n)
+        args.tpa = args.tpa or tuned["tpa"]
+        args.block = args.block or tuned["block"]
+        args.skin = args.skin or tuned["skin"]
+    eng = capi.Engine(TERSOFF_FILE, ILP_FILE, elements=elements, device=local, precision=prec)
     eng.set_option("tpa", args.tpa)
+    eng.set_option("block", args.block)
+    eng.set_option("skin", args.skin)
     eng.upload(s)
     eng.run_nve(args.warmup, 0.001)
     eng.set_option("count_pairs", 1)
@@ -281,8 +299,10 @@ def main():
         fb = torch.empty((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
         xa[:] = s.x
         xb[:] = s.x + np.random.default_rng(1).normal(0.0, 0.01, s.x.shape)
-        eng2 = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=prec)
+        eng2 = capi.Engine(TERSOFF_FILE, ILP_FILE, elements=elements, device=local, precision=prec)
         eng2.set_option("tpa", args.tpa)
+        eng2.set_option("block", args.block)
+        eng2.set_option("skin", args.skin)
         eng2.set_box(s.box_lo, s.box_hi, s.periodic)
         eng2.compute(xa, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb, overwrite=True)
         eng2.compute(xb, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb, overwrite=True, same_atoms=True)
@@ -300,7 +320,7 @@ def main():
 
     peaks = measured_peaks()
     peak_name = "fp32" if prec == capi.MIXED else "fp64"
-    peak = fp_peak_tflops(peak_name) if rank == 0 else 0.0
+    peak = fp_peak_tflops(peak_name) if (rank == 0 and not args.no_peak) else 0.0
     achieved = flops / k_avg / 1e12
     roofline = {"bound": peak_name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None, "traffic": None,
@@ -325,7 +345,11 @@ def main():
                 "vs_baseline": None, "dtype": "f32" if prec == capi.MIXED else "f64", "data": "synthetic",
                 "config": {"workload": "10-layer AB graphite slab, 2,694,960 atoms, 300 K NVE dt 1 fs"
                            if args.workload == "graphite_2p7m" else args.workload,
-                           "natoms": s.n, "precision": args.precision, "tpa": args.tpa,
+                           "natoms": s.n, "precision": args.precision, "tpa": args.tpa, "block": args.block,
+                           "skin": args.skin, "elements": list(elements),
+                           "autotune": None if tuned is None else {
+                               "probe_atoms": tuned["probe_atoms"], "picked": [tuned["tpa"], tuned["block"], tuned["skin"]],
+                               "score_ms_probe": tuned["score_ms"]},
                            "l2": "inputs larger than L2 (pair list ~15 GB), no flush",
                            "parallelism": f"replicas x{world}", "wall_s": wall},
                 "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,

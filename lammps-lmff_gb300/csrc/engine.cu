@@ -33,7 +33,8 @@ namespace lmff {
   void upload_pot(const PotConst<R> &p, cudaStream_t s);                                                   \
   void launch_short(const ForceArgs<R> &a, const double *cutILPsq64, double tcutmaxsq64, cudaStream_t s); \
   void launch_tersoff(const ForceArgs<R> &a, bool ev, bool eatom, cudaStream_t s);                        \
-  void launch_ilp(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, cudaStream_t s);         \
+  void launch_ilp(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, bool one_element,       \
+                  cudaStream_t s);                                                                         \
   void launch_nderiv(const ForceArgs<R> &a, bool ev, cudaStream_t s);                                      \
   void launch_finish(const ForceArgs<R> &a, bool eatom, cudaStream_t s);                                   \
   }
@@ -227,6 +228,7 @@ struct Engine {
   HostTersoff ht;
   HostIlp hi;
   bool t_on = false, i_on = false;
+  bool i_one = false;  // ILP maps every type to one element
   double cut_global = 16.0;
   int tap = 1;
   PotConst<double> pot64;
@@ -392,6 +394,7 @@ struct Engine {
       hi.cutILPsq.assign(p->ilp_cutILPsq, p->ilp_cutILPsq + ne * ne);
       hi.elements.resize(ne);
     }
+    i_one = i_on && p->ilp_nelements == 1;
     cut_global = p->ilp_cut_global;
     tap = p->ilp_tap_flag;
     skin = p->skin;
@@ -411,6 +414,9 @@ struct Engine {
       P.i_map[t] = (i_on && t >= 1 && t <= ntypes) ? hi.map[t] : -1;
     }
     P.tap = tap;
+    P.ilp_typemask = 0;
+    for (int t = 1; t <= ntypes && t < 32; t++)
+      if (P.i_map[t] >= 0) P.ilp_typemask |= 1u << t;
     P.vdw_sym = 1;
     P.rep_sym = 1;
     P.t_cutmaxsq = (R)(ht.cutmax * ht.cutmax);
@@ -864,7 +870,7 @@ struct Engine {
     if (a.do_ters) timed(1, [&] { ft(a, ev, eatom, stream); });
     else if (ev) cudaMemsetAsync(stat_ters, 0, sizeof(double) * 8 * (size_t)n, stream);
     if (a.do_ilp) {
-      timed(0, [&] { fi(a, ev, eatom, tpa, block, stream); });
+      timed(0, [&] { fi(a, ev, eatom, tpa, block, i_one, stream); });
       timed(2, [&] { fn(a, ev, stream); });
     }
     else if (ev) cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)n, stream);
@@ -1544,7 +1550,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
     if (a.do_ters) f64::launch_tersoff(a, ev, false, st);
     else CK2(cudaMemsetAsync(stat_ters, 0, sizeof(double) * 8 * (size_t)nn, st));
     if (a.do_ilp) {
-      f64::launch_ilp(a, ev, false, g.tpa, g.block, st);
+      f64::launch_ilp(a, ev, false, g.tpa, g.block, g.i_one, st);
       f64::launch_nderiv(a, ev, st);
     } else {
       CK2(cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)nn, st));
@@ -1557,7 +1563,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
     if (a.do_ters) f32::launch_tersoff(a, ev, false, st);
     else CK2(cudaMemsetAsync(stat_ters, 0, sizeof(double) * 8 * (size_t)nn, st));
     if (a.do_ilp) {
-      f32::launch_ilp(a, ev, false, g.tpa, g.block, st);
+      f32::launch_ilp(a, ev, false, g.tpa, g.block, g.i_one, st);
       f32::launch_nderiv(a, ev, st);
     } else {
       CK2(cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)nn, st));

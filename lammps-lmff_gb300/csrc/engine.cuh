@@ -72,6 +72,7 @@ struct PotConst {
   int tap;
   int vdw_sym;                // vdW constants symmetric in (i,j) for every pair
   int rep_sym;                // Tersoff repulsion constants of (i,j,j) equal those of (j,i,i)
+  unsigned ilp_typemask;      // bit t set when atom type t is mapped to an ILP element
   R t_cutmaxsq;
   R i_cutsq;                  // cut_global^2
   R i_inv_rcut;               // 1 / cut_global

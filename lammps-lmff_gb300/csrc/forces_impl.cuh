@@ -415,7 +415,9 @@ __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
 // Lane 0 of the group then applies the normal derivatives of i (calc_normal's dnormdri
 // and dnormal, :893-926 / :1043-1067) to g_i in FP64: the force on i itself and the
 // force on each intralayer neighbour (ilp_c slots).
-template <int TPA, bool EV, bool EATOM>
+// ONE: every ILP-mapped type is the same element, so the pair parameters are read at a
+// compile-time constant index (constant-bank operands, no per-pair loads).
+template <int TPA, bool EV, bool EATOM, bool ONE>
 __global__ void __launch_bounds__(256) k_ilp(ForceArgs<R> a) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gtid / TPA;
@@ -435,6 +437,14 @@ __global__ void __launch_bounds__(256) k_ilp(ForceArgs<R> a) {
   R fx = 0, fy = 0, fz = 0, gxa = 0, gya = 0, gza = 0;
   R evdw = 0, erep = 0, w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
   const R cutsq = c_pot.i_cutsq;
+  const unsigned tmask = c_pot.ilp_typemask;
+  SysDesc sdl;  // box of i's system in registers for the image shifts
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    sdl.L[d] = sd.L[d];
+    sdl.Lhi[d] = sd.Lhi[d];
+    sdl.Llo[d] = sd.Llo[d];
+  }
   if (valid && ie >= 0) {
     const int64_t b = a.list_off[i], end = a.list_off[i + 1];
     for (int64_t k = b + lane; k < end; k += TPA) {
@@ -443,14 +453,15 @@ __global__ void __launch_bounds__(256) k_ilp(ForceArgs<R> a) {
       decode_entry(e, a.lc, j, sx, sy, sz);
       R dx, dy, dz;
       long long jinfo;
-      ai.disp(a.A, sd, j, sx, sy, sz, dx, dy, dz, jinfo);
+      ai.disp(a.A, sdl, j, sx, sy, sz, dx, dy, dz, jinfo);
       R rsq = dx * dx + dy * dy + dz * dz;
       if (!(rsq < cutsq)) continue;
       if (info_mol(jinfo) == mi) continue;
-      const int je = c_pot.i_map[info_type(jinfo)];
-      if (je < 0) continue;
-      const IlpP<R> &pij = c_pot.ilp[ie * MAXELEM + je];
-      const IlpP<R> &pji = c_pot.ilp[je * MAXELEM + ie];
+      const int tj = info_type(jinfo);
+      if (!((tmask >> tj) & 1u)) continue;
+      const int je = ONE ? 0 : c_pot.i_map[tj];
+      const IlpP<R> &pij = ONE ? c_pot.ilp[0] : c_pot.ilp[ie * MAXELEM + je];
+      const IlpP<R> &pji = ONE ? c_pot.ilp[0] : c_pot.ilp[je * MAXELEM + ie];
       R njx, njy, njz;
       if constexpr (sizeof(R) == 8) { d4 q = a.nrm64[j]; njx = q.x; njy = q.y; njz = q.z; }
       else { float4 q = __ldg(&a.nrm32[j]); njx = q.x; njy = q.y; njz = q.z; }
@@ -744,23 +755,29 @@ void launch_tersoff(const ForceArgs<R> &a, bool ev, bool eatom, cudaStream_t s) 
   if (ev && eatom) k_ters_eatom_own<<<g, 128, 0, s>>>(a);
 }
 
-template <int TPA>
+template <int TPA, bool ONE>
 static void launch_ilp_t(const ForceArgs<R> &a, bool ev, bool eatom, int block, cudaStream_t s) {
   long long threads = (long long)a.n * TPA;
   int g = (int)((threads + block - 1) / block);
-  if (ev && eatom) k_ilp<TPA, true, true><<<g, block, 0, s>>>(a);
-  else if (ev) k_ilp<TPA, true, false><<<g, block, 0, s>>>(a);
-  else k_ilp<TPA, false, false><<<g, block, 0, s>>>(a);
+  if (ev && eatom) k_ilp<TPA, true, true, ONE><<<g, block, 0, s>>>(a);
+  else if (ev) k_ilp<TPA, true, false, ONE><<<g, block, 0, s>>>(a);
+  else k_ilp<TPA, false, false, ONE><<<g, block, 0, s>>>(a);
 }
 
-void launch_ilp(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, cudaStream_t s) {
-  if (a.n == 0) return;
+template <bool ONE>
+static void launch_ilp_one(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, cudaStream_t s) {
   switch (tpa) {
-    case 4: launch_ilp_t<4>(a, ev, eatom, block, s); break;
-    case 8: launch_ilp_t<8>(a, ev, eatom, block, s); break;
-    case 16: launch_ilp_t<16>(a, ev, eatom, block, s); break;
-    default: launch_ilp_t<32>(a, ev, eatom, block, s); break;
+    case 4: launch_ilp_t<4, ONE>(a, ev, eatom, block, s); break;
+    case 8: launch_ilp_t<8, ONE>(a, ev, eatom, block, s); break;
+    case 16: launch_ilp_t<16, ONE>(a, ev, eatom, block, s); break;
+    default: launch_ilp_t<32, ONE>(a, ev, eatom, block, s); break;
   }
+}
+
+void launch_ilp(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, bool one_element, cudaStream_t s) {
+  if (a.n == 0) return;
+  if (one_element) launch_ilp_one<true>(a, ev, eatom, tpa, block, s);
+  else launch_ilp_one<false>(a, ev, eatom, tpa, block, s);
 }
 
 void launch_nderiv(const ForceArgs<R> &a, bool ev, cudaStream_t s) {

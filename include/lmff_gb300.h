@@ -4,7 +4,11 @@
  * (per-atom normals and their derivatives) + the neighbour build that feeds both.
  *
  * C ABI: plain pointers and sizes, no C++ or CUDA types.  One engine handle drives one
- * GPU through one CUDA stream; calls on one handle are not reentrant.
+ * GPU through one CUDA stream; calls on one handle are not reentrant.  Every call returns
+ * with its GPU work finished.  Engines on one device share that device's constant
+ * memory for the potential tables: the library serialises calls per device and reloads
+ * the tables whenever another engine ran in between, so several engines (for example
+ * one per LAMMPS sub-style) may be used from one or several host threads.
  *
  * What each entry point replaces in the reference (paths relative to the reference
  * snapshot's source trees):

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <mutex>
 #include <cmath>
 #include <cstdio>
@@ -209,6 +210,15 @@ __global__ void k_nve2(int n, double *v, const double *f, const double *mass, do
 
 // ------------------------------------------------------------------ engine
 
+// The potential tables live in __constant__ memory, one copy per device and module,
+// shared by every engine of the process.  Each device remembers which engine uploaded
+// the current tables; an engine re-uploads when another one ran in between, and every
+// device-touching API call holds the device's mutex so that no upload can overlap
+// another engine's kernels.
+static std::mutex g_device_mu[64];
+static uint64_t g_const_owner[64] = {0};
+static std::atomic<uint64_t> g_engine_uid{0};
+
 template <class T>
 static cudaError_t dalloc(T *&p, size_t count) {
   if (p) cudaFree(p);
@@ -218,6 +228,7 @@ static cudaError_t dalloc(T *&p, size_t count) {
 }
 
 struct Engine {
+  uint64_t uid = ++g_engine_uid;
   int device = 0;
   cudaStream_t stream = nullptr;
   int precision = LMFF_FP64;
@@ -548,7 +559,8 @@ struct Engine {
   }
 
   int push_consts() {
-    if (!pot_dirty) return LMFF_OK;
+    if (device < 0 || device >= 64) return fail(LMFF_EINVAL, "device ordinal out of range");
+    if (!pot_dirty && g_const_owner[device] == uid) return LMFF_OK;
     f64::upload_pot(pot64, stream);
     f32::upload_pot(pot32, stream);
     nb_upload_const(nbc, stream);
@@ -561,6 +573,7 @@ struct Engine {
     CK(cudaMemcpyAsync(d_cutILPsq, c, sizeof c, cudaMemcpyHostToDevice, stream));
     CK(cudaGetLastError());
     pot_dirty = false;
+    g_const_owner[device] = uid;
     return LMFF_OK;
   }
 
@@ -1600,6 +1613,14 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
 
 using lmff::Engine;
 
+// holds the engine's device mutex for the duration of one API call
+struct DeviceCall {
+  std::unique_lock<std::mutex> lk;
+  explicit DeviceCall(Engine &g) : lk(lmff::g_device_mu[(g.device >= 0 && g.device < 64) ? g.device : 0]) {
+    cudaSetDevice(g.device);
+  }
+};
+
 // ====================================================================== C ABI
 
 struct lmff_engine {
@@ -1728,7 +1749,7 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
       e->e.klaunch[q] = 0;
     }
   } else if (k == "count_pairs") {
-    cudaSetDevice(e->e.device);
+    DeviceCall dc(e->e);
     return e->e.count_pairs();
   } else {
     return e->e.fail(LMFF_EINVAL, "unknown option " + k);
@@ -1739,14 +1760,14 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
 int lmff_compute(lmff_engine *e, int natoms, const double *x, const int *type, const int64_t *mol, const int64_t *tag,
                  int which, int eflag, int vflag, double *f, double *eatom, lmff_result *res) {
   if (!e || natoms < 0 || (natoms > 0 && (!x || !type))) return LMFF_EINVAL;
-  cudaSetDevice(e->e.device);
+  DeviceCall dc(e->e);
   return e->e.compute_host(natoms, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
 }
 
 int lmff_compute_device(lmff_engine *e, int natoms, const double *d_x, const int *d_type, const int64_t *d_mol,
                         const int64_t *d_tag, int which, int eflag, int vflag, double *d_f, lmff_result *res) {
   if (!e || natoms < 0 || (natoms > 0 && (!d_x || !d_type))) return LMFF_EINVAL;
-  cudaSetDevice(e->e.device);
+  DeviceCall dc(e->e);
   return e->e.compute_device(natoms, d_x, d_type, d_mol, d_tag, which, eflag, vflag, d_f, res);
 }
 
@@ -1754,22 +1775,21 @@ int lmff_compute_device_noalloc(lmff_engine *e, int natoms, const double *d_x, c
                                 const int64_t *d_mol, int which, int eflag, int vflag, double *d_f, lmff_result *res) {
   if (!e || !d_x || !d_type || !d_f) return LMFF_EINVAL;
   if (!d_mol) return e->e.fail(LMFF_EINVAL, "lmff_compute_device_noalloc: d_mol is required");
-  cudaError_t rc = cudaSetDevice(e->e.device);
-  if (rc != cudaSuccess) return e->e.cuda_fail(rc, "cudaSetDevice");
+  DeviceCall dc(e->e);
   return lmff::noalloc_compute(e->e, natoms, d_x, d_type, d_mol, which, eflag, vflag, d_f, res);
 }
 
 int lmff_upload(lmff_engine *e, int natoms, const double *x, const double *v, const int *type, const int64_t *mol,
                 const int64_t *tag, const double *mass) {
   if (!e || natoms < 0 || (natoms > 0 && (!x || !type))) return LMFF_EINVAL;
-  cudaSetDevice(e->e.device);
+  DeviceCall dc(e->e);
   return e->e.upload(natoms, x, v, type, mol, tag, mass);
 }
 
 int lmff_compute_resident(lmff_engine *e, int which, int eflag, int vflag, lmff_result *res) {
   if (!e) return LMFF_EINVAL;
   if (!e->e.loaded) return e->e.fail(LMFF_EINVAL, "no resident system");
-  cudaSetDevice(e->e.device);
+  DeviceCall dc(e->e);
   int rc = e->e.maybe_rebuild();
   if (rc) return rc;
   std::vector<lmff_result> hr;
@@ -1781,25 +1801,25 @@ int lmff_compute_resident(lmff_engine *e, int which, int eflag, int vflag, lmff_
 
 int lmff_run_nve(lmff_engine *e, int nsteps, double dt, int thermo_every, lmff_thermo *thermo) {
   if (!e || nsteps < 0 || thermo_every < 0) return LMFF_EINVAL;
-  cudaSetDevice(e->e.device);
+  DeviceCall dc(e->e);
   return e->e.run_nve(nsteps, dt, thermo_every, thermo);
 }
 
 int lmff_download(lmff_engine *e, double *x, double *v, double *f) {
   if (!e) return LMFF_EINVAL;
-  cudaSetDevice(e->e.device);
+  DeviceCall dc(e->e);
   return e->e.download(x, v, f);
 }
 
 int lmff_batch_set(lmff_engine *e, int nsys, const lmff_system_desc *sys) {
   if (!e || !sys) return LMFF_EINVAL;
-  cudaSetDevice(e->e.device);
+  DeviceCall dc(e->e);
   return e->e.batch_set(nsys, sys);
 }
 
 int lmff_batch_compute(lmff_engine *e, double *f_out, lmff_result *res) {
   if (!e) return LMFF_EINVAL;
-  cudaSetDevice(e->e.device);
+  DeviceCall dc(e->e);
   return e->e.batch_compute(f_out, res);
 }
 
@@ -1831,7 +1851,7 @@ int lmff_get_stats(lmff_engine *e, lmff_stats *out) {
 
 int64_t lmff_export_list(lmff_engine *e, int which, int64_t *out, int64_t cap) {
   if (!e) return LMFF_EINVAL;
-  cudaSetDevice(e->e.device);
+  DeviceCall dc(e->e);
   return e->e.export_list(which, out, cap);
 }
 

@@ -1,0 +1,36 @@
+/* -*- c++ -*- ----------------------------------------------------------
+   ilp/graphene/hbn/gb300: pair_style ilp/graphene/hbn evaluated by the GB300
+   engine.  settings/coeff/read_file/init_one are the stock ones
+   (USER-MISC/pair_ilp_graphene_hbn.cpp:132-387); compute() (:428-443: ILP_neigh,
+   calc_normal, calc_FvdW, calc_FRep) is replaced by one engine call.
+------------------------------------------------------------------------- */
+
+#ifdef PAIR_CLASS
+
+PairStyle(ilp/graphene/hbn/gb300,PairILPGrapheneHBNGB300)
+
+#else
+
+#ifndef LMP_PAIR_ILP_GRAPHENE_HBN_GB300_H
+#define LMP_PAIR_ILP_GRAPHENE_HBN_GB300_H
+
+#include "pair_ilp_graphene_hbn.h"
+#include "lmff_lammps_adapter.h"
+
+namespace LAMMPS_NS {
+
+class PairILPGrapheneHBNGB300 : public PairILPGrapheneHBN {
+ public:
+  PairILPGrapheneHBNGB300(class LAMMPS *);
+  virtual ~PairILPGrapheneHBNGB300() {}
+  virtual void compute(int, int);
+  void init_style();
+
+ protected:
+  lmff_lammps::Adapter gb;
+};
+
+}
+
+#endif
+#endif

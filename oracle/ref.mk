@@ -78,3 +78,40 @@ $(OUT)/lmff_ref: $(OBJS) $(OBJ)/ref_harness.o
 	@$(CXX) -o $@ $^ -lm
 
 .PHONY: all
+
+# ---------------------------------------------------------------------------------
+# lmp_gb300: the same reference LAMMPS with the GB300 package's pair styles
+# (lammps-lmff_gb300/lammps) registered, linked against liblmff_gb300.so.  Only the
+# two core files that include the pair-style table (force.cpp, lammps.cpp) are
+# recompiled with a table that adds the package's headers.  Used by the CPU test of
+# the drop-in wiring (tests/test_lammps_package.py); the package itself is product code.
+PKGDIR := lammps-lmff_gb300/lammps
+GEN2 := $(OUT)/gen_gb300
+OBJ2 := $(OUT)/obj_gb300
+LIBDIR := lammps-lmff_gb300/lmff_gb300
+PKG_SRC := $(PKGDIR)/pair_tersoff_gb300.cpp $(PKGDIR)/pair_ilp_graphene_hbn_gb300.cpp $(PKGDIR)/lmff_lammps_adapter.cpp
+CXXFLAGS2 := -O2 -std=c++11 -w -ffp-contract=off -DLAMMPS_MEMALIGN=64 -DLAMMPS_SMALLBIG \
+             -I$(GEN2) -I$(GEN) -I$(SRC) -I$(SRC)/STUBS -I$(SRC)/MOLECULE -I$(SRC)/MANYBODY -I$(SRC)/USER-MISC \
+             -I$(PKGDIR) -Iinclude
+
+$(GEN2)/style_pair.h: $(GEN)/.stamp
+	@mkdir -p $(GEN2) $(OBJ2)
+	@cp $(GEN)/style_pair.h $@
+	@echo '#include "pair_tersoff_gb300.h"' >> $@
+	@echo '#include "pair_ilp_graphene_hbn_gb300.h"' >> $@
+
+$(OBJ2)/%.o: $(PKGDIR)/%.cpp $(GEN2)/style_pair.h
+	@$(CXX) $(CXXFLAGS2) -c $< -o $@
+
+$(OBJ2)/force.o: $(SRC)/force.cpp $(GEN2)/style_pair.h
+	@$(CXX) $(CXXFLAGS2) -c $< -o $@
+
+$(OBJ2)/lammps.o: $(SRC)/lammps.cpp $(GEN2)/style_pair.h
+	@$(CXX) $(CXXFLAGS2) -c $< -o $@
+
+$(OUT)/lmp_gb300: $(filter-out $(OBJ)/force.o $(OBJ)/lammps.o $(OBJ)/ref_harness.o,$(OBJS)) $(OBJ2)/force.o \
+                  $(OBJ2)/lammps.o $(OBJ)/ref_harness.o $(patsubst $(PKGDIR)/%.cpp,$(OBJ2)/%.o,$(PKG_SRC))
+	@$(CXX) -o $@ $^ -L$(LIBDIR) -llmff_gb300 -Wl,-rpath,$(abspath $(LIBDIR)) -lm
+
+gb300: $(OUT)/lmp_gb300
+.PHONY: gb300

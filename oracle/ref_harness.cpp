@@ -4,7 +4,10 @@
 //
 // Test infrastructure only (built by oracle/ref.mk into oracle/_ref/).
 //
-//   lmff_ref <input-script> <out.bin> [lists]
+//   lmff_ref <input-script> <out.bin> [lists] [-- <LAMMPS command-line arguments>]
+//
+// Without "--" LAMMPS runs quietly (-log none -screen none); after "--" the given
+// arguments are passed to LAMMPS instead (e.g. -sf gb300 -screen stdout).
 //
 // out.bin is a sequence of records: char name[16], char kind ('d' double, 'q' int64),
 // int64 count, then count elements.  Atoms are reported in tag order.
@@ -73,9 +76,15 @@ int main(int argc, char **argv) {
     return 2;
   }
   bool lists = argc > 3 && strcmp(argv[3], "lists") == 0;
+  std::vector<const char *> largs = {"lmff_ref", "-log", "none", "-screen", "none", "-nocite"};
+  for (int a = 3; a < argc; a++)
+    if (strcmp(argv[a], "--") == 0) {
+      largs.assign(1, "lmff_ref");
+      for (int b = a + 1; b < argc; b++) largs.push_back(argv[b]);
+      break;
+    }
   MPI_Init(&argc, &argv);
-  const char *largs[] = {"lmff_ref", "-log", "none", "-screen", "none", "-nocite"};
-  LAMMPS *lmp = new LAMMPS(6, (char **)largs, MPI_COMM_WORLD);
+  LAMMPS *lmp = new LAMMPS((int)largs.size(), (char **)largs.data(), MPI_COMM_WORLD);
   lmp->input->file(argv[1]);
 
   g_out = fopen(argv[2], "wb");

@@ -230,3 +230,20 @@ def test_mixed_vs_fp64_large():
     r32 = capi.Engine(TERSOFF, ILP, precision=capi.MIXED).compute_system(s)
     assert np.abs(r32["f"] - r64["f"]).max() <= MIX_F_ABS
     assert abs(r32["e_ilp"] - r64["e_ilp"]) <= MIX_E_REL * abs(r64["e_ilp"])
+
+
+def test_two_engines_interleaved_share_constant_memory_safely():
+    """Two engines with different parameter sets (Tersoff-only, ILP-only, as the two
+    LAMMPS sub-styles hold them) alternate on one device; each call must use its own
+    engine's tables."""
+    g = load_golden("bilayer_small")
+    et = capi.Engine(TERSOFF, None)
+    ei = capi.Engine(None, ILP)
+    for eng in (et, ei):
+        eng.set_box(g["box_lo"], g["box_hi"], g["periodic"])
+    for call in range(3):
+        rt = et.compute(g["x"], g["type"], g["mol"], g["tag"], which=capi.TERSOFF, same_atoms=call > 0)
+        ri = ei.compute(g["x"], g["type"], g["mol"], g["tag"], which=capi.ILP, same_atoms=call > 0)
+        assert abs(rt["e_tersoff"] - g["e_tersoff"]) <= F64_TOL * abs(g["e_tersoff"]), call
+        assert abs(ri["e_ilp"] - g["e_ilp"]) <= F64_TOL * abs(g["e_ilp"]), call
+        assert rel_max(rt["f"] + ri["f"], g["f"]) <= F64_TOL, call

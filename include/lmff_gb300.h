@@ -138,6 +138,9 @@ typedef struct lmff_stats {
   /* interlayer pairs within the ILP cutoff in the current configuration (option
    * "count_pairs" = 1 counts them once, outside any timed region) */
   int64_t pairs_in_cutoff;
+  /* steps lmff_run_nve ran through the step graph (see option "graphs"), and chunks
+   * redone host-driven after a graph's rebuild outgrew the captured list capacity */
+  int64_t graph_steps, graph_redos;
 } lmff_stats;
 
 /* ---- lifecycle ------------------------------------------------------------------- */
@@ -161,7 +164,14 @@ int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double 
  * block, "list_full" 1 = keep same-molecule pairs in the pair list (the reference's
  * full list, for set comparisons), "skin" neighbour skin in Angstrom,
  * "kernel_timing" 1 = record per-kernel device time, "reset_timing" clears it,
- * "count_pairs" counts interlayer pairs within the cutoff now (see lmff_stats). */
+ * "count_pairs" counts interlayer pairs within the cutoff now (see lmff_stats),
+ * "graphs" 1 (default) = lmff_run_nve replays steps between thermo samples as one CUDA
+ * graph per step (integrate, displacement test, conditional list rebuild, forces,
+ * integrate) with no host synchronisation; 0 = one host-driven step at a time.
+ * Per-kernel timing uses the host-driven loop.  "graph_list_cap" > 0 lowers the
+ * pair-list capacity a graph's rebuild may fill (testing the overflow redo: a chunk
+ * whose rebuild overflows is redone host-driven from its first step, rebuilding the
+ * list there, so it equals the uninterrupted run up to summation order). */
 int lmff_set_option(lmff_engine *e, const char *key, double value);
 
 /* ---- one-shot evaluation on host buffers (the pair-style drop-in) ------------------ */

@@ -14,6 +14,7 @@
 #include <array>
 #include <atomic>
 #include <mutex>
+#include <shared_mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -208,16 +209,39 @@ __global__ void k_nve2(int n, double *v, const double *f, const double *mass, do
   if (ke) ke[q] = 0.5 * MVV2E * mass[q] * (vx * vx + vy * vy + vz * vz);
 }
 
+// sets the step graph's rebuild condition: any atom moved more than skin/2 since the
+// last build (neighbor.cpp:1947-1976 check_distance)
+__global__ void k_setcond(cudaGraphConditionalHandle h, const unsigned long long *maxdisp, double trig2) {
+  double d2 = __longlong_as_double((long long)*maxdisp);
+  cudaGraphSetConditional(h, d2 > trig2 ? 1u : 0u);
+}
+
+// Pair-list offsets past the capacity the step graph was captured with: clamp them so
+// that fill and the force kernels stay inside the array, and flag the overflow (the
+// host then redoes the chunk on the eager path, which grows the list).
+__global__ void k_clamp_off(int n, int64_t *off, int64_t cap, int *status, unsigned long long *rebuilds) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  if (i == 0) atomicAdd(rebuilds, 1ull);
+  int64_t o = off[i];
+  if (o > cap) {
+    off[i] = cap;
+    atomicOr(status, ST_LIST_OVERFLOW);
+  }
+}
+
 // ------------------------------------------------------------------ engine
 
 // The potential tables live in __constant__ memory, one copy per device and module,
-// shared by every engine of the process.  Each device remembers which engine uploaded
-// the current tables; an engine re-uploads when another one ran in between, and every
-// device-touching API call holds the device's mutex so that no upload can overlap
-// another engine's kernels.
-static std::mutex g_device_mu[64];
-static uint64_t g_const_owner[64] = {0};
-static std::atomic<uint64_t> g_engine_uid{0};
+// shared by every engine of the process.  Each device records the content hash of the
+// tables it holds.  Every device-touching API call holds the device's lock in shared
+// mode for its whole duration (all calls finish their GPU work before returning);
+// an engine whose tables differ from the device's takes the lock exclusively, waits for
+// the device to drain and uploads.  Engines with identical tables (e.g. serving slots)
+// therefore run concurrently on their own streams; engines with different tables (the
+// two LAMMPS sub-styles) alternate safely.
+static std::shared_mutex g_dev_rw[64];
+static uint64_t g_dev_tables[64] = {0};
 
 template <class T>
 static cudaError_t dalloc(T *&p, size_t count) {
@@ -228,7 +252,7 @@ static cudaError_t dalloc(T *&p, size_t count) {
 }
 
 struct Engine {
-  uint64_t uid = ++g_engine_uid;
+  uint64_t table_hash = 0;  // content hash of the constant tables (pot64, pot32, nbc, cutILPsq)
   int device = 0;
   cudaStream_t stream = nullptr;
   int precision = LMFF_FP64;
@@ -374,6 +398,19 @@ struct Engine {
     d_cutILPsq = nullptr;
     if (h_pinned) cudaFreeHost(h_pinned);
     h_pinned = nullptr;
+    drop_graph();
+    void *bks[] = {bk_xq, bk_v, bk_f, bk_mass, bk_tag, bk_perm, bk_sysid};
+    for (void *b : bks)
+      if (b) cudaFree(b);
+    bk_xq = nullptr;
+    bk_v = bk_f = bk_mass = nullptr;
+    bk_tag = nullptr;
+    bk_perm = bk_sysid = nullptr;
+    bk_cap = 0;
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+    cap_stream = nullptr;
+    if (d_graph_rebuilds) cudaFree(d_graph_rebuilds);
+    d_graph_rebuilds = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
   }
@@ -536,6 +573,7 @@ struct Engine {
     rshort = std::max(rmaxilp, t_on ? ht.cutmax : 0.0) + skin;
     nbc.rshortsq_d = rshort * rshort;
     nbc.rshortsq_f = (float)(rshort * rshort);
+    hash_tables();
     pot_dirty = true;
     built = false;
     return LMFF_OK;
@@ -558,12 +596,10 @@ struct Engine {
     return LMFF_OK;
   }
 
+  // The device's constant tables are this engine's (guaranteed by DeviceCall); only the
+  // engine-owned copy of the intralayer cutoffs may still need refreshing.
   int push_consts() {
-    if (device < 0 || device >= 64) return fail(LMFF_EINVAL, "device ordinal out of range");
-    if (!pot_dirty && g_const_owner[device] == uid) return LMFF_OK;
-    f64::upload_pot(pot64, stream);
-    f32::upload_pot(pot32, stream);
-    nb_upload_const(nbc, stream);
+    if (!pot_dirty) return LMFF_OK;
     double c[MAXELEM * MAXELEM] = {0};
     if (i_on) {
       int ne = (int)hi.elements.size();
@@ -573,8 +609,31 @@ struct Engine {
     CK(cudaMemcpyAsync(d_cutILPsq, c, sizeof c, cudaMemcpyHostToDevice, stream));
     CK(cudaGetLastError());
     pot_dirty = false;
-    g_const_owner[device] = uid;
     return LMFF_OK;
+  }
+
+  // Upload the constant tables to the device (caller holds the device lock exclusively
+  // and the device is idle); synchronous so that other streams see them complete.
+  int upload_tables() {
+    f64::upload_pot(pot64, stream);
+    f32::upload_pot(pot32, stream);
+    nb_upload_const(nbc, stream);
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaGetLastError());
+    return LMFF_OK;
+  }
+
+  static uint64_t fnv(const void *p, size_t n, uint64_t h) {
+    const unsigned char *b = (const unsigned char *)p;
+    for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 1099511628211ull;
+    return h;
+  }
+  void hash_tables() {
+    uint64_t h = 1469598103934665603ull;
+    h = fnv(&pot64, sizeof pot64, h);
+    h = fnv(&pot32, sizeof pot32, h);
+    h = fnv(&nbc, sizeof nbc, h);
+    table_hash = h ? h : 1;
   }
 
   // ---------------------------------------------------------------- capacity
@@ -619,6 +678,19 @@ struct Engine {
     if (bytes <= h_pinned_bytes) return LMFF_OK;
     if (h_pinned) cudaFreeHost(h_pinned);
     h_pinned = nullptr;
+    drop_graph();
+    void *bks[] = {bk_xq, bk_v, bk_f, bk_mass, bk_tag, bk_perm, bk_sysid};
+    for (void *b : bks)
+      if (b) cudaFree(b);
+    bk_xq = nullptr;
+    bk_v = bk_f = bk_mass = nullptr;
+    bk_tag = nullptr;
+    bk_perm = bk_sysid = nullptr;
+    bk_cap = 0;
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+    cap_stream = nullptr;
+    if (d_graph_rebuilds) cudaFree(d_graph_rebuilds);
+    d_graph_rebuilds = nullptr;
     CK(cudaMallocHost(&h_pinned, bytes));
     h_pinned_bytes = bytes;
     return LMFF_OK;
@@ -812,7 +884,7 @@ struct Engine {
     return LMFF_OK;
   }
 
-  void hilo_all() { nb_hilo(n, d.xq, d.sys, d.sysid, d.xh, d.xl, stream); }
+  void hilo_all(cudaStream_t s = nullptr) { nb_hilo(n, d.xq, d.sys, d.sysid, d.xh, d.xl, s ? s : stream); }
 
   int status_error(int st) {
     CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
@@ -1133,6 +1205,245 @@ struct Engine {
     return load_from_staging(nn, v != nullptr, false);
   }
 
+  // ---------------------------------------------------------------- step graph
+  // One velocity-Verlet step as a CUDA graph: k_nve1 -> k_setcond -> IF(rebuild) ->
+  // forces -> k_nve2, replayed with no host synchronisation between steps.  Kernel
+  // arguments are frozen at capture, so the graph's rebuild permutes into the spare
+  // arrays and copies back, and the pair list keeps the capacity it had at capture
+  // (an overflow raises ST_LIST_OVERFLOW; the chunk is then redone on the eager path
+  // from a checkpoint of its first step, equal to the uninterrupted run up to the
+  // summation order of a list built at a different step).
+  bool use_graphs = true;
+  cudaGraphExec_t step_exec = nullptr;
+  cudaStream_t cap_stream = nullptr;
+  struct StepKey {
+    int n, prec, tpa, block, full;
+    double dt, skin;
+    const void *list, *xq;
+    int64_t cap;
+    bool operator==(const StepKey &o) const { return memcmp(this, &o, sizeof o) == 0; }
+  } step_key;
+  // chunk-start checkpoint for the overflow redo
+  d4 *bk_xq = nullptr;
+  double *bk_v = nullptr, *bk_f = nullptr, *bk_mass = nullptr;
+  int64_t *bk_tag = nullptr;
+  int *bk_perm = nullptr, *bk_sysid = nullptr;
+  int bk_cap = 0;
+  int64_t graph_steps = 0, graph_redos = 0;
+  unsigned long long *d_graph_rebuilds = nullptr;
+  int64_t graph_cap = 0;           // pair-list capacity the step graph's rebuild fills up to
+  int64_t graph_cap_limit = 0;     // > 0: lower it to this (exercises the overflow redo)
+
+  cudaError_t enqueue_rebuild_fixed(cudaStream_t s) {
+    nb_wrap_bin(n, d.xq, d.sys, d.sysid, d.bin_key, d.idx, s);
+    cudaError_t e = nb_sort(d.cub_tmp, d.cub_tmp_bytes, d.bin_key, d.bin_key2, d.idx, d.idx2, n, (int)nbit_bins, s);
+    if (e != cudaSuccess) return e;
+    nb_permute(n, d.idx2, d.xq, xq2, d.v, v2, d.tag, tag2, d.perm, perm2, d.sysid, sysid2, d.mass, mass2, s);
+    cudaMemcpyAsync(d.xq, xq2, sizeof(d4) * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d.v, v2, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d.tag, tag2, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d.perm, perm2, sizeof(int) * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d.sysid, sysid2, sizeof(int) * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d.mass, mass2, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(d.bin_start, 0, sizeof(int) * d.nbins, s);
+    cudaMemsetAsync(d.bin_end, 0, sizeof(int) * d.nbins, s);
+    nb_bin_ranges(n, d.bin_key2, d.bin_start, d.bin_end, s);
+    hilo_all(s);
+    NbArgs a;
+    memset(&a, 0, sizeof a);
+    a.n = n;
+    a.xq = d.xq;
+    a.xh = d.xh;
+    a.xl = d.xl;
+    a.sys = d.sys;
+    a.sysid = d.sysid;
+    a.bin_start = d.bin_start;
+    a.bin_end = d.bin_end;
+    a.list_off = d.list_off;
+    a.list = d.list;
+    a.list_cap = graph_cap;
+    a.cnt = d.cnt_tmp;
+    a.short_cnt = d.short_cnt;
+    a.short_nb = d.short_nb;
+    a.lc = lc;
+    a.full = list_full;
+    a.status = d.status;
+    cudaMemsetAsync(d.cnt_tmp + n, 0, sizeof(int64_t), s);
+    nb_list(a, false, s);
+    e = nb_scan(d.cub_tmp, d.cub_tmp_bytes, d.cnt_tmp, d.list_off, n, s);
+    if (e != cudaSuccess) return e;
+    k_clamp_off<<<(n + 256) / 256, 256, 0, s>>>(n, d.list_off, graph_cap, d.status, d_graph_rebuilds);
+    nb_list(a, true, s);
+    nb_copy_hold(n, d.xq, d.xhold, s);
+    cudaMemsetAsync(d.maxdisp, 0, sizeof(unsigned long long), s);
+    return cudaGetLastError();
+  }
+
+  void drop_graph() {
+    if (step_exec) cudaGraphExecDestroy(step_exec);
+    step_exec = nullptr;
+  }
+
+  int build_step_graph(double dt) {
+    drop_graph();
+    if (!cap_stream) CK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+    if (!d_graph_rebuilds) {
+      CK(cudaMalloc(&d_graph_rebuilds, sizeof(unsigned long long)));
+      CK(cudaMemsetAsync(d_graph_rebuilds, 0, sizeof(unsigned long long), stream));
+    }
+    int prc = push_consts();
+    if (prc) return prc;
+    if (!built) {
+      prc = rebuild();
+      if (prc) return prc;
+    }
+    // headroom so that a rebuild inside the graph rarely outgrows the list
+    int64_t want = list_total + list_total / 4 + 4096;
+    if (want > d.list_cap) {
+      // grow the list and carry the current entries over (no rebuild: the trajectory
+      // stays the one the host-driven loop would produce)
+      uint32_t *nl = nullptr;
+      cudaError_t e = cudaMalloc(&nl, sizeof(uint32_t) * want);
+      if (e != cudaSuccess) return fail(LMFF_ENOMEM, "pair list headroom for the step graph does not fit on the device");
+      if (list_total > 0) CK(cudaMemcpyAsync(nl, d.list, sizeof(uint32_t) * list_total, cudaMemcpyDeviceToDevice, stream));
+      CK(cudaStreamSynchronize(stream));
+      if (d.list) cudaFree(d.list);
+      d.list = nl;
+      d.list_cap = want;
+    }
+    graph_cap = d.list_cap;
+    if (graph_cap_limit > 0 && graph_cap_limit < graph_cap) graph_cap = graph_cap_limit;
+    double dtf = 0.5 * dt * FTM2V;
+    bool mixed = precision == LMFF_MIXED;
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+    CK(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, d.mass, dtf, dt, d.xhold, d.maxdisp, d.sys,
+                                                d.sysid, d.xh, d.xl, mixed ? 1 : 0);
+    k_setcond<<<1, 1, 0, stream>>>(h, d.maxdisp, 0.25 * skin * skin);
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(stream, &cs, nullptr, nullptr, &deps, nullptr, &nd));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cn;
+    CK(cudaGraphAddNode(&cn, g, deps, nullptr, nd, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    cudaError_t eb = enqueue_rebuild_fixed(cap_stream);
+    CK(cudaStreamEndCapture(cap_stream, &body));
+    if (eb != cudaSuccess) return cuda_fail(eb, "capturing the rebuild body");
+    CK(cudaStreamUpdateCaptureDependencies(stream, &cn, nullptr, 1, cudaStreamSetCaptureDependencies));
+    bool kt = ktiming;
+    ktiming = false;
+    if (precision == LMFF_FP64)
+      run_kernels(args<double>(), LMFF_TERSOFF | LMFF_ILP, false, false, f64::launch_short, f64::launch_tersoff,
+                  f64::launch_ilp, f64::launch_nderiv, f64::launch_finish);
+    else
+      run_kernels(args<float>(), LMFF_TERSOFF | LMFF_ILP, false, false, f32::launch_short, f32::launch_tersoff,
+                  f32::launch_ilp, f32::launch_nderiv, f32::launch_finish);
+    ktiming = kt;
+    k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, dtf, nullptr);
+    cudaGraph_t gout = nullptr;
+    CK(cudaStreamEndCapture(stream, &gout));
+    cudaError_t ei = cudaGraphInstantiate(&step_exec, gout, 0);
+    cudaGraphDestroy(gout);
+    if (ei != cudaSuccess) {
+      step_exec = nullptr;
+      return cuda_fail(ei, "cudaGraphInstantiate(step graph)");
+    }
+    memset(&step_key, 0, sizeof step_key);
+    step_key = StepKey{n, precision, tpa, block, list_full, dt, skin, d.list, d.xq, d.list_cap};
+    return LMFF_OK;
+  }
+
+  int checkpoint(bool restore) {
+    if (!restore && bk_cap < cap_n) {
+      CK(dalloc(bk_xq, cap_n)); CK(dalloc(bk_v, 3 * (size_t)cap_n)); CK(dalloc(bk_f, 3 * (size_t)cap_n));
+      CK(dalloc(bk_mass, cap_n)); CK(dalloc(bk_tag, cap_n)); CK(dalloc(bk_perm, cap_n)); CK(dalloc(bk_sysid, cap_n));
+      bk_cap = cap_n;
+    }
+    auto cp = [&](void *dst, const void *src, size_t b) { return cudaMemcpyAsync(dst, src, b, cudaMemcpyDeviceToDevice, stream); };
+    if (!restore) {
+      CK(cp(bk_xq, d.xq, sizeof(d4) * n)); CK(cp(bk_v, d.v, sizeof(double) * 3 * n)); CK(cp(bk_f, d.f, sizeof(double) * 3 * n));
+      CK(cp(bk_mass, d.mass, sizeof(double) * n)); CK(cp(bk_tag, d.tag, sizeof(int64_t) * n));
+      CK(cp(bk_perm, d.perm, sizeof(int) * n)); CK(cp(bk_sysid, d.sysid, sizeof(int) * n));
+    } else {
+      CK(cp(d.xq, bk_xq, sizeof(d4) * n)); CK(cp(d.v, bk_v, sizeof(double) * 3 * n)); CK(cp(d.f, bk_f, sizeof(double) * 3 * n));
+      CK(cp(d.mass, bk_mass, sizeof(double) * n)); CK(cp(d.tag, bk_tag, sizeof(int64_t) * n));
+      CK(cp(d.perm, bk_perm, sizeof(int) * n)); CK(cp(d.sysid, bk_sysid, sizeof(int) * n));
+    }
+    return LMFF_OK;
+  }
+
+  // nsteps NVE steps through the step graph; falls back to the eager loop on overflow
+  int run_steps_graph(int nsteps, double dt) {
+    StepKey want{n, precision, tpa, block, list_full, dt, skin, d.list, d.xq, d.list_cap};
+    if (!step_exec || !(step_key == want)) {
+      int rc = build_step_graph(dt);
+      if (rc) return rc;
+    }
+    int rc = checkpoint(false);
+    if (rc) return rc;
+    for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(step_exec, stream));
+    int st = 0;
+    unsigned long long nrb = 0;
+    CK(cudaMemcpyAsync(&st, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(&nrb, d_graph_rebuilds, sizeof nrb, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemsetAsync(d_graph_rebuilds, 0, sizeof nrb, stream));
+    CK(cudaStreamSynchronize(stream));
+    hilo_fresh = precision == LMFF_MIXED;
+    if (st & (ST_LIST_OVERFLOW | ST_SHORT_OVERFLOW)) {
+      // redo the chunk on the eager path, which grows the list as needed
+      CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
+      rc = checkpoint(true);
+      if (rc) return rc;
+      drop_graph();
+      // the graph's rebuild reordered atoms and overwrote the list: build both again
+      // for the restored positions, and the forces in that order (the checkpointed
+      // forces are in the chunk-start order)
+      built = false;
+      rc = rebuild();
+      if (rc) return rc;
+      rc = forces(LMFF_TERSOFF | LMFF_ILP, false, false, nullptr);
+      if (rc) return rc;
+      graph_redos++;
+      return run_steps_eager(nsteps, dt);
+    }
+    if (st) return status_error(st);
+    rebuilds += (int64_t)nrb;
+    graph_steps += nsteps;
+    steps += nsteps;
+    return LMFF_OK;
+  }
+
+  int run_steps_eager(int nsteps, double dt) {
+    double dtf = 0.5 * dt * FTM2V;
+    for (int s = 1; s <= nsteps; s++) {
+      bool mixed = precision == LMFF_MIXED;
+      timed(4, [&] {
+        k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, d.mass, dtf, dt, d.xhold, d.maxdisp, d.sys,
+                                                    d.sysid, d.xh, d.xl, mixed ? 1 : 0);
+      });
+      CK(cudaGetLastError());
+      hilo_fresh = mixed;
+      int rc = maybe_rebuild();
+      if (rc) return rc;
+      rc = forces(LMFF_TERSOFF | LMFF_ILP, false, false, nullptr);
+      if (rc) return rc;
+      timed(4, [&] { k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, dtf, nullptr); });
+      CK(cudaGetLastError());
+      steps++;
+    }
+    return LMFF_OK;
+  }
+
   int run_nve(int nsteps, double dt, int thermo_every, lmff_thermo *thermo) {
     if (!loaded) return fail(LMFF_EINVAL, "no resident system: call lmff_upload first");
     double dtf = 0.5 * dt * FTM2V, dtv = dt;
@@ -1180,26 +1491,42 @@ struct Engine {
     cudaEventCreate(&r0);
     cudaEventCreate(&r1);
     cudaEventRecord(r0, stream);
-    for (int s = 1; s <= nsteps; s++) {
-      bool mixed = precision == LMFF_MIXED;
-      timed(4, [&] {
+    // steps between thermo samples go through the step graph (or the eager loop when
+    // per-kernel timing is on); a thermo step runs eagerly with energies and virial
+    const bool graphs = use_graphs && !ktiming && n > 0;
+    int done = 0;
+    while (done < nsteps) {
+      int chunk = nsteps - done;
+      bool th_at_end = false;
+      if (thermo_every > 0) {
+        int to_next = thermo_every - done % thermo_every;
+        if (to_next <= chunk) {
+          chunk = to_next;
+          th_at_end = true;
+        }
+      }
+      int plain = th_at_end ? chunk - 1 : chunk;
+      if (plain > 0) {
+        rc = graphs ? run_steps_graph(plain, dt) : run_steps_eager(plain, dt);
+        if (rc) return rc;
+      }
+      if (th_at_end) {
+        bool mixed = precision == LMFF_MIXED;
         k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, d.mass, dtf, dtv, d.xhold, d.maxdisp, d.sys,
                                                     d.sysid, d.xh, d.xl, mixed ? 1 : 0);
-      });
-      CK(cudaGetLastError());
-      hilo_fresh = mixed;
-      rc = maybe_rebuild();
-      if (rc) return rc;
-      bool th = thermo_every > 0 && (s % thermo_every == 0);
-      rc = forces(LMFF_TERSOFF | LMFF_ILP, th, false, th ? &hr : nullptr);
-      if (rc) return rc;
-      timed(4, [&] { k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, dtf, th ? ke : nullptr); });
-      CK(cudaGetLastError());
-      steps++;
-      if (th) {
+        CK(cudaGetLastError());
+        hilo_fresh = mixed;
+        rc = maybe_rebuild();
+        if (rc) return rc;
+        rc = forces(LMFF_TERSOFF | LMFF_ILP, true, false, &hr);
+        if (rc) return rc;
+        k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, dtf, ke);
+        CK(cudaGetLastError());
+        steps++;
         rc = sample(steps, hr);
         if (rc) return rc;
       }
+      done += chunk;
     }
     cudaEventRecord(r1, stream);
     CK(cudaStreamSynchronize(stream));
@@ -1613,11 +1940,24 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
 
 using lmff::Engine;
 
-// holds the engine's device mutex for the duration of one API call
+// One API call on an engine: holds the device lock in shared mode and makes sure the
+// device's constant tables are this engine's (uploading them under the exclusive lock
+// when another engine's tables are resident).
 struct DeviceCall {
-  std::unique_lock<std::mutex> lk;
-  explicit DeviceCall(Engine &g) : lk(lmff::g_device_mu[(g.device >= 0 && g.device < 64) ? g.device : 0]) {
+  std::shared_lock<std::shared_mutex> lk;
+  explicit DeviceCall(Engine &g) {
+    int dev = (g.device >= 0 && g.device < 64) ? g.device : 0;
     cudaSetDevice(g.device);
+    for (int attempt = 0;; attempt++) {
+      lk = std::shared_lock<std::shared_mutex>(lmff::g_dev_rw[dev]);
+      if (lmff::g_dev_tables[dev] == g.table_hash || attempt == 3) break;  // 3 failed uploads: the call reports the CUDA error
+      lk.unlock();
+      std::unique_lock<std::shared_mutex> ex(lmff::g_dev_rw[dev]);
+      if (lmff::g_dev_tables[dev] != g.table_hash) {
+        cudaDeviceSynchronize();
+        if (g.upload_tables() == LMFF_OK) lmff::g_dev_tables[dev] = g.table_hash;
+      }
+    }
   }
 };
 
@@ -1741,6 +2081,12 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
     e->e.skin = value;
     e->e.build_consts();
     e->e.loaded = false;
+  } else if (k == "graphs") {
+    e->e.use_graphs = value != 0.0;
+    e->e.drop_graph();
+  } else if (k == "graph_list_cap") {
+    e->e.graph_cap_limit = value > 0 ? (int64_t)value : 0;
+    e->e.drop_graph();
   } else if (k == "kernel_timing") {
     e->e.ktiming = value != 0.0;
   } else if (k == "reset_timing") {
@@ -1839,6 +2185,8 @@ int lmff_get_stats(lmff_engine *e, lmff_stats *out) {
   out->tpa = g.tpa;
   out->block = g.block;
   out->ms_last_run = g.ms_run;
+  out->graph_steps = g.graph_steps;
+  out->graph_redos = g.graph_redos;
   for (int q = 0; q < 6; q++) {
     out->kernel_ms[q] = g.kms[q];
     out->kernel_launches[q] = g.klaunch[q];

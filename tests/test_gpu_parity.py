@@ -247,3 +247,47 @@ def test_two_engines_interleaved_share_constant_memory_safely():
         assert abs(rt["e_tersoff"] - g["e_tersoff"]) <= F64_TOL * abs(g["e_tersoff"]), call
         assert abs(ri["e_ilp"] - g["e_ilp"]) <= F64_TOL * abs(g["e_ilp"]), call
         assert rel_max(rt["f"] + ri["f"], g["f"]) <= F64_TOL, call
+
+
+def _graph_vs_host_loop(prec, graph_list_cap=0, steps=60, thermo_every=20):
+    """The same NVE run through the step graph and through the host-driven loop."""
+    s = S.thermalize(S.twisted_bilayer(8, 8, 3.0, top="hbn"), 1500.0, seed=11)
+    out = []
+    for graphs in (1, 0):
+        eng = capi.Engine(TERSOFF, ILP, precision=prec, skin=0.4)
+        eng.set_option("graphs", graphs)
+        if graph_list_cap:
+            eng.set_option("graph_list_cap", graph_list_cap)
+        eng.upload(s)
+        th = eng.run_nve(steps, 0.001, thermo_every=thermo_every)
+        x, v, f = eng.download()
+        out.append((x, v, f, th, eng.stats()))
+    out.append(s)
+    return out
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.MIXED])
+def test_step_graph_bitwise_equals_host_loop(prec):
+    """Steps replayed as CUDA graphs (conditional rebuild node) give the bitwise-same
+    trajectory, thermo output and rebuild count as the host-driven loop."""
+    (xg, vg, fg, thg, sg), (xe, ve, fe, the, se), _ = _graph_vs_host_loop(prec)
+    assert sg["graph_steps"] > 0 and se["graph_steps"] == 0
+    assert se["rebuilds"] > 2                        # the small skin forces rebuilds inside graph chunks
+    assert sg["rebuilds"] == se["rebuilds"]
+    assert np.array_equal(xg, xe) and np.array_equal(vg, ve) and np.array_equal(fg, fe)
+    assert [t["etotal"] for t in thg] == [t["etotal"] for t in the]
+    assert len(thg) == 60 // 20 + 1
+
+
+def test_step_graph_overflow_redo():
+    """A graph whose rebuild overflows its captured list capacity redoes the chunk on
+    the host-driven path from a checkpoint of the chunk's first step.  The redo builds
+    the list at that step, so sums run in another order: FP64 agreement, not bitwise."""
+    (xg, vg, fg, thg, sg), (xe, ve, fe, the, se), s = _graph_vs_host_loop(capi.FP64, graph_list_cap=1000)
+    assert sg["graph_redos"] > 0
+    assert sg["steps"] == se["steps"]
+    # positions are wrapped at rebuilds, which the redo moves: compare modulo the box
+    assert np.abs(min_image(xg - xe, s.box_lo, s.box_hi, s.periodic)).max() < 1e-9
+    assert rel_max(vg, ve) < 1e-7 and rel_max(fg, fe) < 1e-7
+    for a, b in zip(thg, the):
+        assert abs(a["etotal"] - b["etotal"]) <= 1e-10 * abs(b["etotal"])

@@ -30,6 +30,7 @@
  *                          (fix_nve.cpp:64-111) and Neighbor::decide / check_distance
  *                          (neighbor.cpp:1947-1976), device resident
  *   lmff_batch_*           no counterpart: many independent systems per launch
+ *   lmff_server_*          no counterpart: a request queue served by continuous batching
  *   lmff_last_error        error->one / error->all messages of both pair styles
  */
 #ifndef LMFF_GB300_H
@@ -54,6 +55,7 @@ extern "C" {
 #define LMFF_EUNSUPPORTED (-8)        /* request outside what the engine implements */
 #define LMFF_ENOMEM (-9)              /* device or host allocation failed */
 #define LMFF_ENODEV (-10)             /* no usable CUDA device */
+#define LMFF_PENDING 1                /* lmff_server_wait: the request has not finished yet */
 
 /* ---- precision modes ------------------------------------------------------------ */
 #define LMFF_FP64 0   /* all-FP64 drop-in */
@@ -124,7 +126,7 @@ typedef struct lmff_thermo {
 
 typedef struct lmff_stats {
   int64_t natoms, list_entries, short_entries, list_capacity, rebuilds, steps;
-  double list_per_atom, bytes_device;
+  double list_per_atom, bytes_device;   /* bytes_device: device memory this engine holds */
   double ms_last_build, ms_last_forces;
   int precision, tpa, block;
   /* device time of the last lmff_run_nve (CUDA events on the engine's stream) */
@@ -230,11 +232,86 @@ typedef struct lmff_system_desc {
   const int64_t *mol;
   double lo[3], hi[3];
   int periodic[3];
+  const double *v;          /* [natoms*3] velocities for lmff_run_nve on the batch, or NULL (zero) */
 } lmff_system_desc;
+/* Makes the batch the engine's resident state: lmff_batch_compute evaluates it,
+ * lmff_run_nve integrates every system at once (masses from lmff_set_masses or
+ * lmff_upload), lmff_download returns the batch in order.  Atoms of a system are
+ * never neighbours of another system's atoms, and each system's forces, energies and
+ * virial are bitwise the ones it gets alone. */
 int lmff_batch_set(lmff_engine *e, int nsys, const lmff_system_desc *sys);
 /* Energies/forces/virials of every system: f_out[sum natoms * 3] in batch order
  * (overwritten), res[nsys]. */
 int lmff_batch_compute(lmff_engine *e, double *f_out, lmff_result *res);
+/* Per-system energies and virials of the last evaluation that computed them (a
+ * lmff_batch_compute, lmff_compute_resident, or a thermo step of lmff_run_nve). */
+int lmff_batch_results(lmff_engine *e, int nsys, lmff_result *res);
+/* mass[t-1] = mass of type t (amu), used by batches loaded afterwards. */
+int lmff_set_masses(lmff_engine *e, int ntypes, const double *mass);
+/* A new engine on the same device with the same parameters, precision and tunables
+ * (no resident state).  Engines with equal parameters share device constant tables. */
+int lmff_clone(const lmff_engine *src, lmff_engine **out);
+
+/* ---- serving: independent requests, continuously batched --------------------------- */
+/* No counterpart in the reference (one simulation per process).  A server owns a worker
+ * thread and two engines cloned from `proto` (parameters, precision, tunables, masses).
+ * Submission is thread-safe and returns at once; the worker admits requests in FIFO
+ * order while the estimated device bytes of admitted requests stay within
+ * hbm_budget_bytes, evaluates the admitted single points together in one batched
+ * launch per kernel, and advances the admitted NVE requests of equal dt as one resident
+ * batch, md_chunk_steps at a time, re-forming it when requests join or leave.  A single
+ * point is bitwise the same alone and in any mix; an NVE run in a batch shares the
+ * batch's list rebuilds, so it matches the run alone up to summation order.  A failing
+ * batch is retried request by request, so an error reaches only its own request. */
+typedef struct lmff_request {
+  int natoms;
+  const double *x;          /* [natoms*3], copied at submission */
+  const double *v;          /* [natoms*3] or NULL (zero); NVE only */
+  const int *type;          /* [natoms] 1..ntypes */
+  const int64_t *mol;       /* [natoms] or NULL (all 0) */
+  double lo[3], hi[3];
+  int periodic[3];
+  int nsteps;               /* 0: single point; > 0: NVE steps */
+  double dt;                /* ps, NVE only */
+  /* caller-owned outputs, written before the request completes (any may be NULL):
+   * forces / energies / virial of the final configuration, final x and v (NVE) */
+  double *f_out;
+  double *x_out, *v_out;
+  lmff_result *res;
+} lmff_request;
+
+typedef struct lmff_server_config {
+  double hbm_budget_bytes;  /* admission budget (0: 64e9) */
+  double bytes_per_atom;    /* starting device-bytes estimate per atom (0: 4096); raised
+                             * to what the engines report once batches have run */
+  int64_t max_batch_atoms;  /* atoms per batched launch (0: 8M) */
+  int md_chunk_steps;       /* NVE steps between batch re-formations (0: 20) */
+} lmff_server_config;
+
+typedef struct lmff_server_stats {
+  int64_t submitted, completed, failed, queued, active;
+  int64_t point_batches, point_systems, md_chunks, md_reforms, md_steps;
+  double admitted_bytes, bytes_per_atom, busy_s;
+  double max_admitted_bytes;  /* high-water mark of admitted_bytes */
+} lmff_server_stats;
+
+typedef struct lmff_server lmff_server;
+int lmff_server_create(lmff_server **out, const lmff_engine *proto, const lmff_server_config *cfg);
+/* Copies the inputs; *ticket identifies the request.  LMFF_ENOMEM if the request alone
+ * exceeds the budget. */
+int lmff_server_submit(lmff_server *s, const lmff_request *req, int64_t *ticket);
+/* Submits reqs[0..nreq) atomically (all queued together, tickets[nreq]); nothing is
+ * queued if any request is invalid or alone exceeds the budget. */
+int lmff_server_submit_many(lmff_server *s, int nreq, const lmff_request *reqs, int64_t *tickets);
+/* Waits up to timeout_s (< 0: forever).  Returns LMFF_PENDING if still running, else
+ * the request's status (its message in lmff_server_last_error) and retires the ticket;
+ * latency_s = completion - submission time. */
+int lmff_server_wait(lmff_server *s, int64_t ticket, double timeout_s, double *latency_s);
+int lmff_server_get_stats(lmff_server *s, lmff_server_stats *out);
+/* Message of this thread's last failed submit or wait. */
+const char *lmff_server_last_error(void);
+/* Finishes every submitted request, then stops the worker and frees the engines. */
+void lmff_server_destroy(lmff_server *s);
 
 /* ---- diagnostics ------------------------------------------------------------------- */
 int lmff_get_stats(lmff_engine *e, lmff_stats *out);

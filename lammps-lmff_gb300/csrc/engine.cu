@@ -299,6 +299,9 @@ struct Engine {
   double *h_pinned = nullptr;
   size_t h_pinned_bytes = 0;
   std::vector<double> mass_type;
+  // per-system energies and virials of the last evaluation that computed them
+  std::vector<lmff_result> last_res;
+  bool last_res_valid = false;
   // stats
   int64_t rebuilds = 0, steps = 0, list_total = 0, short_total = 0;
   double ms_build = 0, ms_forces = 0, ms_run = 0;
@@ -579,6 +582,28 @@ struct Engine {
     return LMFF_OK;
   }
 
+  // same parameters and tunables as o, fresh device state
+  int clone_from(const Engine &o) {
+    ntypes = o.ntypes;
+    ht = o.ht;
+    hi = o.hi;
+    t_on = o.t_on;
+    i_on = o.i_on;
+    i_one = o.i_one;
+    cut_global = o.cut_global;
+    tap = o.tap;
+    skin = o.skin;
+    precision = o.precision;
+    tpa = o.tpa;
+    block = o.block;
+    list_full = o.list_full;
+    use_graphs = o.use_graphs;
+    mass_type = o.mass_type;
+    int rc = build_consts();
+    if (rc) return rc;
+    return init_device(o.device);
+  }
+
   int init_device(int dev) {
     int cnt = 0;
     if (cudaGetDeviceCount(&cnt) != cudaSuccess || cnt == 0) return fail(LMFF_ENODEV, "no CUDA device");
@@ -643,6 +668,7 @@ struct Engine {
     if (nn <= cap_n) return LMFF_OK;
     int c = nn + nn / 8 + 64;
     CK(cudaStreamSynchronize(stream));
+    drop_graph();
     CK(dalloc(d.xq, c)); CK(dalloc(xq2, c)); CK(dalloc(d.xh, c)); CK(dalloc(d.xl, c));
     CK(dalloc(d.v, 3 * (size_t)c)); CK(dalloc(v2, 3 * (size_t)c)); CK(dalloc(d.f, 3 * (size_t)c));
     CK(dalloc(d.xhold, 3 * (size_t)c));
@@ -674,23 +700,27 @@ struct Engine {
     return LMFF_OK;
   }
 
+  // device bytes this engine holds (the arrays of ensure_atoms, the pair list, bins,
+  // sort workspace and the step graph's checkpoint)
+  double device_bytes() const {
+    double c = cap_n;
+    double per_atom = 2 * sizeof(*d.xq) + sizeof(*d.xh) + sizeof(*d.xl) + 3 * (3 * sizeof(double)) +
+                      3 * sizeof(double) + 2 * sizeof(*d.tag) + 4 * sizeof(int) + 2 * sizeof(double) +
+                      sizeof(*d.nrm64) + sizeof(*d.nrm32) + sizeof(*d.ilp_cnt) + MAXILP * sizeof(*d.ilp_nb) +
+                      sizeof(*d.ters_cnt) + MAXTERS * (sizeof(*d.ters_nb) + sizeof(*d.ters_g)) +
+                      2 * 3 * sizeof(double) + MAXILP * sizeof(*d.ilp_c) + sizeof(*d.ilp_g) + 16 * sizeof(double) +
+                      3 * sizeof(double) + sizeof(*d.list_off) + sizeof(*d.short_cnt) + MAXSHORT * sizeof(*d.short_nb) +
+                      2 * sizeof(*d.bin_key) + 2 * sizeof(*d.idx) + sizeof(*d.cnt_tmp) + 3 * 3 * sizeof(double) +
+                      sizeof(double) + 2 * sizeof(int) + 2 * sizeof(int64_t);
+    if (bk_cap) per_atom += sizeof(d4) + 7 * sizeof(double) + sizeof(int64_t) + 2 * sizeof(int);
+    return c * per_atom + (double)d.list_cap * sizeof(uint32_t) + (double)d.cub_tmp_bytes +
+           (double)d.nbins_cap * 2 * sizeof(int);
+  }
+
   int ensure_pinned(size_t bytes) {
     if (bytes <= h_pinned_bytes) return LMFF_OK;
     if (h_pinned) cudaFreeHost(h_pinned);
     h_pinned = nullptr;
-    drop_graph();
-    void *bks[] = {bk_xq, bk_v, bk_f, bk_mass, bk_tag, bk_perm, bk_sysid};
-    for (void *b : bks)
-      if (b) cudaFree(b);
-    bk_xq = nullptr;
-    bk_v = bk_f = bk_mass = nullptr;
-    bk_tag = nullptr;
-    bk_perm = bk_sysid = nullptr;
-    bk_cap = 0;
-    if (cap_stream) cudaStreamDestroy(cap_stream);
-    cap_stream = nullptr;
-    if (d_graph_rebuilds) cudaFree(d_graph_rebuilds);
-    d_graph_rebuilds = nullptr;
     CK(cudaMallocHost(&h_pinned, bytes));
     h_pinned_bytes = bytes;
     return LMFF_OK;
@@ -747,6 +777,7 @@ struct Engine {
   }
 
   int upload_sys() {
+    drop_graph();   // bins, image code and sort width are frozen in a captured step
     if ((int)hsys.size() > cap_sys) {
       CK(dalloc(d.sys, hsys.size()));
       CK(dalloc(d.red_out, hsys.size() * 16));
@@ -764,6 +795,7 @@ struct Engine {
 
   // ---------------------------------------------------------------- load / rebuild
   int load_from_staging(int nn, bool have_v, bool have_sysid) {
+    drop_graph();
     n = nn;
     d.n = nn;
     if ((int64_t)n >= (1LL << lc.ibits))
@@ -777,7 +809,19 @@ struct Engine {
     loaded = true;
     built = false;
     forces_valid = false;
+    last_res_valid = false;
     return rebuild();
+  }
+
+  // the sorted copies back into the primary arrays, so device pointers stay fixed
+  // across rebuilds (a captured step graph holds them)
+  cudaError_t copy_back_permuted(cudaStream_t s) {
+    cudaMemcpyAsync(d.xq, xq2, sizeof(d4) * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d.v, v2, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d.tag, tag2, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d.perm, perm2, sizeof(int) * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d.sysid, sysid2, sizeof(int) * n, cudaMemcpyDeviceToDevice, s);
+    return cudaMemcpyAsync(d.mass, mass2, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
   }
 
   int rebuild() {
@@ -795,12 +839,7 @@ struct Engine {
     nb_wrap_bin(n, d.xq, d.sys, d.sysid, d.bin_key, d.idx, stream);
     CK(nb_sort(d.cub_tmp, d.cub_tmp_bytes, d.bin_key, d.bin_key2, d.idx, d.idx2, n, (int)nbit_bins, stream));
     nb_permute(n, d.idx2, d.xq, xq2, d.v, v2, d.tag, tag2, d.perm, perm2, d.sysid, sysid2, d.mass, mass2, stream);
-    std::swap(d.xq, xq2);
-    std::swap(d.v, v2);
-    std::swap(d.tag, tag2);
-    std::swap(d.perm, perm2);
-    std::swap(d.sysid, sysid2);
-    std::swap(d.mass, mass2);
+    CK(copy_back_permuted(stream));
     CK(cudaMemsetAsync(d.bin_start, 0, sizeof(int) * d.nbins, stream));
     CK(cudaMemsetAsync(d.bin_end, 0, sizeof(int) * d.nbins, stream));
     nb_bin_ranges(n, d.bin_key2, d.bin_start, d.bin_end, stream);
@@ -836,6 +875,7 @@ struct Engine {
       return fail(LMFF_EOVERFLOW, "pair-list count out of range (" + std::to_string(total) + ")");
     if (total > d.list_cap) {
       int64_t cap = total + total / 8 + 1024;
+      drop_graph();
       if (d.list) cudaFree(d.list);
       d.list = nullptr;
       cudaError_t e = cudaMalloc(&d.list, sizeof(uint32_t) * cap);
@@ -1008,6 +1048,7 @@ struct Engine {
     ms_forces = ms;
     if (st) return status_error(st);
     forces_valid = true;
+    if (ev && hres) last_res_valid = true;
     if (hres) {
       hres->assign(hsys.size(), lmff_result());
       for (size_t s = 0; s < hsys.size(); s++) {
@@ -1022,6 +1063,7 @@ struct Engine {
         r.e_tersoff = q[8];
         for (int k = 0; k < 6; k++) r.virial_tersoff[k] = q[10 + k];
       }
+      if (ev) last_res = *hres;
     }
     return LMFF_OK;
   }
@@ -1239,12 +1281,7 @@ struct Engine {
     cudaError_t e = nb_sort(d.cub_tmp, d.cub_tmp_bytes, d.bin_key, d.bin_key2, d.idx, d.idx2, n, (int)nbit_bins, s);
     if (e != cudaSuccess) return e;
     nb_permute(n, d.idx2, d.xq, xq2, d.v, v2, d.tag, tag2, d.perm, perm2, d.sysid, sysid2, d.mass, mass2, s);
-    cudaMemcpyAsync(d.xq, xq2, sizeof(d4) * n, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(d.v, v2, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(d.tag, tag2, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(d.perm, perm2, sizeof(int) * n, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(d.sysid, sysid2, sizeof(int) * n, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(d.mass, mass2, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    copy_back_permuted(s);
     cudaMemsetAsync(d.bin_start, 0, sizeof(int) * d.nbins, s);
     cudaMemsetAsync(d.bin_end, 0, sizeof(int) * d.nbins, s);
     nb_bin_ranges(n, d.bin_key2, d.bin_start, d.bin_end, s);
@@ -1596,14 +1633,18 @@ struct Engine {
     if (rc) return rc;
     rc = ensure_atoms(nn);
     if (rc) return rc;
-    std::vector<double> x(3 * (size_t)nn);
+    std::vector<double> x(3 * (size_t)nn), v;
     std::vector<int> t(nn), sid(nn);
     std::vector<int64_t> m(nn), g(nn);
+    bool have_v = false;
+    for (int s = 0; s < nsys; s++) have_v = have_v || sys[s].v;
+    if (have_v) v.assign(3 * (size_t)nn, 0.0);
     for (int s = 0; s < nsys; s++) {
       int o = batch_offsets[s];
       rc = check_mol(sys[s].natoms, sys[s].mol, sys[s].type);
       if (rc) return rc;
       memcpy(&x[3 * (size_t)o], sys[s].x, sizeof(double) * 3 * sys[s].natoms);
+      if (sys[s].v) memcpy(&v[3 * (size_t)o], sys[s].v, sizeof(double) * 3 * sys[s].natoms);
       for (int p = 0; p < sys[s].natoms; p++) {
         t[o + p] = sys[s].type[p];
         m[o + p] = sys[s].mol ? sys[s].mol[p] : 0;
@@ -1616,8 +1657,13 @@ struct Engine {
     CK(cudaMemcpyAsync(d_min, m.data(), sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_gin, g.data(), sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_sysin, sid.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, stream));
+    if (have_v) CK(cudaMemcpyAsync(d_vin, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, stream));
+    if (!mass_type.empty()) {
+      if (!d_massT) CK(cudaMalloc(&d_massT, sizeof(double) * (MAXTYPE + 1)));
+      CK(cudaMemcpyAsync(d_massT, mass_type.data(), sizeof(double) * mass_type.size(), cudaMemcpyHostToDevice, stream));
+    }
     CK(cudaStreamSynchronize(stream));
-    return load_from_staging(nn, false, true);
+    return load_from_staging(nn, have_v, true);
   }
 
   int batch_compute(double *f_out, lmff_result *res) {
@@ -2169,6 +2215,38 @@ int lmff_batch_compute(lmff_engine *e, double *f_out, lmff_result *res) {
   return e->e.batch_compute(f_out, res);
 }
 
+int lmff_batch_results(lmff_engine *e, int nsys, lmff_result *res) {
+  if (!e || !res || nsys < 0) return LMFF_EINVAL;
+  Engine &g = e->e;
+  if (!g.last_res_valid) return g.fail(LMFF_EINVAL, "no energies computed since the last upload");
+  if ((size_t)nsys != g.last_res.size())
+    return g.fail(LMFF_EINVAL, "nsys does not match the resident batch (" + std::to_string(g.last_res.size()) + ")");
+  for (int s = 0; s < nsys; s++) res[s] = g.last_res[s];
+  return LMFF_OK;
+}
+
+int lmff_set_masses(lmff_engine *e, int ntypes, const double *mass) {
+  if (!e || !mass || ntypes < 1 || ntypes > lmff::MAXTYPE) return LMFF_EINVAL;
+  e->e.mass_type.assign(lmff::MAXTYPE + 1, 1.0);
+  for (int t = 0; t < ntypes; t++) e->e.mass_type[t] = mass[t];
+  return LMFF_OK;
+}
+
+int lmff_clone(const lmff_engine *src, lmff_engine **out) {
+  if (!src || !out) return LMFF_EINVAL;
+  *out = nullptr;
+  lmff_engine *h = new (std::nothrow) lmff_engine;
+  if (!h) return LMFF_ENOMEM;
+  int rc = h->e.clone_from(src->e);
+  if (rc != LMFF_OK) {
+    g_create_error = h->e.err;
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return LMFF_OK;
+}
+
 int lmff_get_stats(lmff_engine *e, lmff_stats *out) {
   if (!e || !out) return LMFF_EINVAL;
   memset(out, 0, sizeof *out);
@@ -2192,8 +2270,7 @@ int lmff_get_stats(lmff_engine *e, lmff_stats *out) {
     out->kernel_launches[q] = g.klaunch[q];
   }
   out->pairs_in_cutoff = g.pairs_in_cut;
-  size_t fr = 0, tot = 0;
-  if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) out->bytes_device = (double)(tot - fr);
+  out->bytes_device = g.device_bytes();
   return LMFF_OK;
 }
 

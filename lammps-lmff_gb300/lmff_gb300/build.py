@@ -20,7 +20,7 @@ INC = os.path.join(REPO, "include")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "liblmff_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-UNITS = ["engine.cu", "neighbor.cu", "forces64.cu", "forces32.cu", "potentials.cpp"]
+UNITS = ["engine.cu", "neighbor.cu", "forces64.cu", "forces32.cu", "potentials.cpp", "server.cpp"]
 
 
 def nvcc() -> str:

@@ -64,7 +64,7 @@ KERNELS = ["pair_ilp", "tersoff", "intralayer_normals", "gather", "integrate", "
 
 class SystemDesc(C.Structure):
     _fields_ = [("natoms", C.c_int), ("x", C.c_void_p), ("type", C.c_void_p), ("mol", C.c_void_p),
-                ("lo", C.c_double * 3), ("hi", C.c_double * 3), ("periodic", C.c_int * 3)]
+                ("lo", C.c_double * 3), ("hi", C.c_double * 3), ("periodic", C.c_int * 3), ("v", C.c_void_p)]
 
 
 _lib = None
@@ -98,6 +98,16 @@ def load_library(path: str = LIB_PATH):
         "lmff_download": ([P, P, P, P], I),
         "lmff_batch_set": ([P, I, P], I),
         "lmff_batch_compute": ([P, P, P], I),
+        "lmff_batch_results": ([P, I, P], I),
+        "lmff_set_masses": ([P, I, P], I),
+        "lmff_clone": ([P, C.POINTER(P)], I),
+        "lmff_server_create": ([C.POINTER(P), P, P], I),
+        "lmff_server_submit": ([P, P, C.POINTER(C.c_int64)], I),
+        "lmff_server_submit_many": ([P, I, P, P], I),
+        "lmff_server_wait": ([P, C.c_int64, D, C.POINTER(D)], I),
+        "lmff_server_get_stats": ([P, P], I),
+        "lmff_server_last_error": ([], C.c_char_p),
+        "lmff_server_destroy": ([P], None),
         "lmff_get_stats": ([P, C.POINTER(Stats)], I),
         "lmff_export_list": ([P, I, P, C.c_int64], C.c_int64),
         "lmff_last_error": ([P], C.c_char_p),
@@ -245,7 +255,13 @@ class Engine:
         return x, v, f
 
     # -------------------------------------------------------------- batch
-    def batch_set(self, systems) -> None:
+    def set_masses(self, masses=(12.011, 10.811, 14.0067)) -> None:
+        m = _f64(masses)
+        self._ck(_lib.lmff_set_masses(self._h, len(m), _p(m)))
+
+    def batch_set(self, systems, velocities: bool = False) -> None:
+        """Load many systems as one resident batch; with velocities=True each system's
+        v (or zeros) is loaded too, for run_nve on the whole batch."""
         self._batch_keep = []
         descs = (SystemDesc * len(systems))()
         for k, s in enumerate(systems):
@@ -257,12 +273,27 @@ class Engine:
             descs[k].x = x.ctypes.data
             descs[k].type = t.ctypes.data
             descs[k].mol = m.ctypes.data
+            if velocities and s.v is not None:
+                v = _f64(s.v)
+                self._batch_keep.append(v)
+                descs[k].v = v.ctypes.data
             for c in range(3):
                 descs[k].lo[c] = float(s.box_lo[c])
                 descs[k].hi[c] = float(s.box_hi[c])
                 descs[k].periodic[c] = int(bool(s.periodic[c]))
         self._batch_n = [s.n for s in systems]
+        self._n = sum(self._batch_n)
         self._ck(_lib.lmff_batch_set(self._h, len(systems), C.cast(descs, C.c_void_p)))
+
+    def batch_results(self) -> List[Dict]:
+        """Per-system energies and virials of the last evaluation that computed them."""
+        res = (Result * len(self._batch_n))()
+        self._ck(_lib.lmff_batch_results(self._h, len(self._batch_n), C.cast(res, C.c_void_p)))
+        return [r.to_dict() for r in res]
+
+    def split(self, a: np.ndarray) -> List[np.ndarray]:
+        """Split a batch-ordered per-atom array into the systems of the batch."""
+        return np.split(a, np.cumsum(self._batch_n)[:-1])
 
     def batch_compute(self):
         ntot = sum(self._batch_n)

@@ -59,6 +59,8 @@ def workload(name: str):
         s = S.graphite_slab(10, 40, 23, spacing=3.35, mol_mode="alternate")
     elif name == "graphite_330k":
         s = S.graphite_slab(10, 120, 69, spacing=3.35, mol_mode="alternate")
+    elif name == "twisted_500k":
+        s = S.twisted_graphene_hbn_500k(seed=2)
     else:
         raise SystemExit(f"unknown workload {name}")
     return S.thermalize(s, 300.0, seed=3)
@@ -196,6 +198,126 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def _sync_wall(fn, reps: int) -> float:
+    """Wall seconds per call of fn (every call returns with its GPU work finished)."""
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        fn()
+    return (time.perf_counter() - t0) / reps
+
+
+def bench_replicas(args, local: int) -> dict:
+    """256 independent bilayer replicas, 50/50 graphene/graphene and graphene/hBN, atom
+    counts log-uniform in [500, 20000], twist U[0, 5] deg, spacing U[3.2, 3.6] A (seeded),
+    each displaced by N(0, 0.02 A): energies, forces and virial of every replica.
+    Batched = one launch per kernel over all replicas (lmff_batch_set +
+    lmff_batch_compute: host arrays in, forces and per-replica energies/virials out).
+    Baseline = the same evaluations one replica at a time through lmff_compute."""
+    from lmff_gb300 import capi
+    from lmff_gb300 import structures as S
+    systems = [S.displace(s, 0.02, seed=k) for k, s in enumerate(S.replica_set(256, 500, 20000, seed=4))]
+    ntot = sum(s.n for s in systems)
+    out = {}
+    for name, prec in (("mixed", capi.MIXED), ("fp64", capi.FP64)):
+        eng = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=prec)
+        eng.batch_set(systems)
+        eng.batch_compute()
+
+        def batched():
+            eng.batch_set(systems)
+            eng.batch_compute()
+        reps = max(3, args.steps // 4)
+        t_b = _sync_wall(batched, reps)
+        t_set = _sync_wall(lambda: eng.batch_set(systems), reps)
+        t_cmp = _sync_wall(eng.batch_compute, reps)
+        st = eng.stats()
+        # device-resident re-evaluation of the loaded batch (no host copies, no rebuild)
+        t_r = _sync_wall(lambda: eng.compute_resident(eflag=True, vflag=True), max(3, args.steps // 4))
+        seq = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=prec)
+        for s_ in systems[:8]:
+            seq.compute_system(s_)
+        t0 = time.perf_counter()
+        for s_ in systems:
+            seq.compute_system(s_)
+        t_s = time.perf_counter() - t0
+        out[name] = {"batched_s": t_b, "batch_set_s": t_set, "batch_compute_s": t_cmp,
+                     "build_ms": st["ms_last_build"], "forces_ms": st["ms_last_forces"],
+                     "resident_s": t_r, "one_at_a_time_s": t_s,
+                     "batched_replicas_per_s": len(systems) / t_b, "one_at_a_time_replicas_per_s": len(systems) / t_s}
+        del eng, seq
+    value = out["mixed"]["batched_replicas_per_s"]
+    return {"metric": "replica evaluations/s (E+F+W), 256 bilayer replicas", "value": value,
+            "unit": "replicas/s", "n_gpus": 1, "higher_is_better": True, "data": "synthetic",
+            "dtype": "f32", "config": {"workload": "256 bilayer replicas, 500-20000 atoms log-uniform",
+                                       "atoms_total": ntot, "precision": "mixed"},
+            "batched_mixed_vs_one_at_a_time_fp64": value / out["fp64"]["one_at_a_time_replicas_per_s"],
+            "atom_evals_per_s_batched_mixed": ntot / out["mixed"]["batched_s"],
+            "atom_evals_per_s_resident_mixed": ntot / out["mixed"]["resident_s"],
+            "detail": out}
+
+
+def bench_serving(args, local: int) -> dict:
+    """Poisson request stream: 200 requests/s, 70 % single points and 30 % 100-step NVE
+    runs at 300 K, bilayers of 1k-200k atoms (log-uniform on a 24-value grid), seeded.
+    The server (mixed precision, 150 GB admission budget) replays the stream in real time
+    (latency p50/p99) and all at once (capacity); the baseline serves a prefix of the same
+    stream one request at a time in plain FP64, and the server serves the same prefix."""
+    from lmff_gb300 import capi, serve
+    stream = serve.poisson_stream(count=args.serve_requests, rate=200.0, seed=7)
+    prefix = stream[:args.serve_prefix]
+    proto = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=capi.MIXED)
+    srv = serve.Server(proto, hbm_budget_bytes=150e9, md_chunk_steps=args.serve_chunk)
+    serve.replay(srv, stream[:8], realtime=False)          # warm-up: allocations, graphs
+    openl = serve.replay(srv, stream, realtime=True)
+    closed = serve.replay(srv, stream, realtime=False)
+    closed_prefix = serve.replay(srv, prefix, realtime=False)
+    st = srv.stats()
+    srv.close()
+    seq64 = serve.replay_sequential(capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=capi.FP64),
+                                    prefix, realtime=False)
+    seqmx = serve.replay_sequential(capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=capi.MIXED),
+                                    prefix, realtime=False)
+    return {"metric": "solves/s, Poisson 200 req/s stream", "value": openl["solves_per_s"], "unit": "solves/s",
+            "n_gpus": 1, "higher_is_better": True, "data": "synthetic", "dtype": "f32",
+            "config": {"workload": f"{len(stream)} requests, 200 req/s, 30% 100-step NVE, 1k-200k atom bilayers",
+                       "precision": "mixed", "md_chunk_steps": args.serve_chunk, "budget_gb": 150,
+                       "prefix_requests": len(prefix)},
+            "open_loop": openl, "closed_loop": closed, "closed_loop_prefix": closed_prefix,
+            "one_at_a_time_fp64_prefix": seq64, "one_at_a_time_mixed_prefix": seqmx,
+            "capacity_vs_one_at_a_time_fp64": closed_prefix["solves_per_s"] / seq64["solves_per_s"],
+            "server_stats": st}
+
+
+def bench_drift(args, local: int) -> dict:
+    """NVE energy drift of the 7,200-atom AB bilayer at 300 K, dt 1 fs: slope of a
+    least-squares line through the total energy sampled every 1000 steps."""
+    from lmff_gb300 import capi
+    from lmff_gb300 import structures as S
+    s = S.thermalize(S.ab_bilayer_graphene(30, 30), 300.0, seed=3)
+    out = {}
+    for name, prec, nsteps in (("mixed", capi.MIXED, args.drift_steps_mixed),
+                               ("fp64", capi.FP64, args.drift_steps_fp64)):
+        eng = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=prec)
+        eng.upload(s)
+        t0 = time.perf_counter()
+        th = eng.run_nve(nsteps, 0.001, thermo_every=1000)
+        wall = time.perf_counter() - t0
+        t_ps = np.array([t["step"] for t in th]) * 0.001
+        e = np.array([t["etotal"] for t in th])
+        slope = np.polyfit(t_ps, e, 1)[0]                  # eV / ps
+        out[name] = {"steps": nsteps, "ns": nsteps * 1e-6, "drift_mev_per_atom_per_ns": slope * 1e3 * 1e3 / s.n,
+                     "etotal_first": float(e[0]), "etotal_last": float(e[-1]),
+                     "max_abs_dev_mev_per_atom": float(np.abs(e - e[0]).max() * 1e3 / s.n),
+                     "temp_last": th[-1]["temp"], "wall_s": wall, "atom_steps_per_s": s.n * nsteps / wall,
+                     "graph_steps": eng.stats()["graph_steps"]}
+    return {"metric": "NVE energy drift, 7200-atom bilayer, 300 K, dt 1 fs", "value":
+            out["mixed"]["drift_mev_per_atom_per_ns"], "unit": "meV/atom/ns", "n_gpus": 1,
+            "higher_is_better": False, "data": "synthetic", "dtype": "f32", "detail": out}
+
+
+SPECIAL = {"replicas_256": bench_replicas, "serve_poisson": bench_serving, "drift_c1": bench_drift}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -211,6 +333,11 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-peak", action="store_true", help="skip the cuBLAS peak measurement")
+    ap.add_argument("--serve-requests", type=int, default=400)
+    ap.add_argument("--serve-prefix", type=int, default=40)
+    ap.add_argument("--serve-chunk", type=int, default=20)
+    ap.add_argument("--drift-steps-mixed", type=int, default=1000000)
+    ap.add_argument("--drift-steps-fp64", type=int, default=100000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -237,6 +364,15 @@ def main():
         dist.barrier()
     if rank != 0:
         build.build()
+
+    if args.workload in SPECIAL:
+        line = SPECIAL[args.workload](args, local)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
 
     s = workload(args.workload)
     prec = capi.MIXED if args.precision == "mixed" else capi.FP64
@@ -347,7 +483,8 @@ def main():
                          f"oracle restatement, {cdt:.1f} s"}
 
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        metric = METRIC if args.workload == "graphite_2p7m" else f"atom-steps/s, workload {args.workload}"
+        line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32" if prec == capi.MIXED else "f64", "data": "synthetic",
                 "config": {"workload": "10-layer AB graphite slab, 2,694,960 atoms, 300 K NVE dt 1 fs"

@@ -143,6 +143,9 @@ typedef struct lmff_stats {
   /* steps lmff_run_nve ran through the step graph (see option "graphs"), and chunks
    * redone host-driven after a graph's rebuild outgrew the captured list capacity */
   int64_t graph_steps, graph_redos;
+  /* device bytes per atom a batch of the current kind needs (per-atom arrays, the pair
+   * list at the current density with headroom, sort workspace): admission estimates */
+  double bytes_per_atom_need;
 } lmff_stats;
 
 /* ---- lifecycle ------------------------------------------------------------------- */
@@ -253,13 +256,14 @@ int lmff_set_masses(lmff_engine *e, int ntypes, const double *mass);
 int lmff_clone(const lmff_engine *src, lmff_engine **out);
 
 /* ---- serving: independent requests, continuously batched --------------------------- */
-/* No counterpart in the reference (one simulation per process).  A server owns a worker
- * thread and two engines cloned from `proto` (parameters, precision, tunables, masses).
- * Submission is thread-safe and returns at once; the worker admits requests in FIFO
- * order while the estimated device bytes of admitted requests stay within
- * hbm_budget_bytes, evaluates the admitted single points together in one batched
- * launch per kernel, and advances the admitted NVE requests of equal dt as one resident
- * batch, md_chunk_steps at a time, re-forming it when requests join or leave.  A single
+/* No counterpart in the reference (one simulation per process).  A server owns two
+ * worker threads, each with an engine cloned from `proto` (parameters, precision,
+ * tunables, masses) on its own stream, so both run on the device at once.  Submission
+ * is thread-safe and returns at once; requests are admitted in FIFO order while the
+ * estimated device bytes of admitted requests stay within hbm_budget_bytes.  One worker
+ * evaluates the admitted single points together in one batched launch per kernel; the
+ * other advances the admitted NVE requests of equal dt as one resident batch,
+ * md_chunk_steps at a time, re-forming it when requests join or leave.  A single
  * point is bitwise the same alone and in any mix; an NVE run in a batch shares the
  * batch's list rebuilds, so it matches the run alone up to summation order.  A failing
  * batch is retried request by request, so an error reaches only its own request. */
@@ -291,7 +295,8 @@ typedef struct lmff_server_config {
 typedef struct lmff_server_stats {
   int64_t submitted, completed, failed, queued, active;
   int64_t point_batches, point_systems, md_chunks, md_reforms, md_steps;
-  double admitted_bytes, bytes_per_atom, busy_s;
+  double admitted_bytes, bytes_per_atom;
+  double busy_s;              /* busy time summed over the two workers */
   double max_admitted_bytes;  /* high-water mark of admitted_bytes */
 } lmff_server_stats;
 

@@ -702,8 +702,7 @@ struct Engine {
 
   // device bytes this engine holds (the arrays of ensure_atoms, the pair list, bins,
   // sort workspace and the step graph's checkpoint)
-  double device_bytes() const {
-    double c = cap_n;
+  double per_atom_bytes() const {
     double per_atom = 2 * sizeof(*d.xq) + sizeof(*d.xh) + sizeof(*d.xl) + 3 * (3 * sizeof(double)) +
                       3 * sizeof(double) + 2 * sizeof(*d.tag) + 4 * sizeof(int) + 2 * sizeof(double) +
                       sizeof(*d.nrm64) + sizeof(*d.nrm32) + sizeof(*d.ilp_cnt) + MAXILP * sizeof(*d.ilp_nb) +
@@ -713,8 +712,19 @@ struct Engine {
                       2 * sizeof(*d.bin_key) + 2 * sizeof(*d.idx) + sizeof(*d.cnt_tmp) + 3 * 3 * sizeof(double) +
                       sizeof(double) + 2 * sizeof(int) + 2 * sizeof(int64_t);
     if (bk_cap) per_atom += sizeof(d4) + 7 * sizeof(double) + sizeof(int64_t) + 2 * sizeof(int);
-    return c * per_atom + (double)d.list_cap * sizeof(uint32_t) + (double)d.cub_tmp_bytes +
+    return per_atom;
+  }
+  double device_bytes() const {
+    return (double)cap_n * per_atom_bytes() + (double)d.list_cap * sizeof(uint32_t) + (double)d.cub_tmp_bytes +
            (double)d.nbins_cap * 2 * sizeof(int);
+  }
+  // device bytes per atom a batch like the current one needs: the per-atom arrays with
+  // their growth margin, the pair list at the current density with the step graph's
+  // headroom, and the sort workspace
+  double bytes_per_atom_need() const {
+    if (n <= 0) return 0.0;
+    double list_pa = (double)list_total / n;
+    return 1.125 * per_atom_bytes() + 1.25 * 4.0 * list_pa + (double)d.cub_tmp_bytes / std::max(cap_n, 1);
   }
 
   int ensure_pinned(size_t bytes) {
@@ -2271,6 +2281,7 @@ int lmff_get_stats(lmff_engine *e, lmff_stats *out) {
   }
   out->pairs_in_cutoff = g.pairs_in_cut;
   out->bytes_device = g.device_bytes();
+  out->bytes_per_atom_need = g.bytes_per_atom_need();
   return LMFF_OK;
 }
 

@@ -3,7 +3,8 @@
 //
 // No counterpart in the reference, which runs one simulation per process.  A request
 // is one system: a single point (forces, energies, virial) or an NVE run of nsteps.
-// One worker thread owns two engines cloned from the caller's:
+// Two worker threads, each owning one engine cloned from the caller's, run
+// concurrently on the device (the engines have their own streams):
 //   * single points admitted since the last iteration are evaluated together, one
 //     batched launch per kernel (lmff_batch_set + lmff_batch_compute);
 //   * NVE requests with the same dt form one resident multi-system batch that advances
@@ -96,20 +97,21 @@ struct lmff_server {
   double admitted_bytes = 0.0;
   double bytes_per_atom = 4096.0;
   bool stop = false;
-  std::thread worker;
+  std::thread w_points, w_md;
   lmff_server_stats st;
-  std::vector<double> fbuf, xbuf, vbuf;
+  std::vector<double> pt_f;                 // points worker: batch forces
+  std::vector<double> md_x, md_v, md_f;     // NVE worker: batch state read back
 };
 
 namespace {
 
 thread_local std::string g_server_err;
 
-// device bytes per atom the engine holds for its current batch
+// device bytes per atom a batch like the engine's current one needs
 double engine_bytes_per_atom(lmff_engine *e) {
   lmff_stats s;
   if (lmff_get_stats(e, &s) != LMFF_OK || s.natoms <= 0) return 0.0;
-  return s.bytes_device / (double)s.natoms;
+  return s.bytes_per_atom_need;
 }
 
 void finish(lmff_server *s, Job *j, int status, const std::string &err) {
@@ -122,6 +124,7 @@ void finish(lmff_server *s, Job *j, int status, const std::string &err) {
   if (status == LMFF_OK) s->st.completed++;
   else s->st.failed++;
   s->cv_done.notify_all();
+  s->cv_work.notify_all();   // budget released: queued requests may be admitted
 }
 
 // FIFO admission while the budget holds (called with the lock held)
@@ -145,10 +148,10 @@ void run_points(lmff_server *s, std::vector<Job *> &batch) {
     descs.push_back(j->desc());
     total += j->natoms;
   }
-  s->fbuf.resize(3 * (size_t)total);
+  s->pt_f.resize(3 * (size_t)total);
   std::vector<lmff_result> res(batch.size());
   int rc = lmff_batch_set(s->pt, (int)descs.size(), descs.data());
-  if (rc == LMFF_OK) rc = lmff_batch_compute(s->pt, s->fbuf.data(), res.data());
+  if (rc == LMFF_OK) rc = lmff_batch_compute(s->pt, s->pt_f.data(), res.data());
   if (rc != LMFF_OK) {
     std::string err = lmff_last_error(s->pt);
     if (batch.size() == 1) {
@@ -165,7 +168,7 @@ void run_points(lmff_server *s, std::vector<Job *> &batch) {
   size_t o = 0;
   for (size_t k = 0; k < batch.size(); k++) {
     Job *j = batch[k];
-    if (j->f_out) memcpy(j->f_out, &s->fbuf[3 * o], sizeof(double) * 3 * j->natoms);
+    if (j->f_out) memcpy(j->f_out, &s->pt_f[3 * o], sizeof(double) * 3 * j->natoms);
     if (j->res) *j->res = res[k];
     o += j->natoms;
     finish(s, j, LMFF_OK, "");
@@ -181,17 +184,17 @@ int sync_resident(lmff_server *s) {
   if (s->resident_synced || s->resident.empty()) return LMFF_OK;
   int64_t total = 0;
   for (Job *j : s->resident) total += j->natoms;
-  s->xbuf.resize(3 * (size_t)total);
-  s->vbuf.resize(3 * (size_t)total);
-  s->fbuf.resize(3 * (size_t)total);
-  int rc = lmff_download(s->md, s->xbuf.data(), s->vbuf.data(), s->fbuf.data());
+  s->md_x.resize(3 * (size_t)total);
+  s->md_v.resize(3 * (size_t)total);
+  s->md_f.resize(3 * (size_t)total);
+  int rc = lmff_download(s->md, s->md_x.data(), s->md_v.data(), s->md_f.data());
   if (rc) return rc;
   size_t o = 0;
   for (Job *j : s->resident) {
     size_t b = 3 * o, nb = 3 * (size_t)j->natoms;
-    std::copy(s->xbuf.begin() + b, s->xbuf.begin() + b + nb, j->x.begin());
+    std::copy(s->md_x.begin() + b, s->md_x.begin() + b + nb, j->x.begin());
     if (j->v.empty()) j->v.assign(nb, 0.0);
-    std::copy(s->vbuf.begin() + b, s->vbuf.begin() + b + nb, j->v.begin());
+    std::copy(s->md_v.begin() + b, s->md_v.begin() + b + nb, j->v.begin());
     o += j->natoms;
   }
   s->resident_synced = true;
@@ -316,7 +319,7 @@ void run_md_chunk(lmff_server *s) {
     }
     if (j->x_out) memcpy(j->x_out, j->x.data(), sizeof(double) * nb);
     if (j->v_out) memcpy(j->v_out, j->v.data(), sizeof(double) * nb);
-    if (j->f_out) memcpy(j->f_out, &s->fbuf[b], sizeof(double) * nb);
+    if (j->f_out) memcpy(j->f_out, &s->md_f[b], sizeof(double) * nb);
     if (j->res) *j->res = res[k];
     drop_active(s, j);
     finish(s, j, LMFF_OK, "");
@@ -328,13 +331,12 @@ void run_md_chunk(lmff_server *s) {
   s->bytes_per_atom = std::max(s->bytes_per_atom, bpa);
 }
 
-void worker_main(lmff_server *s) {
+// single points: one batched evaluation of everything admitted, then again
+void points_main(lmff_server *s) {
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
     admit(s);
-    s->st.queued = (int64_t)s->queue.size();
-    s->st.active = (int64_t)(s->points.size() + s->md_active.size());
-    if (s->points.empty() && s->md_active.empty()) {
+    if (s->points.empty()) {
       if (s->stop && s->queue.empty()) break;
       s->cv_work.wait(lk);
       continue;
@@ -349,11 +351,28 @@ void worker_main(lmff_server *s) {
       atoms += j->natoms;
     }
     s->points.erase(s->points.begin(), s->points.begin() + k);
-    bool md_work = !s->md_active.empty();
     lk.unlock();
     double t0 = now_s();
-    if (!pts.empty()) run_points(s, pts);
-    if (md_work) run_md_chunk(s);
+    run_points(s, pts);
+    double t1 = now_s();
+    lk.lock();
+    s->st.busy_s += t1 - t0;
+  }
+}
+
+// NVE requests: one chunk of the resident batch at a time
+void md_main(lmff_server *s) {
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    admit(s);
+    if (s->md_active.empty()) {
+      if (s->stop && s->queue.empty()) break;
+      s->cv_work.wait(lk);
+      continue;
+    }
+    lk.unlock();
+    double t0 = now_s();
+    run_md_chunk(s);
     double t1 = now_s();
     lk.lock();
     s->st.busy_s += t1 - t0;
@@ -383,7 +402,8 @@ int lmff_server_create(lmff_server **out, const lmff_engine *proto, const lmff_s
     delete s;
     return rc;
   }
-  s->worker = std::thread(worker_main, s);
+  s->w_points = std::thread(points_main, s);
+  s->w_md = std::thread(md_main, s);
   *out = s;
   return LMFF_OK;
 }
@@ -448,7 +468,7 @@ int enqueue(lmff_server *s, std::vector<Job *> &js, int64_t *tickets) {
     s->st.submitted++;
     tickets[k] = j->ticket;
   }
-  s->cv_work.notify_one();
+  s->cv_work.notify_all();
   return LMFF_OK;
 }
 
@@ -516,7 +536,8 @@ void lmff_server_destroy(lmff_server *s) {
     s->stop = true;
     s->cv_work.notify_all();
   }
-  if (s->worker.joinable()) s->worker.join();
+  if (s->w_points.joinable()) s->w_points.join();
+  if (s->w_md.joinable()) s->w_md.join();
   for (auto &kv : s->jobs) delete kv.second;
   lmff_destroy(s->pt);
   lmff_destroy(s->md);

@@ -58,7 +58,8 @@ class Stats(C.Structure):
                 ("list_per_atom", C.c_double), ("bytes_device", C.c_double), ("ms_last_build", C.c_double),
                 ("ms_last_forces", C.c_double), ("precision", C.c_int), ("tpa", C.c_int), ("block", C.c_int),
                 ("ms_last_run", C.c_double), ("kernel_ms", C.c_double * 6), ("kernel_launches", C.c_int64 * 6),
-                ("pairs_in_cutoff", C.c_int64), ("graph_steps", C.c_int64), ("graph_redos", C.c_int64)]
+                ("pairs_in_cutoff", C.c_int64), ("graph_steps", C.c_int64), ("graph_redos", C.c_int64),
+                ("bytes_per_atom_need", C.c_double)]
 KERNELS = ["pair_ilp", "tersoff", "intralayer_normals", "gather", "integrate", "neighbor_build"]
 
 

@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
+import os
 from typing import Dict, List, Optional
 
 import numpy as np
@@ -44,8 +45,15 @@ class System:
     def n(self) -> int:
         return int(self.x.shape[0])
 
+    def type_masses(self) -> np.ndarray:
+        """Mass of each type (index t-1): a data file's Masses section, else the 1=C,
+        2=B, 3=N convention."""
+        if "type_masses" in self.meta:
+            return np.asarray(self.meta["type_masses"], dtype=np.float64)
+        return np.array([MASSES[t] for t in range(1, 4)])
+
     def masses(self) -> np.ndarray:
-        return np.array([MASSES[int(t)] for t in range(1, 4)])[self.type - 1]
+        return self.type_masses()[self.type - 1]
 
     def copy(self) -> "System":
         return System(self.x.copy(), self.type.copy(), self.mol.copy(), self.tag.copy(),
@@ -307,6 +315,166 @@ def replica_set(count: int = 256, nmin: int = 500, nmax: int = 20000, seed: int 
         best.meta["replica"] = r
         out.append(best)
     return out
+
+
+# ----------------------------------------------------------------- replicate
+
+def replicate(s: System, nx: int, ny: int, nz: int) -> System:
+    """LAMMPS ``replicate nx ny nz`` on an orthogonal box (replicate.cpp): the box grows
+    to n times each length from the same lower corner; copy (ix, iy, iz) of an atom is
+    shifted by (ix Lx, iy Ly, iz Lz), wrapped into the new box on periodic dimensions
+    (Domain::remap), and gets tag + k*maxtag and, when its molecule id is positive,
+    mol + k*maxmol, with k = iz*ny*nx + iy*nx + ix.  Copies are appended in the loop
+    order ix, iy, iz (outer to inner) and atoms in their order within each copy.
+    Note the molecule offset: a layer replicated in-plane becomes several molecules, as
+    in the reference, which the ILP style then treats as different layers."""
+    if min(nx, ny, nz) < 1:
+        raise ValueError("replicate counts must be >= 1")
+    L = s.box_hi - s.box_lo
+    maxtag = int(s.tag.max()) if s.n else 0
+    maxmol = int(s.mol.max()) if s.n else 0
+    new_hi = s.box_lo + L * np.array([nx, ny, nz])
+    xs, ts, ms, gs, vs = [], [], [], [], []
+    for ix in range(nx):
+        for iy in range(ny):
+            for iz in range(nz):
+                k = iz * ny * nx + iy * nx + ix
+                x = s.x + L * np.array([ix, iy, iz])
+                for c in range(3):
+                    if s.periodic[c]:
+                        Lc = new_hi[c] - s.box_lo[c]
+                        x[:, c] = s.box_lo[c] + np.mod(x[:, c] - s.box_lo[c], Lc)
+                xs.append(x)
+                ts.append(s.type.copy())
+                ms.append(np.where(s.mol > 0, s.mol + k * maxmol, s.mol))
+                gs.append(s.tag + k * maxtag)
+                if s.v is not None:
+                    vs.append(s.v.copy())
+    meta = dict(s.meta)
+    meta["replicate"] = (nx, ny, nz)
+    return System(np.concatenate(xs), np.concatenate(ts).astype(np.int32), np.concatenate(ms).astype(np.int64),
+                  np.concatenate(gs).astype(np.int64), s.box_lo.copy(), new_hi, s.periodic.copy(),
+                  np.concatenate(vs) if vs else None, meta)
+
+
+# ------------------------------------------------------------------------- input
+
+_HEADER_KEYS = {"atoms", "bonds", "angles", "dihedrals", "impropers", "atom types", "bond types", "angle types",
+                "dihedral types", "improper types", "extra bond per atom", "extra angle per atom",
+                "extra dihedral per atom", "extra improper per atom", "extra special per atom", "ellipsoids",
+                "lines", "triangles", "bodies"}
+_SECTIONS = {"Atoms", "Velocities", "Masses", "Bonds", "Angles", "Dihedrals", "Impropers", "Pair Coeffs",
+             "PairIJ Coeffs", "Bond Coeffs", "Angle Coeffs", "Dihedral Coeffs", "Improper Coeffs",
+             "BondBond Coeffs", "BondAngle Coeffs", "MiddleBondTorsion Coeffs", "EndBondTorsion Coeffs",
+             "AngleTorsion Coeffs", "AngleAngleTorsion Coeffs", "BondBond13 Coeffs", "AngleAngle Coeffs",
+             "Ellipsoids", "Lines", "Triangles", "Bodies"}
+
+
+def read_lammps_data(path: str, periodic=(True, True, True)) -> System:
+    """A LAMMPS data file in atom_style full (read_data, read_data.cpp): header counts
+    and box, then sections.  Atoms lines are ``id mol type q x y z [ix iy iz]``
+    (coordinates kept as written, image flags kept in meta["image"]); Masses and
+    Velocities are read; other sections are skipped by their header counts.  Atoms are
+    returned in file order.  Tilted boxes are rejected.  ``periodic`` is the input
+    script's ``boundary`` (a data file does not carry it)."""
+    lines = open(path).read().split("\n")
+    counts: Dict[str, int] = {}
+    lo = np.zeros(3)
+    hi = np.zeros(3)
+    k = 1                                     # line 1 is a title
+    while k < len(lines):
+        raw = lines[k].split("#", 1)[0].strip()
+        if not raw:
+            k += 1
+            continue
+        if raw in _SECTIONS or raw.split()[0] in _SECTIONS:
+            break
+        w = raw.split()
+        if len(w) >= 4 and w[-2:] in (["xlo", "xhi"], ["ylo", "yhi"], ["zlo", "zhi"]):
+            c = "xyz".index(w[-2][0])
+            lo[c], hi[c] = float(w[0]), float(w[1])
+        elif len(w) >= 6 and w[-3:] == ["xy", "xz", "yz"]:
+            if any(float(t) != 0.0 for t in w[:3]):
+                raise ValueError("tilted (triclinic) boxes are not supported")
+        else:
+            key = " ".join(w[1:])
+            if key not in _HEADER_KEYS:
+                raise ValueError(f"{path}:{k + 1}: unknown header line '{raw}'")
+            counts[key] = int(w[0])
+        k += 1
+    natoms = counts.get("atoms", 0)
+    ntypes = counts.get("atom types", 0)
+    x = np.zeros((natoms, 3))
+    typ = np.zeros(natoms, dtype=np.int32)
+    mol = np.zeros(natoms, dtype=np.int64)
+    tag = np.zeros(natoms, dtype=np.int64)
+    img = np.zeros((natoms, 3), dtype=np.int64)
+    v = None
+    tmass = np.zeros(ntypes)
+    have_atoms = False
+    section_len = {"Atoms": natoms, "Velocities": natoms, "Masses": ntypes, "Bonds": counts.get("bonds", 0),
+                   "Angles": counts.get("angles", 0), "Dihedrals": counts.get("dihedrals", 0),
+                   "Impropers": counts.get("impropers", 0)}
+    coeff_len = {"Bond Coeffs": "bond types", "Angle Coeffs": "angle types", "Dihedral Coeffs": "dihedral types",
+                 "Improper Coeffs": "improper types"}
+
+    def body(start, n):
+        out, j = [], start
+        while len(out) < n:
+            if j >= len(lines):
+                raise ValueError(f"{path}: section ended after {len(out)} of {n} lines")
+            t = lines[j].split("#", 1)[0].strip()
+            if t:
+                out.append(t.split())
+            j += 1
+        return out, j
+
+    while k < len(lines):
+        raw = lines[k].split("#", 1)[0].strip()
+        if not raw:
+            k += 1
+            continue
+        name = raw
+        if name not in _SECTIONS:
+            raise ValueError(f"{path}:{k + 1}: unknown section '{raw}'")
+        if name in section_len:
+            n = section_len[name]
+        elif name in coeff_len:
+            n = counts.get(coeff_len[name], 0)
+        elif name in ("Pair Coeffs",):
+            n = ntypes
+        elif name == "PairIJ Coeffs":
+            n = ntypes * (ntypes + 1) // 2
+        else:
+            raise ValueError(f"{path}: section '{name}' is not supported")
+        rows, k = body(k + 1, n)
+        if name == "Atoms":
+            have_atoms = True
+            for r, w in enumerate(rows):
+                if len(w) not in (7, 10):
+                    raise ValueError(f"{path}: Atoms line '{' '.join(w)}' is not atom_style full")
+                tag[r], mol[r], typ[r] = int(w[0]), int(w[1]), int(w[2])
+                x[r] = [float(w[4]), float(w[5]), float(w[6])]
+                if len(w) == 10:
+                    img[r] = [int(w[7]), int(w[8]), int(w[9])]
+        elif name == "Masses":
+            for w in rows:
+                tmass[int(w[0]) - 1] = float(w[1])
+        elif name == "Velocities":
+            if not have_atoms:
+                raise ValueError(f"{path}: Velocities before Atoms")
+            index = {int(t): r for r, t in enumerate(tag)}
+            v = np.zeros((natoms, 3))
+            for w in rows:
+                v[index[int(w[0])]] = [float(w[1]), float(w[2]), float(w[3])]
+    if not have_atoms:
+        raise ValueError(f"{path}: no Atoms section")
+    if typ.size and (typ.min() < 1 or typ.max() > ntypes):
+        raise ValueError(f"{path}: atom type outside 1..{ntypes}")
+    meta = {"kind": "data_file", "path": os.path.basename(path), "ntypes": ntypes, "image": img}
+    if np.all(tmass > 0):
+        meta["type_masses"] = tmass
+    return System(x, typ, mol, tag, lo, hi, np.array(periodic, dtype=bool), v, meta)
 
 
 # ------------------------------------------------------------------------- output

@@ -4,7 +4,7 @@
 //
 // Test infrastructure only (built by oracle/ref.mk into oracle/_ref/).
 //
-//   lmff_ref <input-script> <out.bin> [lists] [-- <LAMMPS command-line arguments>]
+//   lmff_ref <input-script> <out.bin> [lists] [min] [-- <LAMMPS command-line arguments>]
 //
 // Without "--" LAMMPS runs quietly (-log none -screen none); after "--" the given
 // arguments are passed to LAMMPS instead (e.g. -sf gb300 -screen stdout).
@@ -14,6 +14,8 @@
 // With "lists", the ILP sub-style's full+ghost list (pair_ilp_graphene_hbn.cpp:402-405)
 // and its intralayer list (ILP_neigh, :681-745) are written as (tag_i, tag_j, image)
 // triples, image = periodic image of j relative to its owned copy.
+// With "min", the last minimize's statistics (Min::niter, neval, stop_condition,
+// einitial, efinal, fnorm2_final, fnorminf_final, alpha_final; min.h:23-27) are written.
 
 #include <cmath>
 #include <cstdio>
@@ -38,6 +40,7 @@
 #include "compute.h"
 #include "neigh_list.h"
 #include "update.h"
+#include "min.h"
 #include "pair_ilp_graphene_hbn.h"
 #undef protected
 
@@ -75,7 +78,11 @@ int main(int argc, char **argv) {
     fprintf(stderr, "usage: %s in.lmp out.bin [lists]\n", argv[0]);
     return 2;
   }
-  bool lists = argc > 3 && strcmp(argv[3], "lists") == 0;
+  bool lists = false, minstats = false;
+  for (int a = 3; a < argc && strcmp(argv[a], "--") != 0; a++) {
+    if (strcmp(argv[a], "lists") == 0) lists = true;
+    if (strcmp(argv[a], "min") == 0) minstats = true;
+  }
   std::vector<const char *> largs = {"lmff_ref", "-log", "none", "-screen", "none", "-nocite"};
   for (int a = 3; a < argc; a++)
     if (strcmp(argv[a], "--") == 0) {
@@ -144,6 +151,14 @@ int main(int argc, char **argv) {
     std::vector<double> ea;
     for (int ii = 0; ii < nlocal; ii++) ea.push_back(lmp->modify->compute[ic]->vector_atom[order[ii]]);
     rec("eatom", 'd', ea.size(), ea.data());
+  }
+
+  if (minstats && lmp->update->minimize) {
+    Min *m = lmp->update->minimize;
+    int64_t q[3] = {m->niter, m->neval, m->stop_condition};
+    rec("min_counts", 'q', 3, q);
+    double d[5] = {m->einitial, m->efinal, m->fnorm2_final, m->fnorminf_final, m->alpha_final};
+    rec("min_values", 'd', 5, d);
   }
 
   if (lists && ilp) {

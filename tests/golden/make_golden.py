@@ -83,6 +83,56 @@ timestep {dt}
         return read_records(out)
 
 
+REF = os.environ.get("LMFF_REFERENCE", "/root/reference")
+CASE = os.path.join(REF, "Cases", "case_5016")
+# the pair setup of the reference's own case script (Cases/case_5016/in.replicate.ilp_tersoff:77-81)
+CASE_PAIR = f"""pair_style hybrid/overlay tersoff ilp/graphene/hbn 16.0 0
+pair_coeff * * tersoff {POT}/C.opt.tersoff NULL C(O) C(O) C(O) C(O) C(O)
+pair_coeff * * ilp/graphene/hbn {POT}/BNCH.ILP C C C C C C
+"""
+
+
+def run_case(extra_setup="", run="run 0", flags=()):
+    """The reference's case_5016 data file through the reference: read_data, the
+    case's pair setup, then `extra_setup` and `run`."""
+    with tempfile.TemporaryDirectory() as td:
+        script = f"""units metal
+atom_style full
+boundary p p p
+atom_modify map array
+read_data {CASE}/inf0.data
+{extra_setup}
+{CASE_PAIR}
+neighbor 2.0 bin
+neigh_modify every 1 delay 0 check yes one 20000 page 200000
+compute peatom all pe/atom pair
+compute pesum all reduce sum c_peatom
+thermo_style custom step pe c_pesum press
+{run}
+"""
+        inp = os.path.join(td, "in.lmp")
+        open(inp, "w").write(script)
+        out = os.path.join(td, "out.bin")
+        subprocess.check_call([HARNESS, inp, out, *flags])
+        return read_records(out)
+
+
+def pack_case(r, extra=None):
+    n = len(r["tag"])
+    d = {"x": r["x"].reshape(n, 3), "f": r["f"].reshape(n, 3), "type": r["type"].astype(np.int32),
+         "mol": r["mol"], "tag": r["tag"], "box_lo": r["box"][:3], "box_hi": r["box"][3:],
+         "periodic": np.ones(3, dtype=np.int32), "e_tersoff": r["e_tersoff"][0], "e_ilp": r["e_ilp"][0],
+         "pvector": r["pvector"], "virial": r["virial"], "eatom": r["eatom"], "tap_flag": 0, "cut_global": 16.0,
+         "skin": 2.0, "tersoff_file": "C.opt.tersoff", "tersoff_elements": "NULL C(O) C(O) C(O) C(O) C(O)",
+         "ilp_elements": "C C C C C C"}
+    if "min_counts" in r:
+        d["min_counts"] = r["min_counts"]
+        d["min_values"] = r["min_values"]
+    if extra:
+        d.update(extra)
+    return d
+
+
 def pack(s: S.System, r, tap_flag, extra=None):
     n = s.n
     d = {
@@ -105,7 +155,12 @@ def pack(s: S.System, r, tap_flag, extra=None):
     return d
 
 
+ONLY = set(sys.argv[1:])     # optional: names of the fixtures to (re)generate
+
+
 def save(name, d):
+    if ONLY and name not in ONLY:
+        return
     path = os.path.join(OUT, f"{name}.npz")
     np.savez_compressed(path, **d)
     print(f"{name}: {len(d['tag'])} atoms, {os.path.getsize(path) / 1024:.0f} KiB")
@@ -144,6 +199,21 @@ def main():
     r20 = run_reference(h, nsteps=20)
     save("hetero_t20", pack(h, r20, 1, {"x0": r0["x"].reshape(-1, 3), "v0": r0["v"].reshape(-1, 3),
                                         "f0": r0["f"].reshape(-1, 3)}))
+    # 9. the reference's own case (Cases/case_5016: 6 graphene layers, 5016 atoms, layer 1
+    #    excluded from Tersoff by NULL, taper off): read_data, then forces
+    save("case5016", pack_case(run_case()))
+    # 10. the same after `replicate 2 1 1` (molecule ids offset per copy, as LAMMPS does)
+    save("case5016_rep2", pack_case(run_case("replicate 2 1 1")))
+    # 11. the case's minimisation (in.replicate.ilp_tersoff:123-125): layer 1 held by
+    #     setforce, CG with the quadratic line search, etol = ftol = 1e-5
+    r0 = run_case()
+    rm = run_case("group l1 type 1", "fix sf l1 setforce 0.0 0.0 0.0\nminimize 1.0e-5 1.0e-5 1000 10000",
+                  flags=("min",))
+    save("case5016_min", pack_case(rm, {"x0": r0["x"].reshape(-1, 3)}))
+    # 12. the same minimisation run to a tight energy tolerance: 135 CG iterations
+    rm = run_case("group l1 type 1", "fix sf l1 setforce 0.0 0.0 0.0\nminimize 1.0e-10 1.0e-3 300 3000",
+                  flags=("min",))
+    save("case5016_min_long", pack_case(rm, {"x0": r0["x"].reshape(-1, 3)}))
 
 
 if __name__ == "__main__":

@@ -29,6 +29,9 @@
  *                          Verlet::run (verlet.cpp:220-339) with FixNVE
  *                          (fix_nve.cpp:64-111) and Neighbor::decide / check_distance
  *                          (neighbor.cpp:1947-1976), device resident
+ *   lmff_minimize          Min::setup/run/cleanup with MinCG::iterate and
+ *                          MinLineSearch::linemin_quadratic (min.cpp, min_cg.cpp,
+ *                          min_linesearch.cpp), device resident
  *   lmff_batch_*           no counterpart: many independent systems per launch
  *   lmff_server_*          no counterpart: a request queue served by continuous batching
  *   lmff_last_error        error->one / error->all messages of both pair styles
@@ -158,6 +161,13 @@ int lmff_create(lmff_engine **out, const lmff_params *p, int device);
 int lmff_create_from_files(lmff_engine **out, const char *tersoff_file, const char *ilp_file,
                            int ntypes, const char *const *elements, double cut_global,
                            int tap_flag, double skin, int device);
+/* Same with one element list per style, as two pair_coeff lines give them, e.g.
+ * `pair_coeff * * tersoff C.opt.tersoff NULL C(O) ...` next to
+ * `pair_coeff * * ilp/graphene/hbn BNCH.ILP C C ...`. */
+int lmff_create_from_files2(lmff_engine **out, const char *tersoff_file,
+                            const char *const *tersoff_elements, const char *ilp_file,
+                            const char *const *ilp_elements, int ntypes, double cut_global,
+                            int tap_flag, double skin, int device);
 void lmff_destroy(lmff_engine *e);
 
 /* ---- configuration ---------------------------------------------------------------- */
@@ -224,6 +234,21 @@ int lmff_compute_resident(lmff_engine *e, int which, int eflag, int vflag, lmff_
 int lmff_run_nve(lmff_engine *e, int nsteps, double dt, int thermo_every, lmff_thermo *thermo);
 /* Copies back in the upload order; any pointer may be NULL. */
 int lmff_download(lmff_engine *e, double *x, double *v, double *f);
+
+/* Energy minimisation of the resident system: LAMMPS `minimize etol ftol maxiter
+ * maxeval` with the default min_style cg (Polak-Ribiere, min_cg.cpp) and quadratic
+ * line search (min_linesearch.cpp linemin_quadratic), min_modify dmax (0.1 A in the
+ * reference) and norm two.  frozen[natoms] (upload order, may be NULL): nonzero atoms
+ * keep zero force, as `fix setforce 0.0 0.0 0.0` on them does.  Positions and forces
+ * stay resident (lmff_download).  stop_condition follows min.h: 0 max iterations,
+ * 1 max evaluations, 2 energy tolerance, 3 force tolerance, 4 search direction not
+ * downhill, 5 linesearch alpha is zero, 6 forces are zero, 7 quadratic factors are zero. */
+typedef struct lmff_min_result {
+  int niter, neval, stop_condition;
+  double einitial, efinal, fnorm2_init, fnorminf_init, fnorm2_final, fnorminf_final, alpha_final;
+} lmff_min_result;
+int lmff_minimize(lmff_engine *e, double etol, double ftol, int maxiter, int maxeval, double dmax,
+                  const int *frozen, lmff_min_result *out);
 
 /* ---- batched independent systems --------------------------------------------------- */
 /* A batch holds many independent periodic systems in one flattened device layout and

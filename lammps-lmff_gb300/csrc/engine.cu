@@ -216,6 +216,117 @@ __global__ void k_setcond(cudaGraphConditionalHandle h, const unsigned long long
   cudaGraphSetConditional(h, d2 > trig2 ? 1u : 0u);
 }
 
+// ---------------------------------------------------------------- minimiser kernels
+// Conjugate-gradient vectors live in the caller's atom order (index o = perm[q]), so
+// list rebuilds, which re-sort the resident atoms, leave them in place.  SoA: [c*n + o].
+
+// fix setforce 0 0 0 on the atoms whose mask is 0 (fix_setforce.cpp min_post_force)
+__global__ void k_min_mask(int n, const int *perm, const int *mask, double *f) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n || mask[perm[q]]) return;
+  f[q] = 0.0;
+  f[n + q] = 0.0;
+  f[2 * n + q] = 0.0;
+}
+
+// mode 0: h = g = f; 1: g = f, h = g + beta h; 2: h = g; 3: x0 = x
+__global__ void k_min_vec(int mode, int n, const int *perm, const double *f, const d4 *xq, double *g, double *h,
+                          double *x0, double beta) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int o = perm[q];
+  if (mode == 3) {
+    d4 w = xq[q];
+    x0[o] = w.x;
+    x0[n + o] = w.y;
+    x0[2 * n + o] = w.z;
+    return;
+  }
+  for (int c = 0; c < 3; c++) {
+    size_t k = (size_t)c * n + o;
+    if (mode == 0) {
+      double v = f[(size_t)c * n + q];
+      g[k] = v;
+      h[k] = v;
+    } else if (mode == 1) {
+      double v = f[(size_t)c * n + q];
+      g[k] = v;
+      h[k] = v + beta * h[k];
+    } else {
+      h[k] = g[k];
+    }
+  }
+}
+
+// per-block partials of f.f, f.g, f.h, g.h (sums) and max|h|, max|f| (per component)
+constexpr int MIN_NQ = 6;
+__global__ void k_min_dots(int n, const int *perm, const double *f, const double *g, const double *h,
+                           double *part) {
+  double acc[MIN_NQ] = {0, 0, 0, 0, 0, 0};
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    int o = perm[q];
+    for (int c = 0; c < 3; c++) {
+      double fv = f[(size_t)c * n + q], gv = g[(size_t)c * n + o], hv = h[(size_t)c * n + o];
+      acc[0] += fv * fv;
+      acc[1] += fv * gv;
+      acc[2] += fv * hv;
+      acc[3] += gv * hv;
+      acc[4] = fmax(acc[4], fabs(hv));
+      acc[5] = fmax(acc[5], fabs(fv));
+    }
+  }
+  __shared__ double sh[MIN_NQ][256];
+  for (int k = 0; k < MIN_NQ; k++) sh[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s)
+      for (int k = 0; k < MIN_NQ; k++)
+        sh[k][threadIdx.x] = k < 4 ? sh[k][threadIdx.x] + sh[k][threadIdx.x + s]
+                                   : fmax(sh[k][threadIdx.x], sh[k][threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x < MIN_NQ) part[blockIdx.x * MIN_NQ + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// x = x0 + alpha h (min_linesearch.cpp alpha_step), with the displacement since the
+// last build for the rebuild test
+__global__ void k_min_step(int n, const int *perm, const double *x0, const double *h, double alpha, d4 *xq,
+                           const double *xhold, unsigned long long *maxdisp) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  double d2 = 0.0;
+  if (q < n) {
+    int o = perm[q];
+    d4 w = xq[q];
+    double a = x0[o], b = x0[n + o], c = x0[2 * n + o];
+    if (alpha > 0.0) {
+      a += alpha * h[o];
+      b += alpha * h[n + o];
+      c += alpha * h[2 * n + o];
+    }
+    xq[q] = make_d4(a, b, c, w.w);
+    double dx = a - xhold[3 * q], dy = b - xhold[3 * q + 1], dz = c - xhold[3 * q + 2];
+    d2 = dx * dx + dy * dy + dz * dz;
+  }
+  for (int o = 16; o > 0; o >>= 1) d2 = fmax(d2, __shfl_xor_sync(0xffffffff, d2, o));
+  if ((threadIdx.x & 31) == 0 && d2 > 0.0) atomicMax(maxdisp, (unsigned long long)__double_as_longlong(d2));
+}
+
+// after a rebuild wrapped atoms into the box: x0 = x + minimum_image(x0 - x)
+// (fix_minimize.cpp reset_coords with domain.cpp minimum_image)
+__global__ void k_min_reset(int n, const int *perm, const d4 *xq, const SysDesc *sys, const int *sysid, double *x0) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int o = perm[q];
+  const SysDesc &sd = sys[sysid[q]];
+  d4 w = xq[q];
+  double x[3] = {w.x, w.y, w.z};
+  for (int c = 0; c < 3; c++) {
+    double d = x0[(size_t)c * n + o] - x[c];
+    if (sd.per[c] && fabs(d) > 0.5 * sd.L[c]) d += d < 0.0 ? sd.L[c] : -sd.L[c];
+    x0[(size_t)c * n + o] = x[c] + d;
+  }
+}
+
 // Pair-list offsets past the capacity the step graph was captured with: clamp them so
 // that fill and the force kernels stay inside the array, and flag the overflow (the
 // host then redoes the chunk on the eager path, which grows the list).
@@ -414,6 +525,12 @@ struct Engine {
     cap_stream = nullptr;
     if (d_graph_rebuilds) cudaFree(d_graph_rebuilds);
     d_graph_rebuilds = nullptr;
+    void *mins[] = {m_x0, m_g, m_h, m_part, m_mask};
+    for (void *b : mins)
+      if (b) cudaFree(b);
+    m_x0 = m_g = m_h = m_part = nullptr;
+    m_mask = nullptr;
+    m_cap = 0;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
   }
@@ -1586,6 +1703,205 @@ struct Engine {
     return LMFF_OK;
   }
 
+  // ---------------------------------------------------------------- minimiser
+  // min_style cg with the quadratic line search (the reference defaults: min_cg.cpp
+  // iterate, min_linesearch.cpp linemin_quadratic / alpha_step, min.cpp setup / run /
+  // energy_force / cleanup; dmax 0.1, norm two, no normalisation of thermo energies).
+  double *m_x0 = nullptr, *m_g = nullptr, *m_h = nullptr, *m_part = nullptr;
+  int *m_mask = nullptr;
+  int m_cap = 0;
+  bool m_masked = false;
+  int m_nblk = 0;
+  double m_red[MIN_NQ];
+
+  int min_alloc() {
+    if (m_cap < cap_n) {
+      CK(dalloc(m_x0, 3 * (size_t)cap_n)); CK(dalloc(m_g, 3 * (size_t)cap_n)); CK(dalloc(m_h, 3 * (size_t)cap_n));
+      CK(dalloc(m_mask, cap_n)); CK(dalloc(m_part, 1024 * MIN_NQ));
+      m_cap = cap_n;
+    }
+    m_nblk = std::min(1024, std::max(1, (n + 255) / 256));
+    return LMFF_OK;
+  }
+
+  // m_red = {f.f, f.g, f.h, g.h, max|h|, max|f|} over all atoms
+  int min_dots() {
+    k_min_dots<<<m_nblk, 256, 0, stream>>>(n, d.perm, d.f, m_g, m_h, m_part);
+    CK(cudaGetLastError());
+    std::vector<double> part((size_t)m_nblk * MIN_NQ);
+    CK(cudaMemcpyAsync(part.data(), m_part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    for (int k = 0; k < MIN_NQ; k++) m_red[k] = 0.0;
+    for (int b = 0; b < m_nblk; b++)
+      for (int k = 0; k < MIN_NQ; k++)
+        m_red[k] = k < 4 ? m_red[k] + part[(size_t)b * MIN_NQ + k] : std::max(m_red[k], part[(size_t)b * MIN_NQ + k]);
+    return LMFF_OK;
+  }
+
+  void min_vec(int mode, double beta) {
+    k_min_vec<<<(n + 255) / 256, 256, 0, stream>>>(mode, n, d.perm, d.f, d.xq, m_g, m_h, m_x0, beta);
+  }
+
+  // Min::energy_force: rebuild if needed, forces and energy; with resetflag, the line
+  // origin follows atoms that the rebuild wrapped across the box
+  int min_energy(int resetflag, double &e) {
+    int64_t rb = rebuilds;
+    int rc = maybe_rebuild();
+    if (rc) return rc;
+    if (rebuilds != rb && resetflag) {
+      k_min_reset<<<(n + 255) / 256, 256, 0, stream>>>(n, d.perm, d.xq, d.sys, d.sysid, m_x0);
+      CK(cudaGetLastError());
+    }
+    std::vector<lmff_result> hr;
+    rc = forces(LMFF_TERSOFF | LMFF_ILP, true, false, &hr);
+    if (rc) return rc;
+    if (m_masked) {
+      k_min_mask<<<(n + 255) / 256, 256, 0, stream>>>(n, d.perm, m_mask, d.f);
+      CK(cudaGetLastError());
+    }
+    e = 0.0;
+    for (auto &r : hr) e += r.e_tersoff + r.e_ilp;
+    return LMFF_OK;
+  }
+
+  // MinLineSearch::alpha_step
+  int min_alpha_step(double alpha, int resetflag, int &neval, double &e) {
+    k_min_step<<<(n + 255) / 256, 256, 0, stream>>>(n, d.perm, m_x0, m_h, alpha, d.xq, d.xhold, d.maxdisp);
+    CK(cudaGetLastError());
+    hilo_fresh = false;
+    forces_valid = false;
+    neval++;
+    return min_energy(resetflag, e);
+  }
+
+  enum { MIN_MAXITER, MIN_MAXEVAL, MIN_ETOL, MIN_FTOL, MIN_DOWNHILL, MIN_ZEROALPHA, MIN_ZEROFORCE, MIN_ZEROQUAD };
+
+  // MinLineSearch::linemin_quadratic; returns 0 or a stop condition
+  int min_linemin(double eoriginal, double &ecurrent, double &alpha, int &neval, double dmax, int &err) {
+    const double ALPHA_MAX = 1.0, ALPHA_REDUCE = 0.5, BACKTRACK_SLOPE = 0.4, QUADRATIC_TOL = 0.1, EMACH = 1.0e-8,
+                 EPS_QUAD = 1.0e-28;
+    err = min_dots();
+    if (err) return 0;
+    double fdothall = m_red[2];
+    if (fdothall <= 0.0) return MIN_DOWNHILL;
+    double hmaxall = m_red[4];
+    if (hmaxall == 0.0) return MIN_ZEROFORCE;
+    double alphamax = std::min(ALPHA_MAX, dmax / hmaxall);
+    min_vec(3, 0.0);
+    alpha = alphamax;
+    double fhprev = fdothall, engprev = eoriginal, alphaprev = 0.0;
+    for (;;) {
+      err = min_alpha_step(alpha, 1, neval, ecurrent);
+      if (err) return 0;
+      err = min_dots();
+      if (err) return 0;
+      double fh = m_red[2];
+      double delfh = fh - fhprev;
+      if (fabs(fh) < EPS_QUAD || fabs(delfh) < EPS_QUAD) {
+        err = min_alpha_step(0.0, 0, neval, ecurrent);
+        return err ? 0 : MIN_ZEROQUAD;
+      }
+      double relerr = fabs(1.0 - (0.5 * (alpha - alphaprev) * (fh + fhprev) + ecurrent) / engprev);
+      double alpha0 = alpha - (alpha - alphaprev) * fh / delfh;
+      if (relerr <= QUADRATIC_TOL && alpha0 > 0.0 && alpha0 < alphamax) {
+        err = min_alpha_step(alpha0, 1, neval, ecurrent);
+        if (err) return 0;
+        if (ecurrent - eoriginal < EMACH) return 0;
+      }
+      double de_ideal = -BACKTRACK_SLOPE * alpha * fdothall;
+      double de = ecurrent - eoriginal;
+      if (de <= de_ideal) return 0;
+      fhprev = fh;
+      engprev = ecurrent;
+      alphaprev = alpha;
+      alpha *= ALPHA_REDUCE;
+      if (alpha <= 0.0 || de_ideal >= -EMACH) {
+        err = min_alpha_step(0.0, 0, neval, ecurrent);
+        return err ? 0 : MIN_ZEROALPHA;
+      }
+    }
+  }
+
+  int minimize(double etol, double ftol, int maxiter, int maxeval, double dmax, const int *frozen,
+               lmff_min_result *out) {
+    if (!loaded) return fail(LMFF_EINVAL, "no resident system: call lmff_upload first");
+    if (!(dmax > 0.0) || maxiter < 0 || maxeval < 0) return fail(LMFF_EINVAL, "minimize: bad tolerance or limit");
+    memset(out, 0, sizeof *out);
+    if (n == 0) return LMFF_OK;
+    int rc = min_alloc();
+    if (rc) return rc;
+    m_masked = frozen != nullptr;
+    if (m_masked) {
+      std::vector<int> mk(n);
+      for (int i = 0; i < n; i++) mk[i] = frozen[i] ? 0 : 1;
+      CK(cudaMemcpyAsync(m_mask, mk.data(), sizeof(int) * n, cudaMemcpyHostToDevice, stream));
+    }
+    const double EPS_ENERGY = 1.0e-8;
+    int neval = 0, niter = 0, err = 0;
+    double ecurrent = 0.0, eprevious = 0.0, alpha_final = 0.0;
+    // Min::setup
+    forces_valid = false;
+    rc = min_energy(0, ecurrent);
+    if (rc) return rc;
+    out->einitial = ecurrent;
+    min_vec(0, 0.0);
+    rc = min_dots();
+    if (rc) return rc;
+    out->fnorm2_init = std::sqrt(m_red[0]);
+    out->fnorminf_init = m_red[5];
+    // MinCG::iterate
+    int64_t nlimit = std::min<int64_t>(INT32_MAX, 3 * (int64_t)n);
+    double gg = m_red[0];
+    int stop = MIN_MAXITER;
+    for (int iter = 0; iter < maxiter; iter++) {
+      niter++;
+      eprevious = ecurrent;
+      int fl = min_linemin(ecurrent, ecurrent, alpha_final, neval, dmax, err);
+      if (err) return err;
+      if (fl) {
+        stop = fl;
+        break;
+      }
+      if (neval >= maxeval) {
+        stop = MIN_MAXEVAL;
+        break;
+      }
+      if (fabs(ecurrent - eprevious) < etol * 0.5 * (fabs(ecurrent) + fabs(eprevious) + EPS_ENERGY)) {
+        stop = MIN_ETOL;
+        break;
+      }
+      rc = min_dots();
+      if (rc) return rc;
+      double ff = m_red[0], fg = m_red[1];
+      if (ftol > 0.0 && ff < ftol * ftol) {
+        stop = MIN_FTOL;
+        break;
+      }
+      double beta = std::max(0.0, (ff - fg) / gg);
+      if ((niter + 1) % nlimit == 0) beta = 0.0;
+      gg = ff;
+      min_vec(1, beta);
+      rc = min_dots();
+      if (rc) return rc;
+      if (m_red[3] <= 0.0) min_vec(2, 0.0);
+    }
+    // Min::run: a final evaluation unless the iteration limit ended it; Min::cleanup
+    if (stop != MIN_MAXITER) {
+      rc = min_energy(0, ecurrent);
+      if (rc) return rc;
+    }
+    rc = min_dots();
+    if (rc) return rc;
+    out->niter = niter;
+    out->neval = neval;
+    out->stop_condition = stop;
+    out->efinal = ecurrent;
+    out->fnorm2_final = std::sqrt(m_red[0]);
+    out->fnorminf_final = m_red[5];
+    out->alpha_final = alpha_final;
+    return LMFF_OK;
+  }
+
   int count_pairs() {
     if (!built || n == 0) {
       pairs_in_cut = 0;
@@ -2051,16 +2367,24 @@ int lmff_create(lmff_engine **out, const lmff_params *p, int device) {
 
 int lmff_create_from_files(lmff_engine **out, const char *tersoff_file, const char *ilp_file, int ntypes,
                            const char *const *elements, double cut_global, int tap_flag, double skin, int device) {
-  if (!out || !elements || ntypes < 1 || ntypes > lmff::MAXTYPE) return LMFF_EINVAL;
+  return lmff_create_from_files2(out, tersoff_file, elements, ilp_file, elements, ntypes, cut_global, tap_flag, skin,
+                                 device);
+}
+
+int lmff_create_from_files2(lmff_engine **out, const char *tersoff_file, const char *const *tersoff_elements,
+                            const char *ilp_file, const char *const *ilp_elements, int ntypes, double cut_global,
+                            int tap_flag, double skin, int device) {
+  if (!out || ntypes < 1 || ntypes > lmff::MAXTYPE) return LMFF_EINVAL;
+  if ((tersoff_file && !tersoff_elements) || (ilp_file && !ilp_elements)) return LMFF_EINVAL;
   *out = nullptr;
   lmff::HostTersoff ht;
   lmff::HostIlp hi;
   std::string err;
-  if (tersoff_file && !lmff::parse_tersoff(tersoff_file, ntypes, elements, ht, err)) {
+  if (tersoff_file && !lmff::parse_tersoff(tersoff_file, ntypes, tersoff_elements, ht, err)) {
     g_create_error = err;
     return LMFF_EBADPARAM;
   }
-  if (ilp_file && !lmff::parse_ilp(ilp_file, ntypes, elements, hi, err)) {
+  if (ilp_file && !lmff::parse_ilp(ilp_file, ntypes, ilp_elements, hi, err)) {
     g_create_error = err;
     return LMFF_EBADPARAM;
   }
@@ -2223,6 +2547,13 @@ int lmff_batch_compute(lmff_engine *e, double *f_out, lmff_result *res) {
   if (!e) return LMFF_EINVAL;
   DeviceCall dc(e->e);
   return e->e.batch_compute(f_out, res);
+}
+
+int lmff_minimize(lmff_engine *e, double etol, double ftol, int maxiter, int maxeval, double dmax,
+                  const int *frozen, lmff_min_result *out) {
+  if (!e || !out) return LMFF_EINVAL;
+  DeviceCall dc(e->e);
+  return e->e.minimize(etol, ftol, maxiter, maxeval, dmax, frozen, out);
 }
 
 int lmff_batch_results(lmff_engine *e, int nsys, lmff_result *res) {

@@ -60,6 +60,12 @@ class Stats(C.Structure):
                 ("ms_last_run", C.c_double), ("kernel_ms", C.c_double * 6), ("kernel_launches", C.c_int64 * 6),
                 ("pairs_in_cutoff", C.c_int64), ("graph_steps", C.c_int64), ("graph_redos", C.c_int64),
                 ("bytes_per_atom_need", C.c_double)]
+class MinResult(C.Structure):
+    _fields_ = [("niter", C.c_int), ("neval", C.c_int), ("stop_condition", C.c_int), ("einitial", C.c_double),
+                ("efinal", C.c_double), ("fnorm2_init", C.c_double), ("fnorminf_init", C.c_double),
+                ("fnorm2_final", C.c_double), ("fnorminf_final", C.c_double), ("alpha_final", C.c_double)]
+
+
 KERNELS = ["pair_ilp", "tersoff", "intralayer_normals", "gather", "integrate", "neighbor_build"]
 
 
@@ -86,6 +92,9 @@ def load_library(path: str = LIB_PATH):
         "lmff_device_count": ([], I),
         "lmff_create": ([C.POINTER(P), P, I], I),
         "lmff_create_from_files": ([C.POINTER(P), C.c_char_p, C.c_char_p, I, C.POINTER(C.c_char_p), D, I, D, I], I),
+        "lmff_create_from_files2": ([C.POINTER(P), C.c_char_p, C.POINTER(C.c_char_p), C.c_char_p,
+                                     C.POINTER(C.c_char_p), I, D, I, D, I], I),
+        "lmff_minimize": ([P, D, D, I, I, D, P, P], I),
         "lmff_destroy": ([P], None),
         "lmff_set_precision": ([P, I], I),
         "lmff_set_box": ([P, P, P, D, D, D, P], I),
@@ -138,16 +147,28 @@ class Engine:
 
     def __init__(self, tersoff_file: Optional[str] = None, ilp_file: Optional[str] = None,
                  elements: Sequence[str] = ("C", "B", "N"), cut_global: float = 16.0, tap_flag: int = 1,
-                 skin: float = 2.0, device: int = 0, precision: int = FP64):
+                 skin: float = 2.0, device: int = 0, precision: int = FP64,
+                 ilp_elements: Optional[Sequence[str]] = None):
+        """elements: type -> element name for both files (pair_coeff * * ... C B N);
+        ilp_elements, if given, a separate list for the ILP file (the Tersoff file then
+        uses `elements`), e.g. elements = NULL C(O) ... with ilp_elements = C C ..."""
         lib = load_library()
         if tersoff_file is None and ilp_file is None:
             tersoff_file = os.path.join(POTENTIALS, "BNC.tersoff")
             ilp_file = os.path.join(POTENTIALS, "BNCH.ILP")
         self._h = C.c_void_p()
         arr = (C.c_char_p * len(elements))(*[e.encode() for e in elements])
-        rc = lib.lmff_create_from_files(C.byref(self._h), tersoff_file.encode() if tersoff_file else None,
-                                        ilp_file.encode() if ilp_file else None, len(elements), arr, cut_global,
-                                        tap_flag, skin, device)
+        if ilp_elements is None:
+            rc = lib.lmff_create_from_files(C.byref(self._h), tersoff_file.encode() if tersoff_file else None,
+                                            ilp_file.encode() if ilp_file else None, len(elements), arr, cut_global,
+                                            tap_flag, skin, device)
+        else:
+            if len(ilp_elements) != len(elements):
+                raise ValueError("elements and ilp_elements must name the same number of types")
+            arr2 = (C.c_char_p * len(ilp_elements))(*[e.encode() for e in ilp_elements])
+            rc = lib.lmff_create_from_files2(C.byref(self._h), tersoff_file.encode() if tersoff_file else None, arr,
+                                             ilp_file.encode() if ilp_file else None, arr2, len(elements),
+                                             cut_global, tap_flag, skin, device)
         if rc != 0:
             raise LmffError(rc, lib.lmff_last_error(None).decode())
         self.ntypes = len(elements)
@@ -225,7 +246,11 @@ class Engine:
         return r.to_dict()
 
     # -------------------------------------------------------------- resident MD
-    def upload(self, s, masses=(12.011, 10.811, 14.0067)):
+    def upload(self, s, masses=None):
+        """Make `s` the resident system.  masses (per type) default to the system's
+        (a data file's Masses section), else C, B, N."""
+        if masses is None:
+            masses = s.type_masses() if hasattr(s, "type_masses") else (12.011, 10.811, 14.0067)
         self.set_box(s.box_lo, s.box_hi, s.periodic)
         x = _f64(s.x)
         v = None if s.v is None else _f64(s.v)
@@ -247,6 +272,16 @@ class Engine:
         self._ck(_lib.lmff_run_nve(self._h, nsteps, dt, thermo_every, C.cast(th, C.c_void_p) if nth else None))
         return [{"step": t.step, "pe": t.pe, "ke": t.ke, "etotal": t.etotal, "temp": t.temp,
                  "virial": np.array(t.virial[:])} for t in th[:nth]]
+
+    def minimize(self, etol: float, ftol: float, maxiter: int, maxeval: int, dmax: float = 0.1,
+                 frozen: Optional[np.ndarray] = None) -> Dict:
+        """LAMMPS `minimize etol ftol maxiter maxeval` (min_style cg, line quadratic) on
+        the resident system; frozen atoms (nonzero, upload order) keep zero force."""
+        r = MinResult()
+        fz = None if frozen is None else np.ascontiguousarray(frozen, dtype=np.int32)
+        self._ck(_lib.lmff_minimize(self._h, etol, ftol, maxiter, maxeval, dmax, _p(fz),
+                                    C.cast(C.pointer(r), C.c_void_p)))
+        return {k: getattr(r, k) for k, _ in MinResult._fields_}
 
     def download(self):
         x = np.zeros((self._n, 3))

@@ -183,7 +183,9 @@ int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double 
  * "graphs" 1 (default) = lmff_run_nve replays steps between thermo samples as one CUDA
  * graph per step (integrate, displacement test, conditional list rebuild, forces,
  * integrate) with no host synchronisation; 0 = one host-driven step at a time.
- * Per-kernel timing uses the host-driven loop.  "graph_list_cap" > 0 lowers the
+ * Per-kernel timing uses the host-driven loop, and so does every engine created while
+ * the environment variable LMFF_GB300_GRAPHS is "0" (profilers cannot look inside a
+ * graph that has conditional nodes).  "graph_list_cap" > 0 lowers the
  * pair-list capacity a graph's rebuild may fill (testing the overflow redo: a chunk
  * whose rebuild overflows is redone host-driven from its first step, rebuilding the
  * list there, so it equals the uninterrupted run up to summation order). */

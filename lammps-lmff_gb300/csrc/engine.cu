@@ -362,6 +362,36 @@ static cudaError_t dalloc(T *&p, size_t count) {
   return cudaMalloc((void **)&p, count * sizeof(T));
 }
 
+// Binning and double-float geometry of one orthogonal box (lo, L, periodicity): bins
+// of at least (cutneigh/2)*1.0001 so that any pair within cutneigh is at most `reach`
+// bins apart whatever the rounding of the bin index; R = periodic images needed.
+static void sys_geometry(SysDesc &sd, const double lo[3], const double L[3], const int per[3], double cutneigh_max,
+                         int &R) {
+  double target = 0.5 * cutneigh_max * 1.0001, maxL = 0.0;
+  for (int k = 0; k < 3; k++) {
+    sd.lo[k] = lo[k];
+    sd.L[k] = L[k];
+    sd.per[k] = per[k] != 0;
+    int nb = std::max(1, (int)std::floor(sd.L[k] / target));
+    if (nb > 4096) nb = 4096;
+    double bs = sd.L[k] / nb;
+    sd.nb[k] = nb;
+    sd.binv[k] = 1.0 / bs;
+    sd.reach[k] = (int)std::ceil(cutneigh_max / bs * (1.0 + 1e-12));
+    // images needed: |s| <= ceil(reach / nb) for a stencil of +-reach bins
+    if (sd.per[k]) R = std::max(R, (sd.reach[k] + nb - 1) / nb);
+    sd.Lhi[k] = (float)sd.L[k];
+    sd.Llo[k] = (float)(sd.L[k] - (double)sd.Lhi[k]);
+    maxL = std::max(maxL, sd.L[k]);
+  }
+  sd.base = std::ldexp(1.0, (int)std::ceil(std::log2(maxL + 64.0)));
+  // hi parts alone differ from the displacement by the lo parts, the lo part of the
+  // image shift and one rounding: a few ulp of 2*base per component
+  double e = 4.0 * std::ldexp(2.0 * sd.base, -23);
+  double r = cutneigh_max + 2.0 * e;
+  sd.prefilt_sq = (float)(r * r * (1.0 + 1e-5));
+}
+
 struct Engine {
   uint64_t table_hash = 0;  // content hash of the constant tables (pot64, pot32, nbc, cutILPsq)
   int device = 0;
@@ -369,6 +399,7 @@ struct Engine {
   int precision = LMFF_FP64;
   int tpa = 16, block = 128;
   int list_full = 0;
+  int ilp_prefetch = 0;   // option "ilp_prefetch": software-pipelined pair kernel
   double skin = 2.0;
   int ntypes = 0;
   HostTersoff ht;
@@ -693,6 +724,7 @@ struct Engine {
     rshort = std::max(rmaxilp, t_on ? ht.cutmax : 0.0) + skin;
     nbc.rshortsq_d = rshort * rshort;
     nbc.rshortsq_f = (float)(rshort * rshort);
+    nbc.innersq_f = (float)(cut_global * cut_global);
     hash_tables();
     pot_dirty = true;
     built = false;
@@ -726,6 +758,10 @@ struct Engine {
     if (cudaGetDeviceCount(&cnt) != cudaSuccess || cnt == 0) return fail(LMFF_ENODEV, "no CUDA device");
     if (dev < 0 || dev >= cnt) return fail(LMFF_EINVAL, "device index out of range");
     device = dev;
+    // LMFF_GB300_GRAPHS=0 turns the step graphs off (profilers cannot look inside a
+    // graph with conditional nodes); the option "graphs" does the same per engine
+    const char *eg = getenv("LMFF_GB300_GRAPHS");
+    if (eg && eg[0] == '0') use_graphs = false;
     CK(cudaSetDevice(dev));
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaMalloc(&d.status, sizeof(int)));
@@ -859,31 +895,20 @@ struct Engine {
   int make_sys(std::vector<SysDesc> &out, const std::vector<std::array<double, 9>> &boxes) {
     out.clear();
     int bin_begin = 0;
-    double target = 0.5 * cutneigh_max * 1.0001;
     int R = 0;
     for (size_t s = 0; s < boxes.size(); s++) {
       const auto &b = boxes[s];
       SysDesc sd;
       memset(&sd, 0, sizeof sd);
-      double maxL = 0.0;
+      double lo[3], L[3];
+      int per[3];
       for (int k = 0; k < 3; k++) {
-        sd.lo[k] = b[k];
-        sd.L[k] = b[3 + k] - b[k];
-        sd.per[k] = b[6 + k] != 0.0;
-        if (!(sd.L[k] > 0.0)) return fail(LMFF_EINVAL, "box length must be positive");
-        int nb = std::max(1, (int)std::floor(sd.L[k] / target));
-        if (nb > 4096) nb = 4096;
-        double bs = sd.L[k] / nb;
-        sd.nb[k] = nb;
-        sd.binv[k] = 1.0 / bs;
-        sd.reach[k] = (int)std::ceil(cutneigh_max / bs * (1.0 + 1e-12));
-        // images needed: |s| <= ceil(reach / nb) for a stencil of +-reach bins
-        if (sd.per[k]) R = std::max(R, (sd.reach[k] + nb - 1) / nb);
-        sd.Lhi[k] = (float)sd.L[k];
-        sd.Llo[k] = (float)(sd.L[k] - (double)sd.Lhi[k]);
-        maxL = std::max(maxL, sd.L[k]);
+        lo[k] = b[k];
+        L[k] = b[3 + k] - b[k];
+        per[k] = b[6 + k] != 0.0;
+        if (!(L[k] > 0.0)) return fail(LMFF_EINVAL, "box length must be positive");
       }
-      sd.base = std::ldexp(1.0, (int)std::ceil(std::log2(maxL + 64.0)));
+      sys_geometry(sd, lo, L, per, cutneigh_max, R);
       sd.bin_begin = bin_begin;
       long long nbins = (long long)sd.nb[0] * sd.nb[1] * sd.nb[2];
       if (bin_begin + nbins > (1LL << 30)) return fail(LMFF_EOVERFLOW, "too many bins");
@@ -983,6 +1008,7 @@ struct Engine {
     a.sysid = d.sysid;
     a.bin_start = d.bin_start;
     a.bin_end = d.bin_end;
+    a.nbins = d.nbins;
     a.list_off = d.list_off;
     a.list = d.list;
     a.list_cap = d.list_cap;
@@ -1110,6 +1136,8 @@ struct Engine {
     a.eatom_ters = eatom_ters;
     a.f_out = d.f;
     a.status = d.status;
+    a.list_full = list_full;
+    a.ilp_prefetch = ilp_prefetch;
     return a;
   }
 
@@ -1423,6 +1451,7 @@ struct Engine {
     a.sysid = d.sysid;
     a.bin_start = d.bin_start;
     a.bin_end = d.bin_end;
+    a.nbins = d.nbins;
     a.list_off = d.list_off;
     a.list = d.list;
     a.list_cap = graph_cap;
@@ -2115,24 +2144,11 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
   // geometry of the one system (same binning rules as the resident path)
   SysDesc sd;
   memset(&sd, 0, sizeof sd);
-  double target = 0.5 * g.cutneigh_max * 1.0001, maxL = 0.0;
   int R = 0;
-  for (int k = 0; k < 3; k++) {
-    sd.lo[k] = g.blo[k];
-    sd.L[k] = g.bhi[k] - g.blo[k];
-    sd.per[k] = g.bper[k];
-    int nb = std::max(1, (int)std::floor(sd.L[k] / target));
-    if (nb > 4096) nb = 4096;
-    double bs = sd.L[k] / nb;
-    sd.nb[k] = nb;
-    sd.binv[k] = 1.0 / bs;
-    sd.reach[k] = (int)std::ceil(g.cutneigh_max / bs * (1.0 + 1e-12));
-    if (sd.per[k]) R = std::max(R, (sd.reach[k] + nb - 1) / nb);
-    sd.Lhi[k] = (float)sd.L[k];
-    sd.Llo[k] = (float)(sd.L[k] - (double)sd.Lhi[k]);
-    maxL = std::max(maxL, sd.L[k]);
+  {
+    double L[3] = {g.bhi[0] - g.blo[0], g.bhi[1] - g.blo[1], g.bhi[2] - g.blo[2]};
+    sys_geometry(sd, g.blo, L, g.bper, g.cutneigh_max, R);
   }
-  sd.base = std::ldexp(1.0, (int)std::ceil(std::log2(maxL + 64.0)));
   sd.atom_begin = 0;
   sd.atom_end = nn;
   long long nbins = (long long)sd.nb[0] * sd.nb[1] * sd.nb[2];
@@ -2202,6 +2218,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
   na.sysid = sysid2;
   na.bin_start = bin_start;
   na.bin_end = bin_end;
+  na.nbins = nbins;
   na.list_off = list_off;
   na.list = list;
   na.list_cap = (int64_t)list_cap;
@@ -2253,6 +2270,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
     a.status = status;
     a.do_ters = g.t_on && (which & LMFF_TERSOFF);
     a.do_ilp = g.i_on && (which & LMFF_ILP);
+    a.list_full = g.list_full;
   };
   const bool ev = true;
   if (g.precision == LMFF_FP64) {
@@ -2461,6 +2479,9 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
     e->e.skin = value;
     e->e.build_consts();
     e->e.loaded = false;
+  } else if (k == "ilp_prefetch") {
+    e->e.ilp_prefetch = value != 0.0;
+    e->e.drop_graph();
   } else if (k == "graphs") {
     e->e.use_graphs = value != 0.0;
     e->e.drop_graph();

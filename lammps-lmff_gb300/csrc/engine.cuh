@@ -92,6 +92,8 @@ struct SysDesc {
   double binv[3];             // 1 / bin size
   double base;                // double-float offset (x - lo + 32 + base in [base, 2 base))
   float Lhi[3], Llo[3];       // L split into two floats
+  float prefilt_sq;           // list build: a candidate whose hi-part distance squared
+                              // exceeds this is beyond every cutoff (rounding margin in)
 };
 
 // list entry: neighbour index in the low IBITS, image code above (3 fields of W bits)

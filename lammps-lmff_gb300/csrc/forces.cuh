@@ -97,6 +97,21 @@ struct AtomI<double> {
     dz = __dsub_rn(z, zj);
     jinfo = __double_as_longlong(q.w);
   }
+  // the same split into a load (issued early) and the arithmetic
+  struct J {
+    d4 q;
+  };
+  __device__ __forceinline__ J fetch(const AtomArrays &A, int j) const { return J{A.xq[j]}; }
+  __device__ __forceinline__ void disp_from(const J &t, const SysDesc &sd, int sx, int sy, int sz, double &dx,
+                                            double &dy, double &dz, long long &jinfo) const {
+    double xj = sx ? __dadd_rn(t.q.x, sx * sd.L[0]) : t.q.x;
+    double yj = sy ? __dadd_rn(t.q.y, sy * sd.L[1]) : t.q.y;
+    double zj = sz ? __dadd_rn(t.q.z, sz * sd.L[2]) : t.q.z;
+    dx = __dsub_rn(x, xj);
+    dy = __dsub_rn(y, yj);
+    dz = __dsub_rn(z, zj);
+    jinfo = __double_as_longlong(t.q.w);
+  }
 };
 
 template <>
@@ -122,6 +137,19 @@ struct AtomI<float> {
     dy = ((hy - h.y) - syh) + ((ly - l.y) - syl);
     dz = ((hz - h.z) - szh) + ((lz - l.z) - szl);
     jinfo = (long long)__float_as_int(h.w);
+  }
+  struct J {
+    float4 h, l;
+  };
+  __device__ __forceinline__ J fetch(const AtomArrays &A, int j) const { return J{__ldg(&A.xh[j]), __ldg(&A.xl[j])}; }
+  __device__ __forceinline__ void disp_from(const J &t, const SysDesc &sd, int sx, int sy, int sz, float &dx, float &dy,
+                                            float &dz, long long &jinfo) const {
+    float sxh = (float)sx * sd.Lhi[0], syh = (float)sy * sd.Lhi[1], szh = (float)sz * sd.Lhi[2];
+    float sxl = (float)sx * sd.Llo[0], syl = (float)sy * sd.Llo[1], szl = (float)sz * sd.Llo[2];
+    dx = ((hx - t.h.x) - sxh) + ((lx - t.l.x) - sxl);
+    dy = ((hy - t.h.y) - syh) + ((ly - t.l.y) - syl);
+    dz = ((hz - t.h.z) - szh) + ((lz - t.l.z) - szl);
+    jinfo = (long long)__float_as_int(t.h.w);
   }
 };
 
@@ -173,6 +201,8 @@ struct ForceArgs {
   double *f_out;       // 3*n SoA (k_finish)
   int *status;
   int do_ters, do_ilp;
+  int list_full;       // the pair list also holds same-molecule / non-ILP pairs
+  int ilp_prefetch;    // pair kernel loads the next pair's data one iteration ahead
 };
 
 }  // namespace lmff

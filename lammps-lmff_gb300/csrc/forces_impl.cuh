@@ -417,8 +417,122 @@ __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
 // force on each intralayer neighbour (ilp_c slots).
 // ONE: every ILP-mapped type is the same element, so the pair parameters are read at a
 // compile-time constant index (constant-bank operands, no per-pair loads).
-template <int TPA, bool EV, bool EATOM, bool ONE>
-__global__ void __launch_bounds__(256) k_ilp(ForceArgs<R> a) {
+// per-atom accumulators of the pair kernel
+struct IlpAcc {
+  R fx = 0, fy = 0, fz = 0, gxa = 0, gya = 0, gza = 0;
+  R evdw = 0, erep = 0, w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
+};
+
+// normal of j as R
+template <class T>
+struct NrmJ;
+template <>
+struct NrmJ<float> {
+  float4 q;
+  __device__ __forceinline__ static NrmJ load(const ForceArgs<float> &a, int j) { return NrmJ{__ldg(&a.nrm32[j])}; }
+};
+template <>
+struct NrmJ<double> {
+  d4 q;
+  __device__ __forceinline__ static NrmJ load(const ForceArgs<double> &a, int j) { return NrmJ{a.nrm64[j]}; }
+};
+
+// One list entry (i, j, image) with j's position and normal already loaded.
+template <bool EV, bool ONE>
+__device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &ai, const SysDesc &sdl, uint32_t e,
+                                         const typename AtomI<R>::J &J, const NrmJ<R> &N, R nix, R niy, R niz,
+                                         int ie, long long mi, long long itag, bool check, IlpAcc &acc) {
+  int j, sx, sy, sz;
+  decode_entry(e, a.lc, j, sx, sy, sz);
+  R dx, dy, dz;
+  long long jinfo;
+  ai.disp_from(J, sdl, sx, sy, sz, dx, dy, dz, jinfo);
+  R rsq = dx * dx + dy * dy + dz * dz;
+  if (!(rsq < c_pot.i_cutsq)) return;
+  if (check && info_mol(jinfo) == mi) return;
+  const int tj = info_type(jinfo);
+  if (check && !((c_pot.ilp_typemask >> tj) & 1u)) return;
+  const int je = ONE ? 0 : c_pot.i_map[tj];
+  const IlpP<R> &pij = ONE ? c_pot.ilp[0] : c_pot.ilp[ie * MAXELEM + je];
+  const IlpP<R> &pji = ONE ? c_pot.ilp[0] : c_pot.ilp[je * MAXELEM + ie];
+  const R njx = N.q.x, njy = N.q.y, njz = N.q.z;
+  R r, rinv;
+  if constexpr (sizeof(R) == 8) { r = sqrt(rsq); rinv = R(1) / r; }
+  else { rinv = rsqrtf(rsq); r = rsq * rinv; }
+  // taper (pair_ilp_graphene_hbn.h:80-115), Tap and dTap in one pass
+  R Tap = 1, dTap = 0;
+  if (c_pot.tap) {
+    R x = r * c_pot.i_inv_rcut;
+    Tap = R(20) * x + R(-70);
+    Tap = Tap * x + R(84);
+    Tap = Tap * x + R(-35);
+    Tap = Tap * x;
+    Tap = Tap * x;
+    Tap = Tap * x;
+    Tap = Tap * x + R(1);
+    R dT = R(140) * x + R(-420);
+    dT = dT * x + R(420);
+    dT = dT * x + R(-140);
+    dT = dT * x;
+    dT = dT * x;
+    dT = dT * x;
+    dTap = dT * c_pot.i_inv_rcut;
+  }
+  // ---- vdW (both ends evaluate the pair force; energy halved)
+  const IlpP<R> &pv = (c_pot.vdw_sym || keep_half(itag, a.tag[j], sx, sy, sz)) ? pij : pji;
+  R r2inv = rinv * rinv;
+  R r6inv = r2inv * r2inv * r2inv;
+  R r8inv = r6inv * r2inv;
+  R TSvdw = R(1) + Math<R>::exp_ts(pv, r);
+  R TSinv = Math<R>::rcp(TSvdw);
+  R Vvdw = -pv.C6 * r6inv * TSinv;
+  R fpv = R(-6) * pv.C6 * r8inv * TSinv + pv.C6 * pv.d_over_seff * (TSvdw - R(1)) * TSinv * TSinv * r8inv * r;
+  R fsum_v = fpv * Tap - Vvdw * dTap * rinv;
+  // ---- repulsion of term (i,j) with n_i
+  R p = nix * dx + niy * dy + niz * dz;
+  R rhosq = rsq - p * p;
+  R exp0 = Math<R>::exp_rep0(pij, r);
+  R exp1 = Math<R>::exp_rep1(pij, rhosq);
+  R frho = exp1 * pij.C;
+  R Erep = pij.eps_half + frho;
+  R V = exp0 * Erep;
+  R fpair1 = R(2) * exp0 * frho * pij.delta2inv;
+  R fsum = pij.lambda * exp0 * rinv * Erep + fpair1;
+  // ---- repulsion of term (j,i) with n_j (del' = -del, prod' = -q)
+  R q = njx * dx + njy * dy + njz * dz;
+  R rhosq2 = rsq - q * q;
+  R exp0b = pji.same_as_swapped ? exp0 : Math<R>::exp_rep0(pji, r);
+  R exp1b = Math<R>::exp_rep1(pji, rhosq2);
+  R frho2 = exp1b * pji.C;
+  R Erep2 = pji.eps_half + frho2;
+  R V2 = exp0b * Erep2;
+  R fpair1b = R(2) * exp0b * frho2 * pji.delta2inv;
+  R fsum2 = pji.lambda * exp0b * rinv * Erep2 + fpair1b;
+  // ---- force on i
+  R tp1 = Tap * p * fpair1;
+  R tq1 = Tap * q * fpair1b;
+  R crad = fsum_v + (fsum + fsum2) * Tap - (V + V2) * dTap * rinv;
+  acc.fx += crad * dx - tp1 * nix - tq1 * njx;
+  acc.fy += crad * dy - tp1 * niy - tq1 * njy;
+  acc.fz += crad * dz - tp1 * niz - tq1 * njz;
+  acc.gxa += tp1 * dx; acc.gya += tp1 * dy; acc.gza += tp1 * dz;
+  if (EV) {
+    acc.evdw += R(0.5) * Vvdw * Tap;
+    acc.erep += R(0.5) * (V + V2) * Tap;
+    // term (i,j): del (x) fkc_ij;  vdW: half of del (x) fsum_v del
+    R cr1 = fsum * Tap - V * dTap * rinv + R(0.5) * fsum_v;
+    R kx = cr1 * dx - tp1 * nix, ky = cr1 * dy - tp1 * niy, kz = cr1 * dz - tp1 * niz;
+    acc.w0 += dx * kx; acc.w1 += dy * ky; acc.w2 += dz * kz;
+    acc.w3 += dx * ky; acc.w4 += dx * kz; acc.w5 += dy * kz;
+  }
+}
+
+// FP32: at least 5 blocks of 256 threads per SM (48 registers) -- the kernel is
+// issue-bound with long-scoreboard stalls on j's data, and 40 resident warps hide them
+// better than 36 (measured: -8 % at 2.7M atoms, -16 % at 490k).  FP64 keeps its
+// registers.
+template <int TPA, bool EV, bool EATOM, bool ONE, bool PF>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R> a) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gtid / TPA;
   const int lane = threadIdx.x & (TPA - 1);
@@ -434,10 +548,7 @@ __global__ void __launch_bounds__(256) k_ilp(ForceArgs<R> a) {
   if constexpr (sizeof(R) == 8) { d4 q = a.nrm64[ii]; nix = q.x; niy = q.y; niz = q.z; }
   else { float4 q = a.nrm32[ii]; nix = q.x; niy = q.y; niz = q.z; }
   const long long itag = c_pot.vdw_sym ? 0 : a.tag[ii];
-  R fx = 0, fy = 0, fz = 0, gxa = 0, gya = 0, gza = 0;
-  R evdw = 0, erep = 0, w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
-  const R cutsq = c_pot.i_cutsq;
-  const unsigned tmask = c_pot.ilp_typemask;
+  IlpAcc acc;
   SysDesc sdl;  // box of i's system in registers for the image shifts
 #pragma unroll
   for (int d = 0; d < 3; d++) {
@@ -445,97 +556,47 @@ __global__ void __launch_bounds__(256) k_ilp(ForceArgs<R> a) {
     sdl.Lhi[d] = sd.Lhi[d];
     sdl.Llo[d] = sd.Llo[d];
   }
+  // a list without list_full holds only interlayer pairs of ILP-mapped types (k_list)
+  const bool check = a.list_full != 0;
   if (valid && ie >= 0) {
-    const int64_t b = a.list_off[i], end = a.list_off[i + 1];
-    for (int64_t k = b + lane; k < end; k += TPA) {
-      uint32_t e = __ldg(&a.list[k]);
-      int j, sx, sy, sz;
-      decode_entry(e, a.lc, j, sx, sy, sz);
-      R dx, dy, dz;
-      long long jinfo;
-      ai.disp(a.A, sdl, j, sx, sy, sz, dx, dy, dz, jinfo);
-      R rsq = dx * dx + dy * dy + dz * dz;
-      if (!(rsq < cutsq)) continue;
-      if (info_mol(jinfo) == mi) continue;
-      const int tj = info_type(jinfo);
-      if (!((tmask >> tj) & 1u)) continue;
-      const int je = ONE ? 0 : c_pot.i_map[tj];
-      const IlpP<R> &pij = ONE ? c_pot.ilp[0] : c_pot.ilp[ie * MAXELEM + je];
-      const IlpP<R> &pji = ONE ? c_pot.ilp[0] : c_pot.ilp[je * MAXELEM + ie];
-      R njx, njy, njz;
-      if constexpr (sizeof(R) == 8) { d4 q = a.nrm64[j]; njx = q.x; njy = q.y; njz = q.z; }
-      else { float4 q = __ldg(&a.nrm32[j]); njx = q.x; njy = q.y; njz = q.z; }
-      R r, rinv;
-      if constexpr (sizeof(R) == 8) { r = sqrt(rsq); rinv = R(1) / r; }
-      else { rinv = rsqrtf(rsq); r = rsq * rinv; }
-      // taper (pair_ilp_graphene_hbn.h:80-115), Tap and dTap in one pass
-      R Tap = 1, dTap = 0;
-      if (c_pot.tap) {
-        R x = r * c_pot.i_inv_rcut;
-        Tap = R(20) * x + R(-70);
-        Tap = Tap * x + R(84);
-        Tap = Tap * x + R(-35);
-        Tap = Tap * x;
-        Tap = Tap * x;
-        Tap = Tap * x;
-        Tap = Tap * x + R(1);
-        R dT = R(140) * x + R(-420);
-        dT = dT * x + R(420);
-        dT = dT * x + R(-140);
-        dT = dT * x;
-        dT = dT * x;
-        dT = dT * x;
-        dTap = dT * c_pot.i_inv_rcut;
+    const int64_t b = a.list_off[i];
+    const uint32_t *lst = a.list + b;
+    const int cnt = (int)(a.list_off[i + 1] - b);
+    if constexpr (!PF) {
+      for (int k = lane; k < cnt; k += TPA) {
+        uint32_t e = __ldg(&lst[k]);
+        const int j = (int)(e & a.lc.imask);
+        ilp_pair<EV, ONE>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi, itag, check,
+                          acc);
       }
-      // ---- vdW (both ends evaluate the pair force; energy halved)
-      const IlpP<R> &pv = (c_pot.vdw_sym || keep_half(itag, a.tag[j], sx, sy, sz)) ? pij : pji;
-      R r2inv = rinv * rinv;
-      R r6inv = r2inv * r2inv * r2inv;
-      R r8inv = r6inv * r2inv;
-      R TSvdw = R(1) + Math<R>::exp_ts(pv, r);
-      R TSinv = Math<R>::rcp(TSvdw);
-      R Vvdw = -pv.C6 * r6inv * TSinv;
-      R fpv = R(-6) * pv.C6 * r8inv * TSinv + pv.C6 * pv.d_over_seff * (TSvdw - R(1)) * TSinv * TSinv * r8inv * r;
-      R fsum_v = fpv * Tap - Vvdw * dTap * rinv;
-      // ---- repulsion of term (i,j) with n_i
-      R p = nix * dx + niy * dy + niz * dz;
-      R rhosq = rsq - p * p;
-      R exp0 = Math<R>::exp_rep0(pij, r);
-      R exp1 = Math<R>::exp_rep1(pij, rhosq);
-      R frho = exp1 * pij.C;
-      R Erep = pij.eps_half + frho;
-      R V = exp0 * Erep;
-      R fpair1 = R(2) * exp0 * frho * pij.delta2inv;
-      R fsum = pij.lambda * exp0 * rinv * Erep + fpair1;
-      // ---- repulsion of term (j,i) with n_j (del' = -del, prod' = -q)
-      R q = njx * dx + njy * dy + njz * dz;
-      R rhosq2 = rsq - q * q;
-      R exp0b = pji.same_as_swapped ? exp0 : Math<R>::exp_rep0(pji, r);
-      R exp1b = Math<R>::exp_rep1(pji, rhosq2);
-      R frho2 = exp1b * pji.C;
-      R Erep2 = pji.eps_half + frho2;
-      R V2 = exp0b * Erep2;
-      R fpair1b = R(2) * exp0b * frho2 * pji.delta2inv;
-      R fsum2 = pji.lambda * exp0b * rinv * Erep2 + fpair1b;
-      // ---- force on i
-      R tp1 = Tap * p * fpair1;
-      R tq1 = Tap * q * fpair1b;
-      R crad = fsum_v + (fsum + fsum2) * Tap - (V + V2) * dTap * rinv;
-      fx += crad * dx - tp1 * nix - tq1 * njx;
-      fy += crad * dy - tp1 * niy - tq1 * njy;
-      fz += crad * dz - tp1 * niz - tq1 * njz;
-      gxa += tp1 * dx; gya += tp1 * dy; gza += tp1 * dz;
-      if (EV) {
-        evdw += R(0.5) * Vvdw * Tap;
-        erep += R(0.5) * (V + V2) * Tap;
-        // term (i,j): del (x) fkc_ij;  vdW: half of del (x) fsum_v del
-        R cr1 = fsum * Tap - V * dTap * rinv + R(0.5) * fsum_v;
-        R kx = cr1 * dx - tp1 * nix, ky = cr1 * dy - tp1 * niy, kz = cr1 * dz - tp1 * niz;
-        w0 += dx * kx; w1 += dy * ky; w2 += dz * kz;
-        w3 += dx * ky; w4 += dx * kz; w5 += dy * kz;
+    } else {
+      // software pipeline: the next entry's position and normal are in flight while
+      // the current pair is evaluated
+      uint32_t e = 0;
+      typename AtomI<R>::J J{};
+      NrmJ<R> N{};
+      if (lane < cnt) {
+        e = __ldg(&lst[lane]);
+        const int j = (int)(e & a.lc.imask);
+        J = ai.fetch(a.A, j);
+        N = NrmJ<R>::load(a, j);
+      }
+      for (int k = lane; k < cnt; k += TPA) {
+        const uint32_t ec = e;
+        const typename AtomI<R>::J Jc = J;
+        const NrmJ<R> Nc = N;
+        if (k + TPA < cnt) {
+          e = __ldg(&lst[k + TPA]);
+          const int j = (int)(e & a.lc.imask);
+          J = ai.fetch(a.A, j);
+          N = NrmJ<R>::load(a, j);
+        }
+        ilp_pair<EV, ONE>(a, ai, sdl, ec, Jc, Nc, nix, niy, niz, ie, mi, itag, check, acc);
       }
     }
   }
+  R fx = acc.fx, fy = acc.fy, fz = acc.fz, gxa = acc.gxa, gya = acc.gya, gza = acc.gza;
+  R evdw = acc.evdw, erep = acc.erep, w0 = acc.w0, w1 = acc.w1, w2 = acc.w2, w3 = acc.w3, w4 = acc.w4, w5 = acc.w5;
   // ---- reduce over the TPA lanes of atom i in R; one conversion to FP64 per atom
 #pragma unroll
   for (int o = TPA / 2; o > 0; o >>= 1) {
@@ -759,9 +820,10 @@ template <int TPA, bool ONE>
 static void launch_ilp_t(const ForceArgs<R> &a, bool ev, bool eatom, int block, cudaStream_t s) {
   long long threads = (long long)a.n * TPA;
   int g = (int)((threads + block - 1) / block);
-  if (ev && eatom) k_ilp<TPA, true, true, ONE><<<g, block, 0, s>>>(a);
-  else if (ev) k_ilp<TPA, true, false, ONE><<<g, block, 0, s>>>(a);
-  else k_ilp<TPA, false, false, ONE><<<g, block, 0, s>>>(a);
+  if (ev && eatom) k_ilp<TPA, true, true, ONE, false><<<g, block, 0, s>>>(a);
+  else if (ev) k_ilp<TPA, true, false, ONE, false><<<g, block, 0, s>>>(a);
+  else if (a.ilp_prefetch) k_ilp<TPA, false, false, ONE, true><<<g, block, 0, s>>>(a);
+  else k_ilp<TPA, false, false, ONE, false><<<g, block, 0, s>>>(a);
 }
 
 template <bool ONE>

@@ -103,97 +103,119 @@ __device__ __forceinline__ bool le_exact(float rsq, float thr, double thr64, con
   return r2 <= thr64;
 }
 
-// One warp per atom i, scanning the bins of its stencil (with periodic images).
+// One block per bin, one thread per i atom of the bin (atoms are contiguous after the
+// sort).  The block walks the bin's stencil; each stencil bin's j atoms are staged in
+// shared memory and every thread tests its i against them in order (all threads read
+// the same j: a broadcast).  Counters and write cursors live in registers.  The
+// entries of each i come out in the order of a per-atom scan: stencil bins (dz, dy,
+// dx), then j ascending.
 // FILL = false: counts pair-list entries into cnt[i] and writes the short list.
-// FILL = true: writes the pair list at list_off[i] in the same deterministic order.
+// FILL = true: writes the pair list at list_off[i], candidates inside the force cutoff
+// from the front and the skin shell from the back (the pair kernel's lanes then mostly
+// accept or reject together).
+constexpr int LT = 128;   // i atoms per block pass and j atoms per staged tile
+
 template <bool FILL>
-__global__ void __launch_bounds__(256) k_list(NbArgs a) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= a.n) return;
-  const int i = warp;
-  const SysDesc &sd = a.sys[a.sysid[i]];
-  const d4 qi = a.xq[i];
-  const float4 hi = a.xh[i];
-  const float4 li = a.xl[i];
-  const int infoi = __float_as_int(hi.w);
-  const int ti = infoi & 255;
-  const int mi = infoi >> 8;
-  const int ilp_i = c_nb.ilp_mapped[ti];
-  int b[3];
-  b[0] = bin_coord(qi.x, sd.lo[0], sd.binv[0], sd.nb[0]);
-  b[1] = bin_coord(qi.y, sd.lo[1], sd.binv[1], sd.nb[1]);
-  b[2] = bin_coord(qi.z, sd.lo[2], sd.binv[2], sd.nb[2]);
-  int64_t nlong = 0;
-  int nshort = 0;
-  const int64_t base = FILL ? a.list_off[i] : 0;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int dz = -sd.reach[2]; dz <= sd.reach[2]; dz++) {
-    int bz = b[2] + dz, sz = 0;
-    if (sd.per[2]) {
-      sz = bz >= 0 ? bz / sd.nb[2] : -((-bz + sd.nb[2] - 1) / sd.nb[2]);
-      bz -= sz * sd.nb[2];
-    } else if (bz < 0 || bz >= sd.nb[2]) continue;
-    for (int dy = -sd.reach[1]; dy <= sd.reach[1]; dy++) {
-      int by = b[1] + dy, sy = 0;
-      if (sd.per[1]) {
-        sy = by >= 0 ? by / sd.nb[1] : -((-by + sd.nb[1] - 1) / sd.nb[1]);
-        by -= sy * sd.nb[1];
-      } else if (by < 0 || by >= sd.nb[1]) continue;
-      for (int dx = -sd.reach[0]; dx <= sd.reach[0]; dx++) {
-        int bx = b[0] + dx, sx = 0;
-        if (sd.per[0]) {
-          sx = bx >= 0 ? bx / sd.nb[0] : -((-bx + sd.nb[0] - 1) / sd.nb[0]);
-          bx -= sx * sd.nb[0];
-        } else if (bx < 0 || bx >= sd.nb[0]) continue;
-        const int gb = sd.bin_begin + (bz * sd.nb[1] + by) * sd.nb[0] + bx;
-        const int start = a.bin_start[gb], end = a.bin_end[gb];
-        const float shx = (float)sx * sd.Lhi[0], shy = (float)sy * sd.Lhi[1], shz = (float)sz * sd.Lhi[2];
-        const float slx = (float)sx * sd.Llo[0], sly = (float)sy * sd.Llo[1], slz = (float)sz * sd.Llo[2];
-        const bool self_image = (sx | sy | sz) == 0;
-        for (int j0 = start; j0 < end; j0 += 32) {
-          const int j = j0 + lane;
-          bool take_long = false, take_short = false;
-          if (j < end && !(self_image && j == i)) {
-            const float4 hj = __ldg(&a.xh[j]);
-            const float4 lj = __ldg(&a.xl[j]);
-            float ddx = ((hi.x - hj.x) - shx) + ((li.x - lj.x) - slx);
-            float ddy = ((hi.y - hj.y) - shy) + ((li.y - lj.y) - sly);
-            float ddz = ((hi.z - hj.z) - shz) + ((li.z - lj.z) - slz);
-            float rsq = ddx * ddx + ddy * ddy + ddz * ddz;
-            const int infoj = __float_as_int(hj.w);
-            const int tj = infoj & 255;
-            const int mj = infoj >> 8;
-            const int tt = ti * (MAXTYPE + 1) + tj;
-            if (a.full || (mj != mi && ilp_i && c_nb.ilp_mapped[tj]))
-              take_long = le_exact(rsq, c_nb.cutnsq_f[tt], c_nb.cutnsq_d[tt], a.xq, sd, i, j, sx, sy, sz);
-            if (!FILL) take_short = le_exact(rsq, c_nb.rshortsq_f, c_nb.rshortsq_d, a.xq, sd, i, j, sx, sy, sz);
-          }
-          const unsigned ml = __ballot_sync(0xffffffff, take_long);
-          if (FILL && take_long) {
-            int64_t pos = base + nlong + __popc(ml & lt);
-            if (pos < a.list_cap) a.list[pos] = encode_entry(j, sx, sy, sz, a.lc);
-          }
-          nlong += __popc(ml);
-          if (!FILL) {
-            const unsigned ms = __ballot_sync(0xffffffff, take_short);
-            if (take_short) {
-              int pos = nshort + __popc(ms & lt);
-              if (pos < MAXSHORT) a.short_nb[(size_t)i * MAXSHORT + pos] = encode_entry(j, sx, sy, sz, a.lc);
+__global__ void __launch_bounds__(LT) k_list(NbArgs a) {
+  const int gb = blockIdx.x;
+  const int i0 = a.bin_start[gb], i1 = a.bin_end[gb];
+  if (i1 <= i0) return;
+  const SysDesc &sd = a.sys[a.sysid[i0]];
+  const int lb = gb - sd.bin_begin;
+  const int b0 = lb % sd.nb[0], b1 = (lb / sd.nb[0]) % sd.nb[1], b2 = lb / (sd.nb[0] * sd.nb[1]);
+  __shared__ float4 jh[LT], jl[LT];
+  const float prefilt = sd.prefilt_sq;
+  for (int it0 = i0; it0 < i1; it0 += LT) {
+    const int i = it0 + threadIdx.x;
+    const bool act = i < i1;
+    float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+    if (act) {
+      hi = a.xh[i];
+      lo = a.xl[i];
+    }
+    const int infoi = __float_as_int(hi.w);
+    const int ti = infoi & 255;
+    const int mi = infoi >> 8;
+    const int ilp_i = c_nb.ilp_mapped[ti];
+    int nlong = 0, nin = 0, nsh = 0, nshort = 0;
+    const int64_t base = (FILL && act) ? a.list_off[i] : 0;
+    const int64_t lend = (FILL && act) ? a.list_off[i + 1] : 0;
+    for (int dz = -sd.reach[2]; dz <= sd.reach[2]; dz++) {
+      int bz = b2 + dz, sz = 0;
+      if (sd.per[2]) {
+        sz = bz >= 0 ? bz / sd.nb[2] : -((-bz + sd.nb[2] - 1) / sd.nb[2]);
+        bz -= sz * sd.nb[2];
+      } else if (bz < 0 || bz >= sd.nb[2]) continue;
+      for (int dy = -sd.reach[1]; dy <= sd.reach[1]; dy++) {
+        int by = b1 + dy, sy = 0;
+        if (sd.per[1]) {
+          sy = by >= 0 ? by / sd.nb[1] : -((-by + sd.nb[1] - 1) / sd.nb[1]);
+          by -= sy * sd.nb[1];
+        } else if (by < 0 || by >= sd.nb[1]) continue;
+        for (int dx = -sd.reach[0]; dx <= sd.reach[0]; dx++) {
+          int bx = b0 + dx, sx = 0;
+          if (sd.per[0]) {
+            sx = bx >= 0 ? bx / sd.nb[0] : -((-bx + sd.nb[0] - 1) / sd.nb[0]);
+            bx -= sx * sd.nb[0];
+          } else if (bx < 0 || bx >= sd.nb[0]) continue;
+          const int gbj = sd.bin_begin + (bz * sd.nb[1] + by) * sd.nb[0] + bx;
+          const int jstart = a.bin_start[gbj], jend = a.bin_end[gbj];
+          const float shx = (float)sx * sd.Lhi[0], shy = (float)sy * sd.Lhi[1], shz = (float)sz * sd.Lhi[2];
+          const float slx = (float)sx * sd.Llo[0], sly = (float)sy * sd.Llo[1], slz = (float)sz * sd.Llo[2];
+          const bool self_image = (sx | sy | sz) == 0;
+          for (int jt0 = jstart; jt0 < jend; jt0 += LT) {
+            const int nj = min(LT, jend - jt0);
+            __syncthreads();
+            if ((int)threadIdx.x < nj) {
+              jh[threadIdx.x] = a.xh[jt0 + threadIdx.x];
+              jl[threadIdx.x] = a.xl[jt0 + threadIdx.x];
             }
-            nshort += __popc(ms);
+            __syncthreads();
+            if (!act) continue;
+            for (int jj = 0; jj < nj; jj++) {
+              const int j = jt0 + jj;
+              const float4 hj = jh[jj];
+              const float hx = (hi.x - hj.x) - shx, hy = (hi.y - hj.y) - shy, hz = (hi.z - hj.z) - shz;
+              if (hx * hx + hy * hy + hz * hz > prefilt) continue;   // most candidates
+              const float4 lj = jl[jj];
+              float ddx = hx + ((lo.x - lj.x) - slx);
+              float ddy = hy + ((lo.y - lj.y) - sly);
+              float ddz = hz + ((lo.z - lj.z) - slz);
+              float rsq = ddx * ddx + ddy * ddy + ddz * ddz;
+              const int infoj = __float_as_int(hj.w);
+              const int tj = infoj & 255;
+              const int mj = infoj >> 8;
+              const int tt = ti * (MAXTYPE + 1) + tj;
+              bool take_long = false;
+              if ((a.full || (mj != mi && ilp_i && c_nb.ilp_mapped[tj])) && !(self_image && j == i))
+                take_long = le_exact(rsq, c_nb.cutnsq_f[tt], c_nb.cutnsq_d[tt], a.xq, sd, i, j, sx, sy, sz);
+              if (FILL) {
+                if (take_long) {
+                  const bool inner = rsq < c_nb.innersq_f;
+                  int64_t pos = inner ? base + nin : lend - 1 - nsh;
+                  if (pos >= base && pos < lend && pos < a.list_cap) a.list[pos] = encode_entry(j, sx, sy, sz, a.lc);
+                  nin += inner;
+                  nsh += !inner;
+                }
+              } else if (!(self_image && j == i) &&
+                         le_exact(rsq, c_nb.rshortsq_f, c_nb.rshortsq_d, a.xq, sd, i, j, sx, sy, sz)) {
+                if (nshort < MAXSHORT) a.short_nb[(size_t)i * MAXSHORT + nshort] = encode_entry(j, sx, sy, sz, a.lc);
+                nshort++;
+              }
+              nlong += take_long;
+            }
           }
         }
       }
     }
-  }
-  if (lane == 0) {
-    if (!FILL) {
-      a.cnt[i] = nlong;
-      a.short_cnt[i] = nshort < MAXSHORT ? nshort : MAXSHORT;
-      if (nshort > MAXSHORT) atomicOr(a.status, ST_SHORT_OVERFLOW);
-    } else if (base + nlong > a.list_cap) {
-      atomicOr(a.status, ST_LIST_OVERFLOW);
+    if (act) {
+      if (!FILL) {
+        a.cnt[i] = nlong;
+        a.short_cnt[i] = nshort < MAXSHORT ? nshort : MAXSHORT;
+        if (nshort > MAXSHORT) atomicOr(a.status, ST_SHORT_OVERFLOW);
+      } else if (base + nlong > a.list_cap) {
+        atomicOr(a.status, ST_LIST_OVERFLOW);
+      }
     }
   }
 }
@@ -249,11 +271,9 @@ void nb_hilo(int n, const d4 *xq, const SysDesc *sys, const int *sysid, float4 *
 }
 
 void nb_list(const NbArgs &a, bool fill, cudaStream_t s) {
-  if (!a.n) return;
-  long long threads = (long long)a.n * 32;
-  int g = (int)((threads + 255) / 256);
-  if (fill) k_list<true><<<g, 256, 0, s>>>(a);
-  else k_list<false><<<g, 256, 0, s>>>(a);
+  if (!a.n || a.nbins <= 0) return;
+  if (fill) k_list<true><<<a.nbins, LT, 0, s>>>(a);
+  else k_list<false><<<a.nbins, LT, 0, s>>>(a);
 }
 
 void nb_copy_hold(int n, const d4 *xq, double *xhold, cudaStream_t s) {

@@ -12,6 +12,7 @@ struct NbConst {
   int ilp_mapped[MAXTYPE + 1];
   float rshortsq_f;
   double rshortsq_d;
+  float innersq_f;   // ILP force cutoff squared: fill puts candidates inside it first
 };
 
 struct NbArgs {
@@ -23,6 +24,7 @@ struct NbArgs {
   const int *sysid;
   const int *bin_start;
   const int *bin_end;
+  int nbins;          // global bins (one list-build block each)
   const int64_t *list_off;
   uint32_t *list;
   int64_t list_cap;

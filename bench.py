@@ -206,6 +206,25 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(x: float, dist=None) -> float:
+    """The largest x over the ranks of the default process group (x itself without one):
+    the job's time is its slowest rank's.  CPU tensor under gloo, device tensor under
+    NCCL."""
+    if dist is None or not dist.is_initialized():
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, natoms: int, steps: int, tmax: float) -> float:
+    """Whole-job atom-steps/s of `world` independent replicas of `natoms` atoms, each
+    running `steps` steps, the slowest taking `tmax` seconds (weak scaling)."""
+    return world * natoms * steps / tmax
+
+
 def _sync_wall(fn, reps: int) -> float:
     """Wall seconds per call of fn (every call returns with its GPU work finished)."""
     t0 = time.perf_counter()
@@ -418,12 +437,8 @@ def main():
     st = eng.stats()
     graph_steps = st["graph_steps"]
     dev_s = st["ms_last_run"] / 1e3
-    tmax = dev_s
-    if dist:
-        t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tmax = float(t.item())
-    value = world * s.n * args.steps / tmax
+    tmax = max_over_ranks(dev_s, dist)
+    value = replica_throughput(world, s.n, args.steps, tmax)
     ms_per_step = tmax / args.steps * 1e3
 
     # dominant kernel: the ILP pair kernel; live per-launch device time from CUDA events

@@ -92,6 +92,18 @@ typedef struct lmff_ilp_param {
   int ielement, jelement;
 } lmff_ilp_param;
 
+/* kolmogorov/crespi/full Param after read_file (pair_kolmogorov_crespi_full.h, :340-365):
+ * energies C0 C2 C4 C A already in eV (file meV x 1e-3 x S). */
+typedef struct lmff_kc_param {
+  double z0, C0, C2, C4, C, delta, lambda, A, S, rcut;
+  double delta2inv, z06;
+  int ielement, jelement;
+} lmff_kc_param;
+
+/* interlayer style held in the ilp_* fields of lmff_params */
+#define LMFF_INTERLAYER_ILP 0   /* ilp/graphene/hbn */
+#define LMFF_INTERLAYER_KC 1    /* kolmogorov/crespi/full */
+
 /* Everything the two pair styles hold after coeff().  Arrays are copied. */
 typedef struct lmff_params {
   int ntypes;                                 /* LAMMPS atom types 1..ntypes (<= 16) */
@@ -110,6 +122,11 @@ typedef struct lmff_params {
   double ilp_cut_global;                      /* pair_style ... ilp/graphene/hbn <cut> */
   int ilp_tap_flag;                           /* pair_style ... <tap_flag> */
   double skin;                                /* neighbor <skin> bin */
+  /* LMFF_INTERLAYER_KC: the interlayer style is kolmogorov/crespi/full; ilp_nparams,
+   * ilp_nelements, ilp_elem2param, ilp_map, ilp_cutILPsq (its cutKCsq), cut_global
+   * and tap_flag describe it, and kc_params replaces ilp_params */
+  int interlayer_model;
+  const lmff_kc_param *kc_params;
 } lmff_params;
 
 /* Energies and virials of one evaluation.  The virial is the global fdotr virial
@@ -168,6 +185,16 @@ int lmff_create_from_files2(lmff_engine **out, const char *tersoff_file,
                             const char *const *tersoff_elements, const char *ilp_file,
                             const char *const *ilp_elements, int ntypes, double cut_global,
                             int tap_flag, double skin, int device);
+/* Tersoff + kolmogorov/crespi/full (12-word entries: elem1 elem2 z0 C0 C2 C4 C delta
+ * lambda A S rcut) as the interlayer style, read as the reference's read_file does
+ * (pair_kolmogorov_crespi_full.cpp:247-392).  Results report it in the e_ilp,
+ * virial_ilp and pvector (vdW, repulsion) fields; without the taper the repulsion
+ * energy carries the reference's offset -A (z0/cut)^6 per directed pair (init_one,
+ * pair_modify shift yes). */
+int lmff_create_kc_from_files(lmff_engine **out, const char *tersoff_file,
+                              const char *const *tersoff_elements, const char *kc_file,
+                              const char *const *kc_elements, int ntypes, double cut_global,
+                              int tap_flag, double skin, int device);
 void lmff_destroy(lmff_engine *e);
 
 /* ---- configuration ---------------------------------------------------------------- */

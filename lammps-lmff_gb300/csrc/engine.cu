@@ -79,14 +79,22 @@ __global__ void k_check_ident(int n, const int *perm, const int *type, const int
 }
 
 // new caller positions into sorted order + max squared displacement since the build
+// New caller positions into the resident state.  On periodic dimensions a position is
+// taken in the periodic image nearest the one the list was built with (the caller may
+// hand unwrapped coordinates, or coordinates it just wrapped): the list's image codes
+// stay valid and an atom that crossed the box edge is not a displacement.
 __global__ void k_update_x(int n, const int *perm, const double *x, d4 *xq, const double *xhold,
-                           unsigned long long *maxdisp) {
+                           unsigned long long *maxdisp, const SysDesc *sys, const int *sysid) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   double d2 = 0.0;
   if (q < n) {
     int o = perm[q];
     d4 w = xq[q];
     double a = x[3 * o], b = x[3 * o + 1], c = x[3 * o + 2];
+    const SysDesc &sd = sys[sysid[q]];
+    if (sd.per[0]) a -= sd.L[0] * rint((a - xhold[3 * q]) / sd.L[0]);
+    if (sd.per[1]) b -= sd.L[1] * rint((b - xhold[3 * q + 1]) / sd.L[1]);
+    if (sd.per[2]) c -= sd.L[2] * rint((c - xhold[3 * q + 2]) / sd.L[2]);
     xq[q] = make_d4(a, b, c, w.w);
     double dx = a - xhold[3 * q], dy = b - xhold[3 * q + 1], dz = c - xhold[3 * q + 2];
     d2 = dx * dx + dy * dy + dz * dz;
@@ -587,7 +595,14 @@ struct Engine {
     if (i_on) {
       int ne = p->ilp_nelements;
       if (ne < 1 || ne > MAXELEM) return fail(LMFF_EUNSUPPORTED, "ilp: at most 4 elements are supported");
-      hi.params.assign(p->ilp_params, p->ilp_params + p->ilp_nparams);
+      if (p->interlayer_model == LMFF_INTERLAYER_KC) {
+        if (!p->kc_params) return fail(LMFF_EINVAL, "kolmogorov/crespi/full: kc_params missing");
+        hi.model = LMFF_INTERLAYER_KC;
+        hi.kc.assign(p->kc_params, p->kc_params + p->ilp_nparams);
+      } else {
+        if (!p->ilp_params) return fail(LMFF_EINVAL, "ilp/graphene/hbn: ilp_params missing");
+        hi.params.assign(p->ilp_params, p->ilp_params + p->ilp_nparams);
+      }
       hi.elem2param.assign(p->ilp_elem2param, p->ilp_elem2param + ne * ne);
       hi.map.assign(p->ilp_map, p->ilp_map + ntypes + 1);
       hi.cutILPsq.assign(p->ilp_cutILPsq, p->ilp_cutILPsq + ne * ne);
@@ -613,6 +628,7 @@ struct Engine {
       P.i_map[t] = (i_on && t >= 1 && t <= ntypes) ? hi.map[t] : -1;
     }
     P.tap = tap;
+    P.kc = i_on && hi.model == LMFF_INTERLAYER_KC;
     P.ilp_typemask = 0;
     for (int t = 1; t <= ntypes && t < 32; t++)
       if (P.i_map[t] >= 0) P.ilp_typemask |= 1u << t;
@@ -625,6 +641,29 @@ struct Engine {
       int ne = P.i_ne;
       for (int a = 0; a < ne; a++)
         for (int b = 0; b < ne; b++) {
+          if (P.kc) {
+            const lmff_kc_param &q = hi.kc[hi.elem2param[a * ne + b]];
+            const lmff_kc_param &s = hi.kc[hi.elem2param[b * ne + a]];
+            IlpP<R> &o = P.ilp[a * MAXELEM + b];
+            o.z0 = (R)q.z0;
+            o.lambda = (R)q.lambda;
+            o.eps_half = (R)(0.5 * q.C);
+            o.C = (R)q.C;
+            o.delta2inv = (R)q.delta2inv;
+            o.lam_l2e = (R)(q.lambda * LOG2E);
+            o.lamz0_l2e = (R)(q.lambda * q.z0 * LOG2E);
+            o.nd2_l2e = (R)(-q.delta2inv * LOG2E);
+            o.kc_C0 = (R)q.C0;
+            o.kc_C2 = (R)q.C2;
+            o.kc_C4 = (R)q.C4;
+            o.kc_Az06 = (R)(q.A * q.z06);
+            o.kc_off = (R)(-q.A * std::pow(q.z0 / cut_global, 6.0));
+            o.same_as_swapped = (q.z0 == s.z0 && q.lambda == s.lambda && q.C == s.C && q.delta2inv == s.delta2inv &&
+                                 q.C0 == s.C0 && q.C2 == s.C2 && q.C4 == s.C4);
+            if (!(q.A * q.z06 == s.A * s.z06)) P.vdw_sym = 0;
+            P.i_cutILPsq[a * MAXELEM + b] = (R)hi.cutILPsq[a * ne + b];
+            continue;
+          }
           const lmff_ilp_param &q = hi.params[hi.elem2param[a * ne + b]];
           const lmff_ilp_param &s = hi.params[hi.elem2param[b * ne + a]];
           IlpP<R> &o = P.ilp[a * MAXELEM + b];
@@ -1138,6 +1177,7 @@ struct Engine {
     a.status = d.status;
     a.list_full = list_full;
     a.ilp_prefetch = ilp_prefetch;
+    a.kc = i_on && hi.model == LMFF_INTERLAYER_KC;
     return a;
   }
 
@@ -1294,7 +1334,7 @@ struct Engine {
       return load_from_staging(nn, false, false);
     }
     if (nn > 0) {
-      k_update_x<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, d_xin, d.xq, d.xhold, d.maxdisp);
+      k_update_x<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, d_xin, d.xq, d.xhold, d.maxdisp, d.sys, d.sysid);
       CK(cudaGetLastError());
     }
     hilo_fresh = false;
@@ -2271,6 +2311,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
     a.do_ters = g.t_on && (which & LMFF_TERSOFF);
     a.do_ilp = g.i_on && (which & LMFF_ILP);
     a.list_full = g.list_full;
+    a.kc = g.i_on && g.hi.model == LMFF_INTERLAYER_KC;
   };
   const bool ev = true;
   if (g.precision == LMFF_FP64) {
@@ -2387,6 +2428,47 @@ int lmff_create_from_files(lmff_engine **out, const char *tersoff_file, const ch
                            const char *const *elements, double cut_global, int tap_flag, double skin, int device) {
   return lmff_create_from_files2(out, tersoff_file, elements, ilp_file, elements, ntypes, cut_global, tap_flag, skin,
                                  device);
+}
+
+int lmff_create_kc_from_files(lmff_engine **out, const char *tersoff_file, const char *const *tersoff_elements,
+                              const char *kc_file, const char *const *kc_elements, int ntypes, double cut_global,
+                              int tap_flag, double skin, int device) {
+  if (!out || ntypes < 1 || ntypes > lmff::MAXTYPE || !kc_file || !kc_elements) return LMFF_EINVAL;
+  if (tersoff_file && !tersoff_elements) return LMFF_EINVAL;
+  *out = nullptr;
+  lmff::HostTersoff ht;
+  lmff::HostIlp hk;
+  std::string err;
+  if (tersoff_file && !lmff::parse_tersoff(tersoff_file, ntypes, tersoff_elements, ht, err)) {
+    g_create_error = err;
+    return LMFF_EBADPARAM;
+  }
+  if (!lmff::parse_kc(kc_file, ntypes, kc_elements, hk, err)) {
+    g_create_error = err;
+    return LMFF_EBADPARAM;
+  }
+  lmff_params p;
+  memset(&p, 0, sizeof p);
+  p.ntypes = ntypes;
+  if (tersoff_file) {
+    p.tersoff_nelements = (int)ht.elements.size();
+    p.tersoff_nparams = (int)ht.params.size();
+    p.tersoff_params = ht.params.data();
+    p.tersoff_elem2param = ht.elem2param.data();
+    p.tersoff_map = ht.map.data();
+    p.tersoff_cutmax = ht.cutmax;
+  }
+  p.ilp_nelements = (int)hk.elements.size();
+  p.ilp_nparams = (int)hk.kc.size();
+  p.ilp_elem2param = hk.elem2param.data();
+  p.ilp_map = hk.map.data();
+  p.ilp_cutILPsq = hk.cutILPsq.data();
+  p.interlayer_model = LMFF_INTERLAYER_KC;
+  p.kc_params = hk.kc.data();
+  p.ilp_cut_global = cut_global;
+  p.ilp_tap_flag = tap_flag;
+  p.skin = skin;
+  return lmff_create(out, &p, device);
 }
 
 int lmff_create_from_files2(lmff_engine **out, const char *tersoff_file, const char *const *tersoff_elements,

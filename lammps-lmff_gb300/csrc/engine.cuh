@@ -43,6 +43,9 @@ struct IlpP {
   R ts_a, ts_b;        // exp(-d (r/seff - 1)) = exp2(ts_b - ts_a r)
   int same_as_swapped; // params of (i,j) equal those of (j,i)
   int pad;
+  // kolmogorov/crespi/full: f(rho) = exp(-x) (C0 + C2 x + C4 x^2), x = rho^2/delta^2,
+  // vdW -A z0^6 / r^6; kc_off = -A (z0/cut)^6, the energy offset without the taper
+  R kc_C0, kc_C2, kc_C4, kc_Az06, kc_off;
 };
 
 // Tersoff parameters of one element triplet (pair_tersoff.h:38-53) plus derived values.
@@ -70,6 +73,7 @@ struct PotConst {
   int t_map[MAXTYPE + 1];
   int i_map[MAXTYPE + 1];
   int tap;
+  int kc;                     // interlayer style is kolmogorov/crespi/full
   int vdw_sym;                // vdW constants symmetric in (i,j) for every pair
   int rep_sym;                // Tersoff repulsion constants of (i,j,j) equal those of (j,i,i)
   unsigned ilp_typemask;      // bit t set when atom type t is mapped to an ILP element

@@ -203,6 +203,7 @@ struct ForceArgs {
   int do_ters, do_ilp;
   int list_full;       // the pair list also holds same-molecule / non-ILP pairs
   int ilp_prefetch;    // pair kernel loads the next pair's data one iteration ahead
+  int kc;              // interlayer style is kolmogorov/crespi/full
 };
 
 }  // namespace lmff

@@ -437,8 +437,31 @@ struct NrmJ<double> {
   __device__ __forceinline__ static NrmJ load(const ForceArgs<double> &a, int j) { return NrmJ{a.nrm64[j]}; }
 };
 
+// Repulsion of one directed term from exp0 = exp(-lambda (r - z0)) and exp1 =
+// exp(-rho^2/delta^2): energy V, the normal-projection factor fpair1 and the radial
+// factor fsum (calc_FRep: pair_ilp_graphene_hbn.cpp:602-621 for ILP,
+// pair_kolmogorov_crespi_full.cpp:615-631 for KC).
+template <bool KC>
+__device__ __forceinline__ void rep_term(const IlpP<R> &p, R exp0, R exp1, R rhosq, R rinv, R &V, R &fpair1, R &fsum) {
+  if constexpr (KC) {
+    R x = rhosq * p.delta2inv;
+    R sumC1 = p.kc_C0 + p.kc_C2 * x + p.kc_C4 * x * x;
+    R sumC11 = (p.kc_C2 + R(2) * p.kc_C4 * x) * p.delta2inv;
+    R Erep = p.eps_half + exp1 * sumC1;
+    V = exp0 * Erep;
+    fpair1 = R(2) * exp0 * exp1 * (p.delta2inv * sumC1 - sumC11);
+    fsum = p.lambda * exp0 * rinv * Erep + fpair1;
+  } else {
+    R frho = exp1 * p.C;
+    R Erep = p.eps_half + frho;
+    V = exp0 * Erep;
+    fpair1 = R(2) * exp0 * frho * p.delta2inv;
+    fsum = p.lambda * exp0 * rinv * Erep + fpair1;
+  }
+}
+
 // One list entry (i, j, image) with j's position and normal already loaded.
-template <bool EV, bool ONE>
+template <bool EV, bool ONE, bool KC>
 __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &ai, const SysDesc &sdl, uint32_t e,
                                          const typename AtomI<R>::J &J, const NrmJ<R> &N, R nix, R niy, R niz,
                                          int ie, long long mi, long long itag, bool check, IlpAcc &acc) {
@@ -483,31 +506,32 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
   R r2inv = rinv * rinv;
   R r6inv = r2inv * r2inv * r2inv;
   R r8inv = r6inv * r2inv;
-  R TSvdw = R(1) + Math<R>::exp_ts(pv, r);
-  R TSinv = Math<R>::rcp(TSvdw);
-  R Vvdw = -pv.C6 * r6inv * TSinv;
-  R fpv = R(-6) * pv.C6 * r8inv * TSinv + pv.C6 * pv.d_over_seff * (TSvdw - R(1)) * TSinv * TSinv * r8inv * r;
+  R Vvdw, fpv;
+  if constexpr (KC) {
+    // pair_kolmogorov_crespi_full.cpp:522-526: undamped -A z0^6 / r^6
+    Vvdw = -pv.kc_Az06 * r6inv;
+    fpv = R(-6) * pv.kc_Az06 * r8inv;
+  } else {
+    R TSvdw = R(1) + Math<R>::exp_ts(pv, r);
+    R TSinv = Math<R>::rcp(TSvdw);
+    Vvdw = -pv.C6 * r6inv * TSinv;
+    fpv = R(-6) * pv.C6 * r8inv * TSinv + pv.C6 * pv.d_over_seff * (TSvdw - R(1)) * TSinv * TSinv * r8inv * r;
+  }
   R fsum_v = fpv * Tap - Vvdw * dTap * rinv;
   // ---- repulsion of term (i,j) with n_i
   R p = nix * dx + niy * dy + niz * dz;
   R rhosq = rsq - p * p;
   R exp0 = Math<R>::exp_rep0(pij, r);
   R exp1 = Math<R>::exp_rep1(pij, rhosq);
-  R frho = exp1 * pij.C;
-  R Erep = pij.eps_half + frho;
-  R V = exp0 * Erep;
-  R fpair1 = R(2) * exp0 * frho * pij.delta2inv;
-  R fsum = pij.lambda * exp0 * rinv * Erep + fpair1;
+  R V, fpair1, fsum;
+  rep_term<KC>(pij, exp0, exp1, rhosq, rinv, V, fpair1, fsum);
   // ---- repulsion of term (j,i) with n_j (del' = -del, prod' = -q)
   R q = njx * dx + njy * dy + njz * dz;
   R rhosq2 = rsq - q * q;
   R exp0b = pji.same_as_swapped ? exp0 : Math<R>::exp_rep0(pji, r);
   R exp1b = Math<R>::exp_rep1(pji, rhosq2);
-  R frho2 = exp1b * pji.C;
-  R Erep2 = pji.eps_half + frho2;
-  R V2 = exp0b * Erep2;
-  R fpair1b = R(2) * exp0b * frho2 * pji.delta2inv;
-  R fsum2 = pji.lambda * exp0b * rinv * Erep2 + fpair1b;
+  R V2, fpair1b, fsum2;
+  rep_term<KC>(pji, exp0b, exp1b, rhosq2, rinv, V2, fpair1b, fsum2);
   // ---- force on i
   R tp1 = Tap * p * fpair1;
   R tq1 = Tap * q * fpair1b;
@@ -518,7 +542,9 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
   acc.gxa += tp1 * dx; acc.gya += tp1 * dy; acc.gza += tp1 * dz;
   if (EV) {
     acc.evdw += R(0.5) * Vvdw * Tap;
-    acc.erep += R(0.5) * (V + V2) * Tap;
+    // Kolmogorov-Crespi without the taper tallies V - offset per directed term
+    const R eoff = (KC && !c_pot.tap) ? pij.kc_off + pji.kc_off : R(0);
+    acc.erep += R(0.5) * ((V + V2) * Tap - eoff);
     // term (i,j): del (x) fkc_ij;  vdW: half of del (x) fsum_v del
     R cr1 = fsum * Tap - V * dTap * rinv + R(0.5) * fsum_v;
     R kx = cr1 * dx - tp1 * nix, ky = cr1 * dy - tp1 * niy, kz = cr1 * dz - tp1 * niz;
@@ -531,7 +557,7 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
 // issue-bound with long-scoreboard stalls on j's data, and 40 resident warps hide them
 // better than 36 (measured: -8 % at 2.7M atoms, -16 % at 490k).  FP64 keeps its
 // registers.
-template <int TPA, bool EV, bool EATOM, bool ONE, bool PF>
+template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R> a) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gtid / TPA;
@@ -566,7 +592,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R
       for (int k = lane; k < cnt; k += TPA) {
         uint32_t e = __ldg(&lst[k]);
         const int j = (int)(e & a.lc.imask);
-        ilp_pair<EV, ONE>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi, itag, check,
+        ilp_pair<EV, ONE, KC>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi, itag, check,
                           acc);
       }
     } else {
@@ -591,7 +617,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R
           J = ai.fetch(a.A, j);
           N = NrmJ<R>::load(a, j);
         }
-        ilp_pair<EV, ONE>(a, ai, sdl, ec, Jc, Nc, nix, niy, niz, ie, mi, itag, check, acc);
+        ilp_pair<EV, ONE, KC>(a, ai, sdl, ec, Jc, Nc, nix, niy, niz, ie, mi, itag, check, acc);
       }
     }
   }
@@ -820,10 +846,16 @@ template <int TPA, bool ONE>
 static void launch_ilp_t(const ForceArgs<R> &a, bool ev, bool eatom, int block, cudaStream_t s) {
   long long threads = (long long)a.n * TPA;
   int g = (int)((threads + block - 1) / block);
-  if (ev && eatom) k_ilp<TPA, true, true, ONE, false><<<g, block, 0, s>>>(a);
-  else if (ev) k_ilp<TPA, true, false, ONE, false><<<g, block, 0, s>>>(a);
-  else if (a.ilp_prefetch) k_ilp<TPA, false, false, ONE, true><<<g, block, 0, s>>>(a);
-  else k_ilp<TPA, false, false, ONE, false><<<g, block, 0, s>>>(a);
+  if (a.kc) {
+    if (ev && eatom) k_ilp<TPA, true, true, ONE, false, true><<<g, block, 0, s>>>(a);
+    else if (ev) k_ilp<TPA, true, false, ONE, false, true><<<g, block, 0, s>>>(a);
+    else k_ilp<TPA, false, false, ONE, false, true><<<g, block, 0, s>>>(a);
+    return;
+  }
+  if (ev && eatom) k_ilp<TPA, true, true, ONE, false, false><<<g, block, 0, s>>>(a);
+  else if (ev) k_ilp<TPA, true, false, ONE, false, false><<<g, block, 0, s>>>(a);
+  else if (a.ilp_prefetch) k_ilp<TPA, false, false, ONE, true, false><<<g, block, 0, s>>>(a);
+  else k_ilp<TPA, false, false, ONE, false, false><<<g, block, 0, s>>>(a);
 }
 
 template <bool ONE>

@@ -225,4 +225,72 @@ bool parse_ilp(const char *path, int ntypes, const char *const *elements, HostIl
   return true;
 }
 
+// pair_kolmogorov_crespi_full.cpp read_file (:247-392): 12 words per entry, energies in
+// meV scaled by S, every ordered element pair exactly once.
+bool parse_kc(const char *path, int ntypes, const char *const *elements, HostIlp &out, std::string &err) {
+  out = HostIlp();
+  out.model = LMFF_INTERLAYER_KC;
+  int ne = map_elements(ntypes, elements, out.map, out.elements);
+  if (ne == 0) {
+    err = "Incorrect args for pair coefficients";
+    return false;
+  }
+  auto find = [&](const std::string &w) {
+    for (int i = 0; i < ne; i++)
+      if (out.elements[i] == w) return i;
+    return -1;
+  };
+  bool ok = read_entries(path, 12, "KC", err, [&](std::vector<std::string> &w) {
+    int ie = find(w[0]), je = find(w[1]);
+    if (ie < 0 || je < 0) return true;
+    lmff_kc_param q;
+    memset(&q, 0, sizeof q);
+    q.ielement = ie;
+    q.jelement = je;
+    q.z0 = atof(w[2].c_str());
+    q.C0 = atof(w[3].c_str());
+    q.C2 = atof(w[4].c_str());
+    q.C4 = atof(w[5].c_str());
+    q.C = atof(w[6].c_str());
+    q.delta = atof(w[7].c_str());
+    q.lambda = atof(w[8].c_str());
+    q.A = atof(w[9].c_str());
+    q.S = atof(w[10].c_str());
+    q.rcut = atof(w[11].c_str());
+    double meV = 1e-3 * q.S;
+    q.C *= meV;
+    q.A *= meV;
+    q.C0 *= meV;
+    q.C2 *= meV;
+    q.C4 *= meV;
+    q.delta2inv = pow(q.delta, -2.0);
+    q.z06 = pow(q.z0, 6.0);
+    out.kc.push_back(q);
+    return true;
+  });
+  if (!ok) return false;
+  out.elem2param.assign(ne * ne, -1);
+  out.cutILPsq.assign(ne * ne, 0.0);
+  for (int i = 0; i < ne; i++)
+    for (int j = 0; j < ne; j++) {
+      int n = -1;
+      for (int m = 0; m < (int)out.kc.size(); m++) {
+        if (out.kc[m].ielement == i && out.kc[m].jelement == j) {
+          if (n >= 0) {
+            err = "Potential file has duplicate entry";
+            return false;
+          }
+          n = m;
+        }
+      }
+      if (n < 0) {
+        err = "Potential file is missing an entry";
+        return false;
+      }
+      out.elem2param[i * ne + j] = n;
+      out.cutILPsq[i * ne + j] = out.kc[n].rcut * out.kc[n].rcut;
+    }
+  return true;
+}
+
 }  // namespace lmff

@@ -95,6 +95,8 @@ def load_library(path: str = LIB_PATH):
         "lmff_create_from_files2": ([C.POINTER(P), C.c_char_p, C.POINTER(C.c_char_p), C.c_char_p,
                                      C.POINTER(C.c_char_p), I, D, I, D, I], I),
         "lmff_minimize": ([P, D, D, I, I, D, P, P], I),
+        "lmff_create_kc_from_files": ([C.POINTER(P), C.c_char_p, C.POINTER(C.c_char_p), C.c_char_p,
+                                       C.POINTER(C.c_char_p), I, D, I, D, I], I),
         "lmff_destroy": ([P], None),
         "lmff_set_precision": ([P, I], I),
         "lmff_set_box": ([P, P, P, D, D, D, P], I),
@@ -148,17 +150,25 @@ class Engine:
     def __init__(self, tersoff_file: Optional[str] = None, ilp_file: Optional[str] = None,
                  elements: Sequence[str] = ("C", "B", "N"), cut_global: float = 16.0, tap_flag: int = 1,
                  skin: float = 2.0, device: int = 0, precision: int = FP64,
-                 ilp_elements: Optional[Sequence[str]] = None):
+                 ilp_elements: Optional[Sequence[str]] = None, kc_file: Optional[str] = None):
         """elements: type -> element name for both files (pair_coeff * * ... C B N);
-        ilp_elements, if given, a separate list for the ILP file (the Tersoff file then
-        uses `elements`), e.g. elements = NULL C(O) ... with ilp_elements = C C ..."""
+        ilp_elements, if given, a separate list for the interlayer file (the Tersoff file
+        then uses `elements`), e.g. elements = NULL C(O) ... with ilp_elements = C C ...
+        kc_file: a kolmogorov/crespi/full parameter file as the interlayer style instead
+        of ilp_file."""
         lib = load_library()
-        if tersoff_file is None and ilp_file is None:
+        if tersoff_file is None and ilp_file is None and kc_file is None:
             tersoff_file = os.path.join(POTENTIALS, "BNC.tersoff")
             ilp_file = os.path.join(POTENTIALS, "BNCH.ILP")
         self._h = C.c_void_p()
         arr = (C.c_char_p * len(elements))(*[e.encode() for e in elements])
-        if ilp_elements is None:
+        if kc_file is not None:
+            ie = elements if ilp_elements is None else ilp_elements
+            arr2 = (C.c_char_p * len(ie))(*[e.encode() for e in ie])
+            rc = lib.lmff_create_kc_from_files(C.byref(self._h), tersoff_file.encode() if tersoff_file else None, arr,
+                                               kc_file.encode(), arr2, len(elements), cut_global, tap_flag, skin,
+                                               device)
+        elif ilp_elements is None:
             rc = lib.lmff_create_from_files(C.byref(self._h), tersoff_file.encode() if tersoff_file else None,
                                             ilp_file.encode() if ilp_file else None, len(elements), arr, cut_global,
                                             tap_flag, skin, device)

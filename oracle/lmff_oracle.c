@@ -231,7 +231,39 @@ static int ilp_entry(orc_pot *p, char **w, void *vctx) {
   return 0;
 }
 
-int orc_read_ilp(orc_pot *p, const char *path, const char *const *elem_of_type) {
+/* pair_kolmogorov_crespi_full.cpp:340-365: 12 words, energies in meV scaled by S */
+static int kc_entry(orc_pot *p, char **w, void *vctx) {
+  struct elem_ctx *e = (struct elem_ctx *)vctx;
+  int ie = find_elem(e, w[0]), je = find_elem(e, w[1]);
+  if (ie < 0 || je < 0) return 0;
+  if (p->i_nparams >= ORC_MAXELEM * ORC_MAXELEM) return -1;
+  orc_ilp_param *q = &p->i_params[p->i_nparams];
+  memset(q, 0, sizeof *q);
+  q->ielement = ie;
+  q->jelement = je;
+  q->z0 = atof(w[2]);
+  q->C0 = atof(w[3]);
+  q->C2 = atof(w[4]);
+  q->C4 = atof(w[5]);
+  q->C = atof(w[6]);
+  q->delta = atof(w[7]);
+  q->lambda = atof(w[8]);
+  q->A = atof(w[9]);
+  q->S = atof(w[10]);
+  q->rcut = atof(w[11]);
+  double meV = 1e-3 * q->S;
+  q->C *= meV;
+  q->A *= meV;
+  q->C0 *= meV;
+  q->C2 *= meV;
+  q->C4 *= meV;
+  q->delta2inv = pow(q->delta, -2.0);
+  q->z06 = pow(q->z0, 6.0);
+  p->i_nparams++;
+  return 0;
+}
+
+static int read_interlayer(orc_pot *p, const char *path, const char *const *elem_of_type, int model) {
   struct elem_ctx e;
   memset(&e, 0, sizeof e);
   e.nelem = map_elements(p->ntypes, elem_of_type, p->i_map, e.names);
@@ -241,7 +273,9 @@ int orc_read_ilp(orc_pot *p, const char *path, const char *const *elem_of_type) 
   }
   p->i_nelements = e.nelem;
   p->i_nparams = 0;
-  if (read_entries(p, path, 13, ilp_entry, &e, "ILP")) return -1;
+  p->i_model = model;
+  if (model == 0 && read_entries(p, path, 13, ilp_entry, &e, "ILP")) return -1;
+  if (model == 1 && read_entries(p, path, 12, kc_entry, &e, "KC")) return -1;
   for (int i = 0; i < e.nelem; i++)
     for (int j = 0; j < e.nelem; j++) {
       int n = -1;
@@ -262,6 +296,14 @@ int orc_read_ilp(orc_pot *p, const char *path, const char *const *elem_of_type) 
     }
   p->i_enabled = 1;
   return 0;
+}
+
+int orc_read_ilp(orc_pot *p, const char *path, const char *const *elem_of_type) {
+  return read_interlayer(p, path, elem_of_type, 0);
+}
+
+int orc_read_kc(orc_pot *p, const char *path, const char *const *elem_of_type) {
+  return read_interlayer(p, path, elem_of_type, 1);
 }
 
 /* ==================================================================== context == */
@@ -766,10 +808,17 @@ static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *
       double r2inv = 1.0 / rsq;
       double r6inv = r2inv * r2inv * r2inv;
       double r8inv = r6inv * r2inv;
-      double TSvdw = 1.0 + exp(-q->d * (r / q->seff - 1.0));
-      double TSvdw2inv = pow(TSvdw, -2.0);
-      double Vilp = -q->C6 * r6inv / TSvdw;
-      double fpair = -6.0 * q->C6 * r8inv / TSvdw + q->C6 * q->d / q->seff * (TSvdw - 1.0) * TSvdw2inv * r8inv * r;
+      double Vilp, fpair;
+      if (p->i_model == 1) {
+        /* pair_kolmogorov_crespi_full.cpp:522-526 */
+        Vilp = -q->A * q->z06 * r6inv;
+        fpair = -6.0 * q->A * q->z06 * r8inv;
+      } else {
+        double TSvdw = 1.0 + exp(-q->d * (r / q->seff - 1.0));
+        double TSvdw2inv = pow(TSvdw, -2.0);
+        Vilp = -q->C6 * r6inv / TSvdw;
+        fpair = -6.0 * q->C6 * r8inv / TSvdw + q->C6 * q->d / q->seff * (TSvdw - 1.0) * TSvdw2inv * r8inv * r;
+      }
       double fsum = fpair * Tap - Vilp * dTap / r;
       f[3 * i] += fsum * delx;
       f[3 * i + 1] += fsum * dely;
@@ -790,11 +839,23 @@ static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *
     double rdsq1 = rhosq1 * q->delta2inv;
     double exp0 = exp(-q->lambda * (r - q->z0));
     double exp1 = exp(-rdsq1);
-    double frho1 = exp1 * q->C;
-    double Erep = 0.5 * q->epsilon + frho1;
-    double Vilp = exp0 * Erep;
-    double fpair = q->lambda * exp0 / r * Erep;
-    double fpair1 = 2.0 * exp0 * frho1 * q->delta2inv;
+    double Vilp, fpair, fpair1;
+    if (p->i_model == 1) {
+      /* pair_kolmogorov_crespi_full.cpp:615-631 */
+      double sumC1 = q->C0 + q->C2 * rdsq1 + q->C4 * rdsq1 * rdsq1;
+      double sumC11 = (q->C2 + 2.0 * q->C4 * rdsq1) * q->delta2inv;
+      double frho_ij = exp1 * sumC1;
+      double sumCff = 0.5 * q->C + frho_ij;
+      Vilp = exp0 * sumCff;
+      fpair = q->lambda * exp0 / r * sumCff;
+      fpair1 = 2.0 * exp0 * exp1 * (q->delta2inv * sumC1 - sumC11);
+    } else {
+      double frho1 = exp1 * q->C;
+      double Erep = 0.5 * q->epsilon + frho1;
+      Vilp = exp0 * Erep;
+      fpair = q->lambda * exp0 / r * Erep;
+      fpair1 = 2.0 * exp0 * frho1 * q->delta2inv;
+    }
     double fsum = fpair + fpair1;
     double del[3] = {delx, dely, delz};
     double dprod[3];
@@ -817,7 +878,8 @@ static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *
         f[3 * k + ip] += (-prodnorm1 * dp * fpair1) * Tap;
       }
     }
-    double ev = Tap * Vilp;
+    /* KC without the taper tallies V - offset, offset = -A (z0/cut)^6 (init_one :235) */
+    double ev = (p->i_model == 1 && !p->tap_flag) ? Vilp + q->A * pow(q->z0 / p->cut_global, 6.0) : Tap * Vilp;
     *erep += ev;
     if (eatom) {
       eatom[i] += 0.5 * ev;

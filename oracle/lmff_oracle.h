@@ -37,9 +37,10 @@ typedef struct {           /* pair_tersoff.h:38-53 */
   int ielement, jelement, kelement, powermint;
 } orc_ters_param;
 
-typedef struct {           /* pair_ilp_graphene_hbn.h:53-57 */
+typedef struct {           /* pair_ilp_graphene_hbn.h:53-57; the KC fields: pair_kolmogorov_crespi_full.h */
   double z0, alpha, epsilon, C, delta, d, sR, reff, C6, S;
   double delta2inv, seff, lambda, rcut;
+  double C0, C2, C4, A, z06;   /* kolmogorov/crespi/full only */
   int ielement, jelement;
 } orc_ilp_param;
 
@@ -51,8 +52,8 @@ typedef struct {
   orc_ters_param t_params[ORC_MAXELEM * ORC_MAXELEM * ORC_MAXELEM];
   int t_e2p[ORC_MAXELEM][ORC_MAXELEM][ORC_MAXELEM];
   double t_cutmax;
-  /* ILP */
-  int i_enabled, i_nelements, i_nparams;
+  /* interlayer style: ILP (i_model 0) or Kolmogorov-Crespi full (i_model 1) */
+  int i_enabled, i_nelements, i_nparams, i_model;
   int i_map[ORC_MAXTYPE + 1];
   orc_ilp_param i_params[ORC_MAXELEM * ORC_MAXELEM];
   int i_e2p[ORC_MAXELEM][ORC_MAXELEM];
@@ -73,6 +74,8 @@ typedef struct {
 int orc_pot_init(orc_pot *p, int ntypes, double cut_global, int tap_flag, double skin);
 int orc_read_tersoff(orc_pot *p, const char *path, const char *const *elem_of_type);
 int orc_read_ilp(orc_pot *p, const char *path, const char *const *elem_of_type);
+/* kolmogorov/crespi/full parameter file (pair_kolmogorov_crespi_full.cpp:247-392) */
+int orc_read_kc(orc_pot *p, const char *path, const char *const *elem_of_type);
 const char *orc_pot_error(const orc_pot *p);
 
 typedef struct orc_ctx orc_ctx;

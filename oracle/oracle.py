@@ -47,6 +47,7 @@ def _load():
         lib.orc_pot_init.argtypes = [P, C.c_int, C.c_double, C.c_int, C.c_double]
         lib.orc_read_tersoff.argtypes = [P, C.c_char_p, C.POINTER(C.c_char_p)]
         lib.orc_read_ilp.argtypes = [P, C.c_char_p, C.POINTER(C.c_char_p)]
+        lib.orc_read_kc.argtypes = [P, C.c_char_p, C.POINTER(C.c_char_p)]
         lib.orc_pot_error.argtypes = [P]
         lib.orc_pot_error.restype = C.c_char_p
         lib.orc_new.argtypes = [P, C.c_int]
@@ -82,7 +83,11 @@ class Oracle:
 
     def __init__(self, tersoff_file: Optional[str], ilp_file: Optional[str],
                  elements: Sequence[str] = ("C", "B", "N"), cut_global: float = 16.0,
-                 tap_flag: int = 1, skin: float = 2.0, nthreads: int = 0):
+                 tap_flag: int = 1, skin: float = 2.0, nthreads: int = 0, kc_file: Optional[str] = None,
+                 interlayer_elements: Optional[Sequence[str]] = None):
+        """kc_file: a kolmogorov/crespi/full parameter file used as the interlayer style
+        instead of ilp_file; interlayer_elements: its own element list (default
+        `elements`)."""
         lib = _load()
         self._pot = C.create_string_buffer(1 << 20)
         ntypes = len(elements)
@@ -91,7 +96,10 @@ class Oracle:
         arr = (C.c_char_p * ntypes)(*[e.encode() for e in elements])
         if tersoff_file and lib.orc_read_tersoff(self._pot, tersoff_file.encode(), arr):
             raise OracleError(lib.orc_pot_error(self._pot).decode())
-        if ilp_file and lib.orc_read_ilp(self._pot, ilp_file.encode(), arr):
+        arr2 = arr if interlayer_elements is None else (C.c_char_p * ntypes)(*[e.encode() for e in interlayer_elements])
+        if ilp_file and lib.orc_read_ilp(self._pot, ilp_file.encode(), arr2):
+            raise OracleError(lib.orc_pot_error(self._pot).decode())
+        if kc_file and lib.orc_read_kc(self._pot, kc_file.encode(), arr2):
             raise OracleError(lib.orc_pot_error(self._pot).decode())
         self.nthreads = nthreads or (os.cpu_count() or 1)
         self._ctx = lib.orc_new(self._pot, self.nthreads)

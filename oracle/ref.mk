@@ -37,7 +37,8 @@ CFLAGS := -O2 -w -I$(SRC)/STUBS
 CORE_CPP := $(filter-out $(SRC)/main.cpp,$(wildcard $(SRC)/*.cpp))
 EXTRA_CPP := $(EXTRA)/atom_vec_ellipsoid.cpp $(EXTRA)/dihedral_hybrid.cpp $(EXTRA)/improper_hybrid.cpp
 EXTRA_H := accelerator_kokkos.h accelerator_omp.h math_vector.h atom_vec_ellipsoid.h dihedral_hybrid.h improper_hybrid.h
-PKG_CPP := $(wildcard $(SRC)/MOLECULE/*.cpp) $(SRC)/MANYBODY/pair_tersoff.cpp $(SRC)/USER-MISC/pair_ilp_graphene_hbn.cpp
+PKG_CPP := $(wildcard $(SRC)/MOLECULE/*.cpp) $(SRC)/MANYBODY/pair_tersoff.cpp $(SRC)/USER-MISC/pair_ilp_graphene_hbn.cpp \
+           $(SRC)/USER-MISC/pair_kolmogorov_crespi_full.cpp
 ALL_CPP := $(CORE_CPP) $(EXTRA_CPP) $(PKG_CPP)
 # headers of the compiled units: these (and only these) feed the style tables
 STYLE_H := $(patsubst %.cpp,%.h,$(ALL_CPP))
@@ -89,7 +90,8 @@ PKGDIR := lammps-lmff_gb300/lammps
 GEN2 := $(OUT)/gen_gb300
 OBJ2 := $(OUT)/obj_gb300
 LIBDIR := lammps-lmff_gb300/lmff_gb300
-PKG_SRC := $(PKGDIR)/pair_tersoff_gb300.cpp $(PKGDIR)/pair_ilp_graphene_hbn_gb300.cpp $(PKGDIR)/lmff_lammps_adapter.cpp
+PKG_SRC := $(PKGDIR)/pair_tersoff_gb300.cpp $(PKGDIR)/pair_ilp_graphene_hbn_gb300.cpp \
+           $(PKGDIR)/pair_kolmogorov_crespi_full_gb300.cpp $(PKGDIR)/lmff_lammps_adapter.cpp
 CXXFLAGS2 := -O2 -std=c++11 -w -ffp-contract=off -DLAMMPS_MEMALIGN=64 -DLAMMPS_SMALLBIG \
              -I$(GEN2) -I$(GEN) -I$(SRC) -I$(SRC)/STUBS -I$(SRC)/MOLECULE -I$(SRC)/MANYBODY -I$(SRC)/USER-MISC \
              -I$(PKGDIR) -Iinclude
@@ -99,6 +101,7 @@ $(GEN2)/style_pair.h: $(GEN)/.stamp
 	@cp $(GEN)/style_pair.h $@
 	@echo '#include "pair_tersoff_gb300.h"' >> $@
 	@echo '#include "pair_ilp_graphene_hbn_gb300.h"' >> $@
+	@echo '#include "pair_kolmogorov_crespi_full_gb300.h"' >> $@
 
 $(OBJ2)/%.o: $(PKGDIR)/%.cpp $(GEN2)/style_pair.h
 	@$(CXX) $(CXXFLAGS2) -c $< -o $@

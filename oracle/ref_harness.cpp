@@ -137,12 +137,12 @@ int main(int argc, char **argv) {
     PairHybrid *h = (PairHybrid *)pair;
     for (int m = 0; m < h->nstyles; m++) {
       std::string kw = h->keywords[m];
-      std::string key = kw == "ilp/graphene/hbn" ? "e_ilp" : "e_" + kw;
+      // the interlayer style (ILP or Kolmogorov-Crespi full) is reported as e_ilp
+      bool inter = kw == "ilp/graphene/hbn" || kw == "kolmogorov/crespi/full";
+      std::string key = inter ? "e_ilp" : "e_" + kw;
       rec(key.c_str(), 'd', 1, &h->styles[m]->eng_vdwl);
-      if (strcmp(h->keywords[m], "ilp/graphene/hbn") == 0) {
-        ilp = (PairILPGrapheneHBN *)h->styles[m];
-        rec("pvector", 'd', 2, ilp->pvector);
-      }
+      if (inter) rec("pvector", 'd', 2, h->styles[m]->pvector);
+      if (kw == "ilp/graphene/hbn") ilp = (PairILPGrapheneHBN *)h->styles[m];
     }
   }
 

@@ -51,7 +51,18 @@ def read_records(path):
     return out
 
 
-def run_reference(s: S.System, tap_flag=1, nsteps=0, dt=0.001, lists=False, cut=16.0):
+def run_reference(s: S.System, tap_flag=1, nsteps=0, dt=0.001, lists=False, cut=16.0, interlayer="ilp"):
+    """interlayer "ilp": ilp/graphene/hbn with BNCH.ILP; "kc": kolmogorov/crespi/full
+    with CC.KC-full (carbon only: types B and N are NULL for it)."""
+    if interlayer == "kc":
+        inter = (f"pair_style hybrid/overlay tersoff kolmogorov/crespi/full {cut} {tap_flag}\n"
+                 f"pair_coeff * * tersoff {POT}/BNC.tersoff C B N\n"
+                 f"pair_coeff * * kolmogorov/crespi/full {POT}/CC.KC-full C NULL NULL\n"
+                 f"pair_modify shift yes")
+    else:
+        inter = (f"pair_style hybrid/overlay tersoff ilp/graphene/hbn {cut} {tap_flag}\n"
+                 f"pair_coeff * * tersoff {POT}/BNC.tersoff C B N\n"
+                 f"pair_coeff * * ilp/graphene/hbn {POT}/BNCH.ILP C B N")
     with tempfile.TemporaryDirectory() as td:
         data = os.path.join(td, "data.lmp")
         S.write_lammps_data(s, data)
@@ -61,9 +72,7 @@ atom_style full
 boundary {bnd}
 atom_modify map array
 read_data {data}
-pair_style hybrid/overlay tersoff ilp/graphene/hbn {cut} {tap_flag}
-pair_coeff * * tersoff {POT}/BNC.tersoff C B N
-pair_coeff * * ilp/graphene/hbn {POT}/BNCH.ILP C B N
+{inter}
 neighbor 2.0 bin
 neigh_modify every 1 delay 0 check yes one 10000 page 200000
 compute peatom all pe/atom pair
@@ -158,6 +167,10 @@ def pack(s: S.System, r, tap_flag, extra=None):
 ONLY = set(sys.argv[1:])     # optional: names of the fixtures to (re)generate
 
 
+def want(*names) -> bool:
+    return not ONLY or any(n in ONLY for n in names)
+
+
 def save(name, d):
     if ONLY and name not in ONLY:
         return
@@ -170,14 +183,37 @@ def main():
     if not os.path.exists(HARNESS):
         sys.exit("reference harness missing: make -f oracle/ref.mk REF=<reference> -j8")
 
+    if want("bilayer_small", "bilayer_small_notaper"):
+        _cases_bilayer_small()
+    if want("hetero_small"):
+        _case_hetero_small()
+    if want("tiny_images", "edges", "trilayer_alt"):
+        _cases_lists()
+    if want("c1_t0", "c1_t100"):
+        _cases_c1()
+    if want("hetero_t20"):
+        _case_hetero_t20()
+    if want("case5016", "case5016_rep2", "case5016_min", "case5016_min_long"):
+        _cases_case5016()
+    if want("kc_bilayer", "kc_bilayer_notaper", "kc_trilayer_t30"):
+        _cases_kc()
+
+
+def _cases_bilayer_small():
     # 1. small AB bilayer graphene, displaced, thermal velocities; lists
     s = S.thermalize(S.displace(S.ab_bilayer_graphene(8, 5), 0.05, seed=11), 300.0, seed=12)
     save("bilayer_small", pack(s, run_reference(s, lists=True), 1))
     # 2. same structure with the taper off
     save("bilayer_small_notaper", pack(s, run_reference(s, tap_flag=0), 0))
+
+
+def _case_hetero_small():
     # 3. twisted graphene/hBN bilayer (B, N, C parameters); lists
     s = S.displace(S.twisted_bilayer(8, 5, 3.0, top="hbn", spacing=3.3, shift=(0.4, 0.7)), 0.03, seed=21)
     save("hetero_small", pack(s, run_reference(s, lists=True), 1, {"strain_max": s.meta["strain_max"]}))
+
+
+def _cases_lists():
     # 4. box shorter than the 18 A neighbour cutoff: several images of each atom; lists
     s = S.displace(S.ab_bilayer_graphene(6, 4), 0.04, seed=31)
     save("tiny_images", pack(s, run_reference(s, lists=True), 1))
@@ -187,18 +223,27 @@ def main():
     # 6. three-layer graphite, alternating molecule ids (layers 1 and 3 share an id); lists
     s = S.displace(S.graphite_slab(3, 8, 5, spacing=3.35, mol_mode="alternate"), 0.04, seed=51)
     save("trilayer_alt", pack(s, run_reference(s, lists=True), 1))
+
+
+def _cases_c1():
     # 7. the 7,200-atom plain-FP64 workload at t=0 and after 100 NVE steps (dt = 1 fs)
     c1 = S.thermalize(S.ab_bilayer_graphene(30, 30), 300.0, seed=1)
     r0 = run_reference(c1)
     save("c1_t0", pack(c1, r0, 1))
     r100 = run_reference(c1, nsteps=100)
     save("c1_t100", pack(c1, r100, 1, {"x0": r0["x"].reshape(-1, 3), "v0": r0["v"].reshape(-1, 3)}))
+
+
+def _case_hetero_t20():
     # 8. short NVE on the hetero cell (exercises B/N masses and parameters)
     h = S.thermalize(S.twisted_bilayer(8, 5, 3.0, top="hbn", spacing=3.3, shift=(0.4, 0.7)), 300.0, seed=61)
     r0 = run_reference(h)
     r20 = run_reference(h, nsteps=20)
     save("hetero_t20", pack(h, r20, 1, {"x0": r0["x"].reshape(-1, 3), "v0": r0["v"].reshape(-1, 3),
                                         "f0": r0["f"].reshape(-1, 3)}))
+
+
+def _cases_case5016():
     # 9. the reference's own case (Cases/case_5016: 6 graphene layers, 5016 atoms, layer 1
     #    excluded from Tersoff by NULL, taper off): read_data, then forces
     save("case5016", pack_case(run_case()))
@@ -214,6 +259,22 @@ def main():
     rm = run_case("group l1 type 1", "fix sf l1 setforce 0.0 0.0 0.0\nminimize 1.0e-10 1.0e-3 300 3000",
                   flags=("min",))
     save("case5016_min_long", pack_case(rm, {"x0": r0["x"].reshape(-1, 3)}))
+
+
+def _cases_kc():
+    # 13-15. Kolmogorov-Crespi full (CC.KC-full) as the interlayer style: a displaced,
+    #        thermal AB bilayer with and without the taper (without it the energy carries
+    #        the reference's offset), and 30 NVE steps of a larger bilayer
+    s = S.thermalize(S.displace(S.ab_bilayer_graphene(8, 5), 0.05, seed=71), 300.0, seed=72)
+    save("kc_bilayer", pack(s, run_reference(s, interlayer="kc"), 1, {"interlayer": "kc"}))
+    save("kc_bilayer_notaper", pack(s, run_reference(s, tap_flag=0, interlayer="kc"), 0, {"interlayer": "kc"}))
+    k = S.thermalize(S.displace(S.graphite_slab(3, 12, 7, spacing=3.35, mol_mode="unique"), 0.03, seed=73), 300.0,
+                     seed=74)
+    r0 = run_reference(k, interlayer="kc")
+    r30 = run_reference(k, nsteps=30, interlayer="kc")
+    save("kc_trilayer_t30", pack(k, r30, 1, {"interlayer": "kc", "x0": r0["x"].reshape(-1, 3),
+                                             "v0": r0["v"].reshape(-1, 3), "f0": r0["f"].reshape(-1, 3),
+                                             "e0": r0["e_ilp"][0]}))
 
 
 if __name__ == "__main__":

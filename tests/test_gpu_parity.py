@@ -291,3 +291,21 @@ def test_step_graph_overflow_redo():
     assert rel_max(vg, ve) < 1e-7 and rel_max(fg, fe) < 1e-7
     for a, b in zip(thg, the):
         assert abs(a["etotal"] - b["etotal"]) <= 1e-10 * abs(b["etotal"])
+
+
+def test_host_positions_in_another_periodic_image_need_no_rebuild():
+    """A caller may pass unwrapped coordinates, or wrap some atoms between calls (LAMMPS
+    does at reneighbouring): the engine takes each position in the image its list was
+    built with, so the forces are unchanged and no rebuild is triggered."""
+    g = load_golden("bilayer_small")
+    eng = engine_for(g)
+    r0 = compute_golden(eng, g)
+    rb = eng.stats()["rebuilds"]
+    L = g["box_hi"] - g["box_lo"]
+    x = np.array(g["x"])
+    x[::3, 0] += L[0]
+    x[1::5, 1] -= 2 * L[1]
+    r1 = eng.compute(x, g["type"], g["mol"], g["tag"], same_atoms=True)
+    assert eng.stats()["rebuilds"] == rb
+    assert rel_max(r1["f"], r0["f"]) < 1e-12
+    assert abs(r1["e_ilp"] - r0["e_ilp"]) <= 1e-12 * abs(r0["e_ilp"])

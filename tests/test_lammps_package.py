@@ -48,3 +48,30 @@ run 0
         assert "tersoff/gb300: no CUDA device" in text  # init_style reached lmff_create
     else:
         assert r.returncode == 0, text
+
+
+def test_suffix_routes_kolmogorov_crespi_full(lmp, tmp_path):
+    """kolmogorov/crespi/full -> kolmogorov/crespi/full/gb300 through the reference's
+    own settings / coeff / read_file (12-word CC.KC-full entries)."""
+    s = S.displace(S.ab_bilayer_graphene(8, 5), 0.03, seed=3)
+    data = tmp_path / "data.lmp"
+    S.write_lammps_data(s, str(data), ntypes=1)     # carbon only: every type pair is set
+    script = tmp_path / "in.lmp"
+    script.write_text(f"""units metal
+atom_style full
+boundary p p f
+read_data {data}
+pair_style hybrid/overlay kolmogorov/crespi/full 16.0 1
+pair_coeff * * kolmogorov/crespi/full {POT}/CC.KC-full C
+pair_modify shift yes
+neighbor 2.0 bin
+run 0
+""")
+    r = subprocess.run([lmp, str(script), str(tmp_path / "out.bin"), "--", "-sf", "gb300", "-log", "none",
+                        "-nocite"], capture_output=True, text=True, cwd=str(tmp_path))
+    text = r.stdout + r.stderr
+    if capi.device_count() == 0:
+        assert r.returncode != 0
+        assert "kolmogorov/crespi/full/gb300: no CUDA device" in text, text
+    else:
+        assert r.returncode == 0, text

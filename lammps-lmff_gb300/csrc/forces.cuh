@@ -44,16 +44,36 @@ struct Math<double> {
   static __device__ __forceinline__ void sincospi_(double a, double *s, double *c) { sincospi(a, s, c); }
 };
 
+// Single hardware approximations (PTX ex2/rsqrt/rcp .approx.ftz): relative error about
+// 2^-22, the accuracy of the FP32 pair arithmetic around them.  Flushing subnormals is
+// harmless here: the exponentials underflow to 0 only far beyond any contribution that
+// matters, and distances are bounded away from 0.
+__device__ __forceinline__ float ex2_ftz(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 template <>
 struct Math<float> {
   static __device__ __forceinline__ float ex(float a) { return expf(a); }
   // lambda log2e (z0 - r): the constant's rounding scales a small argument instead of
   // shifting every pair's exponent by the same absolute amount
-  static __device__ __forceinline__ float exp_rep0(const IlpP<float> &p, float r) { return exp2f(p.lam_l2e * (p.z0 - r)); }
-  static __device__ __forceinline__ float exp_rep1(const IlpP<float> &p, float rhosq) { return exp2f(p.nd2_l2e * rhosq); }
+  static __device__ __forceinline__ float exp_rep0(const IlpP<float> &p, float r) { return ex2_ftz(p.lam_l2e * (p.z0 - r)); }
+  static __device__ __forceinline__ float exp_rep1(const IlpP<float> &p, float rhosq) { return ex2_ftz(p.nd2_l2e * rhosq); }
   // exp(-d (r/seff - 1)) = exp2((d/seff) log2e (seff - r))
-  static __device__ __forceinline__ float exp_ts(const IlpP<float> &p, float r) { return exp2f(p.ts_a * (p.seff - r)); }
-  static __device__ __forceinline__ float rcp(float a) { return __fdividef(1.0f, a); }
+  static __device__ __forceinline__ float exp_ts(const IlpP<float> &p, float r) { return ex2_ftz(p.ts_a * (p.seff - r)); }
+  static __device__ __forceinline__ float rcp(float a) { return rcp_ftz(a); }
   static __device__ __forceinline__ float sqrt_(float a) { return sqrtf(a); }
   static __device__ __forceinline__ float pow_(float a, float b) { return powf(a, b); }
   static __device__ __forceinline__ void sincospi_(float a, float *s, float *c) { sincospif(a, s, c); }

@@ -481,7 +481,7 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
   const R njx = N.q.x, njy = N.q.y, njz = N.q.z;
   R r, rinv;
   if constexpr (sizeof(R) == 8) { r = sqrt(rsq); rinv = R(1) / r; }
-  else { rinv = rsqrtf(rsq); r = rsq * rinv; }
+  else { rinv = rsqrt_ftz(rsq); r = rsq * rinv; }
   // taper (pair_ilp_graphene_hbn.h:80-115), Tap and dTap in one pass
   R Tap = 1, dTap = 0;
   if (c_pot.tap) {

@@ -557,6 +557,141 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
 // issue-bound with long-scoreboard stalls on j's data, and 40 resident warps hide them
 // better than 36 (measured: -8 % at 2.7M atoms, -16 % at 490k).  FP64 keeps its
 // registers.
+#ifdef LMFF_PACKED_X2
+// ---- packed FP32x2 form of the same pair body (sm_100+ FFMA2/FADD2/FMUL2)
+// The kernel is issue-bound in FP32, and the pair body is full of independent twin
+// operations: the repulsion of term (i,j) with n_i and of term (j,i) with n_j, the x and
+// y components, and the two Horner chains of Tap and dTap.  Each twin pair is one packed
+// instruction.  Same formulas as ilp_pair; the rounding differs from it only by the
+// order of a few additions.
+__device__ __forceinline__ float2 p2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+
+template <bool EV, bool ONE, bool KC>
+__device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const AtomI<float> &ai, const SysDesc &sdl,
+                                            uint32_t e, const AtomI<float>::J &J, const NrmJ<float> &N, float nix,
+                                            float niy, float niz, int ie, long long mi, long long itag, bool check,
+                                            IlpAcc &acc) {
+  int j, sx, sy, sz;
+  decode_entry(e, a.lc, j, sx, sy, sz);
+  // del = x_i - x_j(image), x and y packed: ((h_i - h_j) - s Lhi) + ((l_i - l_j) - s Llo)
+  const float2 sfx = p2((float)sx, (float)sy);
+  float2 hxy = add2(p2(ai.hx, ai.hy), p2(-J.h.x, -J.h.y));
+  hxy = add2(hxy, mul2(sfx, p2(-sdl.Lhi[0], -sdl.Lhi[1])));
+  float2 lxy = add2(p2(ai.lx, ai.ly), p2(-J.l.x, -J.l.y));
+  lxy = add2(lxy, mul2(sfx, p2(-sdl.Llo[0], -sdl.Llo[1])));
+  const float2 dxy = add2(hxy, lxy);
+  const float dz = ((ai.hz - J.h.z) - (float)sz * sdl.Lhi[2]) + ((ai.lz - J.l.z) - (float)sz * sdl.Llo[2]);
+  const float2 sq = mul2(dxy, dxy);
+  const float rsq = fmaf(dz, dz, sq.x + sq.y);
+  if (!(rsq < c_pot.i_cutsq)) return;
+  const long long jinfo = (long long)__float_as_int(J.h.w);
+  if (check && info_mol(jinfo) == mi) return;
+  const int tj = info_type(jinfo);
+  if (check && !((c_pot.ilp_typemask >> tj) & 1u)) return;
+  const int je = ONE ? 0 : c_pot.i_map[tj];
+  const IlpP<float> &pij = ONE ? c_pot.ilp[0] : c_pot.ilp[ie * MAXELEM + je];
+  const IlpP<float> &pji = ONE ? c_pot.ilp[0] : c_pot.ilp[je * MAXELEM + ie];
+  const float dx = dxy.x, dy = dxy.y;
+  const float njx = N.q.x, njy = N.q.y, njz = N.q.z;
+  const float rinv = rsqrt_ftz(rsq);
+  const float r = rsq * rinv;
+  // Tap and dTap/dx as one packed Horner pass (pair_ilp_graphene_hbn.h:80-115)
+  float Tap = 1.f, dTap = 0.f;
+  if (c_pot.tap) {
+    const float x = r * c_pot.i_inv_rcut;
+    const float2 xx = p2(x, x);
+    float2 t = fma2(p2(20.f, 140.f), xx, p2(-70.f, -420.f));
+    t = fma2(t, xx, p2(84.f, 420.f));
+    t = fma2(t, xx, p2(-35.f, -140.f));
+    t = mul2(t, xx);
+    t = mul2(t, xx);
+    t = mul2(t, xx);
+    Tap = fmaf(t.x, x, 1.f);
+    dTap = t.y * c_pot.i_inv_rcut;
+  }
+  // ---- vdW (both ends evaluate the pair force; energy halved)
+  const IlpP<float> &pv = (c_pot.vdw_sym || keep_half(itag, a.tag[j], sx, sy, sz)) ? pij : pji;
+  const float r2inv = rinv * rinv;
+  const float r6inv = r2inv * r2inv * r2inv;
+  const float r8inv = r6inv * r2inv;
+  float Vvdw, fpv;
+  if constexpr (KC) {
+    Vvdw = -pv.kc_Az06 * r6inv;
+    fpv = -6.f * pv.kc_Az06 * r8inv;
+  } else {
+    const float TSvdw = 1.f + Math<float>::exp_ts(pv, r);
+    const float TSinv = Math<float>::rcp(TSvdw);
+    const float c6t = pv.C6 * TSinv;
+    Vvdw = -c6t * r6inv;
+    fpv = c6t * r8inv * (-6.f + pv.d_over_seff * (TSvdw - 1.f) * TSinv * r);
+  }
+  const float fsum_v = fpv * Tap - Vvdw * dTap * rinv;
+  // ---- the two repulsion terms packed: .x = (i,j) with n_i, .y = (j,i) with n_j
+  const float2 PQ = fma2(p2(nix, njx), p2(dx, dx), fma2(p2(niy, njy), p2(dy, dy), mul2(p2(niz, njz), p2(dz, dz))));
+  const float2 RH = fma2(p2(-PQ.x, -PQ.y), PQ, p2(rsq, rsq));
+  const float e0 = Math<float>::exp_rep0(pij, r);
+  const float e0b = pji.same_as_swapped ? e0 : Math<float>::exp_rep0(pji, r);
+  const float2 E0 = p2(e0, e0b);
+  const float2 EA = mul2(p2(pij.nd2_l2e, pji.nd2_l2e), RH);
+  const float2 E1 = p2(ex2_ftz(EA.x), ex2_ftz(EA.y));
+  const float2 D2 = p2(pij.delta2inv, pji.delta2inv);
+  float2 V, FP1;
+  float2 ER;
+  if constexpr (KC) {
+    const float2 X = mul2(RH, D2);
+    const float2 S1 = fma2(fma2(p2(pij.kc_C4, pji.kc_C4), X, p2(pij.kc_C2, pji.kc_C2)), X, p2(pij.kc_C0, pji.kc_C0));
+    const float2 S11 = mul2(fma2(p2(2.f * pij.kc_C4, 2.f * pji.kc_C4), X, p2(pij.kc_C2, pji.kc_C2)), D2);
+    ER = fma2(E1, S1, p2(pij.eps_half, pji.eps_half));
+    V = mul2(E0, ER);
+    FP1 = mul2(mul2(p2(2.f, 2.f), mul2(E0, E1)), fma2(D2, S1, p2(-S11.x, -S11.y)));
+  } else {
+    const float2 FR = mul2(E1, p2(pij.C, pji.C));
+    ER = add2(p2(pij.eps_half, pji.eps_half), FR);
+    V = mul2(E0, ER);
+    FP1 = mul2(mul2(E0, FR), p2(2.f * pij.delta2inv, 2.f * pji.delta2inv));
+  }
+  const float2 FS = fma2(mul2(p2(pij.lambda, pji.lambda), V), p2(rinv, rinv), FP1);
+  const float2 TPQ = mul2(mul2(p2(Tap, Tap), PQ), FP1);   // (tp1, tq1)
+  const float Vsum = V.x + V.y;
+  const float crad = fsum_v + (FS.x + FS.y) * Tap - Vsum * dTap * rinv;
+  // ---- force on i; g_i += tp1 del
+  float2 fxy = fma2(p2(crad, crad), dxy, p2(acc.fx, acc.fy));
+  fxy = fma2(p2(-TPQ.x, -TPQ.x), p2(nix, niy), fxy);
+  fxy = fma2(p2(-TPQ.y, -TPQ.y), p2(njx, njy), fxy);
+  acc.fx = fxy.x;
+  acc.fy = fxy.y;
+  acc.fz += crad * dz - TPQ.x * niz - TPQ.y * njz;
+  const float2 gxy = fma2(p2(TPQ.x, TPQ.x), dxy, p2(acc.gxa, acc.gya));
+  acc.gxa = gxy.x;
+  acc.gya = gxy.y;
+  acc.gza += TPQ.x * dz;
+  if (EV) {
+    acc.evdw += 0.5f * Vvdw * Tap;
+    const float eoff = (KC && !c_pot.tap) ? pij.kc_off + pji.kc_off : 0.f;
+    acc.erep += 0.5f * (Vsum * Tap - eoff);
+    const float cr1 = FS.x * Tap - V.x * dTap * rinv + 0.5f * fsum_v;
+    const float kx = cr1 * dx - TPQ.x * nix, ky = cr1 * dy - TPQ.x * niy, kz = cr1 * dz - TPQ.x * niz;
+    acc.w0 += dx * kx; acc.w1 += dy * ky; acc.w2 += dz * kz;
+    acc.w3 += dx * ky; acc.w4 += dx * kz; acc.w5 += dy * kz;
+  }
+}
+#endif  // LMFF_PACKED_X2
+
+// the pair body of this precision: packed FP32x2 for the mixed path, scalar FP64
+template <bool EV, bool ONE, bool KC>
+__device__ __forceinline__ void pair_body(const ForceArgs<R> &a, const AtomI<R> &ai, const SysDesc &sdl, uint32_t e,
+                                          const typename AtomI<R>::J &J, const NrmJ<R> &N, R nix, R niy, R niz, int ie,
+                                          long long mi, long long itag, bool check, IlpAcc &acc) {
+#ifdef LMFF_PACKED_X2
+  ilp_pair_x2<EV, ONE, KC>(a, ai, sdl, e, J, N, nix, niy, niz, ie, mi, itag, check, acc);
+#else
+  ilp_pair<EV, ONE, KC>(a, ai, sdl, e, J, N, nix, niy, niz, ie, mi, itag, check, acc);
+#endif
+}
+
 template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R> a) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -588,12 +723,24 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R
     const int64_t b = a.list_off[i];
     const uint32_t *lst = a.list + b;
     const int cnt = (int)(a.list_off[i + 1] - b);
-    if constexpr (!PF) {
+    if constexpr (!PF && ONE) {
+      // the next list entry is loaded one iteration ahead, so that only j's data (not
+      // the list read before it) is on the dependence chain of a pair (-9 % on the
+      // 2.7M-atom graphite; the multi-element body has no registers to spare for it)
+      uint32_t e_next = lane < cnt ? __ldg(&lst[lane]) : 0u;
       for (int k = lane; k < cnt; k += TPA) {
-        uint32_t e = __ldg(&lst[k]);
+        const uint32_t e = e_next;
+        if (k + TPA < cnt) e_next = __ldg(&lst[k + TPA]);
         const int j = (int)(e & a.lc.imask);
-        ilp_pair<EV, ONE, KC>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi, itag, check,
-                          acc);
+        pair_body<EV, ONE, KC>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi, itag, check,
+                               acc);
+      }
+    } else if constexpr (!PF) {
+      for (int k = lane; k < cnt; k += TPA) {
+        const uint32_t e = __ldg(&lst[k]);
+        const int j = (int)(e & a.lc.imask);
+        pair_body<EV, ONE, KC>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi, itag, check,
+                               acc);
       }
     } else {
       // software pipeline: the next entry's position and normal are in flight while
@@ -617,7 +764,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R
           J = ai.fetch(a.A, j);
           N = NrmJ<R>::load(a, j);
         }
-        ilp_pair<EV, ONE, KC>(a, ai, sdl, ec, Jc, Nc, nix, niy, niz, ie, mi, itag, check, acc);
+        pair_body<EV, ONE, KC>(a, ai, sdl, ec, Jc, Nc, nix, niy, niz, ie, mi, itag, check, acc);
       }
     }
   }

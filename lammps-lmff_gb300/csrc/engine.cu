@@ -173,16 +173,23 @@ __global__ void k_count_pairs(int n, const d4 *xq, const SysDesc *sys, const int
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
 }
 
+// dtf / mass per atom type, computed on the host: the same FP64 quotient fix_nve.cpp
+// forms per atom (dtfm = dtf / mass[type[i]], :64-84), without a division per atom (FP64
+// division is a long sequence on a GPU whose FP64 rate is 1/64 of FP32)
+struct DtfmTab {
+  double v[MAXTYPE + 1];
+};
+
 // velocity Verlet halves (fix_nve.cpp:64-111); the first also moves x, refreshes the
 // double-float split and tracks the displacement since the last build
-__global__ void k_nve1(int n, d4 *xq, double *v, const double *f, const double *mass, double dtf, double dtv,
+__global__ void k_nve1(int n, d4 *xq, double *v, const double *f, DtfmTab tab, double dtv,
                        const double *xhold, unsigned long long *maxdisp, const SysDesc *sys, const int *sysid,
                        float4 *xh, float4 *xl, int do_hilo) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   double d2 = 0.0;
   if (q < n) {
-    double dtfm = dtf / mass[q];
     d4 w = xq[q];
+    double dtfm = tab.v[__double_as_longlong(w.w) & 255];
     double vx = v[q] + dtfm * f[q];
     double vy = v[n + q] + dtfm * f[n + q];
     double vz = v[2 * n + q] + dtfm * f[2 * n + q];
@@ -206,10 +213,11 @@ __global__ void k_nve1(int n, d4 *xq, double *v, const double *f, const double *
   if ((threadIdx.x & 31) == 0 && d2 > 0.0) atomicMax(maxdisp, (unsigned long long)__double_as_longlong(d2));
 }
 
-__global__ void k_nve2(int n, double *v, const double *f, const double *mass, double dtf, double *ke) {
+__global__ void k_nve2(int n, double *v, const double *f, const d4 *xq, const double *mass, DtfmTab tab, double *ke) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
-  double dtfm = dtf / mass[q];
+  const long long info = *reinterpret_cast<const long long *>(&xq[q].w);
+  double dtfm = tab.v[info & 255];
   double vx = v[q] + dtfm * f[q];
   double vy = v[n + q] + dtfm * f[n + q];
   double vz = v[2 * n + q] + dtfm * f[2 * n + q];
@@ -1048,6 +1056,7 @@ struct Engine {
     a.bin_start = d.bin_start;
     a.bin_end = d.bin_end;
     a.nbins = d.nbins;
+    a.bin_key = d.bin_key2;
     a.list_off = d.list_off;
     a.list = d.list;
     a.list_cap = d.list_cap;
@@ -1492,6 +1501,7 @@ struct Engine {
     a.bin_start = d.bin_start;
     a.bin_end = d.bin_end;
     a.nbins = d.nbins;
+    a.bin_key = d.bin_key2;
     a.list_off = d.list_off;
     a.list = d.list;
     a.list_cap = graph_cap;
@@ -1515,6 +1525,15 @@ struct Engine {
   void drop_graph() {
     if (step_exec) cudaGraphExecDestroy(step_exec);
     step_exec = nullptr;
+  }
+
+  DtfmTab dtfm_table(double dtf) const {
+    DtfmTab t;
+    for (int k = 0; k <= MAXTYPE; k++) {
+      double m = (k >= 1 && (size_t)(k - 1) < mass_type.size()) ? mass_type[k - 1] : 1.0;
+      t.v[k] = dtf / m;
+    }
+    return t;
   }
 
   int build_step_graph(double dt) {
@@ -1553,7 +1572,7 @@ struct Engine {
     cudaGraphConditionalHandle h;
     CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
     CK(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, d.mass, dtf, dt, d.xhold, d.maxdisp, d.sys,
+    k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
                                                 d.sysid, d.xh, d.xl, mixed ? 1 : 0);
     k_setcond<<<1, 1, 0, stream>>>(h, d.maxdisp, 0.25 * skin * skin);
     cudaStreamCaptureStatus cs;
@@ -1582,7 +1601,7 @@ struct Engine {
       run_kernels(args<float>(), LMFF_TERSOFF | LMFF_ILP, false, false, f32::launch_short, f32::launch_tersoff,
                   f32::launch_ilp, f32::launch_nderiv, f32::launch_finish);
     ktiming = kt;
-    k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, dtf, nullptr);
+    k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.xq, d.mass, dtfm_table(dtf), nullptr);
     cudaGraph_t gout = nullptr;
     CK(cudaStreamEndCapture(stream, &gout));
     cudaError_t ei = cudaGraphInstantiate(&step_exec, gout, 0);
@@ -1661,7 +1680,7 @@ struct Engine {
     for (int s = 1; s <= nsteps; s++) {
       bool mixed = precision == LMFF_MIXED;
       timed(4, [&] {
-        k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, d.mass, dtf, dt, d.xhold, d.maxdisp, d.sys,
+        k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
                                                     d.sysid, d.xh, d.xl, mixed ? 1 : 0);
       });
       CK(cudaGetLastError());
@@ -1670,7 +1689,7 @@ struct Engine {
       if (rc) return rc;
       rc = forces(LMFF_TERSOFF | LMFF_ILP, false, false, nullptr);
       if (rc) return rc;
-      timed(4, [&] { k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, dtf, nullptr); });
+      timed(4, [&] { k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.xq, d.mass, dtfm_table(dtf), nullptr); });
       CK(cudaGetLastError());
       steps++;
     }
@@ -1709,14 +1728,14 @@ struct Engine {
       rc = forces(LMFF_TERSOFF | LMFF_ILP, thermo_every > 0, false, &hr);
       if (rc) return rc;
       if (thermo_every > 0) {
-        k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, 0.0, ke);
+        k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.xq, d.mass, dtfm_table(0.0), ke);
         rc = sample(steps, hr);
         if (rc) return rc;
       }
     } else if (thermo_every > 0) {
       rc = forces(LMFF_TERSOFF | LMFF_ILP, true, false, &hr);
       if (rc) return rc;
-      k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, 0.0, ke);
+      k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.xq, d.mass, dtfm_table(0.0), ke);
       rc = sample(steps, hr);
       if (rc) return rc;
     }
@@ -1745,7 +1764,7 @@ struct Engine {
       }
       if (th_at_end) {
         bool mixed = precision == LMFF_MIXED;
-        k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, d.mass, dtf, dtv, d.xhold, d.maxdisp, d.sys,
+        k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dtv, d.xhold, d.maxdisp, d.sys,
                                                     d.sysid, d.xh, d.xl, mixed ? 1 : 0);
         CK(cudaGetLastError());
         hilo_fresh = mixed;
@@ -1753,7 +1772,7 @@ struct Engine {
         if (rc) return rc;
         rc = forces(LMFF_TERSOFF | LMFF_ILP, true, false, &hr);
         if (rc) return rc;
-        k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.mass, dtf, ke);
+        k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.xq, d.mass, dtfm_table(dtf), ke);
         CK(cudaGetLastError());
         steps++;
         rc = sample(steps, hr);
@@ -2259,6 +2278,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
   na.bin_start = bin_start;
   na.bin_end = bin_end;
   na.nbins = nbins;
+  na.bin_key = key2;
   na.list_off = list_off;
   na.list = list;
   na.list_cap = (int64_t)list_cap;
@@ -2673,6 +2693,7 @@ int lmff_set_masses(lmff_engine *e, int ntypes, const double *mass) {
   if (!e || !mass || ntypes < 1 || ntypes > lmff::MAXTYPE) return LMFF_EINVAL;
   e->e.mass_type.assign(lmff::MAXTYPE + 1, 1.0);
   for (int t = 0; t < ntypes; t++) e->e.mass_type[t] = mass[t];
+  e->e.drop_graph();   // a captured step holds dt/mass per type
   return LMFF_OK;
 }
 

@@ -9,6 +9,8 @@
 //     cutmax) + skin, from which each step picks the ILP intralayer and Tersoff lists.
 // Periodic images are explicit image codes, never minimum image, so boxes shorter than
 // the cutoff (several images of one atom, self images) are exact.
+#include <climits>
+
 #include <cub/cub.cuh>
 
 #include "engine.cuh"
@@ -103,81 +105,103 @@ __device__ __forceinline__ bool le_exact(float rsq, float thr, double thr64, con
   return r2 <= thr64;
 }
 
-// One block per bin, one thread per i atom of the bin (atoms are contiguous after the
-// sort).  The block walks the bin's stencil; each stencil bin's j atoms are staged in
-// shared memory and every thread tests its i against them in order (all threads read
-// the same j: a broadcast).  Counters and write cursors live in registers.  The
-// entries of each i come out in the order of a per-atom scan: stencil bins (dz, dy,
+// One warp per 32 consecutive atoms of the sorted order, one lane per atom.  Atoms are
+// sorted by bin and bins are numbered x fastest, so the lanes of a warp almost always
+// share one bin row (same system, y and z bin) and sit in one or two neighbouring x
+// bins.  The warp walks the union of its lanes' stencils (the x range widened by the
+// lanes' spread; a lane skips x bins outside its own stencil), staging each stencil
+// bin's j atoms 32 at a time in warp-private shared memory; every lane then tests its i
+// against them in order (a broadcast).  Lanes of another row (a warp that straddles a
+// row boundary) are handled in a second pass.  No block-wide barrier is involved.
+// The entries of each i come out in the order of a per-atom scan: stencil bins (dz, dy,
 // dx), then j ascending.
 // FILL = false: counts pair-list entries into cnt[i] and writes the short list.
 // FILL = true: writes the pair list at list_off[i], candidates inside the force cutoff
 // from the front and the skin shell from the back (the pair kernel's lanes then mostly
 // accept or reject together).
-constexpr int LT = 128;   // i atoms per block pass and j atoms per staged tile
+constexpr int LW = 4;   // warps per block
 
 template <bool FILL>
-__global__ void __launch_bounds__(LT) k_list(NbArgs a) {
-  const int gb = blockIdx.x;
-  const int i0 = a.bin_start[gb], i1 = a.bin_end[gb];
-  if (i1 <= i0) return;
-  const SysDesc &sd = a.sys[a.sysid[i0]];
-  const int lb = gb - sd.bin_begin;
-  const int b0 = lb % sd.nb[0], b1 = (lb / sd.nb[0]) % sd.nb[1], b2 = lb / (sd.nb[0] * sd.nb[1]);
-  __shared__ float4 jh[LT], jl[LT];
-  const float prefilt = sd.prefilt_sq;
-  for (int it0 = i0; it0 < i1; it0 += LT) {
-    const int i = it0 + threadIdx.x;
-    const bool act = i < i1;
-    float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
-    if (act) {
-      hi = a.xh[i];
-      lo = a.xl[i];
-    }
-    const int infoi = __float_as_int(hi.w);
-    const int ti = infoi & 255;
-    const int mi = infoi >> 8;
-    const int ilp_i = c_nb.ilp_mapped[ti];
-    int nlong = 0, nin = 0, nsh = 0, nshort = 0;
-    const int64_t base = (FILL && act) ? a.list_off[i] : 0;
-    const int64_t lend = (FILL && act) ? a.list_off[i + 1] : 0;
+__global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
+  const int wg = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  const int wl = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  if (wg * 32 >= a.n) return;                       // whole warps only
+  __shared__ float4 th[LW][32], tl[LW][32];
+  const int i = wg * 32 + lane;
+  const bool act = i < a.n;
+  int sys = -1, bx = 0, by = 0, bz = 0;
+  float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+  if (act) {
+    sys = a.sysid[i];
+    const SysDesc &sd = a.sys[sys];
+    const int lb = (int)a.bin_key[i] - sd.bin_begin;
+    bx = lb % sd.nb[0];
+    by = (lb / sd.nb[0]) % sd.nb[1];
+    bz = lb / (sd.nb[0] * sd.nb[1]);
+    hi = a.xh[i];
+    lo = a.xl[i];
+  }
+  const int infoi = __float_as_int(hi.w);
+  const int ti = infoi & 255;
+  const int mi = infoi >> 8;
+  const int ilp_i = c_nb.ilp_mapped[ti];
+  int nlong = 0, nin = 0, nsh = 0, nshort = 0;
+  const int64_t base = (FILL && act) ? a.list_off[i] : 0;
+  const int64_t lend = (FILL && act) ? a.list_off[i + 1] : 0;
+  unsigned todo = __ballot_sync(FULL, act);
+  while (todo) {
+    const int leader = __ffs(todo) - 1;
+    const int rs = __shfl_sync(FULL, sys, leader);
+    const int ry = __shfl_sync(FULL, by, leader);
+    const int rz = __shfl_sync(FULL, bz, leader);
+    const bool mine = ((todo >> lane) & 1u) && sys == rs && by == ry && bz == rz;
+    todo &= ~__ballot_sync(FULL, mine);
+    const int xmin = __reduce_min_sync(FULL, mine ? bx : INT_MAX);
+    const int xmax = __reduce_max_sync(FULL, mine ? bx : INT_MIN);
+    const SysDesc &sd = a.sys[rs];
+    const float prefilt = sd.prefilt_sq;
     for (int dz = -sd.reach[2]; dz <= sd.reach[2]; dz++) {
-      int bz = b2 + dz, sz = 0;
+      int jz = rz + dz, sz = 0;
       if (sd.per[2]) {
-        sz = bz >= 0 ? bz / sd.nb[2] : -((-bz + sd.nb[2] - 1) / sd.nb[2]);
-        bz -= sz * sd.nb[2];
-      } else if (bz < 0 || bz >= sd.nb[2]) continue;
+        sz = jz >= 0 ? jz / sd.nb[2] : -((-jz + sd.nb[2] - 1) / sd.nb[2]);
+        jz -= sz * sd.nb[2];
+      } else if (jz < 0 || jz >= sd.nb[2]) continue;
       for (int dy = -sd.reach[1]; dy <= sd.reach[1]; dy++) {
-        int by = b1 + dy, sy = 0;
+        int jy = ry + dy, sy = 0;
         if (sd.per[1]) {
-          sy = by >= 0 ? by / sd.nb[1] : -((-by + sd.nb[1] - 1) / sd.nb[1]);
-          by -= sy * sd.nb[1];
-        } else if (by < 0 || by >= sd.nb[1]) continue;
-        for (int dx = -sd.reach[0]; dx <= sd.reach[0]; dx++) {
-          int bx = b0 + dx, sx = 0;
+          sy = jy >= 0 ? jy / sd.nb[1] : -((-jy + sd.nb[1] - 1) / sd.nb[1]);
+          jy -= sy * sd.nb[1];
+        } else if (jy < 0 || jy >= sd.nb[1]) continue;
+        for (int xu = xmin - sd.reach[0]; xu <= xmax + sd.reach[0]; xu++) {
+          int jx = xu, sx = 0;
           if (sd.per[0]) {
-            sx = bx >= 0 ? bx / sd.nb[0] : -((-bx + sd.nb[0] - 1) / sd.nb[0]);
-            bx -= sx * sd.nb[0];
-          } else if (bx < 0 || bx >= sd.nb[0]) continue;
-          const int gbj = sd.bin_begin + (bz * sd.nb[1] + by) * sd.nb[0] + bx;
+            sx = jx >= 0 ? jx / sd.nb[0] : -((-jx + sd.nb[0] - 1) / sd.nb[0]);
+            jx -= sx * sd.nb[0];
+          } else if (jx < 0 || jx >= sd.nb[0]) continue;
+          const bool use = mine && xu >= bx - sd.reach[0] && xu <= bx + sd.reach[0];
+          if (!__any_sync(FULL, use)) continue;
+          const int gbj = sd.bin_begin + (jz * sd.nb[1] + jy) * sd.nb[0] + jx;
           const int jstart = a.bin_start[gbj], jend = a.bin_end[gbj];
           const float shx = (float)sx * sd.Lhi[0], shy = (float)sy * sd.Lhi[1], shz = (float)sz * sd.Lhi[2];
           const float slx = (float)sx * sd.Llo[0], sly = (float)sy * sd.Llo[1], slz = (float)sz * sd.Llo[2];
           const bool self_image = (sx | sy | sz) == 0;
-          for (int jt0 = jstart; jt0 < jend; jt0 += LT) {
-            const int nj = min(LT, jend - jt0);
-            __syncthreads();
-            if ((int)threadIdx.x < nj) {
-              jh[threadIdx.x] = a.xh[jt0 + threadIdx.x];
-              jl[threadIdx.x] = a.xl[jt0 + threadIdx.x];
+          for (int jt0 = jstart; jt0 < jend; jt0 += 32) {
+            const int nj = min(32, jend - jt0);
+            __syncwarp();
+            if (lane < nj) {
+              th[wl][lane] = a.xh[jt0 + lane];
+              tl[wl][lane] = a.xl[jt0 + lane];
             }
-            __syncthreads();
-            if (!act) continue;
+            __syncwarp();
+            if (!use) continue;
             for (int jj = 0; jj < nj; jj++) {
               const int j = jt0 + jj;
-              const float4 hj = jh[jj];
+              const float4 hj = th[wl][jj];
               const float hx = (hi.x - hj.x) - shx, hy = (hi.y - hj.y) - shy, hz = (hi.z - hj.z) - shz;
               if (hx * hx + hy * hy + hz * hz > prefilt) continue;   // most candidates
-              const float4 lj = jl[jj];
+              const float4 lj = tl[wl][jj];
               float ddx = hx + ((lo.x - lj.x) - slx);
               float ddy = hy + ((lo.y - lj.y) - sly);
               float ddz = hz + ((lo.z - lj.z) - slz);
@@ -208,14 +232,14 @@ __global__ void __launch_bounds__(LT) k_list(NbArgs a) {
         }
       }
     }
-    if (act) {
-      if (!FILL) {
-        a.cnt[i] = nlong;
-        a.short_cnt[i] = nshort < MAXSHORT ? nshort : MAXSHORT;
-        if (nshort > MAXSHORT) atomicOr(a.status, ST_SHORT_OVERFLOW);
-      } else if (base + nlong > a.list_cap) {
-        atomicOr(a.status, ST_LIST_OVERFLOW);
-      }
+  }
+  if (act) {
+    if (!FILL) {
+      a.cnt[i] = nlong;
+      a.short_cnt[i] = nshort < MAXSHORT ? nshort : MAXSHORT;
+      if (nshort > MAXSHORT) atomicOr(a.status, ST_SHORT_OVERFLOW);
+    } else if (base + nlong > a.list_cap) {
+      atomicOr(a.status, ST_LIST_OVERFLOW);
     }
   }
 }
@@ -271,9 +295,10 @@ void nb_hilo(int n, const d4 *xq, const SysDesc *sys, const int *sysid, float4 *
 }
 
 void nb_list(const NbArgs &a, bool fill, cudaStream_t s) {
-  if (!a.n || a.nbins <= 0) return;
-  if (fill) k_list<true><<<a.nbins, LT, 0, s>>>(a);
-  else k_list<false><<<a.nbins, LT, 0, s>>>(a);
+  if (!a.n) return;
+  const int g = (a.n + 32 * LW - 1) / (32 * LW);
+  if (fill) k_list<true><<<g, 32 * LW, 0, s>>>(a);
+  else k_list<false><<<g, 32 * LW, 0, s>>>(a);
 }
 
 void nb_copy_hold(int n, const d4 *xq, double *xhold, cudaStream_t s) {

@@ -24,7 +24,8 @@ struct NbArgs {
   const int *sysid;
   const int *bin_start;
   const int *bin_end;
-  int nbins;          // global bins (one list-build block each)
+  int nbins;          // global bins
+  const uint32_t *bin_key;   // global bin of each atom (sorted order)
   const int64_t *list_off;
   uint32_t *list;
   int64_t list_cap;

@@ -535,7 +535,7 @@ struct Engine {
 
   void release() {
     if (device >= 0) cudaSetDevice(device);
-    void *ptrs[] = {d.xq, d.xh, d.xl, d.v, d.f, d.xhold, d.tag, d.perm, d.sysid, d.mass, d.nrm64, d.nrm32, d.ilp_cnt,
+    void *ptrs[] = {d.xq, d.xh, d.xl, d.v, d.f, d.xhold, d.tag, d.perm, d.sysid, d.mass, d.nrm64, d.nrm32, d.jrec, d.ilp_cnt,
                     d.ilp_nb, d.ters_cnt, d.ters_nb, d.ters_g, d.ters_f, d.ilp_f, d.ilp_c, d.ilp_g, d.list_off, d.list,
                     d.short_cnt, d.short_nb, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.cub_tmp,
                     d.cnt_tmp, d.sys, d.red_out, d.status, d.maxdisp, d_xin, d_fin, d_vin, d_ein, d_tin, d_sysin,
@@ -874,7 +874,7 @@ struct Engine {
     CK(dalloc(d.xhold, 3 * (size_t)c));
     CK(dalloc(d.tag, c)); CK(dalloc(tag2, c)); CK(dalloc(d.perm, c)); CK(dalloc(perm2, c));
     CK(dalloc(d.sysid, c)); CK(dalloc(sysid2, c)); CK(dalloc(d.mass, c)); CK(dalloc(mass2, c));
-    CK(dalloc(d.nrm64, c)); CK(dalloc(d.nrm32, c));
+    CK(dalloc(d.nrm64, c)); CK(dalloc(d.nrm32, c)); CK(dalloc(d.jrec, 3 * (size_t)c));
     CK(dalloc(d.ilp_cnt, c)); CK(dalloc(d.ilp_nb, (size_t)c * MAXILP));
     CK(dalloc(d.ters_cnt, c)); CK(dalloc(d.ters_nb, (size_t)c * MAXTERS));
     CK(dalloc(d.ters_g, (size_t)c * MAXTERS)); CK(dalloc(d.ters_f, 3 * (size_t)c));
@@ -905,7 +905,7 @@ struct Engine {
   double per_atom_bytes() const {
     double per_atom = 2 * sizeof(*d.xq) + sizeof(*d.xh) + sizeof(*d.xl) + 3 * (3 * sizeof(double)) +
                       3 * sizeof(double) + 2 * sizeof(*d.tag) + 4 * sizeof(int) + 2 * sizeof(double) +
-                      sizeof(*d.nrm64) + sizeof(*d.nrm32) + sizeof(*d.ilp_cnt) + MAXILP * sizeof(*d.ilp_nb) +
+                      sizeof(*d.nrm64) + sizeof(*d.nrm32) + 3 * sizeof(*d.jrec) + sizeof(*d.ilp_cnt) + MAXILP * sizeof(*d.ilp_nb) +
                       sizeof(*d.ters_cnt) + MAXTERS * (sizeof(*d.ters_nb) + sizeof(*d.ters_g)) +
                       2 * 3 * sizeof(double) + MAXILP * sizeof(*d.ilp_c) + sizeof(*d.ilp_g) + 16 * sizeof(double) +
                       3 * sizeof(double) + sizeof(*d.list_off) + sizeof(*d.short_cnt) + MAXSHORT * sizeof(*d.short_nb) +
@@ -1158,6 +1158,7 @@ struct Engine {
     a.A.xq = d.xq;
     a.A.xh = d.xh;
     a.A.xl = d.xl;
+    a.A.jrec = d.jrec;
     a.A.sys = d.sys;
     a.A.sysid = d.sysid;
     a.lc = lc;
@@ -1173,6 +1174,7 @@ struct Engine {
     a.ters_nb = d.ters_nb;
     a.nrm64 = d.nrm64;
     a.nrm32 = d.nrm32;
+    a.jrec = d.jrec;
     a.ters_g = d.ters_g;
     a.ters_f = d.ters_f;
     a.ilp_f = d.ilp_f;
@@ -2228,6 +2230,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
   Carve cv{(unsigned char *)basev, (unsigned char *)basev + NOALLOC_BYTES};
   d4 *xq = cv.take<d4>(c), *xq2 = cv.take<d4>(c), *nrm64 = cv.take<d4>(c), *ilp_g = cv.take<d4>(c);
   float4 *xh = cv.take<float4>(c), *xl = cv.take<float4>(c), *nrm32 = cv.take<float4>(c);
+  float4 *jrec = cv.take<float4>(3 * (size_t)c);
   double *v = cv.take<double>(3 * c), *v2 = cv.take<double>(3 * c), *mass = cv.take<double>(c),
          *mass2 = cv.take<double>(c);
   int64_t *tag = cv.take<int64_t>(c), *tag2 = cv.take<int64_t>(c);
@@ -2302,6 +2305,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
     a.A.xq = xq2;
     a.A.xh = xh;
     a.A.xl = xl;
+    a.A.jrec = jrec;
     a.A.sys = dsys;
     a.A.sysid = sysid2;
     a.lc = lc;
@@ -2317,6 +2321,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
     a.ters_nb = ters_nb;
     a.nrm64 = nrm64;
     a.nrm32 = nrm32;
+    a.jrec = jrec;
     a.ters_g = ters_g;
     a.ters_f = ters_f;
     a.ilp_f = ilp_f;

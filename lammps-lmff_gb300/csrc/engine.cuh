@@ -137,6 +137,7 @@ struct DevState {
   // normals, per-step lists and gather slots
   d4 *nrm64 = nullptr;   // FP64 path normals
   float4 *nrm32 = nullptr;    // mixed path normals
+  float4 *jrec = nullptr;     // 3 per atom: mixed pair kernel's j data (hi+info, lo, normal)
   int *ilp_cnt = nullptr;
   uint32_t *ilp_nb = nullptr; // n * MAXILP
   int *ters_cnt = nullptr;

@@ -91,6 +91,9 @@ struct AtomArrays {
   const float4 *xl;
   const SysDesc *sys;
   const int *sysid;
+  // mixed pair kernel's j data, one 48-byte record per atom written by k_short each
+  // step: hi parts + info, lo parts, normal -- the three loads of a pair hit one line
+  const float4 *jrec;
 };
 
 template <class R>
@@ -161,7 +164,9 @@ struct AtomI<float> {
   struct J {
     float4 h, l;
   };
-  __device__ __forceinline__ J fetch(const AtomArrays &A, int j) const { return J{__ldg(&A.xh[j]), __ldg(&A.xl[j])}; }
+  __device__ __forceinline__ J fetch(const AtomArrays &A, int j) const {
+    return J{__ldg(&A.jrec[3 * (size_t)j]), __ldg(&A.jrec[3 * (size_t)j + 1])};
+  }
   __device__ __forceinline__ void disp_from(const J &t, const SysDesc &sd, int sx, int sy, int sz, float &dx, float &dy,
                                             float &dz, long long &jinfo) const {
     float sxh = (float)sx * sd.Lhi[0], syh = (float)sy * sd.Lhi[1], szh = (float)sz * sd.Lhi[2];
@@ -209,6 +214,7 @@ struct ForceArgs {
   uint32_t *ters_nb;
   d4 *nrm64;
   float4 *nrm32;
+  float4 *jrec;        // 3 per atom (mixed path): see AtomArrays::jrec
   d4 *ters_g;
   double *ters_f;
   double *ilp_f;

@@ -115,8 +115,14 @@ __global__ void k_short(ForceArgs<R> a, const double *cutILPsq64, double tcutmax
       nx = n1x / nn; ny = n1y / nn; nz = n1z / nn;
     }
   }
-  if constexpr (sizeof(R) == 8) a.nrm64[i] = make_d4(nx, ny, nz, 0.0);
-  else a.nrm32[i] = make_float4(nx, ny, nz, 0.f);
+#ifdef LMFF_PACKED_X2
+  a.nrm32[i] = make_float4(nx, ny, nz, 0.f);
+  a.jrec[3 * (size_t)i] = make_float4(ai.hx, ai.hy, ai.hz, __int_as_float((int)ai.info));
+  a.jrec[3 * (size_t)i + 1] = make_float4(ai.lx, ai.ly, ai.lz, 0.f);
+  a.jrec[3 * (size_t)i + 2] = make_float4(nx, ny, nz, 0.f);
+#else
+  a.nrm64[i] = make_d4(nx, ny, nz, 0.0);
+#endif
 }
 
 // ============================================================ Tersoff math ========
@@ -429,7 +435,9 @@ struct NrmJ;
 template <>
 struct NrmJ<float> {
   float4 q;
-  __device__ __forceinline__ static NrmJ load(const ForceArgs<float> &a, int j) { return NrmJ{__ldg(&a.nrm32[j])}; }
+  __device__ __forceinline__ static NrmJ load(const ForceArgs<float> &a, int j) {
+    return NrmJ{__ldg(&a.A.jrec[3 * (size_t)j + 2])};
+  }
 };
 template <>
 struct NrmJ<double> {

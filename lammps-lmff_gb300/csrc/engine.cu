@@ -736,6 +736,9 @@ struct Engine {
             o.rhi64 = q.bigr + q.bigd;
             o.pi4D64 = 0.78539816339744830962 / q.bigd;
             o.cutsq64 = q.cutsq;
+            o.nl1x32 = -32.0 * q.lam1;
+            o.nl2x32 = -32.0 * q.lam2;
+            o.h64 = q.h;
             o.powermint = q.powermint;
           }
       for (int a = 0; a < ne; a++)

@@ -61,6 +61,8 @@ struct TersP {
   // FP64 copies of the radial constants: the bond's repulsion and attraction are
   // evaluated in FP64 in both precision modes
   double A64, B64, lam1_64, lam2_64, R64, D64, rlo64, rhi64, pi4D64, cutsq64;
+  double nl1x32, nl2x32;       // -32 lam1, -32 lam2 (argument scale of the table exp)
+  double h64;                 // h (FP32 mode: u = h - cos(theta) in FP64)
   int powermint;
   int pad;
 };

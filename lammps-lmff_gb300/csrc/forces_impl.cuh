@@ -161,6 +161,18 @@ __device__ __forceinline__ R ters_gijk_d(R costheta, const TersP<R> &p) {
   return p.gamma * numerator * den * den;
 }
 
+// g(theta) and dg/dcos(theta) from u = h - cos(theta) (FP32 mode: u comes from an FP64
+// cosine, since h - cos(theta) cancels to ~0.07 for carbon)
+__device__ __forceinline__ R ters_g_u(R u, const TersP<R> &p) {
+  R u2 = u * u;
+  return p.gamma * (R(1) + p.c2 * u2 / (p.d2 * (p.d2 + u2)));
+}
+
+__device__ __forceinline__ R ters_gd_u(R u, const TersP<R> &p) {
+  R den = R(1) / (p.d2 + u * u);
+  return p.gamma * (R(-2) * p.c2 * u) * den * den;
+}
+
 __device__ __forceinline__ R ters_exdelr(R rij, R rik, const TersP<R> &p) {
   R arg = p.powermint == 3 ? (p.lam3 * (rij - rik)) * (p.lam3 * (rij - rik)) * (p.lam3 * (rij - rik))
                            : p.lam3 * (rij - rik);
@@ -207,10 +219,11 @@ __device__ __forceinline__ bool keep_half(long long itag, long long jtag, int sx
 // end (:132-175).  Forces on bond partners go to ters_g slots (gathered in k_finish).
 //
 // Precision: the radial bond terms (repulsion A e^{-lam1 r} and the attraction
-// b_ij f_A(r), which nearly cancel at the equilibrium bond length) are evaluated in
-// FP64 in both modes, from FP64 displacements; b_ij enters as 1 + delta with delta
-// computed as expm1(-log1p((beta zeta)^n)/(2n)), which keeps its full relative accuracy
-// in FP32.  zeta, g(theta) and the three-body derivatives are evaluated in R.
+// b_ij f_A(r), which nearly cancel at the equilibrium bond length) keep FP64 accuracy in
+// both modes, from FP64 displacements (in FP32 mode through exp_x32 and rsqrt_nr below,
+// ~1e-9 relative); b_ij enters as 1 + delta with delta computed as
+// expm1(-log1p((beta zeta)^n)/(2n)), which keeps its full relative accuracy in FP32.
+// zeta, g(theta) and the three-body derivatives are evaluated in R.
 __device__ __forceinline__ void ters_fc_both64(double r, const TersP<R> &p, double &fc, double &fcd) {
   if (r < p.rlo64) { fc = 1.0; fcd = 0.0; return; }
   if (r > p.rhi64) { fc = 0.0; fcd = 0.0; return; }
@@ -253,56 +266,131 @@ __device__ __forceinline__ void ters_bij_delta(R zeta, const TersP<R> &p, double
   bd = R(-0.5) * Math<R>::pow_(R(1) + tmp_n, R(-1) - p.inv2n) * tmp_n / zeta;
 }
 
-template <bool EV, bool EATOM>
-__global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+// ---- FP32-mode radial helpers: the bond terms keep FP64 accuracy with a fraction of the
+// FP64 instructions of sqrt, division and exp (the FP64 pipe runs at 1/64 of the FP32
+// rate on this GPU).
+//
+// e^x by Tang's table-driven method (P. T. P. Tang, "Table-driven implementation of the
+// exponential function in IEEE floating-point arithmetic", ACM TOMS 15, 1989): with
+// t = 32 x = k + f, k = rint(t), |f| <= 1/2, e^x = e^{k/32} e^{f/32}.  e^{k/32} comes
+// from a table of FP64 values; e^{f/32} - 1 (|f/32| <= 1/64) from its Taylor series to
+// 4th order in FP32 (truncation < 1e-11, rounding ~3e-9 of the result).
+constexpr int EXP_TAB_N = 1024;   // e^{-m/32}, m = 0..1023: arguments down to -31.97
+__device__ double g_exptab[EXP_TAB_N];
+
+__global__ void k_fill_exptab() {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < EXP_TAB_N) g_exptab[m] = exp(-(double)m / 32.0);
+}
+
+// e^{t/32}; outside the table's range the FP64 library exp
+__device__ __forceinline__ double exp_x32(double t) {
+  const double magic = 6755399441055744.0;   // 1.5 * 2^52: adding it rounds to an integer
+  const double tm = __dadd_rn(t, magic);
+  const int k = __double2loint(tm);           // the integer, two's complement, low word
+  const double kd = __dsub_rn(tm, magic);
+  const int m = -k;
+  if (m < 0 || m >= EXP_TAB_N) return exp(t * 0.03125);
+  const float f = (float)__dsub_rn(t, kd) * 0.03125f;
+  const float q = f * (1.f + f * (0.5f + f * (1.f / 6.f + f * (1.f / 24.f))));
+  const double T = __ldg(&g_exptab[m]);
+  return fma(T, (double)q, T);
+}
+
+// 1/sqrt(x) for x in the FP32 normal range: FP32 estimate and one FP64 Newton step
+// (relative error ~1e-13)
+__device__ __forceinline__ double rsqrt_nr(double x) {
+  const double y = (double)rsqrt_ftz((float)x);
+  const double e = fma(-(x * y), y, 1.0);
+  return fma(0.5 * y, e, y);
+}
+
+// One centre atom's bonds.  NB is the number of bond slots held in registers (loops
+// fully unrolled when NB is small; cnt <= NB).
+template <int NB, bool EV>
+__device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int ie, int cnt) {
+  constexpr bool F32 = sizeof(R) == 4;
+  constexpr int UNR = NB <= 4 ? NB : 1;
   const SysDesc &sd = a.A.sys[a.A.sysid[i]];
-  const long long iinfo = __double_as_longlong(a.A.xq[i].w);
-  int ie = c_pot.t_map[info_type(iinfo)];
-  int cnt = a.ters_cnt[i];
-  if (ie < 0) cnt = 0;
-  double dxd[MAXTERS], dyd[MAXTERS], dzd[MAXTERS], r64[MAXTERS], rs64[MAXTERS];
-  R dx[MAXTERS], dy[MAXTERS], dz[MAXTERS], rr[MAXTERS];
-  int el[MAXTERS];
-  double gx[MAXTERS], gy[MAXTERS], gz[MAXTERS], ge[MAXTERS];
-  int sxv[MAXTERS], syv[MAXTERS], szv[MAXTERS], jv[MAXTERS];
+  double dxd[NB], dyd[NB], dzd[NB], r64[NB], ri64[NB], rs64[NB];
+  R dx[NB], dy[NB], dz[NB];
+  int el[NB], jv[NB];
+  uint32_t ev_[NB];
+  // radial force on each partner (gx), three-body forces on each partner (tx), bond energy
+  double gx[NB], gy[NB], gz[NB], ge[NB], tx[NB], ty[NB], tz[NB];
+  double cs64[NB][NB];   // FP32 mode: cos(theta_jik) of each bond pair in FP64
   double fx = 0, fy = 0, fz = 0, eng = 0;
   double v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
-  for (int s = 0; s < cnt; s++) {
-    uint32_t e = a.ters_nb[(size_t)i * MAXTERS + s];
-    int j, sx, sy, sz;
-    decode_entry(e, a.lc, j, sx, sy, sz);
-    double ddx, ddy, ddz;
-    disp64(a.A.xq, sd, i, j, sx, sy, sz, ddx, ddy, ddz);
-    dxd[s] = -ddx; dyd[s] = -ddy; dzd[s] = -ddz;  // delr = x_j - x_i
-    double rs = rsq_rn(ddx, ddy, ddz);
-    rs64[s] = rs;
-    r64[s] = sqrt(rs);
-    dx[s] = (R)dxd[s]; dy[s] = (R)dyd[s]; dz[s] = (R)dzd[s];
-    rr[s] = (R)rs;
-    el[s] = c_pot.t_map[info_type(__double_as_longlong(a.A.xq[j].w))];
-    jv[s] = j; sxv[s] = sx; syv[s] = sy; szv[s] = sz;
-    gx[s] = gy[s] = gz[s] = ge[s] = 0.0;
+#pragma unroll UNR
+  for (int s = 0; s < NB; s++) {
+    if (s < cnt) {
+      const uint32_t e = a.ters_nb[(size_t)i * MAXTERS + s];
+      int j, sx, sy, sz;
+      decode_entry(e, a.lc, j, sx, sy, sz);
+      double ddx, ddy, ddz;
+      disp64(a.A.xq, sd, i, j, sx, sy, sz, ddx, ddy, ddz);
+      dxd[s] = -ddx; dyd[s] = -ddy; dzd[s] = -ddz;  // delr = x_j - x_i
+      const double rs = rsq_rn(ddx, ddy, ddz);
+      rs64[s] = rs;
+      if constexpr (F32) {
+        const double ri = rsqrt_nr(rs);
+        ri64[s] = ri;
+        r64[s] = rs * ri;
+      } else {
+        r64[s] = sqrt(rs);
+        ri64[s] = 0.0;
+      }
+      dx[s] = (R)dxd[s]; dy[s] = (R)dyd[s]; dz[s] = (R)dzd[s];
+      el[s] = c_pot.t_map[info_type(__double_as_longlong(a.A.xq[j].w))];
+      jv[s] = j;
+      ev_[s] = e;
+      gx[s] = gy[s] = gz[s] = ge[s] = 0.0;
+      tx[s] = ty[s] = tz[s] = 0.0;
+    }
   }
-  long long itag = c_pot.rep_sym ? 0 : a.tag[i];
-  for (int s = 0; s < cnt; s++) {
-    int je = el[s];
+  if constexpr (F32) {
+#pragma unroll UNR
+    for (int s = 0; s < NB; s++) {
+#pragma unroll UNR
+      for (int k = s + 1; k < NB; k++) {
+        if (k < cnt) {
+          const double c = (dxd[s] * dxd[k] + dyd[s] * dyd[k] + dzd[s] * dzd[k]) * (ri64[s] * ri64[k]);
+          cs64[s][k] = c;
+          cs64[k][s] = c;
+        }
+      }
+    }
+  }
+  const long long itag = c_pot.rep_sym ? 0 : a.tag[i];
+#pragma unroll UNR
+  for (int s = 0; s < NB; s++) {
+    if (s >= cnt) continue;
+    const int je = el[s];
     const TersP<R> &pij = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + je];
     const double r = r64[s];
     const R rR = (R)r;
+    double fr = 0.0;   // radial force on i along delr, from both terms of this bond
     // ---- repulsion (:584-595) in FP64, from both ends of the bond, with the parameters
     // of the end the reference's half list keeps
     {
       const TersP<R> *pr = &pij;
-      if (!c_pot.rep_sym && !keep_half(itag, a.tag[jv[s]], sxv[s], syv[s], szv[s]))
-        pr = &c_pot.ters[(je * MAXELEM + ie) * MAXELEM + ie];
+      if (!c_pot.rep_sym) {
+        int j, sx, sy, sz;
+        decode_entry(ev_[s], a.lc, j, sx, sy, sz);
+        if (!keep_half(itag, a.tag[j], sx, sy, sz)) pr = &c_pot.ters[(je * MAXELEM + ie) * MAXELEM + ie];
+      }
       if (rs64[s] < pr->cutsq64) {
         double fc, fcd;
         ters_fc_both64(r, *pr, fc, fcd);
-        double tmp_exp = exp(-pr->lam1_64 * r);
-        double fpair = -pr->A64 * tmp_exp * (fcd - fc * pr->lam1_64) / r;
-        fx -= dxd[s] * fpair; fy -= dyd[s] * fpair; fz -= dzd[s] * fpair;
+        double tmp_exp, fpair;
+        if constexpr (F32) {
+          tmp_exp = exp_x32(r * pr->nl1x32);
+          fpair = -pr->A64 * tmp_exp * (fcd - fc * pr->lam1_64) * ri64[s];
+        } else {
+          tmp_exp = exp(-pr->lam1_64 * r);
+          fpair = -pr->A64 * tmp_exp * (fcd - fc * pr->lam1_64) / r;
+        }
+        fr -= fpair;
         if (EV) {
           eng += 0.5 * fc * pr->A64 * tmp_exp;
           double h = 0.5 * fpair;
@@ -311,17 +399,27 @@ __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
         }
       }
     }
-    if (!(rs64[s] < pij.cutsq64)) continue;
+    if (!(rs64[s] < pij.cutsq64)) {
+      fx += dxd[s] * fr; fy += dyd[s] * fr; fz += dzd[s] * fr;
+      continue;
+    }
     // ---- zeta_ij over k (:197-210), in R
     R zeta = 0;
-    for (int k = 0; k < cnt; k++) {
-      if (k == s) continue;
+#pragma unroll UNR
+    for (int k = 0; k < NB; k++) {
+      if (k == s || k >= cnt) continue;
       const TersP<R> &pk = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + el[k]];
       if (!(rs64[k] < pk.cutsq64)) continue;
       R rik = (R)r64[k];
-      R cost = (dx[s] * dx[k] + dy[s] * dy[k] + dz[s] * dz[k]) / (rR * rik);
       R ex = pk.lam3 == R(0) ? R(1) : ters_exdelr(rR, rik, pk);
-      zeta += ters_fc(rik, pk) * ters_gijk(cost, pk) * ex;
+      R g;
+      if constexpr (F32) {
+        g = ters_g_u((R)(pk.h64 - cs64[s][k]), pk);
+      } else {
+        R cost = (dx[s] * dx[k] + dy[s] * dy[k] + dz[s] * dz[k]) / (rR * rik);
+        g = ters_gijk(cost, pk);
+      }
+      zeta += ters_fc(rik, pk) * g * ex;
     }
     // ---- force_zeta (:621-634): radial part in FP64
     double fa = 0.0, fa_d = 0.0;
@@ -329,7 +427,7 @@ __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
       double fc, fcd;
       ters_fc_both64(r, pij, fc, fcd);
       if (!(r > pij.rhi64)) {
-        double ex2 = exp(-pij.lam2_64 * r);
+        const double ex2 = F32 ? exp_x32(r * pij.nl2x32) : exp(-pij.lam2_64 * r);
         fa = -pij.B64 * ex2 * fc;
         fa_d = pij.B64 * ex2 * (pij.lam2_64 * fc - fcd);
       }
@@ -338,10 +436,12 @@ __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
     R bd;
     ters_bij_delta(zeta, pij, bm1, bd);
     const double bij = 1.0 + bm1;
-    const double fpair = 0.5 * bij * fa_d / r;
+    const double fpair = F32 ? 0.5 * bij * fa_d * ri64[s] : 0.5 * bij * fa_d / r;
     const R prefactor = (R)(-0.5 * fa) * bd;
-    fx += dxd[s] * fpair; fy += dyd[s] * fpair; fz += dzd[s] * fpair;
-    double fjx = -dxd[s] * fpair, fjy = -dyd[s] * fpair, fjz = -dzd[s] * fpair;
+    fr += fpair;
+    fx += dxd[s] * fr; fy += dyd[s] * fr; fz += dzd[s] * fr;
+    const double fjx = -dxd[s] * fpair, fjy = -dyd[s] * fpair, fjz = -dzd[s] * fpair;
+    gx[s] += fjx; gy[s] += fjy; gz[s] += fjz;
     if (EV) {
       double eb = 0.5 * bij * fa;
       eng += eb;
@@ -349,13 +449,16 @@ __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
       v0 += dxd[s] * fjx; v1 += dyd[s] * fjy; v2 += dzd[s] * fjz;
       v3 += dxd[s] * fjy; v4 += dxd[s] * fjz; v5 += dyd[s] * fjz;
     }
-    // ---- attractive over k (:228-254) -> ters_zetaterm_d (:738-793), in R
+    // ---- attractive over k (:228-254) -> ters_zetaterm_d (:738-793), in R.  The force
+    // on i is minus the forces on j and k (:766-774); it is taken from the partners'
+    // three-body totals after the loop.
     if (prefactor != R(0)) {
       R rinv = R(1) / rR;
       R rhx = dx[s] * rinv, rhy = dy[s] * rinv, rhz = dz[s] * rinv;
       R ajx = 0, ajy = 0, ajz = 0;
-      for (int k = 0; k < cnt; k++) {
-        if (k == s) continue;
+#pragma unroll UNR
+      for (int k = 0; k < NB; k++) {
+        if (k == s || k >= cnt) continue;
         const TersP<R> &pk = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + el[k]];
         if (!(rs64[k] < pk.cutsq64)) continue;
         R rik = (R)r64[k];
@@ -373,35 +476,45 @@ __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
                                     : pk.lam3 * exd;
         }
         R cs = rhx * khx + rhy * khy + rhz * khz;
-        R g = ters_gijk(cs, pk), gd = ters_gijk_d(cs, pk);
+        R g, gd;
+        if constexpr (F32) {
+          const R u = (R)(pk.h64 - cs64[s][k]);
+          g = ters_g_u(u, pk);
+          gd = ters_gd_u(u, pk);
+        } else {
+          g = ters_gijk(cs, pk);
+          gd = ters_gijk_d(cs, pk);
+        }
         // costheta_d (:797-811)
         R djx = (-cs * rhx + khx) * rinv, djy = (-cs * rhy + khy) * rinv, djz = (-cs * rhz + khz) * rinv;
         R dkx = (-cs * khx + rhx) * rikinv, dky = (-cs * khy + rhy) * rikinv, dkz = (-cs * khz + rhz) * rikinv;
         R A1 = fck * gd * exd, A2 = fck * g * exd_d, A3 = dfck * g * exd;
-        R fjx_ = prefactor * (A1 * djx + A2 * rhx);
-        R fjy_ = prefactor * (A1 * djy + A2 * rhy);
-        R fjz_ = prefactor * (A1 * djz + A2 * rhz);
         R fkx_ = prefactor * (A3 * khx + A1 * dkx - A2 * khx);
         R fky_ = prefactor * (A3 * khy + A1 * dky - A2 * khy);
         R fkz_ = prefactor * (A3 * khz + A1 * dkz - A2 * khz);
-        // fi = -(fj + fk) (:766-774)
-        fx -= (double)(fjx_ + fkx_); fy -= (double)(fjy_ + fky_); fz -= (double)(fjz_ + fkz_);
-        ajx += fjx_; ajy += fjy_; ajz += fjz_;
-        gx[k] += (double)fkx_; gy[k] += (double)fky_; gz[k] += (double)fkz_;
+        ajx += prefactor * (A1 * djx + A2 * rhx);
+        ajy += prefactor * (A1 * djy + A2 * rhy);
+        ajz += prefactor * (A1 * djz + A2 * rhz);
+        tx[k] += (double)fkx_; ty[k] += (double)fky_; tz[k] += (double)fkz_;
         if (EV) {
           v0 += (double)(dx[k] * fkx_); v1 += (double)(dy[k] * fky_); v2 += (double)(dz[k] * fkz_);
           v3 += (double)(dx[k] * fky_); v4 += (double)(dx[k] * fkz_); v5 += (double)(dy[k] * fkz_);
         }
       }
-      fjx += (double)ajx; fjy += (double)ajy; fjz += (double)ajz;
+      tx[s] += (double)ajx; ty[s] += (double)ajy; tz[s] += (double)ajz;
       if (EV) {
         v0 += (double)(dx[s] * ajx); v1 += (double)(dy[s] * ajy); v2 += (double)(dz[s] * ajz);
         v3 += (double)(dx[s] * ajy); v4 += (double)(dx[s] * ajz); v5 += (double)(dy[s] * ajz);
       }
     }
-    gx[s] += fjx; gy[s] += fjy; gz[s] += fjz;
   }
-  for (int s = 0; s < cnt; s++) a.ters_g[(size_t)i * MAXTERS + s] = make_d4(gx[s], gy[s], gz[s], ge[s]);
+#pragma unroll UNR
+  for (int s = 0; s < NB; s++) {
+    if (s < cnt) {
+      fx -= tx[s]; fy -= ty[s]; fz -= tz[s];
+      a.ters_g[(size_t)i * MAXTERS + s] = make_d4(gx[s] + tx[s], gy[s] + ty[s], gz[s] + tz[s], ge[s]);
+    }
+  }
   a.ters_f[i] = fx;
   a.ters_f[a.n + i] = fy;
   a.ters_f[2 * a.n + i] = fz;
@@ -412,6 +525,18 @@ __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
     st[(size_t)2 * a.n + i] = v0; st[(size_t)3 * a.n + i] = v1; st[(size_t)4 * a.n + i] = v2;
     st[(size_t)5 * a.n + i] = v3; st[(size_t)6 * a.n + i] = v4; st[(size_t)7 * a.n + i] = v5;
   }
+}
+
+// sp2 layers give 3 bonds per atom: those atoms run with their bonds in registers
+template <bool EV, bool EATOM>
+__global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const long long iinfo = __double_as_longlong(a.A.xq[i].w);
+  const int ie = c_pot.t_map[info_type(iinfo)];
+  const int cnt = ie < 0 ? 0 : a.ters_cnt[i];
+  if (cnt <= 3) tersoff_atom<3, EV>(a, i, ie, cnt);
+  else tersoff_atom<MAXTERS, EV>(a, i, ie, cnt);
 }
 
 // ============================================================== k_ilp ============
@@ -561,10 +686,6 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
   }
 }
 
-// FP32: at least 5 blocks of 256 threads per SM (48 registers) -- the kernel is
-// issue-bound with long-scoreboard stalls on j's data, and 40 resident warps hide them
-// better than 36 (measured: -8 % at 2.7M atoms, -16 % at 490k).  FP64 keeps its
-// registers.
 #ifdef LMFF_PACKED_X2
 // ---- packed FP32x2 form of the same pair body (sm_100+ FFMA2/FADD2/FMUL2)
 // The kernel is issue-bound in FP32, and the pair body is full of independent twin
@@ -700,6 +821,10 @@ __device__ __forceinline__ void pair_body(const ForceArgs<R> &a, const AtomI<R> 
 #endif
 }
 
+// FP32: at least 5 blocks of 256 threads per SM (48 registers) -- the kernel is
+// issue-bound with long-scoreboard stalls on j's data, and 40 resident warps hide them
+// better than 36 (measured: -8 % at 2.7M atoms, -16 % at 490k).  FP64 keeps its
+// registers.
 template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R> a) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -982,6 +1107,7 @@ __global__ void k_ters_eatom_own(ForceArgs<R> a) {
 
 void upload_pot(const PotConst<R> &p, cudaStream_t s) {
   cudaMemcpyToSymbolAsync(c_pot, &p, sizeof(p), 0, cudaMemcpyHostToDevice, s);
+  if (sizeof(R) == 4) k_fill_exptab<<<EXP_TAB_N / 256, 256, 0, s>>>();
 }
 
 void launch_short(const ForceArgs<R> &a, const double *cutILPsq64, double tcutmaxsq64, cudaStream_t s) {

@@ -739,6 +739,12 @@ struct Engine {
             o.nl1x32 = -32.0 * q.lam1;
             o.nl2x32 = -32.0 * q.lam2;
             o.h64 = q.h;
+            o.Al1_64 = q.biga * q.lam1;
+            o.Bl2_64 = q.bigb * q.lam2;
+            o.nl1h = (float)o.nl1x32;
+            o.nl1l = (float)(o.nl1x32 - (double)o.nl1h);
+            o.nl2h = (float)o.nl2x32;
+            o.nl2l = (float)(o.nl2x32 - (double)o.nl2h);
             o.powermint = q.powermint;
           }
       for (int a = 0; a < ne; a++)

@@ -188,9 +188,14 @@ __device__ __forceinline__ void disp64(const d4 *xq, const SysDesc &sd, int i, i
                                        double &dx, double &dy, double &dz) {
   d4 a = xq[i];
   d4 b = xq[j];
-  double xj = sx ? __dadd_rn(b.x, sx * sd.L[0]) : b.x;
-  double yj = sy ? __dadd_rn(b.y, sy * sd.L[1]) : b.y;
-  double zj = sz ? __dadd_rn(b.z, sz * sd.L[2]) : b.z;
+  double xj = b.x, yj = b.y, zj = b.z;
+  // one branch for the (rare) periodic image: b + 0 * L = b, so a zero component of a
+  // non-zero shift gives the same value as no shift
+  if ((sx | sy | sz) != 0) {
+    xj = __dadd_rn(b.x, sx * sd.L[0]);
+    yj = __dadd_rn(b.y, sy * sd.L[1]);
+    zj = __dadd_rn(b.z, sz * sd.L[2]);
+  }
   dx = __dsub_rn(a.x, xj);
   dy = __dsub_rn(a.y, yj);
   dz = __dsub_rn(a.z, zj);

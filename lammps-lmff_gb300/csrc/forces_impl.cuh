@@ -283,16 +283,18 @@ __global__ void k_fill_exptab() {
   if (m < EXP_TAB_N) g_exptab[m] = exp(-(double)m / 32.0);
 }
 
-// e^{t/32}; outside the table's range the FP64 library exp
-__device__ __forceinline__ double exp_x32(double t) {
-  const double magic = 6755399441055744.0;   // 1.5 * 2^52: adding it rounds to an integer
-  const double tm = __dadd_rn(t, magic);
-  const int k = __double2loint(tm);           // the integer, two's complement, low word
-  const double kd = __dsub_rn(tm, magic);
-  const int m = -k;
-  if (m < 0 || m >= EXP_TAB_N) return exp(t * 0.03125);
-  const float f = (float)__dsub_rn(t, kd) * 0.03125f;
-  const float q = f * (1.f + f * (0.5f + f * (1.f / 6.f + f * (1.f / 24.f))));
+// e^{t/32} with t = r c given as FP32 pairs r = rh + rl, c = ch + cl (|rl| <= ulp(rh)/2,
+// |cl| <= ulp(ch)/2): the product's rounding error is recovered exactly with an FMA
+// (Dekker's error-free product), so f = t - k is accurate to ~3e-8 without FP64 work.
+__device__ __forceinline__ double exp_x32f(float rh, float rl, float ch, float cl) {
+  const float th = __fmul_rn(rh, ch);
+  const float te = __fmaf_rn(rh, ch, -th);
+  const float k = rintf(th);
+  const float f = __fadd_rn(__fsub_rn(th, k), te + __fmaf_rn(rh, cl, rl * ch));
+  const int m = -(int)k;
+  if (m < 0 || m >= EXP_TAB_N) return exp(((double)rh + (double)rl) * ((double)ch + (double)cl) * 0.03125);
+  const float x = f * 0.03125f;
+  const float q = x * (1.f + x * (0.5f + x * (1.f / 6.f + x * (1.f / 24.f))));
   const double T = __ldg(&g_exptab[m]);
   return fma(T, (double)q, T);
 }
@@ -307,18 +309,26 @@ __device__ __forceinline__ double rsqrt_nr(double x) {
 
 // One centre atom's bonds.  NB is the number of bond slots held in registers (loops
 // fully unrolled when NB is small; cnt <= NB).
+//
+// FP32 mode keeps the FP64 pipe (1/64 of the FP32 rate) for what needs it: positions,
+// bond lengths, the radial terms' final products and the force sums.  Cut-off tests run
+// on FP32 bond lengths (every term vanishes continuously at its cut-off), h - cos(theta)
+// is formed in FP64 once per bond pair, and the three-body forces on each partner are
+// summed in FP32 before one FP64 addition.
 template <int NB, bool EV>
 __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int ie, int cnt) {
   constexpr bool F32 = sizeof(R) == 4;
   constexpr int UNR = NB <= 4 ? NB : 1;
   const SysDesc &sd = a.A.sys[a.A.sysid[i]];
   double dxd[NB], dyd[NB], dzd[NB], r64[NB], ri64[NB], rs64[NB];
-  R dx[NB], dy[NB], dz[NB];
-  int el[NB], jv[NB];
+  R dx[NB], dy[NB], dz[NB], rf[NB], rl[NB];
+  int el[NB];
   uint32_t ev_[NB];
   // radial force on each partner (gx), three-body forces on each partner (tx), bond energy
-  double gx[NB], gy[NB], gz[NB], ge[NB], tx[NB], ty[NB], tz[NB];
+  double gx[NB], gy[NB], gz[NB], ge[NB];
+  R tx[NB], ty[NB], tz[NB];
   double cs64[NB][NB];   // FP32 mode: cos(theta_jik) of each bond pair in FP64
+  R uf[NB][NB];          // FP32 mode: h_ijk - cos(theta_jik)
   double fx = 0, fy = 0, fz = 0, eng = 0;
   double v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
 #pragma unroll UNR
@@ -334,18 +344,22 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
       rs64[s] = rs;
       if constexpr (F32) {
         const double ri = rsqrt_nr(rs);
+        const double r = rs * ri;
         ri64[s] = ri;
-        r64[s] = rs * ri;
+        r64[s] = r;
+        rf[s] = (R)r;
+        rl[s] = (R)(r - (double)rf[s]);
       } else {
         r64[s] = sqrt(rs);
         ri64[s] = 0.0;
+        rf[s] = r64[s];
+        rl[s] = 0.0;
       }
       dx[s] = (R)dxd[s]; dy[s] = (R)dyd[s]; dz[s] = (R)dzd[s];
       el[s] = c_pot.t_map[info_type(__double_as_longlong(a.A.xq[j].w))];
-      jv[s] = j;
       ev_[s] = e;
       gx[s] = gy[s] = gz[s] = ge[s] = 0.0;
-      tx[s] = ty[s] = tz[s] = 0.0;
+      tx[s] = ty[s] = tz[s] = R(0);
     }
   }
   if constexpr (F32) {
@@ -368,7 +382,7 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
     const int je = el[s];
     const TersP<R> &pij = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + je];
     const double r = r64[s];
-    const R rR = (R)r;
+    const R rR = rf[s];
     double fr = 0.0;   // radial force on i along delr, from both terms of this bond
     // ---- repulsion (:584-595) in FP64, from both ends of the bond, with the parameters
     // of the end the reference's half list keeps
@@ -379,14 +393,21 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
         decode_entry(ev_[s], a.lc, j, sx, sy, sz);
         if (!keep_half(itag, a.tag[j], sx, sy, sz)) pr = &c_pot.ters[(je * MAXELEM + ie) * MAXELEM + ie];
       }
-      if (rs64[s] < pr->cutsq64) {
-        double fc, fcd;
-        ters_fc_both64(r, *pr, fc, fcd);
-        double tmp_exp, fpair;
+      if (F32 ? rR < pr->rhi : rs64[s] < pr->cutsq64) {
+        double tmp_exp, fpair, fc;
         if constexpr (F32) {
-          tmp_exp = exp_x32(r * pr->nl1x32);
-          fpair = -pr->A64 * tmp_exp * (fcd - fc * pr->lam1_64) * ri64[s];
+          tmp_exp = exp_x32f(rR, rl[s], pr->nl1h, pr->nl1l);
+          if (rR < pr->rlo) {   // fc = 1, fc' = 0
+            fc = 1.0;
+            fpair = pr->Al1_64 * tmp_exp * ri64[s];
+          } else {
+            double fcd;
+            ters_fc_both64(r, *pr, fc, fcd);
+            fpair = -pr->A64 * tmp_exp * (fcd - fc * pr->lam1_64) * ri64[s];
+          }
         } else {
+          double fcd;
+          ters_fc_both64(r, *pr, fc, fcd);
           tmp_exp = exp(-pr->lam1_64 * r);
           fpair = -pr->A64 * tmp_exp * (fcd - fc * pr->lam1_64) / r;
         }
@@ -399,7 +420,7 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
         }
       }
     }
-    if (!(rs64[s] < pij.cutsq64)) {
+    if (!(F32 ? rR < pij.rhi : rs64[s] < pij.cutsq64)) {
       fx += dxd[s] * fr; fy += dyd[s] * fr; fz += dzd[s] * fr;
       continue;
     }
@@ -409,12 +430,13 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
     for (int k = 0; k < NB; k++) {
       if (k == s || k >= cnt) continue;
       const TersP<R> &pk = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + el[k]];
-      if (!(rs64[k] < pk.cutsq64)) continue;
-      R rik = (R)r64[k];
+      const R rik = rf[k];
+      if (!(F32 ? rik < pk.rhi : rs64[k] < pk.cutsq64)) continue;
       R ex = pk.lam3 == R(0) ? R(1) : ters_exdelr(rR, rik, pk);
       R g;
       if constexpr (F32) {
-        g = ters_g_u((R)(pk.h64 - cs64[s][k]), pk);
+        uf[s][k] = (R)(pk.h64 - cs64[s][k]);
+        g = ters_g_u(uf[s][k], pk);
       } else {
         R cost = (dx[s] * dx[k] + dy[s] * dy[k] + dz[s] * dz[k]) / (rR * rik);
         g = ters_gijk(cost, pk);
@@ -423,11 +445,22 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
     }
     // ---- force_zeta (:621-634): radial part in FP64
     double fa = 0.0, fa_d = 0.0;
-    {
+    if constexpr (F32) {
+      const double ex2 = exp_x32f(rR, rl[s], pij.nl2h, pij.nl2l);
+      if (rR < pij.rlo) {   // fc = 1, fc' = 0
+        fa = -pij.B64 * ex2;
+        fa_d = pij.Bl2_64 * ex2;
+      } else {
+        double fc, fcd;
+        ters_fc_both64(r, pij, fc, fcd);
+        fa = -pij.B64 * ex2 * fc;
+        fa_d = pij.B64 * ex2 * (pij.lam2_64 * fc - fcd);
+      }
+    } else {
       double fc, fcd;
       ters_fc_both64(r, pij, fc, fcd);
       if (!(r > pij.rhi64)) {
-        const double ex2 = F32 ? exp_x32(r * pij.nl2x32) : exp(-pij.lam2_64 * r);
+        double ex2 = exp(-pij.lam2_64 * r);
         fa = -pij.B64 * ex2 * fc;
         fa_d = pij.B64 * ex2 * (pij.lam2_64 * fc - fcd);
       }
@@ -460,8 +493,8 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
       for (int k = 0; k < NB; k++) {
         if (k == s || k >= cnt) continue;
         const TersP<R> &pk = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + el[k]];
-        if (!(rs64[k] < pk.cutsq64)) continue;
-        R rik = (R)r64[k];
+        const R rik = rf[k];
+        if (!(F32 ? rik < pk.rhi : rs64[k] < pk.cutsq64)) continue;
         R rikinv = R(1) / rik;
         R khx = dx[k] * rikinv, khy = dy[k] * rikinv, khz = dz[k] * rikinv;
         R fck, dfck;
@@ -478,9 +511,8 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
         R cs = rhx * khx + rhy * khy + rhz * khz;
         R g, gd;
         if constexpr (F32) {
-          const R u = (R)(pk.h64 - cs64[s][k]);
-          g = ters_g_u(u, pk);
-          gd = ters_gd_u(u, pk);
+          g = ters_g_u(uf[s][k], pk);
+          gd = ters_gd_u(uf[s][k], pk);
         } else {
           g = ters_gijk(cs, pk);
           gd = ters_gijk_d(cs, pk);
@@ -495,13 +527,13 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
         ajx += prefactor * (A1 * djx + A2 * rhx);
         ajy += prefactor * (A1 * djy + A2 * rhy);
         ajz += prefactor * (A1 * djz + A2 * rhz);
-        tx[k] += (double)fkx_; ty[k] += (double)fky_; tz[k] += (double)fkz_;
+        tx[k] += fkx_; ty[k] += fky_; tz[k] += fkz_;
         if (EV) {
           v0 += (double)(dx[k] * fkx_); v1 += (double)(dy[k] * fky_); v2 += (double)(dz[k] * fkz_);
           v3 += (double)(dx[k] * fky_); v4 += (double)(dx[k] * fkz_); v5 += (double)(dy[k] * fkz_);
         }
       }
-      tx[s] += (double)ajx; ty[s] += (double)ajy; tz[s] += (double)ajz;
+      tx[s] += ajx; ty[s] += ajy; tz[s] += ajz;
       if (EV) {
         v0 += (double)(dx[s] * ajx); v1 += (double)(dy[s] * ajy); v2 += (double)(dz[s] * ajz);
         v3 += (double)(dx[s] * ajy); v4 += (double)(dx[s] * ajz); v5 += (double)(dy[s] * ajz);
@@ -511,8 +543,9 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
 #pragma unroll UNR
   for (int s = 0; s < NB; s++) {
     if (s < cnt) {
-      fx -= tx[s]; fy -= ty[s]; fz -= tz[s];
-      a.ters_g[(size_t)i * MAXTERS + s] = make_d4(gx[s] + tx[s], gy[s] + ty[s], gz[s] + tz[s], ge[s]);
+      const double ux = (double)tx[s], uy = (double)ty[s], uz = (double)tz[s];
+      fx -= ux; fy -= uy; fz -= uz;
+      a.ters_g[(size_t)i * MAXTERS + s] = make_d4(gx[s] + ux, gy[s] + uy, gz[s] + uz, ge[s]);
     }
   }
   a.ters_f[i] = fx;
@@ -959,7 +992,9 @@ __global__ void k_nderiv(ForceArgs<R> a) {
   double c0x = 0, c0y = 0, c0z = 0, c1x = 0, c1y = 0, c1z = 0, c2x = 0, c2y = 0, c2z = 0;
   double v[MAXILP][3];
   if (cont >= 2) {
-    for (int m = 0; m < cont; m++) {
+#pragma unroll
+    for (int m = 0; m < MAXILP; m++) {
+      if (m >= cont) break;
       int j, sx, sy, sz;
       decode_entry(a.ilp_nb[(size_t)i * MAXILP + m], a.lc, j, sx, sy, sz);
       double ddx, ddy, ddz;
@@ -976,11 +1011,14 @@ __global__ void k_nderiv(ForceArgs<R> a) {
       n1x += v[1][1] * v[2][2] - v[2][1] * v[1][2];
       n1y += v[1][2] * v[2][0] - v[2][2] * v[1][0];
       n1z += v[1][0] * v[2][1] - v[2][0] * v[1][1];
-      n1x /= 3.0; n1y /= 3.0; n1z /= 3.0;
+      // the reference averages the three products (n1 / 3); the unnormalised sum gives the
+      // same n, and h / 3 absorbs the 1/3 of each product's derivative
     }
-    double nn = sqrt(n1x * n1x + n1y * n1y + n1z * n1z);
-    if (nn > 0.0) {
-      double inn = 1.0 / nn;
+    const double nn2 = n1x * n1x + n1y * n1y + n1z * n1z;
+    if (nn2 > 0.0) {
+      double inn;
+      if constexpr (sizeof(R) == 4) inn = nn2 > 1e-30 ? rsqrt_nr(nn2) : 1.0 / sqrt(nn2);
+      else inn = 1.0 / sqrt(nn2);
       double nx = n1x * inn, ny = n1y * inn, nz = n1z * inn;
       double ng = nx * Gx + ny * Gy + nz * Gz;
       double hx = (Gx - nx * ng) * inn, hy = (Gy - ny * ng) * inn, hz = (Gz - nz * ng) * inn;
@@ -994,13 +1032,9 @@ __global__ void k_nderiv(ForceArgs<R> a) {
         crs(v[0][0], v[0][1], v[0][2], hx, hy, hz, c1x, c1y, c1z);
         Fx = -(c0x + c1x); Fy = -(c0y + c1y); Fz = -(c0z + c1z);
       } else {
-        const double t = 1.0 / 3.0;
         crs(v[2][0] - v[1][0], v[2][1] - v[1][1], v[2][2] - v[1][2], hx, hy, hz, c0x, c0y, c0z);
         crs(v[0][0] - v[2][0], v[0][1] - v[2][1], v[0][2] - v[2][2], hx, hy, hz, c1x, c1y, c1z);
         crs(v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2], hx, hy, hz, c2x, c2y, c2z);
-        c0x *= t; c0y *= t; c0z *= t;
-        c1x *= t; c1y *= t; c1z *= t;
-        c2x *= t; c2y *= t; c2z *= t;
       }
       if (EV) {
         // virial of the neighbour forces relative to i (the term's forces sum to zero)

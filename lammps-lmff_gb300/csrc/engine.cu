@@ -537,7 +537,7 @@ struct Engine {
     if (device >= 0) cudaSetDevice(device);
     void *ptrs[] = {d.xq, d.xh, d.xl, d.v, d.f, d.xhold, d.tag, d.perm, d.sysid, d.mass, d.nrm64, d.nrm32, d.jrec, d.ilp_cnt,
                     d.ilp_nb, d.ters_cnt, d.ters_nb, d.ters_g, d.ters_f, d.ilp_f, d.ilp_c, d.ilp_g, d.list_off, d.list,
-                    d.short_cnt, d.short_nb, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.cub_tmp,
+                    d.short_cnt, d.short_nb, d.list_img, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.cub_tmp,
                     d.cnt_tmp, d.sys, d.red_out, d.status, d.maxdisp, d_xin, d_fin, d_vin, d_ein, d_tin, d_sysin,
                     d_min, d_gin, d_massT, xq2, v2, mass2, tag2, perm2, sysid2, stat_ilp, stat_ters, eatom_ilp,
                     eatom_ters, ke, d_arrs, d_karrs, d_kout, d_cutILPsq};
@@ -891,6 +891,7 @@ struct Engine {
     CK(dalloc(stat_ilp, 8 * (size_t)c)); CK(dalloc(stat_ters, 8 * (size_t)c));
     CK(dalloc(eatom_ilp, c)); CK(dalloc(eatom_ters, c)); CK(dalloc(ke, c));
     CK(dalloc(d.list_off, (size_t)c + 1)); CK(dalloc(d.short_cnt, c)); CK(dalloc(d.short_nb, (size_t)c * MAXSHORT));
+    CK(dalloc(d.list_img, c));
     CK(dalloc(d.bin_key, c)); CK(dalloc(d.bin_key2, c)); CK(dalloc(d.idx, c)); CK(dalloc(d.idx2, c));
     CK(dalloc(d.cnt_tmp, (size_t)c + 1));
     CK(dalloc(d_xin, 3 * (size_t)c)); CK(dalloc(d_fin, 3 * (size_t)c)); CK(dalloc(d_vin, 3 * (size_t)c));
@@ -917,7 +918,7 @@ struct Engine {
                       sizeof(*d.nrm64) + sizeof(*d.nrm32) + 3 * sizeof(*d.jrec) + sizeof(*d.ilp_cnt) + MAXILP * sizeof(*d.ilp_nb) +
                       sizeof(*d.ters_cnt) + MAXTERS * (sizeof(*d.ters_nb) + sizeof(*d.ters_g)) +
                       2 * 3 * sizeof(double) + MAXILP * sizeof(*d.ilp_c) + sizeof(*d.ilp_g) + 16 * sizeof(double) +
-                      3 * sizeof(double) + sizeof(*d.list_off) + sizeof(*d.short_cnt) + MAXSHORT * sizeof(*d.short_nb) +
+                      3 * sizeof(double) + sizeof(*d.list_off) + sizeof(*d.list_img) + sizeof(*d.short_cnt) + MAXSHORT * sizeof(*d.short_nb) +
                       2 * sizeof(*d.bin_key) + 2 * sizeof(*d.idx) + sizeof(*d.cnt_tmp) + 3 * 3 * sizeof(double) +
                       sizeof(double) + 2 * sizeof(int) + 2 * sizeof(int64_t);
     if (bk_cap) per_atom += sizeof(d4) + 7 * sizeof(double) + sizeof(int64_t) + 2 * sizeof(int);
@@ -1072,6 +1073,7 @@ struct Engine {
     a.cnt = d.cnt_tmp;
     a.short_cnt = d.short_cnt;
     a.short_nb = d.short_nb;
+    a.img = d.list_img;
     a.lc = lc;
     a.full = list_full;
     a.status = d.status;
@@ -1175,6 +1177,7 @@ struct Engine {
     a.tag = d.tag;
     a.list_off = d.list_off;
     a.list = d.list;
+    a.list_img = d.list_img;
     a.short_cnt = d.short_cnt;
     a.short_nb = d.short_nb;
     a.ilp_cnt = d.ilp_cnt;
@@ -1519,6 +1522,7 @@ struct Engine {
     a.cnt = d.cnt_tmp;
     a.short_cnt = d.short_cnt;
     a.short_nb = d.short_nb;
+    a.img = d.list_img;
     a.lc = lc;
     a.full = list_full;
     a.status = d.status;
@@ -2247,6 +2251,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
   int *ilp_cnt = cv.take<int>(c), *ters_cnt = cv.take<int>(c), *short_cnt = cv.take<int>(c);
   uint32_t *ilp_nb = cv.take<uint32_t>((size_t)c * MAXILP), *ters_nb = cv.take<uint32_t>((size_t)c * MAXTERS);
   uint32_t *short_nb = cv.take<uint32_t>((size_t)c * MAXSHORT);
+  uint8_t *list_img = cv.take<uint8_t>(c);
   d4 *ters_g = cv.take<d4>((size_t)c * MAXTERS), *ilp_c = cv.take<d4>((size_t)c * MAXILP);
   double *ters_f = cv.take<double>(3 * c), *ilp_f = cv.take<double>(3 * c), *fs = cv.take<double>(3 * c);
   double *stat_ilp = cv.take<double>(8 * c), *stat_ters = cv.take<double>(8 * c);
@@ -2297,6 +2302,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
   na.cnt = cnt;
   na.short_cnt = short_cnt;
   na.short_nb = short_nb;
+  na.img = list_img;
   na.lc = lc;
   na.full = g.list_full;
   na.status = status;
@@ -2322,6 +2328,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
     a.tag = tag2;
     a.list_off = list_off;
     a.list = list;
+    a.list_img = list_img;
     a.short_cnt = short_cnt;
     a.short_nb = short_nb;
     a.ilp_cnt = ilp_cnt;

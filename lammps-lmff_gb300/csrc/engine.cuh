@@ -157,6 +157,7 @@ struct DevState {
   int64_t *list_off = nullptr; // n+1
   uint32_t *list = nullptr;
   int64_t list_cap = 0;
+  uint8_t *list_img = nullptr;   // per atom: 1 when its pair list holds periodic-image entries
   int *short_cnt = nullptr;
   uint32_t *short_nb = nullptr; // n * MAXSHORT
   // binning

@@ -211,6 +211,7 @@ struct ForceArgs {
   const int64_t *tag;
   const int64_t *list_off;
   const uint32_t *list;
+  const uint8_t *list_img;    // 1 when atom i's list holds periodic-image entries
   const int *short_cnt;
   const uint32_t *short_nb;
   int *ilp_cnt;

@@ -2,6 +2,8 @@
 // (LMFF_REAL = float), each of which owns one __constant__ copy of the potential.
 #pragma once
 
+#include <type_traits>
+
 #include "forces.cuh"
 
 namespace lmff {
@@ -627,12 +629,15 @@ __device__ __forceinline__ void rep_term(const IlpP<R> &p, R exp0, R exp1, R rho
 }
 
 // One list entry (i, j, image) with j's position and normal already loaded.
-template <bool EV, bool ONE, bool KC>
+// IMG: the entry may carry a periodic image shift (false: every entry of i's list is
+// unshifted, and the image decode and shift are left out)
+template <bool EV, bool ONE, bool KC, bool IMG>
 __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &ai, const SysDesc &sdl, uint32_t e,
                                          const typename AtomI<R>::J &J, const NrmJ<R> &N, R nix, R niy, R niz,
                                          int ie, long long mi, long long itag, bool check, IlpAcc &acc) {
-  int j, sx, sy, sz;
-  decode_entry(e, a.lc, j, sx, sy, sz);
+  int j, sx = 0, sy = 0, sz = 0;
+  if (IMG) decode_entry(e, a.lc, j, sx, sy, sz);
+  else j = (int)(e & a.lc.imask);
   R dx, dy, dz;
   long long jinfo;
   ai.disp_from(J, sdl, sx, sy, sz, dx, dy, dz, jinfo);
@@ -731,21 +736,27 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 
-template <bool EV, bool ONE, bool KC>
+template <bool EV, bool ONE, bool KC, bool IMG>
 __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const AtomI<float> &ai, const SysDesc &sdl,
                                             uint32_t e, const AtomI<float>::J &J, const NrmJ<float> &N, float nix,
                                             float niy, float niz, int ie, long long mi, long long itag, bool check,
                                             IlpAcc &acc) {
-  int j, sx, sy, sz;
-  decode_entry(e, a.lc, j, sx, sy, sz);
   // del = x_i - x_j(image), x and y packed: ((h_i - h_j) - s Lhi) + ((l_i - l_j) - s Llo)
-  const float2 sfx = p2((float)sx, (float)sy);
+  int j, sx = 0, sy = 0, sz = 0;
   float2 hxy = add2(p2(ai.hx, ai.hy), p2(-J.h.x, -J.h.y));
-  hxy = add2(hxy, mul2(sfx, p2(-sdl.Lhi[0], -sdl.Lhi[1])));
   float2 lxy = add2(p2(ai.lx, ai.ly), p2(-J.l.x, -J.l.y));
-  lxy = add2(lxy, mul2(sfx, p2(-sdl.Llo[0], -sdl.Llo[1])));
+  float dz;
+  if constexpr (IMG) {
+    decode_entry(e, a.lc, j, sx, sy, sz);
+    const float2 sfx = p2((float)sx, (float)sy);
+    hxy = add2(hxy, mul2(sfx, p2(-sdl.Lhi[0], -sdl.Lhi[1])));
+    lxy = add2(lxy, mul2(sfx, p2(-sdl.Llo[0], -sdl.Llo[1])));
+    dz = ((ai.hz - J.h.z) - (float)sz * sdl.Lhi[2]) + ((ai.lz - J.l.z) - (float)sz * sdl.Llo[2]);
+  } else {
+    j = (int)(e & a.lc.imask);
+    dz = (ai.hz - J.h.z) + (ai.lz - J.l.z);
+  }
   const float2 dxy = add2(hxy, lxy);
-  const float dz = ((ai.hz - J.h.z) - (float)sz * sdl.Lhi[2]) + ((ai.lz - J.l.z) - (float)sz * sdl.Llo[2]);
   const float2 sq = mul2(dxy, dxy);
   const float rsq = fmaf(dz, dz, sq.x + sq.y);
   if (!(rsq < c_pot.i_cutsq)) return;
@@ -843,14 +854,14 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
 #endif  // LMFF_PACKED_X2
 
 // the pair body of this precision: packed FP32x2 for the mixed path, scalar FP64
-template <bool EV, bool ONE, bool KC>
+template <bool EV, bool ONE, bool KC, bool IMG>
 __device__ __forceinline__ void pair_body(const ForceArgs<R> &a, const AtomI<R> &ai, const SysDesc &sdl, uint32_t e,
                                           const typename AtomI<R>::J &J, const NrmJ<R> &N, R nix, R niy, R niz, int ie,
                                           long long mi, long long itag, bool check, IlpAcc &acc) {
 #ifdef LMFF_PACKED_X2
-  ilp_pair_x2<EV, ONE, KC>(a, ai, sdl, e, J, N, nix, niy, niz, ie, mi, itag, check, acc);
+  ilp_pair_x2<EV, ONE, KC, IMG>(a, ai, sdl, e, J, N, nix, niy, niz, ie, mi, itag, check, acc);
 #else
-  ilp_pair<EV, ONE, KC>(a, ai, sdl, e, J, N, nix, niy, niz, ie, mi, itag, check, acc);
+  ilp_pair<EV, ONE, KC, IMG>(a, ai, sdl, e, J, N, nix, niy, niz, ie, mi, itag, check, acc);
 #endif
 }
 
@@ -889,25 +900,34 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R
     const int64_t b = a.list_off[i];
     const uint32_t *lst = a.list + b;
     const int cnt = (int)(a.list_off[i + 1] - b);
-    if constexpr (!PF && ONE) {
-      // the next list entry is loaded one iteration ahead, so that only j's data (not
-      // the list read before it) is on the dependence chain of a pair (-9 % on the
-      // 2.7M-atom graphite; the multi-element body has no registers to spare for it)
-      uint32_t e_next = lane < cnt ? __ldg(&lst[lane]) : 0u;
-      for (int k = lane; k < cnt; k += TPA) {
-        const uint32_t e = e_next;
-        if (k + TPA < cnt) e_next = __ldg(&lst[k + TPA]);
-        const int j = (int)(e & a.lc.imask);
-        pair_body<EV, ONE, KC>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi, itag, check,
-                               acc);
+    // atoms whose list holds no periodic-image entry (most of a large box) run the loop
+    // without the image decode and shift
+    auto run = [&](auto img_t) {
+      constexpr bool IMG = decltype(img_t)::value;
+      if constexpr (ONE) {
+        // the next list entry is loaded one iteration ahead, so that only j's data (not
+        // the list read before it) is on the dependence chain of a pair (-9 % on the
+        // 2.7M-atom graphite; the multi-element body has no registers to spare for it)
+        uint32_t e_next = lane < cnt ? __ldg(&lst[lane]) : 0u;
+        for (int k = lane; k < cnt; k += TPA) {
+          const uint32_t e = e_next;
+          if (k + TPA < cnt) e_next = __ldg(&lst[k + TPA]);
+          const int j = (int)(e & a.lc.imask);
+          pair_body<EV, ONE, KC, IMG>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi,
+                                      itag, check, acc);
+        }
+      } else {
+        for (int k = lane; k < cnt; k += TPA) {
+          const uint32_t e = __ldg(&lst[k]);
+          const int j = (int)(e & a.lc.imask);
+          pair_body<EV, ONE, KC, IMG>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi,
+                                      itag, check, acc);
+        }
       }
-    } else if constexpr (!PF) {
-      for (int k = lane; k < cnt; k += TPA) {
-        const uint32_t e = __ldg(&lst[k]);
-        const int j = (int)(e & a.lc.imask);
-        pair_body<EV, ONE, KC>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi, itag, check,
-                               acc);
-      }
+    };
+    if constexpr (!PF) {
+      if (a.list_img[i]) run(std::true_type{});
+      else run(std::false_type{});
     } else {
       // software pipeline: the next entry's position and normal are in flight while
       // the current pair is evaluated
@@ -930,7 +950,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R
           J = ai.fetch(a.A, j);
           N = NrmJ<R>::load(a, j);
         }
-        pair_body<EV, ONE, KC>(a, ai, sdl, ec, Jc, Nc, nix, niy, niz, ie, mi, itag, check, acc);
+        pair_body<EV, ONE, KC, true>(a, ai, sdl, ec, Jc, Nc, nix, niy, niz, ie, mi, itag, check, acc);
       }
     }
   }

@@ -148,6 +148,7 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
   const int mi = infoi >> 8;
   const int ilp_i = c_nb.ilp_mapped[ti];
   int nlong = 0, nin = 0, nsh = 0, nshort = 0;
+  bool img = false;
   const int64_t base = (FILL && act) ? a.list_off[i] : 0;
   const int64_t lend = (FILL && act) ? a.list_off[i + 1] : 0;
   unsigned todo = __ballot_sync(FULL, act);
@@ -220,6 +221,7 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
                   if (pos >= base && pos < lend && pos < a.list_cap) a.list[pos] = encode_entry(j, sx, sy, sz, a.lc);
                   nin += inner;
                   nsh += !inner;
+                  img |= !self_image;
                 }
               } else if (!(self_image && j == i) &&
                          le_exact(rsq, c_nb.rshortsq_f, c_nb.rshortsq_d, a.xq, sd, i, j, sx, sy, sz)) {
@@ -238,8 +240,9 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
       a.cnt[i] = nlong;
       a.short_cnt[i] = nshort < MAXSHORT ? nshort : MAXSHORT;
       if (nshort > MAXSHORT) atomicOr(a.status, ST_SHORT_OVERFLOW);
-    } else if (base + nlong > a.list_cap) {
-      atomicOr(a.status, ST_LIST_OVERFLOW);
+    } else {
+      a.img[i] = img;
+      if (base + nlong > a.list_cap) atomicOr(a.status, ST_LIST_OVERFLOW);
     }
   }
 }

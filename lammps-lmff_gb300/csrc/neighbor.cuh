@@ -32,6 +32,7 @@ struct NbArgs {
   int64_t *cnt;       // per-atom pair-list counts (int64: totals exceed 2^31)
   int *short_cnt;
   uint32_t *short_nb;
+  uint8_t *img;       // fill pass: 1 per atom whose list holds periodic-image entries
   ListCode lc;
   int full;
   int *status;

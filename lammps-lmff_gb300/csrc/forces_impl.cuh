@@ -736,6 +736,16 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 
+// Operand pairs of the packed body in constant memory, so that an FP32x2 instruction
+// reads them as one 64-bit constant operand instead of a register pair built per pair:
+// the Horner coefficients of (Tap, dTap/dx) and, for the single-element path, the
+// (i,j) and (j,i) repulsion constants of element 0.
+struct PairX2Const {
+  float2 tap0, tap1, tap2, tap3;
+  float2 nd2_l2e, C, eps_half, d2x2, lambda;
+};
+__constant__ PairX2Const c_x2;
+
 template <bool EV, bool ONE, bool KC, bool IMG>
 __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const AtomI<float> &ai, const SysDesc &sdl,
                                             uint32_t e, const AtomI<float>::J &J, const NrmJ<float> &N, float nix,
@@ -776,9 +786,16 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
   if (c_pot.tap) {
     const float x = r * c_pot.i_inv_rcut;
     const float2 xx = p2(x, x);
-    float2 t = fma2(p2(20.f, 140.f), xx, p2(-70.f, -420.f));
-    t = fma2(t, xx, p2(84.f, 420.f));
-    t = fma2(t, xx, p2(-35.f, -140.f));
+    float2 t;
+    if constexpr (ONE) {   // (measured: the multi-element body is faster with immediates)
+      t = fma2(c_x2.tap0, xx, c_x2.tap1);
+      t = fma2(t, xx, c_x2.tap2);
+      t = fma2(t, xx, c_x2.tap3);
+    } else {
+      t = fma2(p2(20.f, 140.f), xx, p2(-70.f, -420.f));
+      t = fma2(t, xx, p2(84.f, 420.f));
+      t = fma2(t, xx, p2(-35.f, -140.f));
+    }
     t = mul2(t, xx);
     t = mul2(t, xx);
     t = mul2(t, xx);
@@ -802,13 +819,14 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
     fpv = c6t * r8inv * (-6.f + pv.d_over_seff * (TSvdw - 1.f) * TSinv * r);
   }
   const float fsum_v = fpv * Tap - Vvdw * dTap * rinv;
-  // ---- the two repulsion terms packed: .x = (i,j) with n_i, .y = (j,i) with n_j
-  const float2 PQ = fma2(p2(nix, njx), p2(dx, dx), fma2(p2(niy, njy), p2(dy, dy), mul2(p2(niz, njz), p2(dz, dz))));
+  // ---- the two repulsion terms packed: .x = (i,j) with n_i, .y = (j,i) with n_j.  The
+  // projections n.del are scalar: packing them would first copy n_j and del into pairs.
+  const float2 PQ = p2(fmaf(niz, dz, fmaf(niy, dy, nix * dx)), fmaf(njz, dz, fmaf(njy, dy, njx * dx)));
   const float2 RH = fma2(p2(-PQ.x, -PQ.y), PQ, p2(rsq, rsq));
   const float e0 = Math<float>::exp_rep0(pij, r);
   const float e0b = pji.same_as_swapped ? e0 : Math<float>::exp_rep0(pji, r);
   const float2 E0 = p2(e0, e0b);
-  const float2 EA = mul2(p2(pij.nd2_l2e, pji.nd2_l2e), RH);
+  const float2 EA = mul2(ONE ? c_x2.nd2_l2e : p2(pij.nd2_l2e, pji.nd2_l2e), RH);
   const float2 E1 = p2(ex2_ftz(EA.x), ex2_ftz(EA.y));
   const float2 D2 = p2(pij.delta2inv, pji.delta2inv);
   float2 V, FP1;
@@ -821,12 +839,12 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
     V = mul2(E0, ER);
     FP1 = mul2(mul2(p2(2.f, 2.f), mul2(E0, E1)), fma2(D2, S1, p2(-S11.x, -S11.y)));
   } else {
-    const float2 FR = mul2(E1, p2(pij.C, pji.C));
-    ER = add2(p2(pij.eps_half, pji.eps_half), FR);
+    const float2 FR = mul2(E1, ONE ? c_x2.C : p2(pij.C, pji.C));
+    ER = add2(ONE ? c_x2.eps_half : p2(pij.eps_half, pji.eps_half), FR);
     V = mul2(E0, ER);
-    FP1 = mul2(mul2(E0, FR), p2(2.f * pij.delta2inv, 2.f * pji.delta2inv));
+    FP1 = mul2(mul2(E0, FR), ONE ? c_x2.d2x2 : p2(2.f * pij.delta2inv, 2.f * pji.delta2inv));
   }
-  const float2 FS = fma2(mul2(p2(pij.lambda, pji.lambda), V), p2(rinv, rinv), FP1);
+  const float2 FS = fma2(mul2(ONE ? c_x2.lambda : p2(pij.lambda, pji.lambda), V), p2(rinv, rinv), FP1);
   const float2 TPQ = mul2(mul2(p2(Tap, Tap), PQ), FP1);   // (tp1, tq1)
   const float Vsum = V.x + V.y;
   const float crad = fsum_v + (FS.x + FS.y) * Tap - Vsum * dTap * rinv;
@@ -1161,6 +1179,22 @@ __global__ void k_ters_eatom_own(ForceArgs<R> a) {
 
 void upload_pot(const PotConst<R> &p, cudaStream_t s) {
   cudaMemcpyToSymbolAsync(c_pot, &p, sizeof(p), 0, cudaMemcpyHostToDevice, s);
+#ifdef LMFF_PACKED_X2
+  {
+    static PairX2Const x2;   // static: the asynchronous copy reads it after return
+    const IlpP<float> &q = p.ilp[0];
+    x2.tap0 = make_float2(20.f, 140.f);
+    x2.tap1 = make_float2(-70.f, -420.f);
+    x2.tap2 = make_float2(84.f, 420.f);
+    x2.tap3 = make_float2(-35.f, -140.f);
+    x2.nd2_l2e = make_float2(q.nd2_l2e, q.nd2_l2e);
+    x2.C = make_float2(q.C, q.C);
+    x2.eps_half = make_float2(q.eps_half, q.eps_half);
+    x2.d2x2 = make_float2(2.f * q.delta2inv, 2.f * q.delta2inv);
+    x2.lambda = make_float2(q.lambda, q.lambda);
+    cudaMemcpyToSymbolAsync(c_x2, &x2, sizeof(x2), 0, cudaMemcpyHostToDevice, s);
+  }
+#endif
   if (sizeof(R) == 4) k_fill_exptab<<<EXP_TAB_N / 256, 256, 0, s>>>();
 }
 

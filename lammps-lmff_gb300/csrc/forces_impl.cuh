@@ -822,7 +822,10 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
   // ---- the two repulsion terms packed: .x = (i,j) with n_i, .y = (j,i) with n_j.  The
   // projections n.del are scalar: packing them would first copy n_j and del into pairs.
   const float2 PQ = p2(fmaf(niz, dz, fmaf(niy, dy, nix * dx)), fmaf(njz, dz, fmaf(njy, dy, njx * dx)));
-  const float2 RH = fma2(p2(-PQ.x, -PQ.y), PQ, p2(rsq, rsq));
+  // (the operand forms here and in the force sums below are the faster of packed and
+  // scalar, measured per path)
+  const float2 RH = ONE ? fma2(p2(-PQ.x, -PQ.y), PQ, p2(rsq, rsq))
+                        : p2(fmaf(-PQ.x, PQ.x, rsq), fmaf(-PQ.y, PQ.y, rsq));
   const float e0 = Math<float>::exp_rep0(pij, r);
   const float e0b = pji.same_as_swapped ? e0 : Math<float>::exp_rep0(pji, r);
   const float2 E0 = p2(e0, e0b);
@@ -849,16 +852,25 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
   const float Vsum = V.x + V.y;
   const float crad = fsum_v + (FS.x + FS.y) * Tap - Vsum * dTap * rinv;
   // ---- force on i; g_i += tp1 del
-  float2 fxy = fma2(p2(crad, crad), dxy, p2(acc.fx, acc.fy));
-  fxy = fma2(p2(-TPQ.x, -TPQ.x), p2(nix, niy), fxy);
-  fxy = fma2(p2(-TPQ.y, -TPQ.y), p2(njx, njy), fxy);
-  acc.fx = fxy.x;
-  acc.fy = fxy.y;
-  acc.fz += crad * dz - TPQ.x * niz - TPQ.y * njz;
-  const float2 gxy = fma2(p2(TPQ.x, TPQ.x), dxy, p2(acc.gxa, acc.gya));
-  acc.gxa = gxy.x;
-  acc.gya = gxy.y;
-  acc.gza += TPQ.x * dz;
+  if constexpr (ONE) {
+    acc.fx += crad * dx - TPQ.x * nix - TPQ.y * njx;
+    acc.fy += crad * dy - TPQ.x * niy - TPQ.y * njy;
+    acc.fz += crad * dz - TPQ.x * niz - TPQ.y * njz;
+    acc.gxa += TPQ.x * dx;
+    acc.gya += TPQ.x * dy;
+    acc.gza += TPQ.x * dz;
+  } else {
+    float2 fxy = fma2(p2(crad, crad), dxy, p2(acc.fx, acc.fy));
+    fxy = fma2(p2(-TPQ.x, -TPQ.x), p2(nix, niy), fxy);
+    fxy = fma2(p2(-TPQ.y, -TPQ.y), p2(njx, njy), fxy);
+    acc.fx = fxy.x;
+    acc.fy = fxy.y;
+    acc.fz += crad * dz - TPQ.x * niz - TPQ.y * njz;
+    const float2 gxy = fma2(p2(TPQ.x, TPQ.x), dxy, p2(acc.gxa, acc.gya));
+    acc.gxa = gxy.x;
+    acc.gya = gxy.y;
+    acc.gza += TPQ.x * dz;
+  }
   if (EV) {
     acc.evdw += 0.5f * Vvdw * Tap;
     const float eoff = (KC && !c_pot.tap) ? pij.kc_off + pji.kc_off : 0.f;

@@ -408,9 +408,10 @@ def main():
     tuned = None
     if not (args.tpa and args.block and args.skin):
         from lmff_gb300 import tune
-        probe = workload("graphite_330k") if args.workload == "graphite_2p7m" else s
-        tuned = tune.tune(probe, TERSOFF_FILE, ILP_FILE, elements=elements, precision=prec, device=local,
-                          tpas=(8, 16, 32), blocks=(128, 256), skins=(1.0, 2.0), use_cache=False, n_full=s.n)
+        # tuned on the workload itself: a smaller patch of the same slab ranks the launch
+        # shapes differently (measured: 16 threads per atom best at 331k, 8 at 2.7M)
+        tuned = tune.tune(s, TERSOFF_FILE, ILP_FILE, elements=elements, precision=prec, device=local,
+                          tpas=(8, 16), blocks=(128, 256), skins=(1.0, 2.0), use_cache=False, n_full=s.n)
         args.tpa = args.tpa or tuned["tpa"]
         args.block = args.block or tuned["block"]
         args.skin = args.skin or tuned["skin"]

@@ -12,6 +12,13 @@ namespace LMFF_NS {
 using R = LMFF_REAL;
 __constant__ PotConst<R> c_pot;
 
+// the mixed single-element pair loop evaluates two list entries per iteration
+#ifdef LMFF_PACKED_X2
+constexpr bool TWO_PAIR_BODY = true;
+#else
+constexpr bool TWO_PAIR_BODY = false;
+#endif
+
 __device__ __forceinline__ R cR(double v) { return (R)v; }
 
 __device__ __forceinline__ void raise_status(int *status, int bit) { atomicOr(status, bit); }
@@ -743,6 +750,10 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a
 struct PairX2Const {
   float2 tap0, tap1, tap2, tap3;
   float2 nd2_l2e, C, eps_half, d2x2, lambda;
+  // the same constants of element 0 duplicated for the two-pair body: taper (Tap in x and
+  // dTap/dr with 1/rcut folded in), 1/rcut, vdW and the repulsion's distance exponent
+  float2 ta0, ta1, ta2, ta3, td0, td1, td2, td3, inv_rcut, one;
+  float2 nts_a, ts_a_seff, C6, d_over_seff, m6, nlam_l2e, lamz0_l2e;
 };
 __constant__ PairX2Const c_x2;
 
@@ -881,6 +892,115 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
     acc.w3 += dx * ky; acc.w4 += dx * kz; acc.w5 += dy * kz;
   }
 }
+
+// ---- two list entries at once (single-element path, no energy/virial): FP32x2 lanes
+// hold pair A and pair B, so that every quantity of the chain r -> Tap -> vdW ->
+// repulsion is naturally a register pair and no operand has to be duplicated.  Same
+// formulas as ilp_pair_x2; a pair outside the cutoff (or filtered by molecule or type)
+// whose partner is inside is evaluated with Tap = dTap = 0, which zeroes every
+// contribution.
+template <bool IMG>
+__device__ __forceinline__ void disp_x2(const ForceArgs<float> &a, const AtomI<float> &ai, const SysDesc &sdl,
+                                        uint32_t e, const AtomI<float>::J &J, float2 &dxy, float &dz) {
+  float2 hxy = add2(p2(ai.hx, ai.hy), p2(-J.h.x, -J.h.y));
+  float2 lxy = add2(p2(ai.lx, ai.ly), p2(-J.l.x, -J.l.y));
+  if constexpr (IMG) {
+    int j, sx, sy, sz;
+    decode_entry(e, a.lc, j, sx, sy, sz);
+    const float2 sfx = p2((float)sx, (float)sy);
+    hxy = add2(hxy, mul2(sfx, p2(-sdl.Lhi[0], -sdl.Lhi[1])));
+    lxy = add2(lxy, mul2(sfx, p2(-sdl.Llo[0], -sdl.Llo[1])));
+    dz = ((ai.hz - J.h.z) - (float)sz * sdl.Lhi[2]) + ((ai.lz - J.l.z) - (float)sz * sdl.Llo[2]);
+  } else {
+    dz = (ai.hz - J.h.z) + (ai.lz - J.l.z);
+  }
+  dxy = add2(hxy, lxy);
+}
+
+template <bool IMG>
+__device__ __forceinline__ void ilp_pair2_one(const ForceArgs<float> &a, const AtomI<float> &ai, const SysDesc &sdl,
+                                              uint32_t eA, const AtomI<float>::J &JA, const NrmJ<float> &NA,
+                                              uint32_t eB, const AtomI<float>::J &JB, const NrmJ<float> &NB,
+                                              float nix, float niy, float niz, long long mi, bool check,
+                                              IlpAcc &acc) {
+  float2 dA, dB;
+  float dzA, dzB;
+  disp_x2<IMG>(a, ai, sdl, eA, JA, dA, dzA);
+  disp_x2<IMG>(a, ai, sdl, eB, JB, dB, dzB);
+  const float2 sqA = mul2(dA, dA), sqB = mul2(dB, dB);
+  const float2 RSQ = p2(fmaf(dzA, dzA, sqA.x + sqA.y), fmaf(dzB, dzB, sqB.x + sqB.y));
+  bool inA = RSQ.x < c_pot.i_cutsq, inB = RSQ.y < c_pot.i_cutsq;
+  if (check) {
+    const long long fA = (long long)__float_as_int(JA.h.w), fB = (long long)__float_as_int(JB.h.w);
+    inA = inA && info_mol(fA) != mi && ((c_pot.ilp_typemask >> info_type(fA)) & 1u);
+    inB = inB && info_mol(fB) != mi && ((c_pot.ilp_typemask >> info_type(fB)) & 1u);
+  }
+  if (!(inA || inB)) return;
+  const float2 RINV = p2(rsqrt_ftz(RSQ.x), rsqrt_ftz(RSQ.y));
+  const float2 R = mul2(RSQ, RINV);
+  // Tap = 1 + x^4 (((20x - 70)x + 84)x - 35); dTap/dr = x^3 (((140x - 420)x + 420)x - 140) / rcut
+  float2 TAP = c_x2.one, DTAP = p2(0.f, 0.f);
+  if (c_pot.tap) {
+    const float2 X = mul2(R, c_x2.inv_rcut);
+    const float2 X2 = mul2(X, X);
+    float2 t = fma2(c_x2.ta0, X, c_x2.ta1);
+    t = fma2(t, X, c_x2.ta2);
+    t = fma2(t, X, c_x2.ta3);
+    TAP = fma2(t, mul2(X2, X2), c_x2.one);
+    float2 u = fma2(c_x2.td0, X, c_x2.td1);
+    u = fma2(u, X, c_x2.td2);
+    u = fma2(u, X, c_x2.td3);
+    DTAP = mul2(u, mul2(X2, X));
+  }
+  if (!inA) { TAP.x = 0.f; DTAP.x = 0.f; }
+  if (!inB) { TAP.y = 0.f; DTAP.y = 0.f; }
+  const float2 DR = mul2(DTAP, RINV);
+  // ---- vdW: V = -C6 r^-6 / TS, TS = 1 + e^{-d (r/seff - 1)}
+  const float2 R2I = mul2(RINV, RINV);
+  const float2 R6I = mul2(mul2(R2I, R2I), R2I);
+  const float2 EXA = fma2(R, c_x2.nts_a, c_x2.ts_a_seff);
+  const float2 EX = p2(ex2_ftz(EXA.x), ex2_ftz(EXA.y));
+  const float2 TSV = add2(EX, c_x2.one);
+  const float2 TSI = p2(rcp_ftz(TSV.x), rcp_ftz(TSV.y));
+  const float2 C6T = mul2(c_x2.C6, TSI);
+  const float2 C6R6 = mul2(C6T, R6I);                       // -V
+  const float2 G = fma2(mul2(mul2(EX, TSI), R), c_x2.d_over_seff, c_x2.m6);
+  const float2 FPV = mul2(mul2(C6R6, R2I), G);
+  const float2 FSUMV = fma2(FPV, TAP, mul2(C6R6, DR));      // fpv Tap - V dTap / r
+  // ---- repulsion, terms (i,j) with n_i and (j,i) with n_j
+  const float2 PQI = p2(fmaf(niz, dzA, fmaf(niy, dA.y, nix * dA.x)), fmaf(niz, dzB, fmaf(niy, dB.y, nix * dB.x)));
+  const float2 PQJ = p2(fmaf(NA.q.z, dzA, fmaf(NA.q.y, dA.y, NA.q.x * dA.x)),
+                        fmaf(NB.q.z, dzB, fmaf(NB.q.y, dB.y, NB.q.x * dB.x)));
+  const float2 RHI = fma2(p2(-PQI.x, -PQI.y), PQI, RSQ);
+  const float2 RHJ = fma2(p2(-PQJ.x, -PQJ.y), PQJ, RSQ);
+  const float2 E0A = fma2(R, c_x2.nlam_l2e, c_x2.lamz0_l2e);
+  const float2 E0 = p2(ex2_ftz(E0A.x), ex2_ftz(E0A.y));
+  const float2 EIA = mul2(c_x2.nd2_l2e, RHI), EJA = mul2(c_x2.nd2_l2e, RHJ);
+  const float2 FRI = mul2(p2(ex2_ftz(EIA.x), ex2_ftz(EIA.y)), c_x2.C);
+  const float2 FRJ = mul2(p2(ex2_ftz(EJA.x), ex2_ftz(EJA.y)), c_x2.C);
+  const float2 VI = mul2(E0, add2(c_x2.eps_half, FRI));
+  const float2 VJ = mul2(E0, add2(c_x2.eps_half, FRJ));
+  const float2 FP1I = mul2(mul2(E0, FRI), c_x2.d2x2);
+  const float2 FP1J = mul2(mul2(E0, FRJ), c_x2.d2x2);
+  const float2 FSS = add2(fma2(mul2(c_x2.lambda, VI), RINV, FP1I), fma2(mul2(c_x2.lambda, VJ), RINV, FP1J));
+  const float2 TPQI = mul2(mul2(TAP, PQI), FP1I);
+  const float2 TPQJ = mul2(mul2(TAP, PQJ), FP1J);
+  const float2 VS = add2(VI, VJ);
+  const float2 CRAD = fma2(p2(-VS.x, -VS.y), DR, fma2(FSS, TAP, FSUMV));
+  // ---- force on i and g_i
+  acc.fx += CRAD.x * dA.x - TPQI.x * nix - TPQJ.x * NA.q.x;
+  acc.fy += CRAD.x * dA.y - TPQI.x * niy - TPQJ.x * NA.q.y;
+  acc.fz += CRAD.x * dzA - TPQI.x * niz - TPQJ.x * NA.q.z;
+  acc.gxa += TPQI.x * dA.x;
+  acc.gya += TPQI.x * dA.y;
+  acc.gza += TPQI.x * dzA;
+  acc.fx += CRAD.y * dB.x - TPQI.y * nix - TPQJ.y * NB.q.x;
+  acc.fy += CRAD.y * dB.y - TPQI.y * niy - TPQJ.y * NB.q.y;
+  acc.fz += CRAD.y * dzB - TPQI.y * niz - TPQJ.y * NB.q.z;
+  acc.gxa += TPQI.y * dB.x;
+  acc.gya += TPQI.y * dB.y;
+  acc.gza += TPQI.y * dzB;
+}
 #endif  // LMFF_PACKED_X2
 
 // the pair body of this precision: packed FP32x2 for the mixed path, scalar FP64
@@ -897,10 +1017,16 @@ __device__ __forceinline__ void pair_body(const ForceArgs<R> &a, const AtomI<R> 
 
 // FP32: at least 5 blocks of 256 threads per SM (48 registers) -- the kernel is
 // issue-bound with long-scoreboard stalls on j's data, and 40 resident warps hide them
-// better than 36 (measured: -8 % at 2.7M atoms, -16 % at 490k).  FP64 keeps its
-// registers.
+// better than 36 (measured: -8 % at 2.7M atoms, -16 % at 490k).  The two-pair body of
+// the single-element path needs 76 registers without spills; 4 blocks (64 registers)
+// measured 3 % faster than 3 blocks at 2.7M atoms.  FP64 keeps its registers.
 template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R> a) {
+constexpr int ilp_min_blocks() {
+  return sizeof(R) == 8 ? 1 : (TWO_PAIR_BODY && ONE && !EV && !KC) ? 4 : 5;
+}
+
+template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC>
+__global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, KC>())) k_ilp(ForceArgs<R> a) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gtid / TPA;
   const int lane = threadIdx.x & (TPA - 1);
@@ -934,6 +1060,28 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_ilp(ForceArgs<R
     // without the image decode and shift
     auto run = [&](auto img_t) {
       constexpr bool IMG = decltype(img_t)::value;
+#ifdef LMFF_PACKED_X2
+      if constexpr (TWO_PAIR_BODY && ONE && !EV && !KC) {
+        // two entries (k, k + TPA) per iteration, loaded one iteration ahead
+        int k = lane;
+        uint32_t eA = k < cnt ? __ldg(&lst[k]) : 0u;
+        uint32_t eB = k + TPA < cnt ? __ldg(&lst[k + TPA]) : 0u;
+        for (; k + TPA < cnt; k += 2 * TPA) {
+          const uint32_t ea = eA, eb = eB;
+          if (k + 2 * TPA < cnt) eA = __ldg(&lst[k + 2 * TPA]);
+          if (k + 3 * TPA < cnt) eB = __ldg(&lst[k + 3 * TPA]);
+          const int ja = (int)(ea & a.lc.imask), jb = (int)(eb & a.lc.imask);
+          ilp_pair2_one<IMG>(a, ai, sdl, ea, ai.fetch(a.A, ja), NrmJ<R>::load(a, ja), eb, ai.fetch(a.A, jb),
+                             NrmJ<R>::load(a, jb), nix, niy, niz, mi, check, acc);
+        }
+        if (k < cnt) {
+          const int j = (int)(eA & a.lc.imask);
+          pair_body<EV, ONE, KC, IMG>(a, ai, sdl, eA, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi,
+                                      itag, check, acc);
+        }
+        return;
+      }
+#endif
       if constexpr (ONE) {
         // the next list entry is loaded one iteration ahead, so that only j's data (not
         // the list read before it) is on the dependence chain of a pair (-9 % on the
@@ -1204,6 +1352,24 @@ void upload_pot(const PotConst<R> &p, cudaStream_t s) {
     x2.eps_half = make_float2(q.eps_half, q.eps_half);
     x2.d2x2 = make_float2(2.f * q.delta2inv, 2.f * q.delta2inv);
     x2.lambda = make_float2(q.lambda, q.lambda);
+    const float irc = p.i_inv_rcut;
+    x2.ta0 = make_float2(20.f, 20.f);
+    x2.ta1 = make_float2(-70.f, -70.f);
+    x2.ta2 = make_float2(84.f, 84.f);
+    x2.ta3 = make_float2(-35.f, -35.f);
+    x2.td0 = make_float2(140.f * irc, 140.f * irc);
+    x2.td1 = make_float2(-420.f * irc, -420.f * irc);
+    x2.td2 = make_float2(420.f * irc, 420.f * irc);
+    x2.td3 = make_float2(-140.f * irc, -140.f * irc);
+    x2.inv_rcut = make_float2(irc, irc);
+    x2.one = make_float2(1.f, 1.f);
+    x2.nts_a = make_float2(-q.ts_a, -q.ts_a);
+    x2.ts_a_seff = make_float2(q.ts_a * q.seff, q.ts_a * q.seff);
+    x2.C6 = make_float2(q.C6, q.C6);
+    x2.d_over_seff = make_float2(q.d_over_seff, q.d_over_seff);
+    x2.m6 = make_float2(-6.f, -6.f);
+    x2.nlam_l2e = make_float2(-q.lam_l2e, -q.lam_l2e);
+    x2.lamz0_l2e = make_float2(q.lamz0_l2e, q.lamz0_l2e);
     cudaMemcpyToSymbolAsync(c_x2, &x2, sizeof(x2), 0, cudaMemcpyHostToDevice, s);
   }
 #endif

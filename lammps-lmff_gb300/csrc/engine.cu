@@ -883,7 +883,7 @@ struct Engine {
     CK(dalloc(d.xhold, 3 * (size_t)c));
     CK(dalloc(d.tag, c)); CK(dalloc(tag2, c)); CK(dalloc(d.perm, c)); CK(dalloc(perm2, c));
     CK(dalloc(d.sysid, c)); CK(dalloc(sysid2, c)); CK(dalloc(d.mass, c)); CK(dalloc(mass2, c));
-    CK(dalloc(d.nrm64, c)); CK(dalloc(d.nrm32, c)); CK(dalloc(d.jrec, 3 * (size_t)c));
+    CK(dalloc(d.nrm64, c)); CK(dalloc(d.nrm32, c)); CK(dalloc(d.jrec, 5 * (size_t)c));
     CK(dalloc(d.ilp_cnt, c)); CK(dalloc(d.ilp_nb, (size_t)c * MAXILP));
     CK(dalloc(d.ters_cnt, c)); CK(dalloc(d.ters_nb, (size_t)c * MAXTERS));
     CK(dalloc(d.ters_g, (size_t)c * MAXTERS)); CK(dalloc(d.ters_f, 3 * (size_t)c));
@@ -915,7 +915,7 @@ struct Engine {
   double per_atom_bytes() const {
     double per_atom = 2 * sizeof(*d.xq) + sizeof(*d.xh) + sizeof(*d.xl) + 3 * (3 * sizeof(double)) +
                       3 * sizeof(double) + 2 * sizeof(*d.tag) + 4 * sizeof(int) + 2 * sizeof(double) +
-                      sizeof(*d.nrm64) + sizeof(*d.nrm32) + 3 * sizeof(*d.jrec) + sizeof(*d.ilp_cnt) + MAXILP * sizeof(*d.ilp_nb) +
+                      sizeof(*d.nrm64) + sizeof(*d.nrm32) + 5 * sizeof(*d.jrec) + sizeof(*d.ilp_cnt) + MAXILP * sizeof(*d.ilp_nb) +
                       sizeof(*d.ters_cnt) + MAXTERS * (sizeof(*d.ters_nb) + sizeof(*d.ters_g)) +
                       2 * 3 * sizeof(double) + MAXILP * sizeof(*d.ilp_c) + sizeof(*d.ilp_g) + 16 * sizeof(double) +
                       3 * sizeof(double) + sizeof(*d.list_off) + sizeof(*d.list_img) + sizeof(*d.short_cnt) + MAXSHORT * sizeof(*d.short_nb) +
@@ -1170,6 +1170,7 @@ struct Engine {
     a.A.xh = d.xh;
     a.A.xl = d.xl;
     a.A.jrec = d.jrec;
+    a.A.jrec2 = d.jrec + 3 * (size_t)cap_n;
     a.A.sys = d.sys;
     a.A.sysid = d.sysid;
     a.lc = lc;
@@ -1187,6 +1188,7 @@ struct Engine {
     a.nrm64 = d.nrm64;
     a.nrm32 = d.nrm32;
     a.jrec = d.jrec;
+    a.jrec2 = d.jrec + 3 * (size_t)cap_n;
     a.ters_g = d.ters_g;
     a.ters_f = d.ters_f;
     a.ilp_f = d.ilp_f;
@@ -2243,7 +2245,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
   Carve cv{(unsigned char *)basev, (unsigned char *)basev + NOALLOC_BYTES};
   d4 *xq = cv.take<d4>(c), *xq2 = cv.take<d4>(c), *nrm64 = cv.take<d4>(c), *ilp_g = cv.take<d4>(c);
   float4 *xh = cv.take<float4>(c), *xl = cv.take<float4>(c), *nrm32 = cv.take<float4>(c);
-  float4 *jrec = cv.take<float4>(3 * (size_t)c);
+  float4 *jrec = cv.take<float4>(3 * (size_t)c), *jrec2 = cv.take<float4>(2 * (size_t)c);
   double *v = cv.take<double>(3 * c), *v2 = cv.take<double>(3 * c), *mass = cv.take<double>(c),
          *mass2 = cv.take<double>(c);
   int64_t *tag = cv.take<int64_t>(c), *tag2 = cv.take<int64_t>(c);
@@ -2321,6 +2323,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
     a.A.xh = xh;
     a.A.xl = xl;
     a.A.jrec = jrec;
+    a.A.jrec2 = jrec2;
     a.A.sys = dsys;
     a.A.sysid = sysid2;
     a.lc = lc;
@@ -2338,6 +2341,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
     a.nrm64 = nrm64;
     a.nrm32 = nrm32;
     a.jrec = jrec;
+    a.jrec2 = jrec2;
     a.ters_g = ters_g;
     a.ters_f = ters_f;
     a.ilp_f = ilp_f;

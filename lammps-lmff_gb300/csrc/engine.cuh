@@ -141,7 +141,8 @@ struct DevState {
   // normals, per-step lists and gather slots
   d4 *nrm64 = nullptr;   // FP64 path normals
   float4 *nrm32 = nullptr;    // mixed path normals
-  float4 *jrec = nullptr;     // 3 per atom: mixed pair kernel's j data (hi+info, lo, normal)
+  float4 *jrec = nullptr;     // 5 per atom: mixed pair kernel's j data, 3 (hi+info, lo, normal)
+                              // for atom i at 3i, then the 2-float4 compact records from 3*cap
   int *ilp_cnt = nullptr;
   uint32_t *ilp_nb = nullptr; // n * MAXILP
   int *ters_cnt = nullptr;

@@ -94,6 +94,9 @@ struct AtomArrays {
   // mixed pair kernel's j data, one 48-byte record per atom written by k_short each
   // step: hi parts + info, lo parts, normal -- the three loads of a pair hit one line
   const float4 *jrec;
+  // the same without the info word, 32 bytes: (hi x, y, z, lo x|y as two FP16), (normal,
+  // lo z as FP16) -- for the single-element loop, which needs no molecule or type
+  const float4 *jrec2;
 };
 
 template <class R>
@@ -221,6 +224,7 @@ struct ForceArgs {
   d4 *nrm64;
   float4 *nrm32;
   float4 *jrec;        // 3 per atom (mixed path): see AtomArrays::jrec
+  float4 *jrec2;       // 2 per atom (mixed path): see AtomArrays::jrec2
   d4 *ters_g;
   double *ters_f;
   double *ilp_f;

@@ -2,6 +2,8 @@
 // (LMFF_REAL = float), each of which owns one __constant__ copy of the potential.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <type_traits>
 
 #include "forces.cuh"
@@ -11,6 +13,18 @@ namespace LMFF_NS {
 
 using R = LMFF_REAL;
 __constant__ PotConst<R> c_pot;
+
+// FP16 pairs <-> 32-bit words (the compact j record's lo parts)
+__device__ __forceinline__ unsigned h2_bits(__half2 h) {
+  unsigned u;
+  memcpy(&u, &h, sizeof u);
+  return u;
+}
+__device__ __forceinline__ __half2 bits_h2(unsigned u) {
+  __half2 h;
+  memcpy(&h, &u, sizeof h);
+  return h;
+}
 
 // the mixed single-element pair loop evaluates two list entries per iteration
 #ifdef LMFF_PACKED_X2
@@ -129,6 +143,8 @@ __global__ void k_short(ForceArgs<R> a, const double *cutILPsq64, double tcutmax
   a.jrec[3 * (size_t)i] = make_float4(ai.hx, ai.hy, ai.hz, __int_as_float((int)ai.info));
   a.jrec[3 * (size_t)i + 1] = make_float4(ai.lx, ai.ly, ai.lz, 0.f);
   a.jrec[3 * (size_t)i + 2] = make_float4(nx, ny, nz, 0.f);
+  a.jrec2[2 * (size_t)i] = make_float4(ai.hx, ai.hy, ai.hz, __uint_as_float(h2_bits(__floats2half2_rn(ai.lx, ai.ly))));
+  a.jrec2[2 * (size_t)i + 1] = make_float4(nx, ny, nz, __uint_as_float(h2_bits(__floats2half2_rn(ai.lz, 0.f))));
 #else
   a.nrm64[i] = make_d4(nx, ny, nz, 0.0);
 #endif
@@ -899,42 +915,43 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
 // formulas as ilp_pair_x2; a pair outside the cutoff (or filtered by molecule or type)
 // whose partner is inside is evaluated with Tap = dTap = 0, which zeroes every
 // contribution.
+// j's compact record: r0 = (hi x, y, z, lo x|y as FP16), r1 = (normal, lo z as FP16).
+// The lo parts carry |lo| <= ulp(hi)/2 to ~3e-8 A; i's own lo parts are rounded the same
+// way (loi), so that both ends of a pair see the same positions.
 template <bool IMG>
-__device__ __forceinline__ void disp_x2(const ForceArgs<float> &a, const AtomI<float> &ai, const SysDesc &sdl,
-                                        uint32_t e, const AtomI<float>::J &J, float2 &dxy, float &dz) {
-  float2 hxy = add2(p2(ai.hx, ai.hy), p2(-J.h.x, -J.h.y));
-  float2 lxy = add2(p2(ai.lx, ai.ly), p2(-J.l.x, -J.l.y));
+__device__ __forceinline__ void disp_x2(const ForceArgs<float> &a, const AtomI<float> &ai, const float3 &loi,
+                                        const SysDesc &sdl, uint32_t e, const float4 &r0, const float4 &r1,
+                                        float2 &dxy, float &dz) {
+  const float2 lj = __half22float2(bits_h2(__float_as_uint(r0.w)));
+  const float ljz = __low2float(bits_h2(__float_as_uint(r1.w)));
+  float2 hxy = add2(p2(ai.hx, ai.hy), p2(-r0.x, -r0.y));
+  float2 lxy = add2(p2(loi.x, loi.y), p2(-lj.x, -lj.y));
   if constexpr (IMG) {
     int j, sx, sy, sz;
     decode_entry(e, a.lc, j, sx, sy, sz);
     const float2 sfx = p2((float)sx, (float)sy);
     hxy = add2(hxy, mul2(sfx, p2(-sdl.Lhi[0], -sdl.Lhi[1])));
     lxy = add2(lxy, mul2(sfx, p2(-sdl.Llo[0], -sdl.Llo[1])));
-    dz = ((ai.hz - J.h.z) - (float)sz * sdl.Lhi[2]) + ((ai.lz - J.l.z) - (float)sz * sdl.Llo[2]);
+    dz = ((ai.hz - r0.z) - (float)sz * sdl.Lhi[2]) + ((loi.z - ljz) - (float)sz * sdl.Llo[2]);
   } else {
-    dz = (ai.hz - J.h.z) + (ai.lz - J.l.z);
+    dz = (ai.hz - r0.z) + (loi.z - ljz);
   }
   dxy = add2(hxy, lxy);
 }
 
+// bvalid = false: only pair A exists (B repeats A and contributes nothing)
 template <bool IMG>
-__device__ __forceinline__ void ilp_pair2_one(const ForceArgs<float> &a, const AtomI<float> &ai, const SysDesc &sdl,
-                                              uint32_t eA, const AtomI<float>::J &JA, const NrmJ<float> &NA,
-                                              uint32_t eB, const AtomI<float>::J &JB, const NrmJ<float> &NB,
-                                              float nix, float niy, float niz, long long mi, bool check,
-                                              IlpAcc &acc) {
+__device__ __forceinline__ void ilp_pair2_one(const ForceArgs<float> &a, const AtomI<float> &ai, const float3 &loi,
+                                              const SysDesc &sdl, uint32_t eA, const float4 &A0, const float4 &A1,
+                                              uint32_t eB, const float4 &B0, const float4 &B1, bool bvalid, float nix,
+                                              float niy, float niz, IlpAcc &acc) {
   float2 dA, dB;
   float dzA, dzB;
-  disp_x2<IMG>(a, ai, sdl, eA, JA, dA, dzA);
-  disp_x2<IMG>(a, ai, sdl, eB, JB, dB, dzB);
+  disp_x2<IMG>(a, ai, loi, sdl, eA, A0, A1, dA, dzA);
+  disp_x2<IMG>(a, ai, loi, sdl, eB, B0, B1, dB, dzB);
   const float2 sqA = mul2(dA, dA), sqB = mul2(dB, dB);
   const float2 RSQ = p2(fmaf(dzA, dzA, sqA.x + sqA.y), fmaf(dzB, dzB, sqB.x + sqB.y));
-  bool inA = RSQ.x < c_pot.i_cutsq, inB = RSQ.y < c_pot.i_cutsq;
-  if (check) {
-    const long long fA = (long long)__float_as_int(JA.h.w), fB = (long long)__float_as_int(JB.h.w);
-    inA = inA && info_mol(fA) != mi && ((c_pot.ilp_typemask >> info_type(fA)) & 1u);
-    inB = inB && info_mol(fB) != mi && ((c_pot.ilp_typemask >> info_type(fB)) & 1u);
-  }
+  const bool inA = RSQ.x < c_pot.i_cutsq, inB = bvalid && RSQ.y < c_pot.i_cutsq;
   if (!(inA || inB)) return;
   const float2 RINV = p2(rsqrt_ftz(RSQ.x), rsqrt_ftz(RSQ.y));
   const float2 R = mul2(RSQ, RINV);
@@ -969,8 +986,7 @@ __device__ __forceinline__ void ilp_pair2_one(const ForceArgs<float> &a, const A
   const float2 FSUMV = fma2(FPV, TAP, mul2(C6R6, DR));      // fpv Tap - V dTap / r
   // ---- repulsion, terms (i,j) with n_i and (j,i) with n_j
   const float2 PQI = p2(fmaf(niz, dzA, fmaf(niy, dA.y, nix * dA.x)), fmaf(niz, dzB, fmaf(niy, dB.y, nix * dB.x)));
-  const float2 PQJ = p2(fmaf(NA.q.z, dzA, fmaf(NA.q.y, dA.y, NA.q.x * dA.x)),
-                        fmaf(NB.q.z, dzB, fmaf(NB.q.y, dB.y, NB.q.x * dB.x)));
+  const float2 PQJ = p2(fmaf(A1.z, dzA, fmaf(A1.y, dA.y, A1.x * dA.x)), fmaf(B1.z, dzB, fmaf(B1.y, dB.y, B1.x * dB.x)));
   const float2 RHI = fma2(p2(-PQI.x, -PQI.y), PQI, RSQ);
   const float2 RHJ = fma2(p2(-PQJ.x, -PQJ.y), PQJ, RSQ);
   const float2 E0A = fma2(R, c_x2.nlam_l2e, c_x2.lamz0_l2e);
@@ -988,15 +1004,15 @@ __device__ __forceinline__ void ilp_pair2_one(const ForceArgs<float> &a, const A
   const float2 VS = add2(VI, VJ);
   const float2 CRAD = fma2(p2(-VS.x, -VS.y), DR, fma2(FSS, TAP, FSUMV));
   // ---- force on i and g_i
-  acc.fx += CRAD.x * dA.x - TPQI.x * nix - TPQJ.x * NA.q.x;
-  acc.fy += CRAD.x * dA.y - TPQI.x * niy - TPQJ.x * NA.q.y;
-  acc.fz += CRAD.x * dzA - TPQI.x * niz - TPQJ.x * NA.q.z;
+  acc.fx += CRAD.x * dA.x - TPQI.x * nix - TPQJ.x * A1.x;
+  acc.fy += CRAD.x * dA.y - TPQI.x * niy - TPQJ.x * A1.y;
+  acc.fz += CRAD.x * dzA - TPQI.x * niz - TPQJ.x * A1.z;
   acc.gxa += TPQI.x * dA.x;
   acc.gya += TPQI.x * dA.y;
   acc.gza += TPQI.x * dzA;
-  acc.fx += CRAD.y * dB.x - TPQI.y * nix - TPQJ.y * NB.q.x;
-  acc.fy += CRAD.y * dB.y - TPQI.y * niy - TPQJ.y * NB.q.y;
-  acc.fz += CRAD.y * dzB - TPQI.y * niz - TPQJ.y * NB.q.z;
+  acc.fx += CRAD.y * dB.x - TPQI.y * nix - TPQJ.y * B1.x;
+  acc.fy += CRAD.y * dB.y - TPQI.y * niy - TPQJ.y * B1.y;
+  acc.fz += CRAD.y * dzB - TPQI.y * niz - TPQJ.y * B1.z;
   acc.gxa += TPQI.y * dB.x;
   acc.gya += TPQI.y * dB.y;
   acc.gza += TPQI.y * dzB;
@@ -1062,24 +1078,29 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
       constexpr bool IMG = decltype(img_t)::value;
 #ifdef LMFF_PACKED_X2
       if constexpr (TWO_PAIR_BODY && ONE && !EV && !KC) {
-        // two entries (k, k + TPA) per iteration, loaded one iteration ahead
-        int k = lane;
-        uint32_t eA = k < cnt ? __ldg(&lst[k]) : 0u;
-        uint32_t eB = k + TPA < cnt ? __ldg(&lst[k + TPA]) : 0u;
-        for (; k + TPA < cnt; k += 2 * TPA) {
-          const uint32_t ea = eA, eb = eB;
-          if (k + 2 * TPA < cnt) eA = __ldg(&lst[k + 2 * TPA]);
-          if (k + 3 * TPA < cnt) eB = __ldg(&lst[k + 3 * TPA]);
-          const int ja = (int)(ea & a.lc.imask), jb = (int)(eb & a.lc.imask);
-          ilp_pair2_one<IMG>(a, ai, sdl, ea, ai.fetch(a.A, ja), NrmJ<R>::load(a, ja), eb, ai.fetch(a.A, jb),
-                             NrmJ<R>::load(a, jb), nix, niy, niz, mi, check, acc);
+        if (!check) {
+          // two entries (k, k + TPA) per iteration, loaded one iteration ahead, j's data
+          // from the compact 32-byte records
+          const float3 loi = make_float3(__half2float(__float2half_rn(ai.lx)), __half2float(__float2half_rn(ai.ly)),
+                                         __half2float(__float2half_rn(ai.lz)));
+          int k = lane;
+          uint32_t eA = k < cnt ? __ldg(&lst[k]) : 0u;
+          uint32_t eB = k + TPA < cnt ? __ldg(&lst[k + TPA]) : 0u;
+          for (; k + TPA < cnt; k += 2 * TPA) {
+            const uint32_t ea = eA, eb = eB;
+            if (k + 2 * TPA < cnt) eA = __ldg(&lst[k + 2 * TPA]);
+            if (k + 3 * TPA < cnt) eB = __ldg(&lst[k + 3 * TPA]);
+            const size_t ja = 2 * (size_t)(ea & a.lc.imask), jb = 2 * (size_t)(eb & a.lc.imask);
+            ilp_pair2_one<IMG>(a, ai, loi, sdl, ea, __ldg(&a.A.jrec2[ja]), __ldg(&a.A.jrec2[ja + 1]), eb,
+                               __ldg(&a.A.jrec2[jb]), __ldg(&a.A.jrec2[jb + 1]), true, nix, niy, niz, acc);
+          }
+          if (k < cnt) {
+            const size_t ja = 2 * (size_t)(eA & a.lc.imask);
+            const float4 r0 = __ldg(&a.A.jrec2[ja]), r1 = __ldg(&a.A.jrec2[ja + 1]);
+            ilp_pair2_one<IMG>(a, ai, loi, sdl, eA, r0, r1, eA, r0, r1, false, nix, niy, niz, acc);
+          }
+          return;
         }
-        if (k < cnt) {
-          const int j = (int)(eA & a.lc.imask);
-          pair_body<EV, ONE, KC, IMG>(a, ai, sdl, eA, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi,
-                                      itag, check, acc);
-        }
-        return;
       }
 #endif
       if constexpr (ONE) {

@@ -91,6 +91,30 @@ def test_mixed_precision_accuracy(name):
     assert rel_max(r["virial"], g["virial"]) <= MIX_W_REL
 
 
+@pytest.mark.parametrize("name", ["c1_t0", "hetero_small", "trilayer_alt", "edges", "tiny_images"])
+@pytest.mark.parametrize("tpa", [8, 16])
+def test_mixed_forces_without_energy_match_reference(name, tpa):
+    """The production force-only pair kernels (no energy/virial: the single-element loop
+    with two list entries per iteration and compact j records, and the multi-element
+    loop), against the reference."""
+    g = load_golden(name)
+    eng = engine_for(g, precision=capi.MIXED, tpa=tpa)
+    r = eng.compute(g["x"], g["type"], g["mol"], g["tag"], eflag=False, vflag=False)
+    assert np.abs(r["f"] - g["f"]).max() <= MIX_F_ABS
+
+
+def test_mixed_forces_without_energy_large():
+    """Force-only mixed evaluation of a 97k-atom displaced graphite slab against the FP64
+    engine, and against the mixed evaluation with energies (another kernel instance)."""
+    s = S.displace(S.graphite_slab(6, 60, 34, mol_mode="alternate"), 0.03, seed=5)
+    r64 = capi.Engine(TERSOFF, ILP).compute_system(s)
+    eng = capi.Engine(TERSOFF, ILP, precision=capi.MIXED)
+    rf = eng.compute_system(s, eflag=False, vflag=False)
+    re = capi.Engine(TERSOFF, ILP, precision=capi.MIXED).compute_system(s)
+    assert np.abs(rf["f"] - r64["f"]).max() <= MIX_F_ABS
+    assert np.abs(rf["f"] - re["f"]).max() <= MIX_F_ABS
+
+
 def test_nve_trajectory_matches_reference():
     """100 velocity-Verlet steps of the 7,200-atom bilayer, device resident, vs the
     reference's own trajectory from the same start."""

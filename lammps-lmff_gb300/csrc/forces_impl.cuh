@@ -4,6 +4,7 @@
 
 #include <cuda_fp16.h>
 
+#include <cmath>
 #include <type_traits>
 
 #include "forces.cuh"
@@ -766,10 +767,11 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a
 struct PairX2Const {
   float2 tap0, tap1, tap2, tap3;
   float2 nd2_l2e, C, eps_half, d2x2, lambda;
-  // the same constants of element 0 duplicated for the two-pair body: taper (Tap in x and
-  // dTap/dr with 1/rcut folded in), 1/rcut, vdW and the repulsion's distance exponent
-  float2 ta0, ta1, ta2, ta3, td0, td1, td2, td3, inv_rcut, one;
-  float2 nts_a, ts_a_seff, C6, d_over_seff, m6, nlam_l2e, lamz0_l2e;
+  // the same constants of element 0 duplicated for the two-pair body: taper in r (Tap
+  // and dTap/dr with the powers of 1/rcut folded into the coefficients), vdW, the
+  // repulsion's distance exponent, log2 C (C e^y = 2^(y log2 e + log2 C)) and eps
+  float2 ta0, ta1, ta2, ta3, td0, td1, td2, td3, one;
+  float2 nts_a, ts_a_seff, C6, d_over_seff, m6, nlam_l2e, lamz0_l2e, log2C, eps;
 };
 __constant__ PairX2Const c_x2;
 
@@ -955,19 +957,19 @@ __device__ __forceinline__ void ilp_pair2_one(const ForceArgs<float> &a, const A
   if (!(inA || inB)) return;
   const float2 RINV = p2(rsqrt_ftz(RSQ.x), rsqrt_ftz(RSQ.y));
   const float2 R = mul2(RSQ, RINV);
-  // Tap = 1 + x^4 (((20x - 70)x + 84)x - 35); dTap/dr = x^3 (((140x - 420)x + 420)x - 140) / rcut
+  // Tap = 1 + x^4 (((20x - 70)x + 84)x - 35), dTap/dr = x^3 (((140x - 420)x + 420)x - 140) / rcut,
+  // x = r / rcut, evaluated in r
   float2 TAP = c_x2.one, DTAP = p2(0.f, 0.f);
   if (c_pot.tap) {
-    const float2 X = mul2(R, c_x2.inv_rcut);
-    const float2 X2 = mul2(X, X);
-    float2 t = fma2(c_x2.ta0, X, c_x2.ta1);
-    t = fma2(t, X, c_x2.ta2);
-    t = fma2(t, X, c_x2.ta3);
-    TAP = fma2(t, mul2(X2, X2), c_x2.one);
-    float2 u = fma2(c_x2.td0, X, c_x2.td1);
-    u = fma2(u, X, c_x2.td2);
-    u = fma2(u, X, c_x2.td3);
-    DTAP = mul2(u, mul2(X2, X));
+    const float2 R2 = mul2(R, R);
+    float2 t = fma2(c_x2.ta0, R, c_x2.ta1);
+    t = fma2(t, R, c_x2.ta2);
+    t = fma2(t, R, c_x2.ta3);
+    TAP = fma2(t, mul2(R2, R2), c_x2.one);
+    float2 u = fma2(c_x2.td0, R, c_x2.td1);
+    u = fma2(u, R, c_x2.td2);
+    u = fma2(u, R, c_x2.td3);
+    DTAP = mul2(u, mul2(R2, R));
   }
   if (!inA) { TAP.x = 0.f; DTAP.x = 0.f; }
   if (!inB) { TAP.y = 0.f; DTAP.y = 0.f; }
@@ -989,19 +991,18 @@ __device__ __forceinline__ void ilp_pair2_one(const ForceArgs<float> &a, const A
   const float2 PQJ = p2(fmaf(A1.z, dzA, fmaf(A1.y, dA.y, A1.x * dA.x)), fmaf(B1.z, dzB, fmaf(B1.y, dB.y, B1.x * dB.x)));
   const float2 RHI = fma2(p2(-PQI.x, -PQI.y), PQI, RSQ);
   const float2 RHJ = fma2(p2(-PQJ.x, -PQJ.y), PQJ, RSQ);
+  // V_t = E0 (eps/2 + C e^{-rho_t^2/delta^2}), fpair1_t = 2 E0 C e^{...} / delta^2, and the
+  // radial factor of both terms together, lambda (V_i + V_j) / r + fpair1_i + fpair1_j
   const float2 E0A = fma2(R, c_x2.nlam_l2e, c_x2.lamz0_l2e);
   const float2 E0 = p2(ex2_ftz(E0A.x), ex2_ftz(E0A.y));
-  const float2 EIA = mul2(c_x2.nd2_l2e, RHI), EJA = mul2(c_x2.nd2_l2e, RHJ);
-  const float2 FRI = mul2(p2(ex2_ftz(EIA.x), ex2_ftz(EIA.y)), c_x2.C);
-  const float2 FRJ = mul2(p2(ex2_ftz(EJA.x), ex2_ftz(EJA.y)), c_x2.C);
-  const float2 VI = mul2(E0, add2(c_x2.eps_half, FRI));
-  const float2 VJ = mul2(E0, add2(c_x2.eps_half, FRJ));
-  const float2 FP1I = mul2(mul2(E0, FRI), c_x2.d2x2);
-  const float2 FP1J = mul2(mul2(E0, FRJ), c_x2.d2x2);
-  const float2 FSS = add2(fma2(mul2(c_x2.lambda, VI), RINV, FP1I), fma2(mul2(c_x2.lambda, VJ), RINV, FP1J));
-  const float2 TPQI = mul2(mul2(TAP, PQI), FP1I);
-  const float2 TPQJ = mul2(mul2(TAP, PQJ), FP1J);
-  const float2 VS = add2(VI, VJ);
+  const float2 EIA = fma2(c_x2.nd2_l2e, RHI, c_x2.log2C), EJA = fma2(c_x2.nd2_l2e, RHJ, c_x2.log2C);
+  const float2 E0FI = mul2(E0, p2(ex2_ftz(EIA.x), ex2_ftz(EIA.y)));
+  const float2 E0FJ = mul2(E0, p2(ex2_ftz(EJA.x), ex2_ftz(EJA.y)));
+  const float2 S = add2(E0FI, E0FJ);
+  const float2 VS = fma2(E0, c_x2.eps, S);
+  const float2 FSS = fma2(mul2(c_x2.lambda, RINV), VS, mul2(S, c_x2.d2x2));
+  const float2 TPQI = mul2(mul2(TAP, PQI), mul2(E0FI, c_x2.d2x2));
+  const float2 TPQJ = mul2(mul2(TAP, PQJ), mul2(E0FJ, c_x2.d2x2));
   const float2 CRAD = fma2(p2(-VS.x, -VS.y), DR, fma2(FSS, TAP, FSUMV));
   // ---- force on i and g_i
   acc.fx += CRAD.x * dA.x - TPQI.x * nix - TPQJ.x * A1.x;
@@ -1078,7 +1079,7 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
       constexpr bool IMG = decltype(img_t)::value;
 #ifdef LMFF_PACKED_X2
       if constexpr (TWO_PAIR_BODY && ONE && !EV && !KC) {
-        if (!check) {
+        if (!check && c_pot.ilp[0].C >= 0.f) {
           // two entries (k, k + TPA) per iteration, loaded one iteration ahead, j's data
           // from the compact 32-byte records
           const float3 loi = make_float3(__half2float(__float2half_rn(ai.lx)), __half2float(__float2half_rn(ai.ly)),
@@ -1373,16 +1374,16 @@ void upload_pot(const PotConst<R> &p, cudaStream_t s) {
     x2.eps_half = make_float2(q.eps_half, q.eps_half);
     x2.d2x2 = make_float2(2.f * q.delta2inv, 2.f * q.delta2inv);
     x2.lambda = make_float2(q.lambda, q.lambda);
-    const float irc = p.i_inv_rcut;
-    x2.ta0 = make_float2(20.f, 20.f);
-    x2.ta1 = make_float2(-70.f, -70.f);
-    x2.ta2 = make_float2(84.f, 84.f);
-    x2.ta3 = make_float2(-35.f, -35.f);
-    x2.td0 = make_float2(140.f * irc, 140.f * irc);
-    x2.td1 = make_float2(-420.f * irc, -420.f * irc);
-    x2.td2 = make_float2(420.f * irc, 420.f * irc);
-    x2.td3 = make_float2(-140.f * irc, -140.f * irc);
-    x2.inv_rcut = make_float2(irc, irc);
+    const double irc = (double)p.i_inv_rcut, i4 = irc * irc * irc * irc;
+    auto dup = [](double v) { return make_float2((float)v, (float)v); };
+    x2.ta0 = dup(20.0 * i4 * irc * irc * irc);
+    x2.ta1 = dup(-70.0 * i4 * irc * irc);
+    x2.ta2 = dup(84.0 * i4 * irc);
+    x2.ta3 = dup(-35.0 * i4);
+    x2.td0 = dup(140.0 * i4 * irc * irc * irc);
+    x2.td1 = dup(-420.0 * i4 * irc * irc);
+    x2.td2 = dup(420.0 * i4 * irc);
+    x2.td3 = dup(-140.0 * i4);
     x2.one = make_float2(1.f, 1.f);
     x2.nts_a = make_float2(-q.ts_a, -q.ts_a);
     x2.ts_a_seff = make_float2(q.ts_a * q.seff, q.ts_a * q.seff);
@@ -1391,6 +1392,10 @@ void upload_pot(const PotConst<R> &p, cudaStream_t s) {
     x2.m6 = make_float2(-6.f, -6.f);
     x2.nlam_l2e = make_float2(-q.lam_l2e, -q.lam_l2e);
     x2.lamz0_l2e = make_float2(q.lamz0_l2e, q.lamz0_l2e);
+    // the two-pair body runs only for C >= 0 (log2 0 = -inf gives 2^-inf = 0)
+    const float l2c = q.C > 0.f ? (float)std::log2((double)q.C) : -INFINITY;
+    x2.log2C = make_float2(l2c, l2c);
+    x2.eps = make_float2(2.f * q.eps_half, 2.f * q.eps_half);
     cudaMemcpyToSymbolAsync(c_x2, &x2, sizeof(x2), 0, cudaMemcpyHostToDevice, s);
   }
 #endif

@@ -739,6 +739,8 @@ struct Engine {
             o.nl1x32 = -32.0 * q.lam1;
             o.nl2x32 = -32.0 * q.lam2;
             o.h64 = q.h;
+            o.hhi = (float)q.h;
+            o.hlo = (float)(q.h - (double)o.hhi);
             o.Al1_64 = q.biga * q.lam1;
             o.Bl2_64 = q.bigb * q.lam2;
             o.nl1h = (float)o.nl1x32;

@@ -62,7 +62,8 @@ struct TersP {
   // evaluated in FP64 in both precision modes
   double A64, B64, lam1_64, lam2_64, R64, D64, rlo64, rhi64, pi4D64, cutsq64;
   double nl1x32, nl2x32;       // -32 lam1, -32 lam2 (argument scale of the table exp)
-  double h64;                 // h (FP32 mode: u = h - cos(theta) in FP64)
+  double h64;                 // h in FP64
+  float hhi, hlo;             // h as an FP32 pair (FP32 mode: u = h - cos(theta) in double-float)
   double Al1_64, Bl2_64;      // A lam1, B lam2
   float nl1h, nl1l, nl2h, nl2l;  // -32 lam1, -32 lam2 as FP32 pairs (hi + lo)
   int powermint;

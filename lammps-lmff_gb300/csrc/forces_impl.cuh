@@ -333,6 +333,32 @@ __device__ __forceinline__ double rsqrt_nr(double x) {
   return fma(0.5 * y, e, y);
 }
 
+// ---- FP32 double-float arithmetic (error-free transformations: Knuth's TwoSum, the
+// FMA-based TwoProduct) for the FP32 mode's bond geometry: lengths and cosines to
+// ~1e-13 relative from the hi/lo position parts, with no FP64 instruction.
+__device__ __forceinline__ void ef_two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (sh, sl) = a . b for vectors a = ah + al, b = bh + bl with |al| << |ah|, |bl| << |bh|
+__device__ __forceinline__ void df_dot3(const float *ah, const float *al, const float *bh, const float *bl, float &sh,
+                                        float &sl) {
+  const float p0 = __fmul_rn(ah[0], bh[0]), e0 = __fmaf_rn(ah[0], bh[0], -p0);
+  const float p1 = __fmul_rn(ah[1], bh[1]), e1 = __fmaf_rn(ah[1], bh[1], -p1);
+  const float p2_ = __fmul_rn(ah[2], bh[2]), e2 = __fmaf_rn(ah[2], bh[2], -p2_);
+  float s0, t1, s1, t2;
+  ef_two_sum(p0, p1, s0, t1);
+  ef_two_sum(s0, p2_, s1, t2);
+  float lo = __fadd_rn(__fadd_rn(e0, e1), __fadd_rn(e2, __fadd_rn(t1, t2)));
+  lo = __fmaf_rn(ah[0], bl[0], __fmaf_rn(al[0], bh[0], lo));
+  lo = __fmaf_rn(ah[1], bl[1], __fmaf_rn(al[1], bh[1], lo));
+  lo = __fmaf_rn(ah[2], bl[2], __fmaf_rn(al[2], bh[2], lo));
+  sh = __fadd_rn(s1, lo);
+  sl = __fsub_rn(lo, __fsub_rn(sh, s1));
+}
+
 // One centre atom's bonds.  NB is the number of bond slots held in registers (loops
 // fully unrolled when NB is small; cnt <= NB).
 //
@@ -348,12 +374,13 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
   const SysDesc &sd = a.A.sys[a.A.sysid[i]];
   double dxd[NB], dyd[NB], dzd[NB], r64[NB], ri64[NB], rs64[NB];
   R dx[NB], dy[NB], dz[NB], rf[NB], rl[NB];
+  float vh[NB][3], vl[NB][3];   // FP32 mode: delr as hi + lo parts
   int el[NB];
   uint32_t ev_[NB];
   // radial force on each partner (gx), three-body forces on each partner (tx), bond energy
   double gx[NB], gy[NB], gz[NB], ge[NB];
   R tx[NB], ty[NB], tz[NB];
-  double cs64[NB][NB];   // FP32 mode: cos(theta_jik) of each bond pair in FP64
+  float cq0[NB][NB], cq1[NB][NB];   // FP32 mode: cos(theta_jik) of each bond pair as hi + lo
   R uf[NB][NB];          // FP32 mode: h_ijk - cos(theta_jik)
   double fx = 0, fy = 0, fz = 0, eng = 0;
   double v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
@@ -363,26 +390,46 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
       const uint32_t e = a.ters_nb[(size_t)i * MAXTERS + s];
       int j, sx, sy, sz;
       decode_entry(e, a.lc, j, sx, sy, sz);
-      double ddx, ddy, ddz;
-      disp64(a.A.xq, sd, i, j, sx, sy, sz, ddx, ddy, ddz);
-      dxd[s] = -ddx; dyd[s] = -ddy; dzd[s] = -ddz;  // delr = x_j - x_i
-      const double rs = rsq_rn(ddx, ddy, ddz);
-      rs64[s] = rs;
       if constexpr (F32) {
-        const double ri = rsqrt_nr(rs);
-        const double r = rs * ri;
-        ri64[s] = ri;
-        r64[s] = r;
-        rf[s] = (R)r;
-        rl[s] = (R)(r - (double)rf[s]);
+        // delr = x_j(image) - x_i from the double-float position parts: the hi sum is
+        // exact (a small multiple of the hi parts' ulp, one FMA), the lo sum carries the
+        // rest; |delr| as an FP32 pair from a double-float dot and one Newton step
+        const float4 hi4 = a.A.xh[i], lo4 = a.A.xl[i];
+        const float4 hj = __ldg(&a.A.xh[j]), lj = __ldg(&a.A.xl[j]);
+        const float fsx = (float)sx, fsy = (float)sy, fsz = (float)sz;
+        vh[s][0] = __fmaf_rn(fsx, sd.Lhi[0], __fsub_rn(hj.x, hi4.x));
+        vh[s][1] = __fmaf_rn(fsy, sd.Lhi[1], __fsub_rn(hj.y, hi4.y));
+        vh[s][2] = __fmaf_rn(fsz, sd.Lhi[2], __fsub_rn(hj.z, hi4.z));
+        vl[s][0] = __fmaf_rn(fsx, sd.Llo[0], __fsub_rn(lj.x, lo4.x));
+        vl[s][1] = __fmaf_rn(fsy, sd.Llo[1], __fsub_rn(lj.y, lo4.y));
+        vl[s][2] = __fmaf_rn(fsz, sd.Llo[2], __fsub_rn(lj.z, lo4.z));
+        float sh, sl;
+        df_dot3(vh[s], vl[s], vh[s], vl[s], sh, sl);
+        const float ri0 = rsqrt_ftz(sh);
+        const float r0 = __fmul_rn(sh, ri0);
+        const float corr = __fmul_rn(__fadd_rn(__fmaf_rn(-r0, r0, sh), sl), __fmul_rn(0.5f, ri0));
+        const float rh = __fadd_rn(r0, corr);
+        rf[s] = rh;
+        rl[s] = __fsub_rn(corr, __fsub_rn(rh, r0));
+        ri64[s] = (double)__fmaf_rn(__fmul_rn(-corr, ri0), ri0, ri0);
+        dx[s] = __fadd_rn(vh[s][0], vl[s][0]);
+        dy[s] = __fadd_rn(vh[s][1], vl[s][1]);
+        dz[s] = __fadd_rn(vh[s][2], vl[s][2]);
+        dxd[s] = (double)dx[s]; dyd[s] = (double)dy[s]; dzd[s] = (double)dz[s];
+        el[s] = c_pot.t_map[info_type((long long)__float_as_int(hj.w))];
       } else {
+        double ddx, ddy, ddz;
+        disp64(a.A.xq, sd, i, j, sx, sy, sz, ddx, ddy, ddz);
+        dxd[s] = -ddx; dyd[s] = -ddy; dzd[s] = -ddz;  // delr = x_j - x_i
+        const double rs = rsq_rn(ddx, ddy, ddz);
+        rs64[s] = rs;
         r64[s] = sqrt(rs);
         ri64[s] = 0.0;
         rf[s] = r64[s];
         rl[s] = 0.0;
+        dx[s] = (R)dxd[s]; dy[s] = (R)dyd[s]; dz[s] = (R)dzd[s];
+        el[s] = c_pot.t_map[info_type(__double_as_longlong(a.A.xq[j].w))];
       }
-      dx[s] = (R)dxd[s]; dy[s] = (R)dyd[s]; dz[s] = (R)dzd[s];
-      el[s] = c_pot.t_map[info_type(__double_as_longlong(a.A.xq[j].w))];
       ev_[s] = e;
       gx[s] = gy[s] = gz[s] = ge[s] = 0.0;
       tx[s] = ty[s] = tz[s] = R(0);
@@ -394,9 +441,16 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
 #pragma unroll UNR
       for (int k = s + 1; k < NB; k++) {
         if (k < cnt) {
-          const double c = (dxd[s] * dxd[k] + dyd[s] * dyd[k] + dzd[s] * dzd[k]) * (ri64[s] * ri64[k]);
-          cs64[s][k] = c;
-          cs64[k][s] = c;
+          // cos = delr_s . delr_k / (r_s r_k) in double-float: q0 + q1
+          float Dh, Dl;
+          df_dot3(vh[s], vl[s], vh[k], vl[k], Dh, Dl);
+          const float nh = __fmul_rn(rf[s], rf[k]);
+          const float nl = __fmaf_rn(rf[s], rl[k], __fmaf_rn(rl[s], rf[k], __fmaf_rn(rf[s], rf[k], -nh)));
+          const float inv = rcp_ftz(nh);
+          const float q0 = __fmul_rn(Dh, inv);
+          const float q1 = __fmul_rn(__fadd_rn(__fmaf_rn(-q0, nh, Dh), __fmaf_rn(-q0, nl, Dl)), inv);
+          cq0[s][k] = cq0[k][s] = q0;
+          cq1[s][k] = cq1[k][s] = q1;
         }
       }
     }
@@ -407,8 +461,10 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
     if (s >= cnt) continue;
     const int je = el[s];
     const TersP<R> &pij = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + je];
-    const double r = r64[s];
     const R rR = rf[s];
+    // FP64 bond length: the FP64 path's own; the FP32 path needs it only inside the
+    // cut-off function's transition region
+    const double r = F32 ? (double)rf[s] + (double)rl[s] : r64[s];
     double fr = 0.0;   // radial force on i along delr, from both terms of this bond
     // ---- repulsion (:584-595) in FP64, from both ends of the bond, with the parameters
     // of the end the reference's half list keeps
@@ -461,7 +517,7 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
       R ex = pk.lam3 == R(0) ? R(1) : ters_exdelr(rR, rik, pk);
       R g;
       if constexpr (F32) {
-        uf[s][k] = (R)(pk.h64 - cs64[s][k]);
+        uf[s][k] = __fadd_rn(__fsub_rn(pk.hhi, cq0[s][k]), __fsub_rn(pk.hlo, cq1[s][k]));
         g = ters_g_u(uf[s][k], pk);
       } else {
         R cost = (dx[s] * dx[k] + dy[s] * dy[k] + dz[s] * dz[k]) / (rR * rik);

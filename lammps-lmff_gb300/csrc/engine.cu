@@ -642,6 +642,7 @@ struct Engine {
       if (P.i_map[t] >= 0) P.ilp_typemask |= 1u << t;
     P.vdw_sym = 1;
     P.rep_sym = 1;
+    P.ilp_cut_sym = 1;
     P.t_cutmaxsq = (R)(ht.cutmax * ht.cutmax);
     P.i_cutsq = (R)(cut_global * cut_global);
     P.i_inv_rcut = (R)(1.0 / cut_global);
@@ -694,6 +695,9 @@ struct Engine {
           if (!(q.C6 == s.C6 && q.d == s.d && q.seff == s.seff)) P.vdw_sym = 0;
           P.i_cutILPsq[a * MAXELEM + b] = (R)hi.cutILPsq[a * ne + b];
         }
+      for (int a = 0; a < ne; a++)
+        for (int b = 0; b < ne; b++)
+          if (!(hi.cutILPsq[a * ne + b] == hi.cutILPsq[b * ne + a])) P.ilp_cut_sym = 0;
     }
     if (t_on) {
       int ne = P.t_ne;

@@ -81,6 +81,7 @@ struct PotConst {
   int kc;                     // interlayer style is kolmogorov/crespi/full
   int vdw_sym;                // vdW constants symmetric in (i,j) for every pair
   int rep_sym;                // Tersoff repulsion constants of (i,j,j) equal those of (j,i,i)
+  int ilp_cut_sym;            // intralayer cutoffs symmetric in the element pair: j in N_ilp(i) <=> i in N_ilp(j)
   unsigned ilp_typemask;      // bit t set when atom type t is mapped to an ILP element
   R t_cutmaxsq;
   R i_cutsq;                  // cut_global^2

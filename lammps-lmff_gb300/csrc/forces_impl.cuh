@@ -1368,15 +1368,19 @@ __global__ void k_finish(ForceArgs<R> a) {
     }
   }
   if (a.do_ilp) {
-    const d4 q = a.A.xq[i];
-    const long long mi = info_mol(__double_as_longlong(q.w));
-    int cnt = a.short_cnt[i];
+    // the atoms j whose intralayer list holds i: with symmetric intralayer cutoffs they
+    // are i's own intralayer neighbours (the exact FP64 distance test is symmetric),
+    // otherwise any short candidate of the same molecule
+    const bool sym = c_pot.ilp_cut_sym != 0;
+    const int cnt = sym ? a.ilp_cnt[i] : a.short_cnt[i];
+    const uint32_t *cand = sym ? a.ilp_nb + (size_t)i * MAXILP : a.short_nb + (size_t)i * MAXSHORT;
+    const long long mi = sym ? 0 : info_mol(__double_as_longlong(a.A.xq[i].w));
     for (int c = 0; c < cnt; c++) {
       int j, sx, sy, sz;
-      decode_entry(a.short_nb[(size_t)i * MAXSHORT + c], a.lc, j, sx, sy, sz);
+      decode_entry(cand[c], a.lc, j, sx, sy, sz);
       int cj = a.ilp_cnt[j];
       if (cj == 0) continue;
-      if (info_mol(__double_as_longlong(a.A.xq[j].w)) != mi) continue;
+      if (!sym && info_mol(__double_as_longlong(a.A.xq[j].w)) != mi) continue;
       uint32_t want = encode_entry(i, -sx, -sy, -sz, a.lc);
       for (int t = 0; t < cj; t++) {
         if (a.ilp_nb[(size_t)j * MAXILP + t] == want) {

@@ -78,6 +78,21 @@ __global__ void k_check_ident(int n, const int *perm, const int *type, const int
   if (bad) atomicOr(flag, 1);
 }
 
+// Largest squared displacement of the block into *maxdisp (non-negative doubles order as
+// their bit patterns): one atomic per block on the shared word, not one per warp.  Every
+// thread of the block calls it.
+__device__ __forceinline__ void block_max_disp(double d2, unsigned long long *maxdisp) {
+  for (int o = 16; o > 0; o >>= 1) d2 = fmax(d2, __shfl_xor_sync(0xffffffff, d2, o));
+  __shared__ double wmax[32];
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = d2;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    d2 = threadIdx.x < (blockDim.x >> 5) ? wmax[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) d2 = fmax(d2, __shfl_xor_sync(0xffffffff, d2, o));
+    if (threadIdx.x == 0 && d2 > 0.0) atomicMax(maxdisp, (unsigned long long)__double_as_longlong(d2));
+  }
+}
+
 // new caller positions into sorted order + max squared displacement since the build
 // New caller positions into the resident state.  On periodic dimensions a position is
 // taken in the periodic image nearest the one the list was built with (the caller may
@@ -99,8 +114,7 @@ __global__ void k_update_x(int n, const int *perm, const double *x, d4 *xq, cons
     double dx = a - xhold[3 * q], dy = b - xhold[3 * q + 1], dz = c - xhold[3 * q + 2];
     d2 = dx * dx + dy * dy + dz * dz;
   }
-  for (int o = 16; o > 0; o >>= 1) d2 = fmax(d2, __shfl_xor_sync(0xffffffff, d2, o));
-  if ((threadIdx.x & 31) == 0 && d2 > 0.0) atomicMax(maxdisp, (unsigned long long)__double_as_longlong(d2));
+  block_max_disp(d2, maxdisp);
 }
 
 __global__ void k_scatter_add(int n, const int *perm, const double *fs, double *fin, int overwrite) {
@@ -209,8 +223,7 @@ __global__ void k_nve1(int n, d4 *xq, double *v, const double *f, DtfmTab tab, d
       xl[q] = make_float4((float)(X - (double)hx), (float)(Y - (double)hy), (float)(Z - (double)hz), 0.f);
     }
   }
-  for (int o = 16; o > 0; o >>= 1) d2 = fmax(d2, __shfl_xor_sync(0xffffffff, d2, o));
-  if ((threadIdx.x & 31) == 0 && d2 > 0.0) atomicMax(maxdisp, (unsigned long long)__double_as_longlong(d2));
+  block_max_disp(d2, maxdisp);
 }
 
 __global__ void k_nve2(int n, double *v, const double *f, const d4 *xq, const double *mass, DtfmTab tab, double *ke) {
@@ -323,8 +336,7 @@ __global__ void k_min_step(int n, const int *perm, const double *x0, const doubl
     double dx = a - xhold[3 * q], dy = b - xhold[3 * q + 1], dz = c - xhold[3 * q + 2];
     d2 = dx * dx + dy * dy + dz * dz;
   }
-  for (int o = 16; o > 0; o >>= 1) d2 = fmax(d2, __shfl_xor_sync(0xffffffff, d2, o));
-  if ((threadIdx.x & 31) == 0 && d2 > 0.0) atomicMax(maxdisp, (unsigned long long)__double_as_longlong(d2));
+  block_max_disp(d2, maxdisp);
 }
 
 // after a rebuild wrapped atoms into the box: x0 = x + minimum_image(x0 - x)

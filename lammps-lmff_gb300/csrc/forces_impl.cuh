@@ -93,7 +93,10 @@ __global__ void k_short(ForceArgs<R> a, const double *cutILPsq64, double tcutmax
         if (lt_exact(rsq, c_pot.i_cutILPsq[pe], a.A.xq, sd, i, j, sx, sy, sz, cutILPsq64[pe])) {
           if (nilp < MAXILP) {
             a.ilp_nb[(size_t)i * MAXILP + nilp] = e;
-            vx[nilp] = -dx; vy[nilp] = -dy; vz[nilp] = -dz;
+            // constant indices keep the bond vectors in registers
+#pragma unroll
+            for (int q = 0; q < MAXILP; q++)
+              if (q == nilp) { vx[q] = -dx; vy[q] = -dy; vz[q] = -dz; }
           }
           nilp++;
         }

@@ -49,9 +49,9 @@ ILP_FILE = os.path.join(ROOT, "lammps-lmff_gb300", "potentials", "BNCH.ILP")
 # FMA = 2).  A list candidate outside the cutoff costs the displacement, r^2 and the
 # test: 9.  `roofline.achieved` uses these.
 # DRAM bytes per pair-list entry of the mixed pair kernel, from one ncu capture of the
-# 331,200-atom graphite slab (k_ilp<8,0,0,1,0,0>: 1.327 GB read + 30.6 MB written for
+# 331,200-atom graphite slab (k_ilp<8,0,0,1,0,0>: 1.303 GB read + 19.7 MB written for
 # 310,301,280 entries; the list is larger than L2, so traffic grows with the entries)
-K_ILP_DRAM_BYTES_PER_ENTRY = (1.327362e9 + 30.629632e6) / 310301280
+K_ILP_DRAM_BYTES_PER_ENTRY = (1.302568e9 + 19.73888e6) / 310301280
 ALG_FLOPS_PER_PAIR = 120
 ALG_FLOPS_PER_REJECTED = 9
 # What the gather kernel executes per directed pair (both repulsion terms and the full
@@ -498,7 +498,7 @@ def main():
                 "frac": achieved / peak if peak else None,
                 "traffic": K_ILP_DRAM_BYTES_PER_ENTRY * cands if prec == capi.MIXED else None,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_ilp launch on the "
-                                  "331,200-atom slab (1.358 GB for 310.3 M list entries), scaled by list entries",
+                                  "331,200-atom slab (1.322 GB for 310.3 M list entries), scaled by list entries",
                 "kernel": "k_ilp (pair kernel)", "kernel_ms_avg": k_avg * 1e3,
                 "peak_source": f"cuBLAS {peak_name.upper()} GEMM measured in this run (SIMT; MEASURED_PEAKS.json has "
                                f"HBM {peaks.get('hbm_gbs')} GB/s and bf16 tensor only)",

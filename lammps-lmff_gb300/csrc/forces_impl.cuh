@@ -712,6 +712,11 @@ __device__ __forceinline__ void rep_term(const IlpP<R> &p, R exp0, R exp1, R rho
 }
 
 // One list entry (i, j, image) with j's position and normal already loaded.
+// Multi-element pair parameters, copied into shared memory by each block of k_ilp: lanes
+// index them by their own element pair, which in constant memory would serialise (one
+// constant-cache access per distinct address in a warp).
+__shared__ IlpP<R> s_ilp[MAXELEM * MAXELEM];
+
 // IMG: the entry may carry a periodic image shift (false: every entry of i's list is
 // unshifted, and the image decode and shift are left out)
 template <bool EV, bool ONE, bool KC, bool IMG>
@@ -730,8 +735,8 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
   const int tj = info_type(jinfo);
   if (check && !((c_pot.ilp_typemask >> tj) & 1u)) return;
   const int je = ONE ? 0 : c_pot.i_map[tj];
-  const IlpP<R> &pij = ONE ? c_pot.ilp[0] : c_pot.ilp[ie * MAXELEM + je];
-  const IlpP<R> &pji = ONE ? c_pot.ilp[0] : c_pot.ilp[je * MAXELEM + ie];
+  const IlpP<R> &pij = ONE ? c_pot.ilp[0] : s_ilp[ie * MAXELEM + je];
+  const IlpP<R> &pji = ONE ? c_pot.ilp[0] : s_ilp[je * MAXELEM + ie];
   const R njx = N.q.x, njy = N.q.y, njz = N.q.z;
   R r, rinv;
   if constexpr (sizeof(R) == 8) { r = sqrt(rsq); rinv = R(1) / r; }
@@ -863,8 +868,8 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
   const int tj = info_type(jinfo);
   if (check && !((c_pot.ilp_typemask >> tj) & 1u)) return;
   const int je = ONE ? 0 : c_pot.i_map[tj];
-  const IlpP<float> &pij = ONE ? c_pot.ilp[0] : c_pot.ilp[ie * MAXELEM + je];
-  const IlpP<float> &pji = ONE ? c_pot.ilp[0] : c_pot.ilp[je * MAXELEM + ie];
+  const IlpP<float> &pij = ONE ? c_pot.ilp[0] : s_ilp[ie * MAXELEM + je];
+  const IlpP<float> &pji = ONE ? c_pot.ilp[0] : s_ilp[je * MAXELEM + ie];
   const float dx = dxy.x, dy = dxy.y;
   const float njx = N.q.x, njy = N.q.y, njz = N.q.z;
   const float rinv = rsqrt_ftz(rsq);
@@ -1128,6 +1133,13 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
   }
   // a list without list_full holds only interlayer pairs of ILP-mapped types (k_list)
   const bool check = a.list_full != 0;
+  if constexpr (!ONE) {
+    const int words = (int)(sizeof(c_pot.ilp) / sizeof(int));
+    const int *src = reinterpret_cast<const int *>(c_pot.ilp);
+    int *dst = reinterpret_cast<int *>(s_ilp);
+    for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+    __syncthreads();
+  }
   if (valid && ie >= 0) {
     const int64_t b = a.list_off[i];
     const uint32_t *lst = a.list + b;

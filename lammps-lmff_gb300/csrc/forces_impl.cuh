@@ -148,7 +148,8 @@ __global__ void k_short(ForceArgs<R> a, const double *cutILPsq64, double tcutmax
   a.jrec[3 * (size_t)i + 1] = make_float4(ai.lx, ai.ly, ai.lz, 0.f);
   a.jrec[3 * (size_t)i + 2] = make_float4(nx, ny, nz, 0.f);
   a.jrec2[2 * (size_t)i] = make_float4(ai.hx, ai.hy, ai.hz, __uint_as_float(h2_bits(__floats2half2_rn(ai.lx, ai.ly))));
-  a.jrec2[2 * (size_t)i + 1] = make_float4(nx, ny, nz, __uint_as_float(h2_bits(__floats2half2_rn(ai.lz, 0.f))));
+  a.jrec2[2 * (size_t)i + 1] = make_float4(
+      nx, ny, nz, __uint_as_float((h2_bits(__floats2half2_rn(ai.lz, 0.f)) & 0xffffu) | ((unsigned)(ie & 0xffff) << 16)));
 #else
   a.nrm64[i] = make_d4(nx, ny, nz, 0.0);
 #endif
@@ -839,6 +840,18 @@ struct PairX2Const {
 };
 __constant__ PairX2Const c_x2;
 
+// Multi-element two-pair body: for atom element a and the elements b, c of the two
+// neighbours of one iteration, the parameter pairs (X[a][b], X[a][c]) of every per-pair
+// constant, one 64-bit shared-memory read each.  Valid when every element pair's
+// parameters equal those of the swapped pair (then both repulsion terms and vdW use
+// X[a][b]) and C >= 0 (c_pair2_multi, set by upload_pot).
+constexpr int X2M_N = 11;   // nd2_l2e, log2C, eps, 2/delta^2, lambda, -lam log2e, lam z0 log2e,
+                            // -ts_a, ts_a seff, C6, d/seff
+constexpr int X2M_ROWS = MAXELEM * MAXELEM * MAXELEM;
+__device__ float2 g_x2m[X2M_ROWS * X2M_N];
+__shared__ float2 s_x2m[X2M_ROWS * X2M_N];
+__constant__ int c_pair2_multi;
+
 template <bool EV, bool ONE, bool KC, bool IMG>
 __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const AtomI<float> &ai, const SysDesc &sdl,
                                             uint32_t e, const AtomI<float>::J &J, const NrmJ<float> &N, float nix,
@@ -1005,12 +1018,27 @@ __device__ __forceinline__ void disp_x2(const ForceArgs<float> &a, const AtomI<f
   dxy = add2(hxy, lxy);
 }
 
-// bvalid = false: only pair A exists (B repeats A and contributes nothing)
-template <bool IMG>
-__device__ __forceinline__ void ilp_pair2_one(const ForceArgs<float> &a, const AtomI<float> &ai, const float3 &loi,
-                                              const SysDesc &sdl, uint32_t eA, const float4 &A0, const float4 &A1,
-                                              uint32_t eB, const float4 &B0, const float4 &B1, bool bvalid, float nix,
-                                              float niy, float niz, IlpAcc &acc) {
+// a per-pair constant pair: element 0's from constant memory (ONE, by value, so that the
+// load keeps its constant address space) or the shared-memory row's
+template <bool ONE>
+__device__ __forceinline__ float2 x2sel(float2 c, const float2 *prow, int k) {
+  if constexpr (ONE) return c;
+  else return prow[k];
+}
+
+// bvalid = false: only pair A exists (B repeats A and contributes nothing).  ONE: the
+// constants of element 0 from constant memory; otherwise the (ie, jeA, jeB) row of s_x2m
+// (the neighbours' elements travel in the upper half of their record's r1.w).
+template <bool ONE, bool IMG>
+__device__ __forceinline__ void ilp_pair2(const ForceArgs<float> &a, const AtomI<float> &ai, const float3 &loi,
+                                          const SysDesc &sdl, uint32_t eA, const float4 &A0, const float4 &A1,
+                                          uint32_t eB, const float4 &B0, const float4 &B1, bool bvalid, float nix,
+                                          float niy, float niz, int ie, IlpAcc &acc) {
+  const float2 *prow = nullptr;
+  if constexpr (!ONE)
+    prow = s_x2m + ((ie * MAXELEM + (int)(__float_as_uint(A1.w) >> 16)) * MAXELEM + (int)(__float_as_uint(B1.w) >> 16)) *
+                       X2M_N;
+#define X2(field, k) x2sel<ONE>(c_x2.field, prow, k)
   float2 dA, dB;
   float dzA, dzB;
   disp_x2<IMG>(a, ai, loi, sdl, eA, A0, A1, dA, dzA);
@@ -1041,13 +1069,13 @@ __device__ __forceinline__ void ilp_pair2_one(const ForceArgs<float> &a, const A
   // ---- vdW: V = -C6 r^-6 / TS, TS = 1 + e^{-d (r/seff - 1)}
   const float2 R2I = mul2(RINV, RINV);
   const float2 R6I = mul2(mul2(R2I, R2I), R2I);
-  const float2 EXA = fma2(R, c_x2.nts_a, c_x2.ts_a_seff);
+  const float2 EXA = fma2(R, X2(nts_a, 7), X2(ts_a_seff, 8));
   const float2 EX = p2(ex2_ftz(EXA.x), ex2_ftz(EXA.y));
   const float2 TSV = add2(EX, c_x2.one);
   const float2 TSI = p2(rcp_ftz(TSV.x), rcp_ftz(TSV.y));
-  const float2 C6T = mul2(c_x2.C6, TSI);
+  const float2 C6T = mul2(X2(C6, 9), TSI);
   const float2 C6R6 = mul2(C6T, R6I);                       // -V
-  const float2 G = fma2(mul2(mul2(EX, TSI), R), c_x2.d_over_seff, c_x2.m6);
+  const float2 G = fma2(mul2(mul2(EX, TSI), R), X2(d_over_seff, 10), c_x2.m6);
   const float2 FPV = mul2(mul2(C6R6, R2I), G);
   const float2 FSUMV = fma2(FPV, TAP, mul2(C6R6, DR));      // fpv Tap - V dTap / r
   // ---- repulsion, terms (i,j) with n_i and (j,i) with n_j
@@ -1057,16 +1085,16 @@ __device__ __forceinline__ void ilp_pair2_one(const ForceArgs<float> &a, const A
   const float2 RHJ = fma2(p2(-PQJ.x, -PQJ.y), PQJ, RSQ);
   // V_t = E0 (eps/2 + C e^{-rho_t^2/delta^2}), fpair1_t = 2 E0 C e^{...} / delta^2, and the
   // radial factor of both terms together, lambda (V_i + V_j) / r + fpair1_i + fpair1_j
-  const float2 E0A = fma2(R, c_x2.nlam_l2e, c_x2.lamz0_l2e);
+  const float2 E0A = fma2(R, X2(nlam_l2e, 5), X2(lamz0_l2e, 6));
   const float2 E0 = p2(ex2_ftz(E0A.x), ex2_ftz(E0A.y));
-  const float2 EIA = fma2(c_x2.nd2_l2e, RHI, c_x2.log2C), EJA = fma2(c_x2.nd2_l2e, RHJ, c_x2.log2C);
+  const float2 EIA = fma2(X2(nd2_l2e, 0), RHI, X2(log2C, 1)), EJA = fma2(X2(nd2_l2e, 0), RHJ, X2(log2C, 1));
   const float2 E0FI = mul2(E0, p2(ex2_ftz(EIA.x), ex2_ftz(EIA.y)));
   const float2 E0FJ = mul2(E0, p2(ex2_ftz(EJA.x), ex2_ftz(EJA.y)));
   const float2 S = add2(E0FI, E0FJ);
-  const float2 VS = fma2(E0, c_x2.eps, S);
-  const float2 FSS = fma2(mul2(c_x2.lambda, RINV), VS, mul2(S, c_x2.d2x2));
-  const float2 TPQI = mul2(mul2(TAP, PQI), mul2(E0FI, c_x2.d2x2));
-  const float2 TPQJ = mul2(mul2(TAP, PQJ), mul2(E0FJ, c_x2.d2x2));
+  const float2 VS = fma2(E0, X2(eps, 2), S);
+  const float2 FSS = fma2(mul2(X2(lambda, 4), RINV), VS, mul2(S, X2(d2x2, 3)));
+  const float2 TPQI = mul2(mul2(TAP, PQI), mul2(E0FI, X2(d2x2, 3)));
+  const float2 TPQJ = mul2(mul2(TAP, PQJ), mul2(E0FJ, X2(d2x2, 3)));
   const float2 CRAD = fma2(p2(-VS.x, -VS.y), DR, fma2(FSS, TAP, FSUMV));
   // ---- force on i and g_i
   acc.fx += CRAD.x * dA.x - TPQI.x * nix - TPQJ.x * A1.x;
@@ -1081,6 +1109,7 @@ __device__ __forceinline__ void ilp_pair2_one(const ForceArgs<float> &a, const A
   acc.gxa += TPQI.y * dB.x;
   acc.gya += TPQI.y * dB.y;
   acc.gza += TPQI.y * dzB;
+#undef X2
 }
 #endif  // LMFF_PACKED_X2
 
@@ -1103,7 +1132,7 @@ __device__ __forceinline__ void pair_body(const ForceArgs<R> &a, const AtomI<R> 
 // measured 3 % faster than 3 blocks at 2.7M atoms.  FP64 keeps its registers.
 template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC>
 constexpr int ilp_min_blocks() {
-  return sizeof(R) == 8 ? 1 : (TWO_PAIR_BODY && ONE && !EV && !KC) ? 4 : 5;
+  return sizeof(R) == 8 ? 1 : (TWO_PAIR_BODY && !EV && !KC) ? 4 : 5;
 }
 
 template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC>
@@ -1138,6 +1167,10 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
     const int *src = reinterpret_cast<const int *>(c_pot.ilp);
     int *dst = reinterpret_cast<int *>(s_ilp);
     for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+#ifdef LMFF_PACKED_X2
+    if (TWO_PAIR_BODY && !EV && !KC && c_pair2_multi)
+      for (int w = threadIdx.x; w < X2M_ROWS * X2M_N; w += blockDim.x) s_x2m[w] = g_x2m[w];
+#endif
     __syncthreads();
   }
   if (valid && ie >= 0) {
@@ -1149,8 +1182,8 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
     auto run = [&](auto img_t) {
       constexpr bool IMG = decltype(img_t)::value;
 #ifdef LMFF_PACKED_X2
-      if constexpr (TWO_PAIR_BODY && ONE && !EV && !KC) {
-        if (!check && c_pot.ilp[0].C >= 0.f) {
+      if constexpr (TWO_PAIR_BODY && !EV && !KC) {
+        if (!check && (ONE ? c_pot.ilp[0].C >= 0.f : c_pair2_multi != 0)) {
           // two entries (k, k + TPA) per iteration, loaded one iteration ahead, j's data
           // from the compact 32-byte records
           const float3 loi = make_float3(__half2float(__float2half_rn(ai.lx)), __half2float(__float2half_rn(ai.ly)),
@@ -1163,13 +1196,13 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
             if (k + 2 * TPA < cnt) eA = __ldg(&lst[k + 2 * TPA]);
             if (k + 3 * TPA < cnt) eB = __ldg(&lst[k + 3 * TPA]);
             const size_t ja = 2 * (size_t)(ea & a.lc.imask), jb = 2 * (size_t)(eb & a.lc.imask);
-            ilp_pair2_one<IMG>(a, ai, loi, sdl, ea, __ldg(&a.A.jrec2[ja]), __ldg(&a.A.jrec2[ja + 1]), eb,
-                               __ldg(&a.A.jrec2[jb]), __ldg(&a.A.jrec2[jb + 1]), true, nix, niy, niz, acc);
+            ilp_pair2<ONE, IMG>(a, ai, loi, sdl, ea, __ldg(&a.A.jrec2[ja]), __ldg(&a.A.jrec2[ja + 1]), eb,
+                                __ldg(&a.A.jrec2[jb]), __ldg(&a.A.jrec2[jb + 1]), true, nix, niy, niz, ie, acc);
           }
           if (k < cnt) {
             const size_t ja = 2 * (size_t)(eA & a.lc.imask);
             const float4 r0 = __ldg(&a.A.jrec2[ja]), r1 = __ldg(&a.A.jrec2[ja + 1]);
-            ilp_pair2_one<IMG>(a, ai, loi, sdl, eA, r0, r1, eA, r0, r1, false, nix, niy, niz, acc);
+            ilp_pair2<ONE, IMG>(a, ai, loi, sdl, eA, r0, r1, eA, r0, r1, false, nix, niy, niz, ie, acc);
           }
           return;
         }
@@ -1472,6 +1505,39 @@ void upload_pot(const PotConst<R> &p, cudaStream_t s) {
     x2.log2C = make_float2(l2c, l2c);
     x2.eps = make_float2(2.f * q.eps_half, 2.f * q.eps_half);
     cudaMemcpyToSymbolAsync(c_x2, &x2, sizeof(x2), 0, cudaMemcpyHostToDevice, s);
+    // kept out of PotConst: growing c_pot changes the single-element pair kernel's
+    // register allocation (measured: a spill and -2 %)
+    static int p2m;
+    p2m = (p.i_enabled && !p.kc && p.vdw_sym) ? 1 : 0;
+    for (int ea = 0; ea < p.i_ne; ea++)
+      for (int eb = 0; eb < p.i_ne; eb++) {
+        const IlpP<float> &o = p.ilp[ea * MAXELEM + eb];
+        if (!o.same_as_swapped || !(o.C >= 0.f)) p2m = 0;
+      }
+    cudaMemcpyToSymbolAsync(c_pair2_multi, &p2m, sizeof(p2m), 0, cudaMemcpyHostToDevice, s);
+    if (p2m) {
+      static float2 tab[X2M_ROWS * X2M_N];
+      for (int ea = 0; ea < MAXELEM; ea++)
+        for (int eb = 0; eb < MAXELEM; eb++)
+          for (int ec = 0; ec < MAXELEM; ec++) {
+            const IlpP<float> &u = p.ilp[ea * MAXELEM + eb], &v = p.ilp[ea * MAXELEM + ec];
+            auto two = [](float x, float y) { return make_float2(x, y); };
+            auto l2c = [](float c) { return c > 0.f ? (float)std::log2((double)c) : -INFINITY; };
+            float2 *t = tab + ((ea * MAXELEM + eb) * MAXELEM + ec) * X2M_N;
+            t[0] = two(u.nd2_l2e, v.nd2_l2e);
+            t[1] = two(l2c(u.C), l2c(v.C));
+            t[2] = two(2.f * u.eps_half, 2.f * v.eps_half);
+            t[3] = two(2.f * u.delta2inv, 2.f * v.delta2inv);
+            t[4] = two(u.lambda, v.lambda);
+            t[5] = two(-u.lam_l2e, -v.lam_l2e);
+            t[6] = two(u.lamz0_l2e, v.lamz0_l2e);
+            t[7] = two(-u.ts_a, -v.ts_a);
+            t[8] = two(u.ts_a * u.seff, v.ts_a * v.seff);
+            t[9] = two(u.C6, v.C6);
+            t[10] = two(u.d_over_seff, v.d_over_seff);
+          }
+      cudaMemcpyToSymbolAsync(g_x2m, tab, sizeof(tab), 0, cudaMemcpyHostToDevice, s);
+    }
   }
 #endif
   if (sizeof(R) == 4) k_fill_exptab<<<EXP_TAB_N / 256, 256, 0, s>>>();

@@ -115,6 +115,21 @@ def test_mixed_forces_without_energy_large():
     assert np.abs(rf["f"] - re["f"]).max() <= MIX_F_ABS
 
 
+def test_mixed_forces_without_energy_hetero_large():
+    """Force-only mixed evaluation of a displaced graphene/hBN twisted bilayer (the
+    multi-element loop with two list entries per iteration) against the FP64 engine."""
+    # a 2,640-atom cell (most atoms near a periodic face: the image-decoding loop) and the
+    # 489,632-atom 0.6 degree cell (mostly the loop without image decode)
+    for s in (S.displace(S.twisted_bilayer(24, 14, 0.9, top="hbn"), 0.03, seed=6),
+              S.displace(S.twisted_graphene_hbn_500k(seed=2), 0.03, seed=7)):
+        r64 = capi.Engine(TERSOFF, ILP).compute_system(s, eflag=False, vflag=False)
+        for tpa in (8, 16):
+            eng = capi.Engine(TERSOFF, ILP, precision=capi.MIXED)
+            eng.set_option("tpa", tpa)
+            rf = eng.compute_system(s, eflag=False, vflag=False)
+            assert np.abs(rf["f"] - r64["f"]).max() <= MIX_F_ABS, (s.n, tpa)
+
+
 def test_nve_trajectory_matches_reference():
     """100 velocity-Verlet steps of the 7,200-atom bilayer, device resident, vs the
     reference's own trajectory from the same start."""

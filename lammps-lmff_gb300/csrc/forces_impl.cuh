@@ -713,6 +713,53 @@ __device__ __forceinline__ void rep_term(const IlpP<R> &p, R exp0, R exp1, R rho
 }
 
 // One list entry (i, j, image) with j's position and normal already loaded.
+// ---- FP64 pair-kernel arithmetic (the plain form): the FP64 pipe runs at 1/64 of the FP32
+// rate, so the exponentials, the square root and the divisions of a pair are written
+// with fewer FP64 instructions at full double accuracy (results within a few ulp of the
+// library functions, far inside the 1e-10 parity bar).
+//
+// e^x by Tang's table-driven method (P. T. P. Tang, ACM TOMS 15, 1989): n = rint(64 x /
+// ln2), r = x - n ln2/64 (|r| <= ln2/128; one FMA with ln2/64 rounded to double costs
+// at most |n| 2^-60 absolute, below 1e-14 relative for |x| < 700), e^x = 2^(n>>6)
+// 2^((n&63)/64) (1 + p(r)), p the degree-6 Taylor polynomial of e^r - 1 (truncation
+// below 1e-19).  Outside |x| < 700 the library exp.
+__device__ double g_exp2_64[64];
+
+__global__ void k_fill_exp2_64() {
+  const int j = threadIdx.x;
+  if (j < 64) g_exp2_64[j] = exp2((double)j / 64.0);
+}
+
+__device__ __forceinline__ double exp_t64(double x) {
+  if (!(fabs(x) < 700.0)) return exp(x);
+  const double magic = 6755399441055744.0;   // 1.5 * 2^52
+  const double tn = __dadd_rn(x * 92.332482616893657, magic);   // 64 / ln2
+  const int n = __double2loint(tn);
+  const double nd = __dsub_rn(tn, magic);
+  const double r = fma(-nd, 0.010830424696249145, x);             // ln2 / 64
+  double p = fma(r, 1.0 / 720.0, 1.0 / 120.0);
+  p = fma(p, r, 1.0 / 24.0);
+  p = fma(p, r, 1.0 / 6.0);
+  p = fma(p, r, 0.5);
+  p = fma(p, r, 1.0);
+  p = p * r;
+  const double T = __ldg(&g_exp2_64[n & 63]);
+  const double v = fma(T, p, T);
+  return __hiloint2double(__double2hiint(v) + (int)((unsigned)(n >> 6) << 20), __double2loint(v));
+}
+
+// 1/sqrt(x), 1/x: FP32 estimates and two FP64 Newton steps
+__device__ __forceinline__ double rsqrt_nr2(double x) {
+  double y = (double)rsqrt_ftz((float)x);
+  y = fma(0.5 * y, fma(-(x * y), y, 1.0), y);
+  return fma(0.5 * y, fma(-(x * y), y, 1.0), y);
+}
+__device__ __forceinline__ double rcp_nr2(double x) {
+  double y = (double)rcp_ftz((float)x);
+  y = fma(y, fma(-x, y, 1.0), y);
+  return fma(y, fma(-x, y, 1.0), y);
+}
+
 // Multi-element pair parameters, copied into shared memory by each block of k_ilp: lanes
 // index them by their own element pair, which in constant memory would serialise (one
 // constant-cache access per distinct address in a warp).
@@ -740,7 +787,7 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
   const IlpP<R> &pji = ONE ? c_pot.ilp[0] : s_ilp[je * MAXELEM + ie];
   const R njx = N.q.x, njy = N.q.y, njz = N.q.z;
   R r, rinv;
-  if constexpr (sizeof(R) == 8) { r = sqrt(rsq); rinv = R(1) / r; }
+  if constexpr (sizeof(R) == 8) { rinv = rsqrt_nr2(rsq); r = rsq * rinv; }
   else { rinv = rsqrt_ftz(rsq); r = rsq * rinv; }
   // taper (pair_ilp_graphene_hbn.h:80-115), Tap and dTap in one pass
   R Tap = 1, dTap = 0;
@@ -772,24 +819,43 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
     Vvdw = -pv.kc_Az06 * r6inv;
     fpv = R(-6) * pv.kc_Az06 * r8inv;
   } else {
-    R TSvdw = R(1) + Math<R>::exp_ts(pv, r);
-    R TSinv = Math<R>::rcp(TSvdw);
+    R TSvdw, TSinv;
+    if constexpr (sizeof(R) == 8) {
+      // exp(-d (r/seff - 1)) = exp(d - (d/seff) r)
+      TSvdw = R(1) + exp_t64(fma(-pv.d_over_seff, r, pv.d));
+      TSinv = rcp_nr2(TSvdw);
+    } else {
+      TSvdw = R(1) + Math<R>::exp_ts(pv, r);
+      TSinv = Math<R>::rcp(TSvdw);
+    }
     Vvdw = -pv.C6 * r6inv * TSinv;
-    fpv = R(-6) * pv.C6 * r8inv * TSinv + pv.C6 * pv.d_over_seff * (TSvdw - R(1)) * TSinv * TSinv * r8inv * r;
+    fpv = pv.C6 * r8inv * TSinv * (R(-6) + pv.d_over_seff * (TSvdw - R(1)) * TSinv * r);
   }
   R fsum_v = fpv * Tap - Vvdw * dTap * rinv;
   // ---- repulsion of term (i,j) with n_i
   R p = nix * dx + niy * dy + niz * dz;
   R rhosq = rsq - p * p;
-  R exp0 = Math<R>::exp_rep0(pij, r);
-  R exp1 = Math<R>::exp_rep1(pij, rhosq);
+  R exp0, exp1;
+  if constexpr (sizeof(R) == 8) {
+    exp0 = exp_t64(-pij.lambda * (r - pij.z0));
+    exp1 = exp_t64(-(rhosq * pij.delta2inv));
+  } else {
+    exp0 = Math<R>::exp_rep0(pij, r);
+    exp1 = Math<R>::exp_rep1(pij, rhosq);
+  }
   R V, fpair1, fsum;
   rep_term<KC>(pij, exp0, exp1, rhosq, rinv, V, fpair1, fsum);
   // ---- repulsion of term (j,i) with n_j (del' = -del, prod' = -q)
   R q = njx * dx + njy * dy + njz * dz;
   R rhosq2 = rsq - q * q;
-  R exp0b = pji.same_as_swapped ? exp0 : Math<R>::exp_rep0(pji, r);
-  R exp1b = Math<R>::exp_rep1(pji, rhosq2);
+  R exp0b, exp1b;
+  if constexpr (sizeof(R) == 8) {
+    exp0b = pji.same_as_swapped ? exp0 : exp_t64(-pji.lambda * (r - pji.z0));
+    exp1b = exp_t64(-(rhosq2 * pji.delta2inv));
+  } else {
+    exp0b = pji.same_as_swapped ? exp0 : Math<R>::exp_rep0(pji, r);
+    exp1b = Math<R>::exp_rep1(pji, rhosq2);
+  }
   R V2, fpair1b, fsum2;
   rep_term<KC>(pji, exp0b, exp1b, rhosq2, rinv, V2, fpair1b, fsum2);
   // ---- force on i
@@ -1469,6 +1535,7 @@ __global__ void k_ters_eatom_own(ForceArgs<R> a) {
 
 void upload_pot(const PotConst<R> &p, cudaStream_t s) {
   cudaMemcpyToSymbolAsync(c_pot, &p, sizeof(p), 0, cudaMemcpyHostToDevice, s);
+  if (sizeof(R) == 8) k_fill_exp2_64<<<1, 64, 0, s>>>();
 #ifdef LMFF_PACKED_X2
   {
     static PairX2Const x2;   // static: the asynchronous copy reads it after return

@@ -792,21 +792,14 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
   // taper (pair_ilp_graphene_hbn.h:80-115), Tap and dTap in one pass
   R Tap = 1, dTap = 0;
   if (c_pot.tap) {
-    R x = r * c_pot.i_inv_rcut;
+    // Tap = 1 + x^4 (((20x - 70)x + 84)x - 35); dTap/dx = 140 x^3 (x - 1)^3
+    const R x = r * c_pot.i_inv_rcut, x2 = x * x;
     Tap = R(20) * x + R(-70);
     Tap = Tap * x + R(84);
     Tap = Tap * x + R(-35);
-    Tap = Tap * x;
-    Tap = Tap * x;
-    Tap = Tap * x;
-    Tap = Tap * x + R(1);
-    R dT = R(140) * x + R(-420);
-    dT = dT * x + R(420);
-    dT = dT * x + R(-140);
-    dT = dT * x;
-    dT = dT * x;
-    dT = dT * x;
-    dTap = dT * c_pot.i_inv_rcut;
+    Tap = Tap * (x2 * x2) + R(1);
+    const R y = x2 - x;
+    dTap = (y * y) * (y * (R(140) * c_pot.i_inv_rcut));
   }
   // ---- vdW (both ends evaluate the pair force; energy halved)
   const IlpP<R> &pv = (c_pot.vdw_sym || keep_half(itag, a.tag[j], sx, sy, sz)) ? pij : pji;

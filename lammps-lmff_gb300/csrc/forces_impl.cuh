@@ -825,36 +825,50 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
     fpv = pv.C6 * r8inv * TSinv * (R(-6) + pv.d_over_seff * (TSvdw - R(1)) * TSinv * r);
   }
   R fsum_v = fpv * Tap - Vvdw * dTap * rinv;
-  // ---- repulsion of term (i,j) with n_i
+  // ---- repulsion of term (i,j) with n_i and of term (j,i) with n_j (del' = -del, prod' = -q)
   R p = nix * dx + niy * dy + niz * dz;
   R rhosq = rsq - p * p;
-  R exp0, exp1;
-  if constexpr (sizeof(R) == 8) {
-    exp0 = exp_t64(-pij.lambda * (r - pij.z0));
-    exp1 = exp_t64(-(rhosq * pij.delta2inv));
-  } else {
-    exp0 = Math<R>::exp_rep0(pij, r);
-    exp1 = Math<R>::exp_rep1(pij, rhosq);
-  }
-  R V, fpair1, fsum;
-  rep_term<KC>(pij, exp0, exp1, rhosq, rinv, V, fpair1, fsum);
-  // ---- repulsion of term (j,i) with n_j (del' = -del, prod' = -q)
   R q = njx * dx + njy * dy + njz * dz;
   R rhosq2 = rsq - q * q;
-  R exp0b, exp1b;
-  if constexpr (sizeof(R) == 8) {
-    exp0b = pji.same_as_swapped ? exp0 : exp_t64(-pji.lambda * (r - pji.z0));
-    exp1b = exp_t64(-(rhosq2 * pji.delta2inv));
+  R V, fpair1, fsum, V2, fpair1b, fsum2, crad;
+  if constexpr (sizeof(R) == 8 && !KC) {
+    // F = E0 C e^{-rho^2/delta^2}: V = E0 eps/2 + F, fpair1 = 2 F / delta^2, and both
+    // terms' radial factors lambda V / r + fpair1 go into crad together
+    const R exp0 = exp_t64(-pij.lambda * (r - pij.z0));
+    const R exp0b = pji.same_as_swapped ? exp0 : exp_t64(-pji.lambda * (r - pji.z0));
+    const R F1 = (exp0 * pij.C) * exp_t64(-(rhosq * pij.delta2inv));
+    const R F2 = (exp0b * pji.C) * exp_t64(-(rhosq2 * pji.delta2inv));
+    V = fma(exp0, pij.eps_half, F1);
+    V2 = fma(exp0b, pji.eps_half, F2);
+    fpair1 = R(2) * (F1 * pij.delta2inv);
+    fpair1b = R(2) * (F2 * pji.delta2inv);
+    const R Tr = Tap * rinv, dTr = dTap * rinv;
+    crad = fsum_v + Tap * (fpair1 + fpair1b) + fma(Tr, pij.lambda, -dTr) * V + fma(Tr, pji.lambda, -dTr) * V2;
+    if (EV) fsum = pij.lambda * rinv * V + fpair1;
   } else {
-    exp0b = pji.same_as_swapped ? exp0 : Math<R>::exp_rep0(pji, r);
-    exp1b = Math<R>::exp_rep1(pji, rhosq2);
+    R exp0, exp1;
+    if constexpr (sizeof(R) == 8) {
+      exp0 = exp_t64(-pij.lambda * (r - pij.z0));
+      exp1 = exp_t64(-(rhosq * pij.delta2inv));
+    } else {
+      exp0 = Math<R>::exp_rep0(pij, r);
+      exp1 = Math<R>::exp_rep1(pij, rhosq);
+    }
+    rep_term<KC>(pij, exp0, exp1, rhosq, rinv, V, fpair1, fsum);
+    R exp0b, exp1b;
+    if constexpr (sizeof(R) == 8) {
+      exp0b = pji.same_as_swapped ? exp0 : exp_t64(-pji.lambda * (r - pji.z0));
+      exp1b = exp_t64(-(rhosq2 * pji.delta2inv));
+    } else {
+      exp0b = pji.same_as_swapped ? exp0 : Math<R>::exp_rep0(pji, r);
+      exp1b = Math<R>::exp_rep1(pji, rhosq2);
+    }
+    rep_term<KC>(pji, exp0b, exp1b, rhosq2, rinv, V2, fpair1b, fsum2);
+    crad = fsum_v + (fsum + fsum2) * Tap - (V + V2) * dTap * rinv;
   }
-  R V2, fpair1b, fsum2;
-  rep_term<KC>(pji, exp0b, exp1b, rhosq2, rinv, V2, fpair1b, fsum2);
   // ---- force on i
   R tp1 = Tap * p * fpair1;
   R tq1 = Tap * q * fpair1b;
-  R crad = fsum_v + (fsum + fsum2) * Tap - (V + V2) * dTap * rinv;
   acc.fx += crad * dx - tp1 * nix - tq1 * njx;
   acc.fy += crad * dy - tp1 * niy - tq1 * njy;
   acc.fz += crad * dz - tp1 * niz - tq1 * njz;

@@ -66,6 +66,21 @@ __global__ void k_load(int n, const double *x, const int *type, const int64_t *m
   mass[p] = mass_t ? mass_t[type[p] - 1] : 1.0;
 }
 
+// per-atom tag (1-based within its system) and system id of a flattened batch, from the
+// systems' atom offsets off[0..nsys]
+__global__ void k_batch_ids(int n, const int *off, int nsys, int64_t *tag, int *sysid) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int lo = 0, hi = nsys;   // off[lo] <= q < off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= q) lo = mid;
+    else hi = mid;
+  }
+  tag[q] = (int64_t)(q - off[lo] + 1);
+  sysid[q] = lo;
+}
+
 // identity check of the caller's arrays against the resident state
 __global__ void k_check_ident(int n, const int *perm, const int *type, const int64_t *mol, const int64_t *tag,
                               const d4 *xq, const int64_t *tag_s, int *flag) {
@@ -466,8 +481,10 @@ struct Engine {
   double **d_arrs = nullptr;
   double **d_karrs = nullptr;
   double *d_kout = nullptr;
-  double *h_pinned = nullptr;
+  double *h_pinned = nullptr;   // batch staging (lmff_batch_set)
   size_t h_pinned_bytes = 0;
+  int *d_boff = nullptr;        // batch system offsets on the device
+  int boff_cap = 0;
   std::vector<double> mass_type;
   // per-system energies and virials of the last evaluation that computed them
   std::vector<lmff_result> last_res;
@@ -571,6 +588,10 @@ struct Engine {
     d_cutILPsq = nullptr;
     if (h_pinned) cudaFreeHost(h_pinned);
     h_pinned = nullptr;
+    h_pinned_bytes = 0;
+    if (d_boff) cudaFree(d_boff);
+    d_boff = nullptr;
+    boff_cap = 0;
     drop_graph();
     void *bks[] = {bk_xq, bk_v, bk_f, bk_mass, bk_tag, bk_perm, bk_sysid};
     for (void *b : bks)
@@ -2082,31 +2103,45 @@ struct Engine {
     if (rc) return rc;
     rc = ensure_atoms(nn);
     if (rc) return rc;
-    std::vector<double> x(3 * (size_t)nn), v;
-    std::vector<int> t(nn), sid(nn);
-    std::vector<int64_t> m(nn), g(nn);
     bool have_v = false;
     for (int s = 0; s < nsys; s++) have_v = have_v || sys[s].v;
-    if (have_v) v.assign(3 * (size_t)nn, 0.0);
+    // one pinned staging block, reused across calls: x | v | mol | type | offsets; tags
+    // and system ids are generated on the device
+    CK(cudaStreamSynchronize(stream));   // the previous batch's copies out of the block are done
+    const size_t bx = sizeof(double) * 3 * (size_t)nn, bm = sizeof(int64_t) * (size_t)nn,
+                 bt = sizeof(int) * (size_t)nn, bo = sizeof(int) * (size_t)(nsys + 1);
+    rc = ensure_pinned(2 * bx + bm + bt + bo);
+    if (rc) return rc;
+    char *hp = reinterpret_cast<char *>(h_pinned);
+    double *hx = reinterpret_cast<double *>(hp), *hv = reinterpret_cast<double *>(hp + bx);
+    int64_t *hm = reinterpret_cast<int64_t *>(hp + 2 * bx);
+    int *ht = reinterpret_cast<int *>(hp + 2 * bx + bm), *hoff = reinterpret_cast<int *>(hp + 2 * bx + bm + bt);
     for (int s = 0; s < nsys; s++) {
-      int o = batch_offsets[s];
-      rc = check_mol(sys[s].natoms, sys[s].mol, sys[s].type);
+      const int o = batch_offsets[s], ns = sys[s].natoms;
+      rc = check_mol(ns, sys[s].mol, sys[s].type);
       if (rc) return rc;
-      memcpy(&x[3 * (size_t)o], sys[s].x, sizeof(double) * 3 * sys[s].natoms);
-      if (sys[s].v) memcpy(&v[3 * (size_t)o], sys[s].v, sizeof(double) * 3 * sys[s].natoms);
-      for (int p = 0; p < sys[s].natoms; p++) {
-        t[o + p] = sys[s].type[p];
-        m[o + p] = sys[s].mol ? sys[s].mol[p] : 0;
-        g[o + p] = p + 1;
-        sid[o + p] = s;
+      memcpy(hx + 3 * (size_t)o, sys[s].x, sizeof(double) * 3 * ns);
+      if (have_v) {
+        if (sys[s].v) memcpy(hv + 3 * (size_t)o, sys[s].v, sizeof(double) * 3 * ns);
+        else memset(hv + 3 * (size_t)o, 0, sizeof(double) * 3 * ns);
       }
+      memcpy(ht + o, sys[s].type, sizeof(int) * ns);
+      if (sys[s].mol) memcpy(hm + o, sys[s].mol, sizeof(int64_t) * ns);
+      else memset(hm + o, 0, sizeof(int64_t) * ns);
     }
-    CK(cudaMemcpyAsync(d_xin, x.data(), sizeof(double) * x.size(), cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d_tin, t.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d_min, m.data(), sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d_gin, g.data(), sizeof(int64_t) * nn, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d_sysin, sid.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, stream));
-    if (have_v) CK(cudaMemcpyAsync(d_vin, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, stream));
+    for (int s = 0; s <= nsys; s++) hoff[s] = batch_offsets[s];
+    if (nsys + 1 > boff_cap) {
+      if (d_boff) cudaFree(d_boff);
+      d_boff = nullptr;
+      CK(cudaMalloc(&d_boff, sizeof(int) * (size_t)(nsys + 1)));
+      boff_cap = nsys + 1;
+    }
+    CK(cudaMemcpyAsync(d_xin, hx, bx, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_tin, ht, bt, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_min, hm, bm, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_boff, hoff, bo, cudaMemcpyHostToDevice, stream));
+    if (have_v) CK(cudaMemcpyAsync(d_vin, hv, bx, cudaMemcpyHostToDevice, stream));
+    if (nn) k_batch_ids<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d_boff, nsys, d_gin, d_sysin);
     if (!mass_type.empty()) {
       if (!d_massT) CK(cudaMalloc(&d_massT, sizeof(double) * (MAXTYPE + 1)));
       CK(cudaMemcpyAsync(d_massT, mass_type.data(), sizeof(double) * mass_type.size(), cudaMemcpyHostToDevice, stream));

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -1342,6 +1343,15 @@ struct Engine {
     return upload_sys();
   }
 
+  // the checks of check_mol without the error message (thread-safe)
+  bool ids_ok(int nn, const int64_t *mol, const int *type) const {
+    for (int p = 0; p < nn; p++) {
+      if (mol && (mol[p] < 0 || mol[p] >= (1LL << 23))) return false;
+      if (type[p] < 1 || type[p] > ntypes) return false;
+    }
+    return true;
+  }
+
   int check_mol(int nn, const int64_t *mol, const int *type) {
     for (int p = 0; p < nn; p++) {
       if (mol && (mol[p] < 0 || mol[p] >= (1LL << 23)))
@@ -2116,18 +2126,45 @@ struct Engine {
     double *hx = reinterpret_cast<double *>(hp), *hv = reinterpret_cast<double *>(hp + bx);
     int64_t *hm = reinterpret_cast<int64_t *>(hp + 2 * bx);
     int *ht = reinterpret_cast<int *>(hp + 2 * bx + bm), *hoff = reinterpret_cast<int *>(hp + 2 * bx + bm + bt);
-    for (int s = 0; s < nsys; s++) {
-      const int o = batch_offsets[s], ns = sys[s].natoms;
-      rc = check_mol(ns, sys[s].mol, sys[s].type);
-      if (rc) return rc;
-      memcpy(hx + 3 * (size_t)o, sys[s].x, sizeof(double) * 3 * ns);
-      if (have_v) {
-        if (sys[s].v) memcpy(hv + 3 * (size_t)o, sys[s].v, sizeof(double) * 3 * ns);
-        else memset(hv + 3 * (size_t)o, 0, sizeof(double) * 3 * ns);
+    // the systems' arrays into the block, by several host threads for a large batch
+    std::atomic<int> first_bad{nsys};
+    auto stage = [&](int s0, int s1) {
+      for (int s = s0; s < s1; s++) {
+        const int o = batch_offsets[s], ns = sys[s].natoms;
+        if (!ids_ok(ns, sys[s].mol, sys[s].type)) {
+          int cur = first_bad.load();
+          while (s < cur && !first_bad.compare_exchange_weak(cur, s)) {}
+          continue;
+        }
+        memcpy(hx + 3 * (size_t)o, sys[s].x, sizeof(double) * 3 * ns);
+        if (have_v) {
+          if (sys[s].v) memcpy(hv + 3 * (size_t)o, sys[s].v, sizeof(double) * 3 * ns);
+          else memset(hv + 3 * (size_t)o, 0, sizeof(double) * 3 * ns);
+        }
+        memcpy(ht + o, sys[s].type, sizeof(int) * ns);
+        if (sys[s].mol) memcpy(hm + o, sys[s].mol, sizeof(int64_t) * ns);
+        else memset(hm + o, 0, sizeof(int64_t) * ns);
       }
-      memcpy(ht + o, sys[s].type, sizeof(int) * ns);
-      if (sys[s].mol) memcpy(hm + o, sys[s].mol, sizeof(int64_t) * ns);
-      else memset(hm + o, 0, sizeof(int64_t) * ns);
+    };
+    const int nth = nn >= (1 << 17) ? (int)std::min(8u, std::max(1u, std::thread::hardware_concurrency())) : 1;
+    if (nth > 1 && nsys > 1) {
+      // contiguous system ranges of about equal atom counts
+      std::vector<std::thread> pool;
+      int s0 = 0;
+      for (int k = 0; k < nth && s0 < nsys; k++) {
+        const int64_t goal = (int64_t)nn * (k + 1) / nth;
+        int s1 = s0;
+        while (s1 < nsys && (k == nth - 1 || batch_offsets[s1 + 1] <= goal || s1 == s0)) s1++;
+        pool.emplace_back(stage, s0, s1);
+        s0 = s1;
+      }
+      for (auto &t : pool) t.join();
+    } else {
+      stage(0, nsys);
+    }
+    if (first_bad.load() < nsys) {
+      const int b = first_bad.load();
+      return check_mol(sys[b].natoms, sys[b].mol, sys[b].type);   // sets the message
     }
     for (int s = 0; s <= nsys; s++) hoff[s] = batch_offsets[s];
     if (nsys + 1 > boff_cap) {

@@ -215,7 +215,11 @@ int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double 
  * graph that has conditional nodes).  "graph_list_cap" > 0 lowers the
  * pair-list capacity a graph's rebuild may fill (testing the overflow redo: a chunk
  * whose rebuild overflows is redone host-driven from its first step, rebuilding the
- * list there, so it equals the uninterrupted run up to summation order). */
+ * list there, so it equals the uninterrupted run up to summation order).
+ * "ters_concurrent" 1 (default) = the Tersoff kernel runs on a second stream beside
+ * the interlayer pair kernel (they write disjoint arrays; joined before the gather);
+ * 0 = one after the other.  "ilp_prefetch" 1 = software-pipelined multi-element pair
+ * loop (j's data one entry ahead). */
 int lmff_set_option(lmff_engine *e, const char *key, double value);
 
 /* ---- one-shot evaluation on host buffers (the pair-style drop-in) ------------------ */

@@ -482,6 +482,9 @@ struct Engine {
   double **d_arrs = nullptr;
   double **d_karrs = nullptr;
   double *d_kout = nullptr;
+  cudaStream_t stream2 = nullptr;   // Tersoff beside the pair kernel
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool ters_concurrent = true;      // option "ters_concurrent"
   double *h_pinned = nullptr;   // batch staging (lmff_batch_set)
   size_t h_pinned_bytes = 0;
   int *d_boff = nullptr;        // batch system offsets on the device
@@ -612,6 +615,11 @@ struct Engine {
     m_x0 = m_g = m_h = m_part = nullptr;
     m_mask = nullptr;
     m_cap = 0;
+    if (stream2) cudaStreamDestroy(stream2);
+    stream2 = nullptr;
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    ev_fork = ev_join = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
   }
@@ -977,6 +985,14 @@ struct Engine {
     return 1.125 * per_atom_bytes() + 1.25 * 4.0 * list_pa + (double)d.cub_tmp_bytes / std::max(cap_n, 1);
   }
 
+  int ensure_stream2() {
+    if (stream2) return LMFF_OK;
+    CK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    return LMFF_OK;
+  }
+
   int ensure_pinned(size_t bytes) {
     if (bytes <= h_pinned_bytes) return LMFF_OK;
     if (h_pinned) cudaFreeHost(h_pinned);
@@ -1252,14 +1268,27 @@ struct Engine {
     a.do_ters = t_on && (which & LMFF_TERSOFF);
     a.do_ilp = i_on && (which & LMFF_ILP);
     timed(2, [&] { fs(a, d_cutILPsq, ht.cutmax * ht.cutmax, stream); });
-    if (a.do_ters) timed(1, [&] { ft(a, ev, eatom, stream); });
-    else if (ev) cudaMemsetAsync(stat_ters, 0, sizeof(double) * 8 * (size_t)n, stream);
+    // Tersoff (FP64-pipe bound) on a second stream beside the pair kernel (FP32 bound):
+    // the two share the SMs and overlap; joined before the gather.  Serial when the
+    // kernels are timed one by one.
+    const bool fork = a.do_ters && a.do_ilp && ters_concurrent && !ktiming && ensure_stream2() == LMFF_OK;
+    if (fork) {
+      cudaEventRecord(ev_fork, stream);
+      cudaStreamWaitEvent(stream2, ev_fork, 0);
+      ft(a, ev, eatom, stream2);
+      cudaEventRecord(ev_join, stream2);
+    } else if (a.do_ters) {
+      timed(1, [&] { ft(a, ev, eatom, stream); });
+    } else if (ev) {
+      cudaMemsetAsync(stat_ters, 0, sizeof(double) * 8 * (size_t)n, stream);
+    }
     if (a.do_ilp) {
       timed(0, [&] { fi(a, ev, eatom, tpa, block, i_one, stream); });
       timed(2, [&] { fn(a, ev, stream); });
     }
     else if (ev) cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)n, stream);
     if (eatom && !a.do_ters) cudaMemsetAsync(eatom_ters, 0, sizeof(double) * (size_t)n, stream);
+    if (fork) cudaStreamWaitEvent(stream, ev_join, 0);
     timed(3, [&] { ff(a, eatom, stream); });
   }
 
@@ -1605,6 +1634,10 @@ struct Engine {
   int build_step_graph(double dt) {
     drop_graph();
     if (!cap_stream) CK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+    if (ters_concurrent) {
+      int rc2 = ensure_stream2();   // before the capture begins
+      if (rc2) return rc2;
+    }
     if (!d_graph_rebuilds) {
       CK(cudaMalloc(&d_graph_rebuilds, sizeof(unsigned long long)));
       CK(cudaMemsetAsync(d_graph_rebuilds, 0, sizeof(unsigned long long), stream));
@@ -2698,6 +2731,9 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
     e->e.loaded = false;
   } else if (k == "ilp_prefetch") {
     e->e.ilp_prefetch = value != 0.0;
+    e->e.drop_graph();
+  } else if (k == "ters_concurrent") {
+    e->e.ters_concurrent = value != 0.0;
     e->e.drop_graph();
   } else if (k == "graphs") {
     e->e.use_graphs = value != 0.0;

@@ -670,6 +670,7 @@ __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
 // per-atom accumulators of the pair kernel
 struct IlpAcc {
   R fx = 0, fy = 0, fz = 0, gxa = 0, gya = 0, gza = 0;
+  R tpi = 0;   // two-pair loop: sum of the n_i coefficients, applied once (f -= tpi n_i)
   R evdw = 0, erep = 0, w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
 };
 
@@ -1172,15 +1173,17 @@ __device__ __forceinline__ void ilp_pair2(const ForceArgs<float> &a, const AtomI
   const float2 TPQJ = mul2(mul2(TAP, PQJ), mul2(E0FJ, X2(d2x2, 3)));
   const float2 CRAD = fma2(p2(-VS.x, -VS.y), DR, fma2(FSS, TAP, FSUMV));
   // ---- force on i and g_i
-  acc.fx += CRAD.x * dA.x - TPQI.x * nix - TPQJ.x * A1.x;
-  acc.fy += CRAD.x * dA.y - TPQI.x * niy - TPQJ.x * A1.y;
-  acc.fz += CRAD.x * dzA - TPQI.x * niz - TPQJ.x * A1.z;
+  // the n_i terms -tp1 n_i of all pairs are applied once, after the loop (acc.tpi)
+  acc.tpi += TPQI.x + TPQI.y;
+  acc.fx += CRAD.x * dA.x - TPQJ.x * A1.x;
+  acc.fy += CRAD.x * dA.y - TPQJ.x * A1.y;
+  acc.fz += CRAD.x * dzA - TPQJ.x * A1.z;
   acc.gxa += TPQI.x * dA.x;
   acc.gya += TPQI.x * dA.y;
   acc.gza += TPQI.x * dzA;
-  acc.fx += CRAD.y * dB.x - TPQI.y * nix - TPQJ.y * B1.x;
-  acc.fy += CRAD.y * dB.y - TPQI.y * niy - TPQJ.y * B1.y;
-  acc.fz += CRAD.y * dzB - TPQI.y * niz - TPQJ.y * B1.z;
+  acc.fx += CRAD.y * dB.x - TPQJ.y * B1.x;
+  acc.fy += CRAD.y * dB.y - TPQJ.y * B1.y;
+  acc.fz += CRAD.y * dzB - TPQJ.y * B1.z;
   acc.gxa += TPQI.y * dB.x;
   acc.gya += TPQI.y * dB.y;
   acc.gza += TPQI.y * dzB;
@@ -1333,7 +1336,8 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
       }
     }
   }
-  R fx = acc.fx, fy = acc.fy, fz = acc.fz, gxa = acc.gxa, gya = acc.gya, gza = acc.gza;
+  R fx = acc.fx - acc.tpi * nix, fy = acc.fy - acc.tpi * niy, fz = acc.fz - acc.tpi * niz;
+  R gxa = acc.gxa, gya = acc.gya, gza = acc.gza;
   R evdw = acc.evdw, erep = acc.erep, w0 = acc.w0, w1 = acc.w1, w2 = acc.w2, w3 = acc.w3, w4 = acc.w4, w5 = acc.w5;
   // ---- reduce over the TPA lanes of atom i in R; one conversion to FP64 per atom
 #pragma unroll

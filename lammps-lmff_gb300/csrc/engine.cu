@@ -482,6 +482,10 @@ struct Engine {
   double **d_arrs = nullptr;
   double **d_karrs = nullptr;
   double *d_kout = nullptr;
+  // single-pass list build: stride of the scratch slices (0: two passes), only grown, so
+  // that a captured rebuild keeps working; largest per-atom count of the last build
+  int stride = 0;
+  int *d_maxcnt = nullptr;
   cudaStream_t stream2 = nullptr;   // Tersoff beside the pair kernel
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool ters_concurrent = true;      // option "ters_concurrent"
@@ -570,7 +574,7 @@ struct Engine {
     if (device >= 0) cudaSetDevice(device);
     void *ptrs[] = {d.xq, d.xh, d.xl, d.v, d.f, d.xhold, d.tag, d.perm, d.sysid, d.mass, d.nrm64, d.nrm32, d.jrec, d.ilp_cnt,
                     d.ilp_nb, d.ters_cnt, d.ters_nb, d.ters_g, d.ters_f, d.ilp_f, d.ilp_c, d.ilp_g, d.list_off, d.list,
-                    d.short_cnt, d.short_nb, d.list_img, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.cub_tmp,
+                    d.short_cnt, d.short_nb, d.list_img, d.nin_tmp, d.list_tmp, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.cub_tmp,
                     d.cnt_tmp, d.sys, d.red_out, d.status, d.maxdisp, d_xin, d_fin, d_vin, d_ein, d_tin, d_sysin,
                     d_min, d_gin, d_massT, xq2, v2, mass2, tag2, perm2, sysid2, stat_ilp, stat_ters, eatom_ilp,
                     eatom_ters, ke, d_arrs, d_karrs, d_kout, d_cutILPsq};
@@ -596,6 +600,9 @@ struct Engine {
     if (d_boff) cudaFree(d_boff);
     d_boff = nullptr;
     boff_cap = 0;
+    if (d_maxcnt) cudaFree(d_maxcnt);
+    d_maxcnt = nullptr;
+    stride = 0;
     drop_graph();
     void *bks[] = {bk_xq, bk_v, bk_f, bk_mass, bk_tag, bk_perm, bk_sysid};
     for (void *b : bks)
@@ -939,7 +946,7 @@ struct Engine {
     CK(dalloc(stat_ilp, 8 * (size_t)c)); CK(dalloc(stat_ters, 8 * (size_t)c));
     CK(dalloc(eatom_ilp, c)); CK(dalloc(eatom_ters, c)); CK(dalloc(ke, c));
     CK(dalloc(d.list_off, (size_t)c + 1)); CK(dalloc(d.short_cnt, c)); CK(dalloc(d.short_nb, (size_t)c * MAXSHORT));
-    CK(dalloc(d.list_img, c));
+    CK(dalloc(d.list_img, c)); CK(dalloc(d.nin_tmp, c));
     CK(dalloc(d.bin_key, c)); CK(dalloc(d.bin_key2, c)); CK(dalloc(d.idx, c)); CK(dalloc(d.idx2, c));
     CK(dalloc(d.cnt_tmp, (size_t)c + 1));
     CK(dalloc(d_xin, 3 * (size_t)c)); CK(dalloc(d_fin, 3 * (size_t)c)); CK(dalloc(d_vin, 3 * (size_t)c));
@@ -966,15 +973,15 @@ struct Engine {
                       sizeof(*d.nrm64) + sizeof(*d.nrm32) + 5 * sizeof(*d.jrec) + sizeof(*d.ilp_cnt) + MAXILP * sizeof(*d.ilp_nb) +
                       sizeof(*d.ters_cnt) + MAXTERS * (sizeof(*d.ters_nb) + sizeof(*d.ters_g)) +
                       2 * 3 * sizeof(double) + MAXILP * sizeof(*d.ilp_c) + sizeof(*d.ilp_g) + 16 * sizeof(double) +
-                      3 * sizeof(double) + sizeof(*d.list_off) + sizeof(*d.list_img) + sizeof(*d.short_cnt) + MAXSHORT * sizeof(*d.short_nb) +
+                      3 * sizeof(double) + sizeof(*d.list_off) + sizeof(*d.list_img) + sizeof(*d.nin_tmp) + sizeof(*d.short_cnt) + MAXSHORT * sizeof(*d.short_nb) +
                       2 * sizeof(*d.bin_key) + 2 * sizeof(*d.idx) + sizeof(*d.cnt_tmp) + 3 * 3 * sizeof(double) +
                       sizeof(double) + 2 * sizeof(int) + 2 * sizeof(int64_t);
     if (bk_cap) per_atom += sizeof(d4) + 7 * sizeof(double) + sizeof(int64_t) + 2 * sizeof(int);
     return per_atom;
   }
   double device_bytes() const {
-    return (double)cap_n * per_atom_bytes() + (double)d.list_cap * sizeof(uint32_t) + (double)d.cub_tmp_bytes +
-           (double)d.nbins_cap * 2 * sizeof(int);
+    return (double)cap_n * per_atom_bytes() + (double)(d.list_cap + d.tmp_cap) * sizeof(uint32_t) +
+           (double)d.cub_tmp_bytes + (double)d.nbins_cap * 2 * sizeof(int);
   }
   // device bytes per atom a batch like the current one needs: the per-atom arrays with
   // their growth margin, the pair list at the current density with the step graph's
@@ -982,7 +989,35 @@ struct Engine {
   double bytes_per_atom_need() const {
     if (n <= 0) return 0.0;
     double list_pa = (double)list_total / n;
-    return 1.125 * per_atom_bytes() + 1.25 * 4.0 * list_pa + (double)d.cub_tmp_bytes / std::max(cap_n, 1);
+    return 1.125 * per_atom_bytes() + 1.25 * 4.0 * list_pa + 4.0 * stride +
+           (double)d.cub_tmp_bytes / std::max(cap_n, 1);
+  }
+
+  // stride for the next builds from the last build's largest count (1/8 + 32 headroom);
+  // off when the scratch would exceed twice the list itself or does not fit
+  void update_stride(int maxcnt) {
+    int want = ((maxcnt + maxcnt / 8 + 32) + 31) & ~31;
+    if (want <= stride && stride > 0) return;
+    const int64_t need = (int64_t)cap_n * want;
+    if (need > 2 * std::max<int64_t>(d.list_cap, 1024)) {
+      stride = 0;
+      return;
+    }
+    if (need > d.tmp_cap) {
+      drop_graph();   // a captured rebuild holds the old scratch pointer and stride
+      if (d.list_tmp) cudaFree(d.list_tmp);
+      d.list_tmp = nullptr;
+      d.tmp_cap = 0;
+      if (cudaMalloc(&d.list_tmp, sizeof(uint32_t) * need) != cudaSuccess) {
+        cudaGetLastError();
+        stride = 0;
+        return;
+      }
+      d.tmp_cap = need;
+    } else {
+      drop_graph();
+    }
+    stride = want;
   }
 
   int ensure_stream2() {
@@ -1133,12 +1168,27 @@ struct Engine {
     a.lc = lc;
     a.full = list_full;
     a.status = d.status;
+    if (!d_maxcnt) CK(cudaMalloc(&d_maxcnt, sizeof(int)));
+    bool strided = stride > 0 && d.list_tmp && (int64_t)n * stride <= d.tmp_cap;
+    a.tmp = d.list_tmp;
+    a.stride = strided ? stride : 0;
+    a.nin = d.nin_tmp;
+    a.maxcnt = d_maxcnt;
+    CK(cudaMemsetAsync(d_maxcnt, 0, sizeof(int), stream));
     CK(cudaMemsetAsync(d.cnt_tmp + n, 0, sizeof(int64_t), stream));
-    nb_list(a, false, stream);
+    nb_list(a, strided ? 2 : 0, stream);
     CK(nb_scan(d.cub_tmp, d.cub_tmp_bytes, d.cnt_tmp, d.list_off, n, stream));
     int64_t total = 0;
+    int st0 = 0, maxcnt = 0;
     CK(cudaMemcpyAsync(&total, d.list_off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(&st0, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(&maxcnt, d_maxcnt, sizeof(int), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
+    if (strided && (st0 & ST_STRIDE_OVERFLOW)) {   // an atom outgrew the stride: fill pass instead
+      strided = false;
+      st0 &= ~(ST_STRIDE_OVERFLOW | ST_LIST_OVERFLOW);
+      CK(cudaMemcpyAsync(d.status, &st0, sizeof(int), cudaMemcpyHostToDevice, stream));
+    }
     if (total < 0 || total > (int64_t)n * 65536)
       return fail(LMFF_EOVERFLOW, "pair-list count out of range (" + std::to_string(total) + ")");
     if (total > d.list_cap) {
@@ -1155,7 +1205,8 @@ struct Engine {
     }
     a.list = d.list;
     a.list_cap = d.list_cap;
-    nb_list(a, true, stream);
+    if (strided) nb_compact(a, d.list_cap, stream);
+    else nb_list(a, 1, stream);
     nb_copy_hold(n, d.xq, d.xhold, stream);
     CK(cudaGetLastError());
     // atoms of one system stay contiguous after the sort (bins of system s precede
@@ -1186,6 +1237,7 @@ struct Engine {
     }
     list_total = total;
     if (st) return status_error(st);
+    update_stride(maxcnt);
     built = true;
     forces_valid = false;
     rebuilds++;
@@ -1606,12 +1658,20 @@ struct Engine {
     a.lc = lc;
     a.full = list_full;
     a.status = d.status;
+    // single pass when the scratch holds the current stride (an atom outgrowing it
+    // raises the list-overflow status: the chunk is redone host-driven, which grows it)
+    const bool strided = stride > 0 && d.list_tmp && (int64_t)n * stride <= d.tmp_cap;
+    a.tmp = d.list_tmp;
+    a.stride = strided ? stride : 0;
+    a.nin = d.nin_tmp;
+    a.maxcnt = nullptr;
     cudaMemsetAsync(d.cnt_tmp + n, 0, sizeof(int64_t), s);
-    nb_list(a, false, s);
+    nb_list(a, strided ? 2 : 0, s);
     e = nb_scan(d.cub_tmp, d.cub_tmp_bytes, d.cnt_tmp, d.list_off, n, s);
     if (e != cudaSuccess) return e;
     k_clamp_off<<<(n + 256) / 256, 256, 0, s>>>(n, d.list_off, graph_cap, d.status, d_graph_rebuilds);
-    nb_list(a, true, s);
+    if (strided) nb_compact(a, graph_cap, s);
+    else nb_list(a, 1, s);
     nb_copy_hold(n, d.xq, d.xhold, s);
     cudaMemsetAsync(d.maxdisp, 0, sizeof(unsigned long long), s);
     return cudaGetLastError();
@@ -2431,7 +2491,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
   na.lc = lc;
   na.full = g.list_full;
   na.status = status;
-  nb_list(na, false, st);
+  nb_list(na, 0, st);
   CK2(nb_scan(tmp, tmp_bytes, cnt, list_off, nn, st));
   int64_t total = 0;
   CK2(cudaMemcpyAsync(&total, list_off + nn, sizeof total, cudaMemcpyDeviceToHost, st));
@@ -2439,7 +2499,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
   if (total < 0 || (size_t)total > list_cap)
     return g.fail(LMFF_EOVERFLOW, "lmff_compute_device_noalloc: pair list of " + std::to_string(total) +
                                       " entries exceeds the scratch capacity of " + std::to_string(list_cap));
-  nb_list(na, true, st);
+  nb_list(na, 1, st);
   auto fill = [&](auto &a) {
     memset(&a, 0, sizeof a);
     a.A.xq = xq2;

@@ -30,6 +30,7 @@ enum : int {
   ST_SHORT_OVERFLOW = 8,
   ST_LIST_OVERFLOW = 16,
   ST_NONFINITE = 32,
+  ST_STRIDE_OVERFLOW = 64,   // internal: an atom's list outgrew the strided build's stride
 };
 
 // ILP parameters of one ordered element pair (pair_ilp_graphene_hbn.h:53-57 after
@@ -160,6 +161,10 @@ struct DevState {
   int64_t *list_off = nullptr; // n+1
   uint32_t *list = nullptr;
   int64_t list_cap = 0;
+  // single-pass build: atom i's entries at list_tmp[i*stride ...] before the compaction
+  uint32_t *list_tmp = nullptr;
+  int64_t tmp_cap = 0;
+  int *nin_tmp = nullptr;     // entries inside the force cutoff per atom
   uint8_t *list_img = nullptr;   // per atom: 1 when its pair list holds periodic-image entries
   int *short_cnt = nullptr;
   uint32_t *short_nb = nullptr; // n * MAXSHORT

@@ -115,14 +115,20 @@ __device__ __forceinline__ bool le_exact(float rsq, float thr, double thr64, con
 // row boundary) are handled in a second pass.  No block-wide barrier is involved.
 // The entries of each i come out in the order of a per-atom scan: stencil bins (dz, dy,
 // dx), then j ascending.
-// FILL = false: counts pair-list entries into cnt[i] and writes the short list.
-// FILL = true: writes the pair list at list_off[i], candidates inside the force cutoff
-// from the front and the skin shell from the back (the pair kernel's lanes then mostly
-// accept or reject together).
+// MODE 0: counts pair-list entries into cnt[i] and writes the short list.
+// MODE 1: writes the pair list at list_off[i], candidates inside the force cutoff from
+// the front and the skin shell from the back (the pair kernel's lanes then mostly accept
+// or reject together).
+// MODE 2: both in one pass over the candidates: counts, short list, and the entries in
+// the same order into atom i's slice of the strided buffer, for nb_compact after the
+// scan; an atom with more entries than the stride raises ST_STRIDE_OVERFLOW (with
+// ST_LIST_OVERFLOW, so that a captured rebuild is redone) and the host falls back to
+// MODE 1.
 constexpr int LW = 4;   // warps per block
 
-template <bool FILL>
+template <int MODE>
 __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
+  constexpr bool FILL = MODE != 0;
   const int wg = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   const int wl = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -149,8 +155,10 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
   const int ilp_i = c_nb.ilp_mapped[ti];
   int nlong = 0, nin = 0, nsh = 0, nshort = 0;
   bool img = false;
-  const int64_t base = (FILL && act) ? a.list_off[i] : 0;
-  const int64_t lend = (FILL && act) ? a.list_off[i + 1] : 0;
+  const int64_t base = !act ? 0 : MODE == 1 ? a.list_off[i] : MODE == 2 ? (int64_t)i * a.stride : 0;
+  const int64_t lend = !act ? 0 : MODE == 1 ? a.list_off[i + 1] : MODE == 2 ? base + a.stride : 0;
+  uint32_t *const dst = MODE == 2 ? a.tmp : a.list;
+  const int64_t dcap = MODE == 2 ? (int64_t)a.n * a.stride : a.list_cap;
   unsigned todo = __ballot_sync(FULL, act);
   while (todo) {
     const int leader = __ffs(todo) - 1;
@@ -214,17 +222,16 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
               bool take_long = false;
               if ((a.full || (mj != mi && ilp_i && c_nb.ilp_mapped[tj])) && !(self_image && j == i))
                 take_long = le_exact(rsq, c_nb.cutnsq_f[tt], c_nb.cutnsq_d[tt], a.xq, sd, i, j, sx, sy, sz);
-              if (FILL) {
-                if (take_long) {
-                  const bool inner = rsq < c_nb.innersq_f;
-                  int64_t pos = inner ? base + nin : lend - 1 - nsh;
-                  if (pos >= base && pos < lend && pos < a.list_cap) a.list[pos] = encode_entry(j, sx, sy, sz, a.lc);
-                  nin += inner;
-                  nsh += !inner;
-                  img |= !self_image;
-                }
-              } else if (!(self_image && j == i) &&
-                         le_exact(rsq, c_nb.rshortsq_f, c_nb.rshortsq_d, a.xq, sd, i, j, sx, sy, sz)) {
+              if (FILL && take_long) {
+                const bool inner = rsq < c_nb.innersq_f;
+                int64_t pos = inner ? base + nin : lend - 1 - nsh;
+                if (pos >= base && pos < lend && pos < dcap) dst[pos] = encode_entry(j, sx, sy, sz, a.lc);
+                nin += inner;
+                nsh += !inner;
+                img |= !self_image;
+              }
+              if (MODE != 1 && !(self_image && j == i) &&
+                  le_exact(rsq, c_nb.rshortsq_f, c_nb.rshortsq_d, a.xq, sd, i, j, sx, sy, sz)) {
                 if (nshort < MAXSHORT) a.short_nb[(size_t)i * MAXSHORT + nshort] = encode_entry(j, sx, sy, sz, a.lc);
                 nshort++;
               }
@@ -236,14 +243,39 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
     }
   }
   if (act) {
-    if (!FILL) {
+    if (MODE != 1) {
       a.cnt[i] = nlong;
       a.short_cnt[i] = nshort < MAXSHORT ? nshort : MAXSHORT;
       if (nshort > MAXSHORT) atomicOr(a.status, ST_SHORT_OVERFLOW);
-    } else {
-      a.img[i] = img;
-      if (base + nlong > a.list_cap) atomicOr(a.status, ST_LIST_OVERFLOW);
     }
+    if (MODE != 0) a.img[i] = img;
+    if (MODE == 1 && base + nlong > a.list_cap) atomicOr(a.status, ST_LIST_OVERFLOW);
+    if (MODE == 2) {
+      a.nin[i] = nin;
+      if (nlong > a.stride) atomicOr(a.status, ST_STRIDE_OVERFLOW | ST_LIST_OVERFLOW);
+    }
+  }
+  if (MODE != 1) {   // largest count, for the next strided build's stride
+    int m = act ? nlong : 0;
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULL, m, o));
+    if (lane == 0 && a.maxcnt) atomicMax(a.maxcnt, m);
+  }
+}
+
+// Strided buffer -> CSR list, one warp per atom: the entries inside the cutoff, then the
+// shell (kept at the end of the atom's slice, in the order MODE 1 writes them), so the
+// list equals MODE 1's.  Does nothing after a stride overflow (the host then fills).
+__global__ void k_compact(int n, int stride, const uint32_t *tmp, const int *nin, const int64_t *off, uint32_t *list,
+                          int64_t list_cap, const int *status) {
+  const int i = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= n || (*status & ST_STRIDE_OVERFLOW)) return;
+  const int64_t b = off[i];
+  const int c = (int)(off[i + 1] - b), ni = nin[i];
+  const uint32_t *src = tmp + (int64_t)i * stride;
+  for (int k = lane; k < c; k += 32) {
+    const uint32_t v = k < ni ? src[k] : src[stride - c + k];
+    if (b + k < list_cap) list[b + k] = v;
   }
 }
 
@@ -297,11 +329,18 @@ void nb_hilo(int n, const d4 *xq, const SysDesc *sys, const int *sysid, float4 *
   if (n) k_hilo<<<(n + 255) / 256, 256, 0, s>>>(n, xq, sys, sysid, xh, xl);
 }
 
-void nb_list(const NbArgs &a, bool fill, cudaStream_t s) {
+void nb_list(const NbArgs &a, int mode, cudaStream_t s) {
   if (!a.n) return;
   const int g = (a.n + 32 * LW - 1) / (32 * LW);
-  if (fill) k_list<true><<<g, 32 * LW, 0, s>>>(a);
-  else k_list<false><<<g, 32 * LW, 0, s>>>(a);
+  if (mode == 1) k_list<1><<<g, 32 * LW, 0, s>>>(a);
+  else if (mode == 2) k_list<2><<<g, 32 * LW, 0, s>>>(a);
+  else k_list<0><<<g, 32 * LW, 0, s>>>(a);
+}
+
+void nb_compact(const NbArgs &a, int64_t list_cap, cudaStream_t s) {
+  if (!a.n) return;
+  k_compact<<<(int)(((int64_t)a.n * 32 + 255) / 256), 256, 0, s>>>(a.n, a.stride, a.tmp, a.nin, a.list_off, a.list,
+                                                                   list_cap, a.status);
 }
 
 void nb_copy_hold(int n, const d4 *xq, double *xhold, cudaStream_t s) {

@@ -33,6 +33,10 @@ struct NbArgs {
   int *short_cnt;
   uint32_t *short_nb;
   uint8_t *img;       // fill pass: 1 per atom whose list holds periodic-image entries
+  uint32_t *tmp;      // strided build: atom i's entries at tmp[i*stride, (i+1)*stride)
+  int stride;
+  int *nin;           // strided build: entries inside the force cutoff per atom
+  int *maxcnt;        // count passes: largest per-atom count (atomicMax)
   ListCode lc;
   int full;
   int *status;
@@ -49,7 +53,10 @@ void nb_permute(int n, const int *idx2, const d4 *xq, d4 *xq2, const double *v, 
                 double *mass2, cudaStream_t s);
 void nb_bin_ranges(int n, const uint32_t *key, int *bs, int *be, cudaStream_t s);
 void nb_hilo(int n, const d4 *xq, const SysDesc *sys, const int *sysid, float4 *xh, float4 *xl, cudaStream_t s);
-void nb_list(const NbArgs &a, bool fill, cudaStream_t s);
+// mode 0: count (+ short lists); 1: fill the CSR list; 2: count and write each atom's
+// entries into the strided buffer, for nb_compact after the scan
+void nb_list(const NbArgs &a, int mode, cudaStream_t s);
+void nb_compact(const NbArgs &a, int64_t list_cap, cudaStream_t s);
 void nb_copy_hold(int n, const d4 *xq, double *xhold, cudaStream_t s);
 
 }  // namespace lmff

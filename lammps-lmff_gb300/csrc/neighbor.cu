@@ -273,9 +273,19 @@ __global__ void k_compact(int n, int stride, const uint32_t *tmp, const int *nin
   const int64_t b = off[i];
   const int c = (int)(off[i + 1] - b), ni = nin[i];
   const uint32_t *src = tmp + (int64_t)i * stride;
-  for (int k = lane; k < c; k += 32) {
-    const uint32_t v = k < ni ? src[k] : src[stride - c + k];
-    if (b + k < list_cap) list[b + k] = v;
+  // four loads in flight per lane before the stores (the copy is latency-bound otherwise)
+  for (int k0 = lane; k0 < c; k0 += 128) {
+    uint32_t v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int k = k0 + 32 * u;
+      v[u] = k >= c ? 0u : k < ni ? src[k] : src[stride - c + k];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int k = k0 + 32 * u;
+      if (k < c && b + k < list_cap) list[b + k] = v[u];
+    }
   }
 }
 

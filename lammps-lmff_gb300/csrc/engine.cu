@@ -214,7 +214,8 @@ struct DtfmTab {
 // double-float split and tracks the displacement since the last build
 __global__ void k_nve1(int n, d4 *xq, double *v, const double *f, DtfmTab tab, double dtv,
                        const double *xhold, unsigned long long *maxdisp, const SysDesc *sys, const int *sysid,
-                       float4 *xh, float4 *xl, int do_hilo) {
+                       float4 *xh, float4 *xl, int do_hilo, cudaGraphConditionalHandle h = 0, double trig2 = 0.0,
+                       unsigned *ticket = nullptr) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   double d2 = 0.0;
   if (q < n) {
@@ -240,6 +241,21 @@ __global__ void k_nve1(int n, d4 *xq, double *v, const double *f, DtfmTab tab, d
     }
   }
   block_max_disp(d2, maxdisp);
+  if (ticket) {
+    // in the step graph: the last block to finish sets the rebuild condition, any atom
+    // moved more than skin/2 since the last build (neighbor.cpp:1947-1976 check_distance)
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+      __threadfence();
+      last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+      *ticket = 0;
+      const double dmax = __longlong_as_double((long long)atomicMax(maxdisp, 0ull));
+      cudaGraphSetConditional(h, dmax > trig2 ? 1u : 0u);
+    }
+  }
 }
 
 __global__ void k_nve2(int n, double *v, const double *f, const d4 *xq, const double *mass, DtfmTab tab, double *ke) {
@@ -252,13 +268,6 @@ __global__ void k_nve2(int n, double *v, const double *f, const d4 *xq, const do
   double vz = v[2 * n + q] + dtfm * f[2 * n + q];
   v[q] = vx; v[n + q] = vy; v[2 * n + q] = vz;
   if (ke) ke[q] = 0.5 * MVV2E * mass[q] * (vx * vx + vy * vy + vz * vz);
-}
-
-// sets the step graph's rebuild condition: any atom moved more than skin/2 since the
-// last build (neighbor.cpp:1947-1976 check_distance)
-__global__ void k_setcond(cudaGraphConditionalHandle h, const unsigned long long *maxdisp, double trig2) {
-  double d2 = __longlong_as_double((long long)*maxdisp);
-  cudaGraphSetConditional(h, d2 > trig2 ? 1u : 0u);
 }
 
 // ---------------------------------------------------------------- minimiser kernels
@@ -616,6 +625,8 @@ struct Engine {
     cap_stream = nullptr;
     if (d_graph_rebuilds) cudaFree(d_graph_rebuilds);
     d_graph_rebuilds = nullptr;
+    if (d_cond_ticket) cudaFree(d_cond_ticket);
+    d_cond_ticket = nullptr;
     void *mins[] = {m_x0, m_g, m_h, m_part, m_mask};
     for (void *b : mins)
       if (b) cudaFree(b);
@@ -1598,8 +1609,9 @@ struct Engine {
   }
 
   // ---------------------------------------------------------------- step graph
-  // One velocity-Verlet step as a CUDA graph: k_nve1 -> k_setcond -> IF(rebuild) ->
-  // forces -> k_nve2, replayed with no host synchronisation between steps.  Kernel
+  // One velocity-Verlet step as a CUDA graph: k_nve1 (whose last block sets the rebuild
+  // condition) -> IF(rebuild) -> forces -> k_nve2, replayed with no host synchronisation
+  // between steps.  Kernel
   // arguments are frozen at capture, so the graph's rebuild permutes into the spare
   // arrays and copies back, and the pair list keeps the capacity it had at capture
   // (an overflow raises ST_LIST_OVERFLOW; the chunk is then redone on the eager path
@@ -1623,6 +1635,7 @@ struct Engine {
   int bk_cap = 0;
   int64_t graph_steps = 0, graph_redos = 0;
   unsigned long long *d_graph_rebuilds = nullptr;
+  unsigned *d_cond_ticket = nullptr;   // k_nve1's block count for the rebuild condition
   int64_t graph_cap = 0;           // pair-list capacity the step graph's rebuild fills up to
   int64_t graph_cap_limit = 0;     // > 0: lower it to this (exercises the overflow redo)
 
@@ -1702,6 +1715,10 @@ struct Engine {
       CK(cudaMalloc(&d_graph_rebuilds, sizeof(unsigned long long)));
       CK(cudaMemsetAsync(d_graph_rebuilds, 0, sizeof(unsigned long long), stream));
     }
+    if (!d_cond_ticket) {
+      CK(cudaMalloc(&d_cond_ticket, sizeof(unsigned)));
+      CK(cudaMemsetAsync(d_cond_ticket, 0, sizeof(unsigned), stream));
+    }
     int prc = push_consts();
     if (prc) return prc;
     if (!built) {
@@ -1732,8 +1749,8 @@ struct Engine {
     CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
     CK(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
-                                                d.sysid, d.xh, d.xl, mixed ? 1 : 0);
-    k_setcond<<<1, 1, 0, stream>>>(h, d.maxdisp, 0.25 * skin * skin);
+                                                d.sysid, d.xh, d.xl, mixed ? 1 : 0, h, 0.25 * skin * skin,
+                                                d_cond_ticket);
     cudaStreamCaptureStatus cs;
     const cudaGraphNode_t *deps = nullptr;
     size_t nd = 0;

@@ -271,6 +271,31 @@ def test_mixed_vs_fp64_large():
     assert abs(r32["e_ilp"] - r64["e_ilp"]) <= MIX_E_REL * abs(r64["e_ilp"])
 
 
+def test_benchmark_slab_full_size():
+    """The 2,694,960-atom 10-layer AB graphite slab at 300 K, at full size, through
+    size-independent properties: 150 mixed NVE steps through the step graph (the first
+    build runs count + fill, the rebuilds inside the graph the single pass with
+    compaction) conserve the total energy; the forces the engine holds at the end, on
+    its rebuilt list, equal a fresh FP64 evaluation at the same positions; the FP64
+    forces sum to zero."""
+    s0 = S.thermalize(S.graphite_slab(10, 342, 197, spacing=3.35, mol_mode="alternate"), 300.0, seed=3)
+    assert s0.n == 2_694_960
+    eng = capi.Engine(TERSOFF, ILP, precision=capi.MIXED, skin=1.0)
+    eng.set_option("tpa", 8)
+    eng.set_option("block", 128)
+    eng.upload(s0)
+    th = eng.run_nve(150, 0.001, thermo_every=150)
+    assert eng.stats()["rebuilds"] >= 2
+    assert abs(th[-1]["etotal"] - th[0]["etotal"]) <= 5e-4 * s0.n
+    x, _, f = eng.download()
+    eng.close()
+    s1 = s0.copy()
+    s1.x = x
+    r64 = capi.Engine(TERSOFF, ILP).compute_system(s1, eflag=False, vflag=False)
+    assert np.abs(f - r64["f"]).max() <= MIX_F_ABS
+    assert np.abs(r64["f"].sum(0)).max() <= 1e-9 * np.abs(r64["f"]).sum(0).max()
+
+
 def test_two_engines_interleaved_share_constant_memory_safely():
     """Two engines with different parameter sets (Tersoff-only, ILP-only, as the two
     LAMMPS sub-styles hold them) alternate on one device; each call must use its own

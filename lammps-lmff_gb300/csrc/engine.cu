@@ -39,7 +39,7 @@ namespace lmff {
   void launch_ilp(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, bool one_element,       \
                   cudaStream_t s);                                                                         \
   void launch_nderiv(const ForceArgs<R> &a, bool ev, cudaStream_t s);                                      \
-  void launch_finish(const ForceArgs<R> &a, bool eatom, cudaStream_t s);                                   \
+  void launch_finish(const ForceArgs<R> &a, bool eatom, const KickArgs *kick, cudaStream_t s);             \
   }
 LMFF_FORCE_API(f64, double)
 LMFF_FORCE_API(f32, float)
@@ -1352,7 +1352,7 @@ struct Engine {
     else if (ev) cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)n, stream);
     if (eatom && !a.do_ters) cudaMemsetAsync(eatom_ters, 0, sizeof(double) * (size_t)n, stream);
     if (fork) cudaStreamWaitEvent(stream, ev_join, 0);
-    timed(3, [&] { ff(a, eatom, stream); });
+    timed(3, [&] { ff(a, eatom, kick_on ? &kick_args : nullptr, stream); });
   }
 
   // forces (+ energies/virials per system into hres when ev) on the resident state
@@ -1695,6 +1695,15 @@ struct Engine {
     step_exec = nullptr;
   }
 
+  // NVE steps: the gather kernel applies the second half-kick (k_nve2's arithmetic)
+  KickArgs kick_args{};
+  bool kick_on = false;
+  void set_kick(double dtf) {
+    kick_args.v = d.v;
+    DtfmTab t = dtfm_table(dtf);
+    for (int k = 0; k <= MAXTYPE; k++) kick_args.dtfm[k] = t.v[k];
+  }
+
   DtfmTab dtfm_table(double dtf) const {
     DtfmTab t;
     for (int k = 0; k <= MAXTYPE; k++) {
@@ -1770,6 +1779,8 @@ struct Engine {
     CK(cudaStreamUpdateCaptureDependencies(stream, &cn, nullptr, 1, cudaStreamSetCaptureDependencies));
     bool kt = ktiming;
     ktiming = false;
+    set_kick(dtf);   // the graph's rebuild copies back, so d.v stays fixed
+    kick_on = true;
     if (precision == LMFF_FP64)
       run_kernels(args<double>(), LMFF_TERSOFF | LMFF_ILP, false, false, f64::launch_short, f64::launch_tersoff,
                   f64::launch_ilp, f64::launch_nderiv, f64::launch_finish);
@@ -1777,7 +1788,7 @@ struct Engine {
       run_kernels(args<float>(), LMFF_TERSOFF | LMFF_ILP, false, false, f32::launch_short, f32::launch_tersoff,
                   f32::launch_ilp, f32::launch_nderiv, f32::launch_finish);
     ktiming = kt;
-    k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.xq, d.mass, dtfm_table(dtf), nullptr);
+    kick_on = false;
     cudaGraph_t gout = nullptr;
     CK(cudaStreamEndCapture(stream, &gout));
     cudaError_t ei = cudaGraphInstantiate(&step_exec, gout, 0);
@@ -1863,10 +1874,11 @@ struct Engine {
       hilo_fresh = mixed;
       int rc = maybe_rebuild();
       if (rc) return rc;
+      set_kick(dtf);   // after any rebuild: it may have moved d.v
+      kick_on = true;
       rc = forces(LMFF_TERSOFF | LMFF_ILP, false, false, nullptr);
+      kick_on = false;
       if (rc) return rc;
-      timed(4, [&] { k_nve2<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.xq, d.mass, dtfm_table(dtf), nullptr); });
-      CK(cudaGetLastError());
       steps++;
     }
     return LMFF_OK;
@@ -2571,7 +2583,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
     } else {
       CK2(cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)nn, st));
     }
-    f64::launch_finish(a, false, st);
+    f64::launch_finish(a, false, nullptr, st);
   } else {
     ForceArgs<float> a;
     fill(a);
@@ -2584,7 +2596,7 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
     } else {
       CK2(cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)nn, st));
     }
-    f32::launch_finish(a, false, st);
+    f32::launch_finish(a, false, nullptr, st);
   }
   k_reduce<<<16, 256, 0, st>>>(nn, 16, (const double *const *)arrs, dsys, red);
   k_scatter_add<<<gb, 256, 0, st>>>(nn, perm2, fs, df, 1);

@@ -206,6 +206,13 @@ __device__ __forceinline__ void disp64(const d4 *xq, const SysDesc &sd, int i, i
 
 // --------------------------------------------------------------- kernel arguments
 
+// the second velocity half-kick of an NVE step, applied by the gather kernel to the force
+// it has just summed (fix_nve.cpp final_integrate: v += dtf / m f): v SoA, dtf / m per type
+struct KickArgs {
+  double *v;
+  double dtfm[MAXTYPE + 1];
+};
+
 template <class R>
 struct ForceArgs {
   AtomArrays A;

@@ -1510,8 +1510,8 @@ __global__ void k_nderiv(ForceArgs<R> a) {
 // Per atom a: its own ILP and Tersoff forces + the slots its neighbours left for it:
 // Tersoff bond/three-body forces from every j with a in N_ters(j) and ILP normal-
 // derivative forces from every j with a in N_ilp(j).  Fixed summation order.
-template <bool EATOM>
-__global__ void k_finish(ForceArgs<R> a) {
+template <bool EATOM, bool KICK>
+__global__ void k_finish(ForceArgs<R> a, KickArgs kick) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   double Fx = 0, Fy = 0, Fz = 0, ea = 0;
@@ -1563,6 +1563,12 @@ __global__ void k_finish(ForceArgs<R> a) {
   a.f_out[i] = Fx;
   a.f_out[a.n + i] = Fy;
   a.f_out[2 * a.n + i] = Fz;
+  if constexpr (KICK) {   // the same arithmetic as k_nve2 on the force just stored
+    const double dtfm = kick.dtfm[__double_as_longlong(a.A.xq[i].w) & 255];
+    kick.v[i] = kick.v[i] + dtfm * Fx;
+    kick.v[a.n + i] = kick.v[a.n + i] + dtfm * Fy;
+    kick.v[2 * a.n + i] = kick.v[2 * a.n + i] + dtfm * Fz;
+  }
   if (EATOM) {
     // per-atom energy as the reference's ev_tally splits it: the Tersoff own share was
     // written by k_ters_eatom_own, the partners' halves are gathered above
@@ -1718,11 +1724,15 @@ void launch_nderiv(const ForceArgs<R> &a, bool ev, cudaStream_t s) {
   else k_nderiv<false><<<g, 128, 0, s>>>(a);
 }
 
-void launch_finish(const ForceArgs<R> &a, bool eatom, cudaStream_t s) {
+void launch_finish(const ForceArgs<R> &a, bool eatom, const KickArgs *kick, cudaStream_t s) {
   if (a.n == 0) return;
   int g = (a.n + 127) / 128;
-  if (eatom) k_finish<true><<<g, 128, 0, s>>>(a);
-  else k_finish<false><<<g, 128, 0, s>>>(a);
+  KickArgs k{};
+  if (kick) k = *kick;
+  if (kick && !eatom) k_finish<false, true><<<g, 128, 0, s>>>(a, k);
+  else if (kick) k_finish<true, true><<<g, 128, 0, s>>>(a, k);
+  else if (eatom) k_finish<true, false><<<g, 128, 0, s>>>(a, k);
+  else k_finish<false, false><<<g, 128, 0, s>>>(a, k);
 }
 
 }  // namespace LMFF_NS

@@ -602,7 +602,7 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
     fr += fpair;
     fx += dxd[s] * fr; fy += dyd[s] * fr; fz += dzd[s] * fr;
     const double fjx = -dxd[s] * fpair, fjy = -dyd[s] * fpair, fjz = -dzd[s] * fpair;
-    gx[s] += fjx; gy[s] += fjy; gz[s] += fjz;
+    gx[s] = fjx; gy[s] = fjy; gz[s] = fjz;   // the only radial contribution to partner s
     if (EV) {
       double eb = 0.5 * bij * fa;
       eng += eb;
@@ -1446,19 +1446,19 @@ __global__ void k_nderiv(ForceArgs<R> a) {
       disp64(a.A.xq, sd, i, j, sx, sy, sz, ddx, ddy, ddz);
       v[m][0] = -ddx; v[m][1] = -ddy; v[m][2] = -ddz;
     }
-    double n1x = v[0][1] * v[1][2] - v[1][1] * v[0][2];
-    double n1y = v[0][2] * v[1][0] - v[1][2] * v[0][0];
-    double n1z = v[0][0] * v[1][1] - v[1][0] * v[0][1];
-    if (cont == 3) {
-      n1x += v[2][1] * v[0][2] - v[0][1] * v[2][2];
-      n1y += v[2][2] * v[0][0] - v[0][2] * v[2][0];
-      n1z += v[2][0] * v[0][1] - v[0][0] * v[2][1];
-      n1x += v[1][1] * v[2][2] - v[2][1] * v[1][2];
-      n1y += v[1][2] * v[2][0] - v[2][2] * v[1][0];
-      n1z += v[1][0] * v[2][1] - v[2][0] * v[1][1];
-      // the reference averages the three products (n1 / 3); the unnormalised sum gives the
-      // same n, and h / 3 absorbs the 1/3 of each product's derivative
-    }
+    // three neighbours: v1 x v2 + v3 x v1 + v2 x v3 = (v2 - v1) x (v3 - v1), one product
+    // instead of three.  The reference averages the three products (n1 / 3); the
+    // unnormalised sum gives the same n, and h / 3 absorbs the 1/3 of each product's
+    // derivative.
+    const double ax = cont == 3 ? v[1][0] - v[0][0] : v[0][0];
+    const double ay = cont == 3 ? v[1][1] - v[0][1] : v[0][1];
+    const double az = cont == 3 ? v[1][2] - v[0][2] : v[0][2];
+    const double bx = cont == 3 ? v[2][0] - v[0][0] : v[1][0];
+    const double by = cont == 3 ? v[2][1] - v[0][1] : v[1][1];
+    const double bz = cont == 3 ? v[2][2] - v[0][2] : v[1][2];
+    const double n1x = ay * bz - by * az;
+    const double n1y = az * bx - bz * ax;
+    const double n1z = ax * by - bx * ay;
     const double nn2 = n1x * n1x + n1y * n1y + n1z * n1z;
     if (nn2 > 0.0) {
       double inn;
@@ -1477,9 +1477,11 @@ __global__ void k_nderiv(ForceArgs<R> a) {
         crs(v[0][0], v[0][1], v[0][2], hx, hy, hz, c1x, c1y, c1z);
         Fx = -(c0x + c1x); Fy = -(c0y + c1y); Fz = -(c0z + c1z);
       } else {
-        crs(v[2][0] - v[1][0], v[2][1] - v[1][1], v[2][2] - v[1][2], hx, hy, hz, c0x, c0y, c0z);
-        crs(v[0][0] - v[2][0], v[0][1] - v[2][1], v[0][2] - v[2][2], hx, hy, hz, c1x, c1y, c1z);
-        crs(v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2], hx, hy, hz, c2x, c2y, c2z);
+        // -(dn1/dv_m)^T h for m = 1, 2, 3: (v3 - v2) x h, (v1 - v3) x h, (v2 - v1) x h; the
+        // three sum to zero (no force on i), so the first is minus the other two
+        crs(-bx, -by, -bz, hx, hy, hz, c1x, c1y, c1z);
+        crs(ax, ay, az, hx, hy, hz, c2x, c2y, c2z);
+        c0x = -(c1x + c2x); c0y = -(c1y + c2y); c0z = -(c1z + c2z);
       }
       if (EV) {
         // virial of the neighbour forces relative to i (the term's forces sum to zero)

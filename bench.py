@@ -11,8 +11,9 @@ files are not available).
 Timing: W untimed warm-up steps, then exactly K steps (default 100, so that the
 neighbour-list rebuilds the run needs fall inside the timed region) timed on the device
 with CUDA events on the engine's stream (lmff_stats.ms_last_run), bracketed by
-torch.cuda.synchronize() (and a barrier with N > 1).  Inputs are far larger than L2
-(the pair list alone is ~15 GB), so no L2 flush is needed.
+torch.cuda.synchronize() (and a barrier with N > 1).  On the 2.7M-atom slab the
+inputs are far larger than L2 (the pair list alone is 10 GB), so no L2 flush is needed;
+config.l2 states the list size of each workload.
 
 Multi-GPU: the path is run as independent replicas (one system per GPU, no data-path
 collective): value = total atom-steps of all ranks / max rank time, scaling "weak".
@@ -52,6 +53,7 @@ ILP_FILE = os.path.join(ROOT, "lammps-lmff_gb300", "potentials", "BNCH.ILP")
 # 331,200-atom graphite slab (k_ilp<8,0,0,1,0,0>: 1.303 GB read + 19.7 MB written for
 # 310,301,280 entries; the list is larger than L2, so traffic grows with the entries)
 K_ILP_DRAM_BYTES_PER_ENTRY = (1.302568e9 + 19.73888e6) / 310301280
+L2_BYTES = 129e6   # GB300 L2
 ALG_FLOPS_PER_PAIR = 120
 ALG_FLOPS_PER_REJECTED = 9
 # What the gather kernel executes per directed pair (both repulsion terms and the full
@@ -516,6 +518,12 @@ def main():
                          f"oracle restatement, {cdt:.1f} s"}
 
     if rank == 0:
+        # the pair list is what every step streams from HBM; say whether it fits in the
+        # 129 MB L2 (no flush between steps either way: the steps of an MD run re-read it)
+        list_bytes = 4.0 * st["list_per_atom"] * s.n
+        l2_note = (f"inputs larger than L2 (pair list {list_bytes / 1e9:.1f} GB), no flush"
+                   if list_bytes > L2_BYTES else
+                   f"pair list {list_bytes / 1e6:.1f} MB fits in L2; no flush (MD steps re-read it)")
         metric = METRIC if args.workload == "graphite_2p7m" else f"atom-steps/s, workload {args.workload}"
         line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -527,7 +535,7 @@ def main():
                            "autotune": None if tuned is None else {
                                "probe_atoms": tuned["probe_atoms"], "picked": [tuned["tpa"], tuned["block"], tuned["skin"]],
                                "score_ms_probe": tuned["score_ms"]},
-                           "l2": "inputs larger than L2 (pair list ~15 GB), no flush",
+                           "l2": l2_note,
                            "parallelism": f"replicas x{world}", "wall_s": wall},
                 "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches_total, "graph_steps_timed": graph_steps,

@@ -416,8 +416,11 @@ def main():
         from lmff_gb300 import tune
         # tuned on the workload itself: a smaller patch of the same slab ranks the launch
         # shapes differently (measured: 16 threads per atom best at 331k, 8 at 2.7M)
+        # small systems also try 32 threads per atom: the pair kernel's time there is one
+        # thread's walk over its share of the list
         tuned = tune.tune(s, TERSOFF_FILE, ILP_FILE, elements=elements, precision=prec, device=local,
-                          tpas=(8, 16), blocks=(128, 256), skins=(1.0, 2.0), use_cache=False, n_full=s.n)
+                          tpas=(8, 16, 32) if s.n < 100_000 else (8, 16), blocks=(128, 256), skins=(1.0, 2.0),
+                          use_cache=False, n_full=s.n)
         args.tpa = args.tpa or tuned["tpa"]
         args.block = args.block or tuned["block"]
         args.skin = args.skin or tuned["skin"]

@@ -92,7 +92,7 @@ def test_mixed_precision_accuracy(name):
 
 
 @pytest.mark.parametrize("name", ["c1_t0", "hetero_small", "trilayer_alt", "edges", "tiny_images"])
-@pytest.mark.parametrize("tpa", [8, 16])
+@pytest.mark.parametrize("tpa", [8, 16, 32])
 def test_mixed_forces_without_energy_match_reference(name, tpa):
     """The production force-only pair kernels (no energy/virial: the single-element loop
     with two list entries per iteration and compact j records, and the multi-element

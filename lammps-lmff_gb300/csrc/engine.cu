@@ -583,7 +583,7 @@ struct Engine {
     if (device >= 0) cudaSetDevice(device);
     void *ptrs[] = {d.xq, d.xh, d.xl, d.v, d.f, d.xhold, d.tag, d.perm, d.sysid, d.mass, d.nrm64, d.nrm32, d.jrec, d.ilp_cnt,
                     d.ilp_nb, d.ters_cnt, d.ters_nb, d.ters_g, d.ters_f, d.ilp_f, d.ilp_c, d.ilp_g, d.list_off, d.list,
-                    d.short_cnt, d.short_nb, d.list_img, d.nin_tmp, d.list_tmp, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.cub_tmp,
+                    d.short_cnt, d.short_nb, d.list_img, d.nin_tmp, d.list_tmp, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.rowocc, d.cub_tmp,
                     d.cnt_tmp, d.sys, d.red_out, d.status, d.maxdisp, d_xin, d_fin, d_vin, d_ein, d_tin, d_sysin,
                     d_min, d_gin, d_massT, xq2, v2, mass2, tag2, perm2, sysid2, stat_ilp, stat_ters, eatom_ilp,
                     eatom_ters, ke, d_arrs, d_karrs, d_kout, d_cutILPsq};
@@ -992,7 +992,7 @@ struct Engine {
   }
   double device_bytes() const {
     return (double)cap_n * per_atom_bytes() + (double)(d.list_cap + d.tmp_cap) * sizeof(uint32_t) +
-           (double)d.cub_tmp_bytes + (double)d.nbins_cap * 2 * sizeof(int);
+           (double)d.cub_tmp_bytes + (double)d.nbins_cap * 3 * sizeof(int);
   }
   // device bytes per atom a batch like the current one needs: the per-atom arrays with
   // their growth margin, the pair list at the current density with the step graph's
@@ -1098,6 +1098,7 @@ struct Engine {
     if (d.nbins > d.nbins_cap) {
       CK(dalloc(d.bin_start, d.nbins));
       CK(dalloc(d.bin_end, d.nbins));
+      CK(dalloc(d.rowocc, d.nbins));
       d.nbins_cap = d.nbins;
     }
     d.nsys = (int)hsys.size();
@@ -1153,7 +1154,8 @@ struct Engine {
     CK(copy_back_permuted(stream));
     CK(cudaMemsetAsync(d.bin_start, 0, sizeof(int) * d.nbins, stream));
     CK(cudaMemsetAsync(d.bin_end, 0, sizeof(int) * d.nbins, stream));
-    nb_bin_ranges(n, d.bin_key2, d.bin_start, d.bin_end, stream);
+    CK(cudaMemsetAsync(d.rowocc, 0, sizeof(int) * d.nbins, stream));
+    nb_bin_ranges(n, d.bin_key2, d.bin_start, d.bin_end, stream, d.sys, d.sysid, d.rowocc);
     // atoms' systems are contiguous after the sort: atom ranges per system
     CK(cudaGetLastError());
     hilo_all();
@@ -1167,6 +1169,7 @@ struct Engine {
     a.sysid = d.sysid;
     a.bin_start = d.bin_start;
     a.bin_end = d.bin_end;
+    a.rowocc = d.rowocc;
     a.nbins = d.nbins;
     a.bin_key = d.bin_key2;
     a.list_off = d.list_off;
@@ -1647,7 +1650,8 @@ struct Engine {
     copy_back_permuted(s);
     cudaMemsetAsync(d.bin_start, 0, sizeof(int) * d.nbins, s);
     cudaMemsetAsync(d.bin_end, 0, sizeof(int) * d.nbins, s);
-    nb_bin_ranges(n, d.bin_key2, d.bin_start, d.bin_end, s);
+    cudaMemsetAsync(d.rowocc, 0, sizeof(int) * d.nbins, s);
+    nb_bin_ranges(n, d.bin_key2, d.bin_start, d.bin_end, s, d.sys, d.sysid, d.rowocc);
     hilo_all(s);
     NbArgs a;
     memset(&a, 0, sizeof a);
@@ -1659,6 +1663,7 @@ struct Engine {
     a.sysid = d.sysid;
     a.bin_start = d.bin_start;
     a.bin_end = d.bin_end;
+    a.rowocc = d.rowocc;
     a.nbins = d.nbins;
     a.bin_key = d.bin_key2;
     a.list_off = d.list_off;

@@ -173,6 +173,7 @@ struct DevState {
   uint32_t *bin_key2 = nullptr;
   int *idx = nullptr, *idx2 = nullptr;
   int *bin_start = nullptr, *bin_end = nullptr;
+  int *rowocc = nullptr;       // per bin: 1 at the first bin of an occupied bin row
   int nbins = 0, nbins_cap = 0;
   void *cub_tmp = nullptr;
   size_t cub_tmp_bytes = 0;

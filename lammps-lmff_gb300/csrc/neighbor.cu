@@ -64,11 +64,21 @@ __global__ void k_permute(int n, const int *idx2, const d4 *xq, d4 *xq2, const d
   mass2[q] = mass[o];
 }
 
-__global__ void k_bin_ranges(int n, const uint32_t *key, int *bin_start, int *bin_end) {
+// Atom range of every occupied bin, and (rowocc) a flag at the first bin of every bin
+// row that holds atoms: the list build skips empty rows of its stencil whole (a bilayer
+// in a box with vacuum leaves most of them empty).
+__global__ void k_bin_ranges(int n, const uint32_t *key, int *bin_start, int *bin_end, const SysDesc *sys,
+                             const int *sysid, int *rowocc) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   uint32_t k = key[q];
-  if (q == 0 || key[q - 1] != k) bin_start[k] = q;
+  if (q == 0 || key[q - 1] != k) {
+    bin_start[k] = q;
+    if (rowocc) {
+      const SysDesc &sd = sys[sysid[q]];
+      rowocc[k - (uint32_t)((int)k - sd.bin_begin) % (uint32_t)sd.nb[0]] = 1;
+    }
+  }
   if (q == n - 1 || key[q + 1] != k) bin_end[k] = q + 1;
 }
 
@@ -183,6 +193,7 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
           sy = jy >= 0 ? jy / sd.nb[1] : -((-jy + sd.nb[1] - 1) / sd.nb[1]);
           jy -= sy * sd.nb[1];
         } else if (jy < 0 || jy >= sd.nb[1]) continue;
+        if (a.rowocc && !a.rowocc[sd.bin_begin + (jz * sd.nb[1] + jy) * sd.nb[0]]) continue;   // empty row
         for (int xu = xmin - sd.reach[0]; xu <= xmax + sd.reach[0]; xu++) {
           int jx = xu, sx = 0;
           if (sd.per[0]) {
@@ -331,8 +342,9 @@ void nb_permute(int n, const int *idx2, const d4 *xq, d4 *xq2, const double *v, 
   if (n) k_permute<<<(n + 255) / 256, 256, 0, s>>>(n, idx2, xq, xq2, v, v2, tag, tag2, perm, perm2, sysid, sysid2, mass, mass2);
 }
 
-void nb_bin_ranges(int n, const uint32_t *key, int *bs, int *be, cudaStream_t s) {
-  if (n) k_bin_ranges<<<(n + 255) / 256, 256, 0, s>>>(n, key, bs, be);
+void nb_bin_ranges(int n, const uint32_t *key, int *bs, int *be, cudaStream_t s, const SysDesc *sys, const int *sysid,
+                   int *rowocc) {
+  if (n) k_bin_ranges<<<(n + 255) / 256, 256, 0, s>>>(n, key, bs, be, sys, sysid, rowocc);
 }
 
 void nb_hilo(int n, const d4 *xq, const SysDesc *sys, const int *sysid, float4 *xh, float4 *xl, cudaStream_t s) {

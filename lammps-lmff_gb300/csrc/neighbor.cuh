@@ -24,6 +24,7 @@ struct NbArgs {
   const int *sysid;
   const int *bin_start;
   const int *bin_end;
+  const int *rowocc;  // 1 at the first bin of every bin row (fixed y, z) holding atoms, or null
   int nbins;          // global bins
   const uint32_t *bin_key;   // global bin of each atom (sorted order)
   const int64_t *list_off;
@@ -51,7 +52,8 @@ cudaError_t nb_scan(void *tmp, size_t tmp_bytes, const int64_t *cnt, int64_t *of
 void nb_permute(int n, const int *idx2, const d4 *xq, d4 *xq2, const double *v, double *v2, const int64_t *tag,
                 int64_t *tag2, const int *perm, int *perm2, const int *sysid, int *sysid2, const double *mass,
                 double *mass2, cudaStream_t s);
-void nb_bin_ranges(int n, const uint32_t *key, int *bs, int *be, cudaStream_t s);
+void nb_bin_ranges(int n, const uint32_t *key, int *bs, int *be, cudaStream_t s, const SysDesc *sys = nullptr,
+                   const int *sysid = nullptr, int *rowocc = nullptr);
 void nb_hilo(int n, const d4 *xq, const SysDesc *sys, const int *sysid, float4 *xh, float4 *xl, cudaStream_t s);
 // mode 0: count (+ short lists); 1: fill the CSR list; 2: count and write each atom's
 // entries into the strided buffer, for nb_compact after the scan

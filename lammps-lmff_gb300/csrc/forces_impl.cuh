@@ -761,34 +761,34 @@ __device__ __forceinline__ void rep_term(const IlpP<R> &p, R exp0, R exp1, R rho
 // with fewer FP64 instructions at full double accuracy (results within a few ulp of the
 // library functions, far inside the 1e-10 parity bar).
 //
-// e^x by Tang's table-driven method (P. T. P. Tang, ACM TOMS 15, 1989): n = rint(64 x /
-// ln2), r = x - n ln2/64 (|r| <= ln2/128; one FMA with ln2/64 rounded to double costs
-// at most |n| 2^-60 absolute, below 1e-14 relative for |x| < 700), e^x = 2^(n>>6)
-// 2^((n&63)/64) (1 + p(r)), p the degree-6 Taylor polynomial of e^r - 1 (truncation
-// below 1e-19).  Outside |x| < 700 the library exp.
-__device__ double g_exp2_64[64];
+// e^x by Tang's table-driven method (P. T. P. Tang, ACM TOMS 15, 1989): n = rint(256 x /
+// ln2), r = x - n ln2/256 (|r| <= ln2/512; one FMA with ln2/256 rounded to double costs
+// at most |n| 2^-62 absolute, below 1e-14 relative for |x| < 700), e^x = 2^(n>>8)
+// 2^((n&255)/256) (1 + p(r)), p the degree-4 Taylor polynomial of e^r - 1 (truncation
+// below 4e-17 relative: the 256-entry table keeps |r| small enough for degree 4, two FP64
+// FMAs fewer than degree 6 over 64 entries).  Outside |x| < 700 the library exp.
+constexpr int EXP2_F64_N = 256;
+__device__ double g_exp2_f64[EXP2_F64_N];
 
-__global__ void k_fill_exp2_64() {
+__global__ void k_fill_exp2_f64() {
   const int j = threadIdx.x;
-  if (j < 64) g_exp2_64[j] = exp2((double)j / 64.0);
+  if (j < EXP2_F64_N) g_exp2_f64[j] = exp2((double)j / EXP2_F64_N);
 }
 
 __device__ __forceinline__ double exp_t64(double x) {
   if (!(fabs(x) < 700.0)) return exp(x);
   const double magic = 6755399441055744.0;   // 1.5 * 2^52
-  const double tn = __dadd_rn(x * 92.332482616893657, magic);   // 64 / ln2
+  const double tn = __dadd_rn(x * 369.3299304675746, magic);   // 256 / ln2
   const int n = __double2loint(tn);
   const double nd = __dsub_rn(tn, magic);
-  const double r = fma(-nd, 0.010830424696249145, x);             // ln2 / 64
-  double p = fma(r, 1.0 / 720.0, 1.0 / 120.0);
-  p = fma(p, r, 1.0 / 24.0);
-  p = fma(p, r, 1.0 / 6.0);
+  const double r = fma(-nd, 0.0027076061740622863, x);          // ln2 / 256
+  double p = fma(r, 1.0 / 24.0, 1.0 / 6.0);
   p = fma(p, r, 0.5);
   p = fma(p, r, 1.0);
   p = p * r;
-  const double T = __ldg(&g_exp2_64[n & 63]);
+  const double T = __ldg(&g_exp2_f64[n & (EXP2_F64_N - 1)]);
   const double v = fma(T, p, T);
-  return __hiloint2double(__double2hiint(v) + (int)((unsigned)(n >> 6) << 20), __double2loint(v));
+  return __hiloint2double(__double2hiint(v) + (int)((unsigned)(n >> 8) << 20), __double2loint(v));
 }
 
 // 1/sqrt(x), 1/x: FP32 estimates (relative error ~2^-22) and one FP64 Newton step
@@ -1598,7 +1598,7 @@ __global__ void k_ters_eatom_own(ForceArgs<R> a) {
 
 void upload_pot(const PotConst<R> &p, cudaStream_t s) {
   cudaMemcpyToSymbolAsync(c_pot, &p, sizeof(p), 0, cudaMemcpyHostToDevice, s);
-  if (sizeof(R) == 8) k_fill_exp2_64<<<1, 64, 0, s>>>();
+  if (sizeof(R) == 8) k_fill_exp2_f64<<<1, EXP2_F64_N, 0, s>>>();
 #ifdef LMFF_PACKED_X2
   {
     static PairX2Const x2;   // static: the asynchronous copy reads it after return

@@ -245,7 +245,9 @@ int lmff_compute_device(lmff_engine *e, int natoms, const double *d_x, const int
  * is allocated: every buffer the kernels need (sorted atoms, bins, neighbour lists,
  * normals, force slots, reductions, sort workspace) lives in one 16 MiB static device
  * array that every GPU loading this library holds until the process exits.  Limits:
- * natoms <= 2048, at most 8192 neighbour bins, and the pair list must fit the space
+ * natoms <= 2048 (natoms = 0, an empty subdomain, returns LMFF_OK with zero energies
+ * and virials, as lmff_compute_device does), at most 8192 neighbour bins, a box whose
+ * periodic images leave the 32-bit list code room for natoms, and the pair list must fit the space
  * left in the array (about 1,600 entries per atom at 2048 atoms); larger requests are
  * rejected with LMFF_EINVAL or LMFF_EOVERFLOW and a message, never truncated.  The
  * engine handle supplies parameters, box, precision and stream.  The first call on a

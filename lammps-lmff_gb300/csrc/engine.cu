@@ -2424,10 +2424,14 @@ struct Carve {
 
 int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const int64_t *dmol, int which, int eflag,
                     int vflag, double *df, lmff_result *res) {
-  if (nn < 1 || nn > NOALLOC_MAX_ATOMS)
-    return g.fail(LMFF_EINVAL, "lmff_compute_device_noalloc: natoms must be in 1.." +
+  if (nn < 0 || nn > NOALLOC_MAX_ATOMS)
+    return g.fail(LMFF_EINVAL, "lmff_compute_device_noalloc: natoms must be in 0.." +
                                    std::to_string(NOALLOC_MAX_ATOMS) + " (got " + std::to_string(nn) + ")");
   if (!g.have_box) return g.fail(LMFF_EINVAL, "lmff_set_box must be called first");
+  if (nn == 0) {   // an empty subdomain: no force, zero energies and virials (as lmff_compute_device)
+    if (res) memset(res, 0, sizeof *res);
+    return LMFF_OK;
+  }
   void *basev = nullptr;
   int rc = noalloc_base(g.device, &basev, g.err);
   if (rc) return rc;
@@ -2455,6 +2459,8 @@ int noalloc_compute(Engine &g, int nn, const double *dx, const int *dtype, const
   lc.ibits = 32 - 3 * lc.w;
   lc.imask = (1u << lc.ibits) - 1u;
   lc.wmask = (1u << lc.w) - 1u;
+  if ((int64_t)nn >= (1LL << lc.ibits))
+    return g.fail(LMFF_EOVERFLOW, "too many atoms for the 32-bit neighbour-list code of this box");
   int nbits = 1;
   while ((1LL << nbits) < nbins) nbits++;
   // carve the scratch array
@@ -2867,8 +2873,8 @@ int lmff_compute_device(lmff_engine *e, int natoms, const double *d_x, const int
 
 int lmff_compute_device_noalloc(lmff_engine *e, int natoms, const double *d_x, const int *d_type,
                                 const int64_t *d_mol, int which, int eflag, int vflag, double *d_f, lmff_result *res) {
-  if (!e || !d_x || !d_type || !d_f) return LMFF_EINVAL;
-  if (!d_mol) return e->e.fail(LMFF_EINVAL, "lmff_compute_device_noalloc: d_mol is required");
+  if (!e || natoms < 0 || (natoms > 0 && (!d_x || !d_type || !d_f))) return LMFF_EINVAL;
+  if (natoms > 0 && !d_mol) return e->e.fail(LMFF_EINVAL, "lmff_compute_device_noalloc: d_mol is required");
   DeviceCall dc(e->e);
   return lmff::noalloc_compute(e->e, natoms, d_x, d_type, d_mol, which, eflag, vflag, d_f, res);
 }

@@ -763,7 +763,8 @@ __device__ __forceinline__ void rep_term(const IlpP<R> &p, R exp0, R exp1, R rho
 //
 // e^x by Tang's table-driven method (P. T. P. Tang, ACM TOMS 15, 1989): n = rint(256 x /
 // ln2), r = x - n ln2/256 (|r| <= ln2/512; one FMA with ln2/256 rounded to double costs
-// at most |n| 2^-62 absolute, below 1e-14 relative for |x| < 700), e^x = 2^(n>>8)
+// at most |n| 2^-62 absolute in r, hence in the relative error of e^x: |n| < 2^18, so
+// below 6e-14 for |x| < 700 and below 4e-15 for |x| < 40), e^x = 2^(n>>8)
 // 2^((n&255)/256) (1 + p(r)), p the degree-4 Taylor polynomial of e^r - 1 (truncation
 // below 4e-17 relative: the 256-entry table keeps |r| small enough for degree 4, two FP64
 // FMAs fewer than degree 6 over 64 entries).  Outside |x| < 700 the library exp.

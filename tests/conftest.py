@@ -10,6 +10,8 @@ for p in (os.path.join(ROOT, "lammps-lmff_gb300"), os.path.join(ROOT, "oracle"),
         sys.path.insert(0, p)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
+# the reference source tree (present where the fixtures were made, absent on GPU hosts)
+REFERENCE = os.environ.get("LMFF_REFERENCE", "/root/reference")
 POT = os.path.join(ROOT, "lammps-lmff_gb300", "potentials")
 TERSOFF = os.path.join(POT, "BNC.tersoff")
 ILP = os.path.join(POT, "BNCH.ILP")

@@ -8,7 +8,7 @@ import os
 
 import numpy as np
 import pytest
-from conftest import ROOT, load_golden, min_image, rel_max, rel_rms
+from conftest import REFERENCE, ROOT, load_golden, min_image, rel_max, rel_rms
 
 from lmff_gb300 import build, capi
 from lmff_gb300 import structures as S
@@ -16,7 +16,7 @@ from lmff_gb300 import structures as S
 POT = os.path.join(ROOT, "lammps-lmff_gb300", "potentials")
 TERSOFF_ELEMS = ("NULL", "C(O)", "C(O)", "C(O)", "C(O)", "C(O)")
 ILP_ELEMS = ("C",) * 6
-CASE_DATA = "/root/reference/Cases/case_5016/inf0.data"
+CASE_DATA = os.path.join(REFERENCE, "Cases", "case_5016", "inf0.data")
 F64_TOL = 1e-10
 MIX_F_ABS = 1e-5
 

@@ -34,6 +34,11 @@ constexpr bool TWO_PAIR_BODY = true;
 constexpr bool TWO_PAIR_BODY = false;
 #endif
 
+// whether the two-pair loop applies (set with the constants by upload_pot, read by the
+// launch): element 0's C >= 0 (single element); symmetric element-pair constants with
+// C >= 0 (several elements)
+static int h_two_one = 0, h_two_multi = 0;
+
 __device__ __forceinline__ R cR(double v) { return (R)v; }
 
 __device__ __forceinline__ void raise_status(int *status, int bit) { atomicOr(status, bit); }
@@ -709,11 +714,110 @@ __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
 // force on each intralayer neighbour (ilp_c slots).
 // ONE: every ILP-mapped type is the same element, so the pair parameters are read at a
 // compile-time constant index (constant-bank operands, no per-pair loads).
-// per-atom accumulators of the pair kernel
+// Pairs a lane sums in R before the lanes' partial sums go into the atom's FP64
+// totals (mixed precision: FP32 pair arithmetic, FP64 per-atom accumulation of forces,
+// dE/dn_i, energies and virial).  A flush combines the TPA lanes' FP32 block sums
+// (reduce-scatter by shuffles, 7 shuffles and adds per lane) and each lane adds the
+// one or two totals it owns in FP64: two FP64 instructions per lane and flush.  Each
+// lane holding FP64 totals of its own instead (14 FP64 conversions and adds per flush,
+// the FP64 pipe being 1/64 of the FP32 rate) cost 9 % of the 2.7M-atom pair kernel;
+// this form costs 3 % at 32 pairs per lane between flushes (2.5 % at 64).
+#ifndef LMFF_ILP_FLUSH_PAIRS
+#define LMFF_ILP_FLUSH_PAIRS 32
+#endif
+constexpr int ILP_FLUSH_PAIRS = LMFF_ILP_FLUSH_PAIRS;
+
+// per-atom accumulators of the pair kernel: one lane's partial sums in R (mixed
+// precision: over at most ILP_FLUSH_PAIRS pairs of the block since the last flush)
 struct IlpAcc {
   R fx = 0, fy = 0, fz = 0, gxa = 0, gya = 0, gza = 0;
   R tpi = 0;   // two-pair loop: sum of the n_i coefficients, applied once (f -= tpi n_i)
   R evdw = 0, erep = 0, w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
+};
+
+// Reduce-scatter over the TPA lanes of one atom (lane = thread index mod TPA, m = the
+// group's shuffle mask): v[H] of every lane in; out, each lane holds in v[0 .. H/TPA)
+// (at least v[0]) the sums over the lanes of the slots rs_slot0(lane) + k.  Halving
+// levels first (a lane keeps the half selected by its lane bit and adds the partner's
+// copy of it), then, with more lanes than slots, full levels (both partners form the
+// same sum, a + b = b + a).  Fixed order: results are bitwise reproducible.
+template <int O, int H>
+struct LaneRS {
+  static __device__ __forceinline__ void run(float *v, int lane, unsigned m) {
+    if constexpr (O > 0) {
+      if constexpr (H > 1) {
+        constexpr int h = H / 2;
+        const bool up = (lane & O) != 0;
+#pragma unroll
+        for (int k = 0; k < h; k++) {
+          const float send = up ? v[k] : v[k + h];
+          const float keep = up ? v[k + h] : v[k];
+          v[k] = keep + __shfl_xor_sync(m, send, O);
+        }
+        LaneRS<O / 2, h>::run(v, lane, m);
+      } else {
+        v[0] += __shfl_xor_sync(m, v[0], O);
+        LaneRS<O / 2, 1>::run(v, lane, m);
+      }
+    }
+  }
+};
+template <int TPA, int NS>
+__device__ __forceinline__ int rs_slot0(int lane) {
+  int base = 0, h = NS;
+#pragma unroll
+  for (int o = TPA / 2; o > 0; o >>= 1)
+    if (h > 1) {
+      h >>= 1;
+      if (lane & o) base += h;
+    }
+  return base;
+}
+
+// The FP64 totals of one atom, spread over its TPA lanes (mixed precision).  Slots:
+// 0-2 force on i (the n_i terms of the two-pair loop folded in), 3-5 dE/dn_i,
+// energy/virial kernels also 6 evdw, 7 erep, 8-13 virial, 14 evdw + erep (per-atom
+// energy).  With TPA > slots several lanes hold the same total ("primary": the first).
+// FP64 (R = double): the accumulators are the totals and nothing here runs.
+constexpr bool ILP_TOT_SPLIT = sizeof(R) == 4;
+template <int TPA, bool EV, bool EATOM>
+struct LaneTot {
+  static constexpr int NS = EV ? 16 : 8;
+  static constexpr int HOLD = NS > TPA ? NS / TPA : 1;
+  // The totals sit in shared memory ([HOLD][256] doubles per block, one column per
+  // thread, 2 KB at 8 lanes per atom) and lane and shuffle mask are recomputed at each
+  // flush, so that the pair loop holds no register for them (held in registers, they
+  // made the two-pair loop spill at 64 registers: 4.3 % slower at 2.7M atoms).
+  double *t;
+  __device__ __forceinline__ void init(double *s) {
+    t = s + threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < HOLD; k++) t[k * 256] = 0.0;
+  }
+  __device__ __forceinline__ double get(int k) const { return t[k * 256]; }
+  __device__ __forceinline__ void flush(IlpAcc &acc, R nix, R niy, R niz) {
+    if constexpr (ILP_TOT_SPLIT) {
+      const int lane = threadIdx.x & (TPA - 1);
+      const unsigned gmask = TPA == 32 ? 0xffffffffu : ((1u << TPA) - 1u) << ((threadIdx.x & 31) & ~(TPA - 1));
+      float v[NS];
+      v[0] = fmaf(-acc.tpi, nix, acc.fx);
+      v[1] = fmaf(-acc.tpi, niy, acc.fy);
+      v[2] = fmaf(-acc.tpi, niz, acc.fz);
+      v[3] = acc.gxa; v[4] = acc.gya; v[5] = acc.gza;
+      if constexpr (EV) {
+        v[6] = acc.evdw; v[7] = acc.erep;
+        v[8] = acc.w0; v[9] = acc.w1; v[10] = acc.w2; v[11] = acc.w3; v[12] = acc.w4; v[13] = acc.w5;
+        v[14] = EATOM ? acc.evdw + acc.erep : 0.f;
+        v[15] = 0.f;
+      } else {
+        v[6] = 0.f; v[7] = 0.f;
+      }
+      LaneRS<TPA / 2, NS>::run(v, lane, gmask);
+#pragma unroll
+      for (int k = 0; k < HOLD; k++) t[k * 256] += (double)v[k];
+      acc = IlpAcc{};
+    }
+  }
 };
 
 // normal of j as R
@@ -963,13 +1067,13 @@ __constant__ PairX2Const c_x2;
 // neighbours of one iteration, the parameter pairs (X[a][b], X[a][c]) of every per-pair
 // constant, one 64-bit shared-memory read each.  Valid when every element pair's
 // parameters equal those of the swapped pair (then both repulsion terms and vdW use
-// X[a][b]) and C >= 0 (c_pair2_multi, set by upload_pot).
+// X[a][b]) and C >= 0 (h_two_multi, set by upload_pot).
 constexpr int X2M_N = 11;   // nd2_l2e, log2C, eps, 2/delta^2, lambda, -lam log2e, lam z0 log2e,
                             // -ts_a, ts_a seff, C6, d/seff
 constexpr int X2M_ROWS = MAXELEM * MAXELEM * MAXELEM;
 __device__ float2 g_x2m[X2M_ROWS * X2M_N];
 __shared__ float2 s_x2m[X2M_ROWS * X2M_N];
-__constant__ int c_pair2_multi;
+
 
 template <bool EV, bool ONE, bool KC, bool IMG>
 __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const AtomI<float> &ai, const SysDesc &sdl,
@@ -1251,13 +1355,16 @@ __device__ __forceinline__ void pair_body(const ForceArgs<R> &a, const AtomI<R> 
 // better than 36 (measured: -8 % at 2.7M atoms, -16 % at 490k).  The two-pair body of
 // the single-element path needs 76 registers without spills; 4 blocks (64 registers)
 // measured 3 % faster than 3 blocks at 2.7M atoms.  FP64 keeps its registers.
-template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC>
+template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC, bool TWO>
 constexpr int ilp_min_blocks() {
-  return sizeof(R) == 8 ? 1 : (TWO_PAIR_BODY && !EV && !KC) ? 4 : 5;
+  return sizeof(R) == 8 ? 1 : TWO ? 4 : 5;
 }
 
-template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC>
-__global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, KC>())) k_ilp(ForceArgs<R> a) {
+// TWO: the two-pair loop alone (mixed precision, forces only, interlayer list, C >= 0
+// and symmetric element-pair constants: the host checks these), in a kernel of its own
+// so that the generic loops do not share its register allocation
+template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC, bool TWO>
+__global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, KC, TWO>())) k_ilp(ForceArgs<R> a) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gtid / TPA;
   const int lane = threadIdx.x & (TPA - 1);
@@ -1274,6 +1381,16 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
   else { float4 q = a.nrm32[ii]; nix = q.x; niy = q.y; niz = q.z; }
   const long long itag = c_pot.vdw_sym ? 0 : a.tag[ii];
   IlpAcc acc;
+  __shared__ double s_tot[ILP_TOT_SPLIT ? LaneTot<TPA, EV, EATOM>::HOLD : 1][256];
+  LaneTot<TPA, EV, EATOM> tot;
+  if constexpr (ILP_TOT_SPLIT) tot.init(&s_tot[0][0]);
+  // a flush after the iteration of lane entry k: every ILP_FLUSH_PAIRS pairs of a lane,
+  // when all TPA lanes run that iteration (then the condition is the same for all of
+  // them); what is left at the end goes with the final flush
+#define ILP_FLUSH_AT(k, step, last)                                                         \
+  if constexpr (ILP_TOT_SPLIT)                                                               \
+    if ((((k) + (step)) & (TPA * ILP_FLUSH_PAIRS - 1)) < TPA && ((k) | (TPA - 1)) + (last) < cnt) \
+      tot.flush(acc, nix, niy, niz);
   SysDesc sdl;  // box of i's system in registers for the image shifts
 #pragma unroll
   for (int d = 0; d < 3; d++) {
@@ -1284,14 +1401,17 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
   // a list without list_full holds only interlayer pairs of ILP-mapped types (k_list)
   const bool check = a.list_full != 0;
   if constexpr (!ONE) {
-    const int words = (int)(sizeof(c_pot.ilp) / sizeof(int));
-    const int *src = reinterpret_cast<const int *>(c_pot.ilp);
-    int *dst = reinterpret_cast<int *>(s_ilp);
-    for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
 #ifdef LMFF_PACKED_X2
-    if (TWO_PAIR_BODY && !EV && !KC && c_pair2_multi)
+    if constexpr (TWO) {
       for (int w = threadIdx.x; w < X2M_ROWS * X2M_N; w += blockDim.x) s_x2m[w] = g_x2m[w];
+    } else
 #endif
+    {
+      const int words = (int)(sizeof(c_pot.ilp) / sizeof(int));
+      const int *src = reinterpret_cast<const int *>(c_pot.ilp);
+      int *dst = reinterpret_cast<int *>(s_ilp);
+      for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+    }
     __syncthreads();
   }
   if (valid && ie >= 0) {
@@ -1303,8 +1423,8 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
     auto run = [&](auto img_t) {
       constexpr bool IMG = decltype(img_t)::value;
 #ifdef LMFF_PACKED_X2
-      if constexpr (TWO_PAIR_BODY && !EV && !KC) {
-        if (!check && (ONE ? c_pot.ilp[0].C >= 0.f : c_pair2_multi != 0)) {
+      if constexpr (TWO) {
+        {
           // two entries (k, k + TPA) per iteration, loaded one iteration ahead, j's data
           // from the compact 32-byte records
           const float3 loi = make_float3(__half2float(__float2half_rn(ai.lx)), __half2float(__float2half_rn(ai.ly)),
@@ -1313,12 +1433,13 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
           uint32_t eA = k < cnt ? __ldg(&lst[k]) : 0u;
           uint32_t eB = k + TPA < cnt ? __ldg(&lst[k + TPA]) : 0u;
           for (; k + TPA < cnt; k += 2 * TPA) {
-            const uint32_t ea = eA, eb = eB;
-            if (k + 2 * TPA < cnt) eA = __ldg(&lst[k + 2 * TPA]);
-            if (k + 3 * TPA < cnt) eB = __ldg(&lst[k + 3 * TPA]);
-            const size_t ja = 2 * (size_t)(ea & a.lc.imask), jb = 2 * (size_t)(eb & a.lc.imask);
-            ilp_pair2<ONE, IMG>(a, ai, loi, sdl, ea, __ldg(&a.A.jrec2[ja]), __ldg(&a.A.jrec2[ja + 1]), eb,
-                                __ldg(&a.A.jrec2[jb]), __ldg(&a.A.jrec2[jb + 1]), true, nix, niy, niz, ie, acc);
+              const uint32_t ea = eA, eb = eB;
+              if (k + 2 * TPA < cnt) eA = __ldg(&lst[k + 2 * TPA]);
+              if (k + 3 * TPA < cnt) eB = __ldg(&lst[k + 3 * TPA]);
+              const size_t ja = 2 * (size_t)(ea & a.lc.imask), jb = 2 * (size_t)(eb & a.lc.imask);
+              ilp_pair2<ONE, IMG>(a, ai, loi, sdl, ea, __ldg(&a.A.jrec2[ja]), __ldg(&a.A.jrec2[ja + 1]), eb,
+                                  __ldg(&a.A.jrec2[jb]), __ldg(&a.A.jrec2[jb + 1]), true, nix, niy, niz, ie, acc);
+              ILP_FLUSH_AT(k, 2 * TPA, TPA)
           }
           if (k < cnt) {
             const size_t ja = 2 * (size_t)(eA & a.lc.imask);
@@ -1327,7 +1448,7 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
           }
           return;
         }
-      }
+      } else
 #endif
       if constexpr (ONE) {
         // the next list entry is loaded one iteration ahead, so that only j's data (not
@@ -1340,6 +1461,7 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
           const int j = (int)(e & a.lc.imask);
           pair_body<EV, ONE, KC, IMG>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi,
                                       itag, check, acc);
+          ILP_FLUSH_AT(k, TPA, 0)
         }
       } else {
         for (int k = lane; k < cnt; k += TPA) {
@@ -1347,6 +1469,7 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
           const int j = (int)(e & a.lc.imask);
           pair_body<EV, ONE, KC, IMG>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi,
                                       itag, check, acc);
+          ILP_FLUSH_AT(k, TPA, 0)
         }
       }
     };
@@ -1376,44 +1499,68 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
           N = NrmJ<R>::load(a, j);
         }
         pair_body<EV, ONE, KC, true>(a, ai, sdl, ec, Jc, Nc, nix, niy, niz, ie, mi, itag, check, acc);
+        ILP_FLUSH_AT(k, TPA, 0)
       }
     }
   }
-  R fx = acc.fx - acc.tpi * nix, fy = acc.fy - acc.tpi * niy, fz = acc.fz - acc.tpi * niz;
-  R gxa = acc.gxa, gya = acc.gya, gza = acc.gza;
-  R evdw = acc.evdw, erep = acc.erep, w0 = acc.w0, w1 = acc.w1, w2 = acc.w2, w3 = acc.w3, w4 = acc.w4, w5 = acc.w5;
-  // ---- reduce over the TPA lanes of atom i in R; one conversion to FP64 per atom
+#undef ILP_FLUSH_AT
+  if constexpr (ILP_TOT_SPLIT) {
+    // final flush (all lanes of atom i reach it), then each primary lane stores the
+    // FP64 totals it holds
+    tot.flush(acc, nix, niy, niz);
+    constexpr int NS = LaneTot<TPA, EV, EATOM>::NS, HOLD = LaneTot<TPA, EV, EATOM>::HOLD;
+    if (!valid || (TPA > NS && (lane & (TPA / NS - 1)) != 0)) return;
+    const int s0 = rs_slot0<TPA, NS>(lane);
 #pragma unroll
-  for (int o = TPA / 2; o > 0; o >>= 1) {
-    fx += __shfl_xor_sync(0xffffffff, fx, o);
-    fy += __shfl_xor_sync(0xffffffff, fy, o);
-    fz += __shfl_xor_sync(0xffffffff, fz, o);
-    gxa += __shfl_xor_sync(0xffffffff, gxa, o);
-    gya += __shfl_xor_sync(0xffffffff, gya, o);
-    gza += __shfl_xor_sync(0xffffffff, gza, o);
-    if (EV) {
-      evdw += __shfl_xor_sync(0xffffffff, evdw, o);
-      erep += __shfl_xor_sync(0xffffffff, erep, o);
-      w0 += __shfl_xor_sync(0xffffffff, w0, o);
-      w1 += __shfl_xor_sync(0xffffffff, w1, o);
-      w2 += __shfl_xor_sync(0xffffffff, w2, o);
-      w3 += __shfl_xor_sync(0xffffffff, w3, o);
-      w4 += __shfl_xor_sync(0xffffffff, w4, o);
-      w5 += __shfl_xor_sync(0xffffffff, w5, o);
+    for (int k = 0; k < HOLD; k++) {
+      const int sl = s0 + k;
+      const double t = tot.get(k);
+      if (sl < 3) a.ilp_f[(size_t)sl * a.n + i] = t;
+      else if (sl < 6) {
+        double *g = reinterpret_cast<double *>(&a.ilp_g[i]);
+        g[sl - 3] = t;
+        if (sl == 3) g[3] = 0.0;
+      } else if (EV && sl < 14) a.stat_ilp[(size_t)(sl - 6) * a.n + i] = t;
+      else if (EV && EATOM && sl == 14) a.eatom_ilp[i] = t;
     }
-  }
-  if (!valid || lane != 0) return;
-  a.ilp_f[i] = (double)fx;
-  a.ilp_f[a.n + i] = (double)fy;
-  a.ilp_f[2 * a.n + i] = (double)fz;
-  a.ilp_g[i] = make_d4((double)gxa, (double)gya, (double)gza, 0.0);
-  if (EV) {
-    double *st = a.stat_ilp;
-    st[i] = (double)evdw;
-    st[(size_t)a.n + i] = (double)erep;
-    st[(size_t)2 * a.n + i] = (double)w0; st[(size_t)3 * a.n + i] = (double)w1; st[(size_t)4 * a.n + i] = (double)w2;
-    st[(size_t)5 * a.n + i] = (double)w3; st[(size_t)6 * a.n + i] = (double)w4; st[(size_t)7 * a.n + i] = (double)w5;
-    if (EATOM) a.eatom_ilp[i] = (double)evdw + (double)erep;
+  } else {
+    double fx = acc.fx - acc.tpi * nix, fy = acc.fy - acc.tpi * niy, fz = acc.fz - acc.tpi * niz;
+    double gxa = acc.gxa, gya = acc.gya, gza = acc.gza;
+    double evdw = acc.evdw, erep = acc.erep, w0 = acc.w0, w1 = acc.w1, w2 = acc.w2, w3 = acc.w3, w4 = acc.w4,
+           w5 = acc.w5;
+    // ---- reduce over the TPA lanes of atom i
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) {
+      fx += __shfl_xor_sync(0xffffffff, fx, o);
+      fy += __shfl_xor_sync(0xffffffff, fy, o);
+      fz += __shfl_xor_sync(0xffffffff, fz, o);
+      gxa += __shfl_xor_sync(0xffffffff, gxa, o);
+      gya += __shfl_xor_sync(0xffffffff, gya, o);
+      gza += __shfl_xor_sync(0xffffffff, gza, o);
+      if (EV) {
+        evdw += __shfl_xor_sync(0xffffffff, evdw, o);
+        erep += __shfl_xor_sync(0xffffffff, erep, o);
+        w0 += __shfl_xor_sync(0xffffffff, w0, o);
+        w1 += __shfl_xor_sync(0xffffffff, w1, o);
+        w2 += __shfl_xor_sync(0xffffffff, w2, o);
+        w3 += __shfl_xor_sync(0xffffffff, w3, o);
+        w4 += __shfl_xor_sync(0xffffffff, w4, o);
+        w5 += __shfl_xor_sync(0xffffffff, w5, o);
+      }
+    }
+    if (!valid || lane != 0) return;
+    a.ilp_f[i] = fx;
+    a.ilp_f[a.n + i] = fy;
+    a.ilp_f[2 * a.n + i] = fz;
+    a.ilp_g[i] = make_d4(gxa, gya, gza, 0.0);
+    if (EV) {
+      double *st = a.stat_ilp;
+      st[i] = evdw;
+      st[(size_t)a.n + i] = erep;
+      st[(size_t)2 * a.n + i] = w0; st[(size_t)3 * a.n + i] = w1; st[(size_t)4 * a.n + i] = w2;
+      st[(size_t)5 * a.n + i] = w3; st[(size_t)6 * a.n + i] = w4; st[(size_t)7 * a.n + i] = w5;
+      if (EATOM) a.eatom_ilp[i] = evdw + erep;
+    }
   }
 }
 
@@ -1645,7 +1792,8 @@ void upload_pot(const PotConst<R> &p, cudaStream_t s) {
         const IlpP<float> &o = p.ilp[ea * MAXELEM + eb];
         if (!o.same_as_swapped || !(o.C >= 0.f)) p2m = 0;
       }
-    cudaMemcpyToSymbolAsync(c_pair2_multi, &p2m, sizeof(p2m), 0, cudaMemcpyHostToDevice, s);
+    h_two_multi = p2m;
+    h_two_one = (p.i_enabled && !p.kc && p.ilp[0].C >= 0.f) ? 1 : 0;
     if (p2m) {
       static float2 tab[X2M_ROWS * X2M_N];
       for (int ea = 0; ea < MAXELEM; ea++)
@@ -1693,15 +1841,17 @@ static void launch_ilp_t(const ForceArgs<R> &a, bool ev, bool eatom, int block, 
   long long threads = (long long)a.n * TPA;
   int g = (int)((threads + block - 1) / block);
   if (a.kc) {
-    if (ev && eatom) k_ilp<TPA, true, true, ONE, false, true><<<g, block, 0, s>>>(a);
-    else if (ev) k_ilp<TPA, true, false, ONE, false, true><<<g, block, 0, s>>>(a);
-    else k_ilp<TPA, false, false, ONE, false, true><<<g, block, 0, s>>>(a);
+    if (ev && eatom) k_ilp<TPA, true, true, ONE, false, true, false><<<g, block, 0, s>>>(a);
+    else if (ev) k_ilp<TPA, true, false, ONE, false, true, false><<<g, block, 0, s>>>(a);
+    else k_ilp<TPA, false, false, ONE, false, true, false><<<g, block, 0, s>>>(a);
     return;
   }
-  if (ev && eatom) k_ilp<TPA, true, true, ONE, false, false><<<g, block, 0, s>>>(a);
-  else if (ev) k_ilp<TPA, true, false, ONE, false, false><<<g, block, 0, s>>>(a);
-  else if (a.ilp_prefetch) k_ilp<TPA, false, false, ONE, true, false><<<g, block, 0, s>>>(a);
-  else k_ilp<TPA, false, false, ONE, false, false><<<g, block, 0, s>>>(a);
+  if (ev && eatom) k_ilp<TPA, true, true, ONE, false, false, false><<<g, block, 0, s>>>(a);
+  else if (ev) k_ilp<TPA, true, false, ONE, false, false, false><<<g, block, 0, s>>>(a);
+  else if (TWO_PAIR_BODY && !a.list_full && (ONE ? h_two_one : h_two_multi))
+    k_ilp<TPA, false, false, ONE, false, false, TWO_PAIR_BODY><<<g, block, 0, s>>>(a);
+  else if (a.ilp_prefetch) k_ilp<TPA, false, false, ONE, true, false, false><<<g, block, 0, s>>>(a);
+  else k_ilp<TPA, false, false, ONE, false, false, false><<<g, block, 0, s>>>(a);
 }
 
 template <bool ONE>

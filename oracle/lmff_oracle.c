@@ -12,6 +12,27 @@
 #include <omp.h>
 #endif
 
+/* Op-count markers: oracle/opcount.cpp compiles this file with an operation-counting
+ * floating-point type and defines these to attribute the operations to categories and
+ * count the units of each (candidates, pairs, triplets, ...).  Empty here. */
+#define ORC_CAT_OTHER 0
+#define ORC_CAT_ILP_CAND 1     /* an interlayer candidate's distance and cutoff test */
+#define ORC_CAT_ILP_PAIR 2     /* a directed pair in the cutoff: taper, repulsion term, forces */
+#define ORC_CAT_ILP_VDW 3      /* the vdW term of the pairs the tag parity selects */
+#define ORC_CAT_ILP_KTERM 4    /* calc_FRep's force on one intralayer neighbour k of i */
+#define ORC_CAT_NORMAL 5       /* calc_normal of one atom: normal and its Jacobians */
+#define ORC_CAT_TERS_CAND 6    /* Tersoff's scan of the full list for short neighbours */
+#define ORC_CAT_TERS_REP 7     /* repulsive term of a bond (tag-parity half) */
+#define ORC_CAT_TERS_BOND 8    /* force_zeta of a directed bond */
+#define ORC_CAT_TERS_ZETA 9    /* zeta term of a triplet */
+#define ORC_CAT_TERS_ATTR 10   /* attractive (three-body force) of a triplet */
+#define ORC_CAT_ILP_DSELF 11   /* calc_FRep's term of dn_i/dx_i (per pair) */
+#define ORC_NCAT 12
+#ifndef ORC_OPCAT
+#define ORC_OPCAT(cat) ((void)0)
+#define ORC_OPUNIT(cat) ((void)0)
+#endif
+
 #define MY_PI2 1.57079632679489661923
 #define MY_PI4 0.78539816339744830962
 #define MAXLINE 1024
@@ -647,7 +668,9 @@ static void cross(const double a[3], const double b[3], double o[3]) {
  * derivative is (I - n n^T) dn1 / |n1|, the same expression as :893-926 / :1043-1067. */
 static int calc_normal(orc_ctx *c) {
   int bad = 0;
+  ORC_OPCAT(ORC_CAT_NORMAL);
   for (int i = 0; i < c->nlocal; i++) {
+    if (c->p.i_map[c->type[i]] >= 0) ORC_OPUNIT(ORC_CAT_NORMAL);
     double *nrm = &c->normal[3 * i];
     double *dri = &c->dnormdri[9 * i];
     double *dk = &c->dnormal[27 * i];
@@ -719,6 +742,7 @@ static int calc_normal(orc_ctx *c) {
         for (int id = 0; id < 3; id++) dri[id * 3 + ip] = dn1i[id][ip] / nn - n1[id] * dni / nn2;
       }
   }
+  ORC_OPCAT(ORC_CAT_OTHER);
   if (bad) {
     snprintf(c->err, sizeof c->err, "The magnitude of the normal vector is zero");
     return -4;
@@ -788,11 +812,15 @@ static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *
     int je = p->i_map[c->type[j]];
     if (je < 0) continue;
     if (c->mol[i] == c->mol[j]) continue;
+    ORC_OPCAT(ORC_CAT_ILP_CAND);
+    ORC_OPUNIT(ORC_CAT_ILP_CAND);
     double delx = xtmp - c->x[3 * j];
     double dely = ytmp - c->x[3 * j + 1];
     double delz = ztmp - c->x[3 * j + 2];
     double rsq = delx * delx + dely * dely + delz * delz;
     if (rsq >= cutsq) continue;
+    ORC_OPCAT(ORC_CAT_ILP_PAIR);
+    ORC_OPUNIT(ORC_CAT_ILP_PAIR);
     const orc_ilp_param *q = &p->i_params[p->i_e2p[ie][je]];
     double r = sqrt(rsq);
     double Tap, dTap;
@@ -805,6 +833,8 @@ static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *
     }
     /* van der Waals, half of the pairs */
     if (!skip_half(c, i, j)) {
+      ORC_OPCAT(ORC_CAT_ILP_VDW);
+      ORC_OPUNIT(ORC_CAT_ILP_VDW);
       double r2inv = 1.0 / rsq;
       double r6inv = r2inv * r2inv * r2inv;
       double r8inv = r6inv * r2inv;
@@ -832,6 +862,7 @@ static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *
         eatom[i] += 0.5 * evdwl;
         eatom[j] += 0.5 * evdwl;
       }
+      ORC_OPCAT(ORC_CAT_ILP_PAIR);
     }
     /* repulsion with the normal of i, every directed pair */
     double prodnorm1 = nrm[0] * delx + nrm[1] * dely + nrm[2] * delz;
@@ -858,25 +889,35 @@ static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *
     }
     double fsum = fpair + fpair1;
     double del[3] = {delx, dely, delz};
-    double dprod[3];
-    for (int ip = 0; ip < 3; ip++)
-      dprod[ip] = dri[0 * 3 + ip] * delx + dri[1 * 3 + ip] * dely + dri[2 * 3 + ip] * delz;
     double fkc[3];
     for (int a = 0; a < 3; a++) {
       double fp1 = prodnorm1 * nrm[a] * fpair1;
       fkc[a] = (del[a] * fsum - fp1) * Tap - Vilp * dTap * del[a] / r;
-      double fprod1 = prodnorm1 * dprod[a] * fpair1;
-      f[3 * i + a] += fkc[a] - fprod1 * Tap;
       f[3 * j + a] -= fkc[a];
     }
+    /* the term of dn_i/dx_i (a k-term with k = i) */
+    ORC_OPCAT(ORC_CAT_ILP_DSELF);
+    ORC_OPUNIT(ORC_CAT_ILP_DSELF);
+    double dprod[3], fi[3];
+    for (int ip = 0; ip < 3; ip++)
+      dprod[ip] = dri[0 * 3 + ip] * delx + dri[1 * 3 + ip] * dely + dri[2 * 3 + ip] * delz;
+    for (int a = 0; a < 3; a++) {
+      double fprod1 = prodnorm1 * dprod[a] * fpair1;
+      fi[a] = fkc[a] - fprod1 * Tap;
+    }
+    ORC_OPCAT(ORC_CAT_ILP_PAIR);
+    for (int a = 0; a < 3; a++) f[3 * i + a] += fi[a];
     for (int kk = 0; kk < c->ilpn[i]; kk++) {
       int k = c->ilpnb[3 * i + kk];
       if (k == i) continue;
+      ORC_OPCAT(ORC_CAT_ILP_KTERM);
+      ORC_OPUNIT(ORC_CAT_ILP_KTERM);
       for (int ip = 0; ip < 3; ip++) {
         double dp = dk[(kk * 3 + 0) * 3 + ip] * delx + dk[(kk * 3 + 1) * 3 + ip] * dely +
                     dk[(kk * 3 + 2) * 3 + ip] * delz;
         f[3 * k + ip] += (-prodnorm1 * dp * fpair1) * Tap;
       }
+      ORC_OPCAT(ORC_CAT_ILP_PAIR);
     }
     /* KC without the taper tallies V - offset, offset = -A (z0/cut)^6 (init_one :235) */
     double ev = (p->i_model == 1 && !p->tap_flag) ? Vilp + q->A * pow(q->z0 / p->cut_global, 6.0) : Tap * Vilp;
@@ -886,6 +927,7 @@ static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *
       eatom[j] += 0.5 * ev;
     }
   }
+  ORC_OPCAT(ORC_CAT_OTHER);
 }
 
 /* =================================================================== Tersoff == */
@@ -1002,6 +1044,8 @@ static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, doubl
     int j = c->nb[jj];
     int jtype = p->t_map[c->type[j]];
     if (jtype < 0) continue;
+    ORC_OPCAT(ORC_CAT_TERS_CAND);
+    ORC_OPUNIT(ORC_CAT_TERS_CAND);
     double delx = xtmp - c->x[3 * j];
     double dely = ytmp - c->x[3 * j + 1];
     double delz = ztmp - c->x[3 * j + 2];
@@ -1014,6 +1058,8 @@ static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, doubl
     const orc_ters_param *q = &p->t_params[p->t_e2p[itype][jtype][jtype]];
     if (rsq >= q->cutsq) continue;
     /* repulsive, :584-595 */
+    ORC_OPCAT(ORC_CAT_TERS_REP);
+    ORC_OPUNIT(ORC_CAT_TERS_REP);
     double r = sqrt(rsq);
     double tmp_fc = ters_fc(r, q), tmp_fc_d = ters_fc_d(r, q);
     double tmp_exp = exp(-q->lam1 * r);
@@ -1035,11 +1081,14 @@ static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, doubl
     int j = neighshort[jj];
     int jtype = p->t_map[c->type[j]];
     const orc_ters_param *qij = &p->t_params[p->t_e2p[itype][jtype][jtype]];
+    ORC_OPCAT(ORC_CAT_TERS_BOND);
     double delr1[3] = {c->x[3 * j] - xtmp, c->x[3 * j + 1] - ytmp, c->x[3 * j + 2] - ztmp};
     double rsq1 = delr1[0] * delr1[0] + delr1[1] * delr1[1] + delr1[2] * delr1[2];
     if (rsq1 >= qij->cutsq) continue;
+    ORC_OPUNIT(ORC_CAT_TERS_BOND);
     double fjx = 0.0, fjy = 0.0, fjz = 0.0;
     double zeta_ij = 0.0;
+    ORC_OPCAT(ORC_CAT_TERS_ZETA);
     for (int kk = 0; kk < numshort; kk++) {
       if (jj == kk) continue;
       int k = neighshort[kk];
@@ -1048,9 +1097,11 @@ static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, doubl
       double delr2[3] = {c->x[3 * k] - xtmp, c->x[3 * k + 1] - ytmp, c->x[3 * k + 2] - ztmp};
       double rsq2 = delr2[0] * delr2[0] + delr2[1] * delr2[1] + delr2[2] * delr2[2];
       if (rsq2 >= qijk->cutsq) continue;
+      ORC_OPUNIT(ORC_CAT_TERS_ZETA);
       zeta_ij += ters_zeta(qijk, rsq1, rsq2, delr1, delr2);
     }
     /* force_zeta, :621-634 */
+    ORC_OPCAT(ORC_CAT_TERS_BOND);
     double r = sqrt(rsq1);
     double fa = ters_fa(r, qij), fa_d = ters_fa_d(r, qij);
     double bij = ters_bij(zeta_ij, qij);
@@ -1068,6 +1119,7 @@ static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, doubl
       eatom[i] += 0.5 * evdwl;
       eatom[j] += 0.5 * evdwl;
     }
+    ORC_OPCAT(ORC_CAT_TERS_ATTR);
     for (int kk = 0; kk < numshort; kk++) {
       if (jj == kk) continue;
       int k = neighshort[kk];
@@ -1076,6 +1128,7 @@ static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, doubl
       double delr2[3] = {c->x[3 * k] - xtmp, c->x[3 * k + 1] - ytmp, c->x[3 * k + 2] - ztmp};
       double rsq2 = delr2[0] * delr2[0] + delr2[1] * delr2[1] + delr2[2] * delr2[2];
       if (rsq2 >= qijk->cutsq) continue;
+      ORC_OPUNIT(ORC_CAT_TERS_ATTR);
       double fi[3], fj[3], fk[3];
       ters_attractive(qijk, prefactor, rsq1, rsq2, delr1, delr2, fi, fj, fk);
       fxtmp += fi[0];
@@ -1092,9 +1145,11 @@ static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, doubl
     f[3 * j + 1] += fjy;
     f[3 * j + 2] += fjz;
   }
+  ORC_OPCAT(ORC_CAT_TERS_BOND);
   f[3 * i] += fxtmp;
   f[3 * i + 1] += fytmp;
   f[3 * i + 2] += fztmp;
+  ORC_OPCAT(ORC_CAT_OTHER);
   return 0;
 }
 

@@ -8,12 +8,22 @@ integration and accumulation).  One step = integrate + [neighbour check/rebuild]
 Tersoff + ILP forces.  Synthetic inputs generated here (the reference's own large data
 files are not available).
 
-Timing: W untimed warm-up steps, then exactly K steps (default 100, so that the
-neighbour-list rebuilds the run needs fall inside the timed region) timed on the device
-with CUDA events on the engine's stream (lmff_stats.ms_last_run), bracketed by
+Timing: W untimed warm-up steps, then exactly K steps timed on the device with CUDA
+events on the engine's stream (lmff_stats.ms_last_run), bracketed by
 torch.cuda.synchronize() (and a barrier with N > 1).  On the 2.7M-atom slab the
 inputs are far larger than L2 (the pair list alone is 10 GB), so no L2 flush is needed;
-config.l2 states the list size of each workload.
+config.l2 states the list size of each workload.  A second, host-driven run of
+max(K, --kernel-steps) steps times every kernel launch with CUDA events: the roofline
+averages, the launches per step, and the neighbour rebuilds (time per rebuild, steps
+between rebuilds, the amortised cost per step); rebuilds_in_timed_region counts the
+rebuilds inside the K timed steps.  Algorithmic flops come from bench/flops.h (the
+oracle's arithmetic, op-counted by oracle/opcount.py).
+
+With one GPU the line also carries the chosen forms' targets, measured in the same run:
+plain_fp64 (the all-FP64 drop-in on the same slab), batched (256 bilayer replicas,
+batched mixed vs one-at-a-time FP64), served (the Poisson stream, the server's
+closed-loop capacity vs one-at-a-time FP64 over the whole stream, and open-loop
+p50/p99), and the benchmark spec (the ratios).  --no-north-star skips them.
 
 Multi-GPU: the path is run as independent replicas (one system per GPU, no data-path
 collective): value = total atom-steps of all ranks / max rank time, scaling "weak".
@@ -43,24 +53,52 @@ UNIT = "atom-steps/s"
 TERSOFF_FILE = os.path.join(ROOT, "lammps-lmff_gb300", "potentials", "BNC.tersoff")
 ILP_FILE = os.path.join(ROOT, "lammps-lmff_gb300", "potentials", "BNCH.ILP")
 
-# Algorithmic work of the ILP pair evaluation per directed interlayer pair inside the
-# cutoff, as the reference computes it (calc_FRep of the pair's own term plus half of
-# calc_FvdW, pair_ilp_graphene_hbn.cpp:449-675 with the taper of .h:80-115): about 115
-# flops + 2.5 exp + 1 sqrt + 2 divisions, each call counted as 1 (add/sub/mul = 1,
-# FMA = 2).  A list candidate outside the cutoff costs the displacement, r^2 and the
-# test: 9.  `roofline.achieved` uses these.
 # DRAM bytes per pair-list entry of the mixed pair kernel, from one ncu capture of the
 # 331,200-atom graphite slab (k_ilp<8,0,0,1,0,0>: 1.303 GB read + 19.7 MB written for
 # 310,301,280 entries; the list is larger than L2, so traffic grows with the entries)
 K_ILP_DRAM_BYTES_PER_ENTRY = (1.302568e9 + 19.73888e6) / 310301280
+# FP64-pipe activity of the two FP64-bound per-atom kernels of the mixed step (ncu
+# sm__pipe_fp64_cycles_active on the 331,200-atom slab, profiles/)
+FP64_PIPE_ACTIVE_NCU = {"k_tersoff": 0.628, "k_nderiv": 0.821}
 L2_BYTES = 129e6   # GB300 L2
-ALG_FLOPS_PER_PAIR = 120
-ALG_FLOPS_PER_REJECTED = 9
-# What the gather kernel executes per directed pair (both repulsion terms and the full
-# vdW force on the owning atom, so that no force is scattered), counted from the kernel
-# source (csrc/forces_impl.cuh k_ilp, no energy/virial), reported beside it.
-EXEC_FLOPS_PER_PAIR = 155
-EXEC_FLOPS_PER_REJECTED = 26
+FLOPS_H = os.path.join(ROOT, "bench", "flops.h")
+
+
+def read_flops(path: str = FLOPS_H) -> dict:
+    """The algorithmic operation counts frozen in bench/flops.h (oracle/opcount.py: the
+    oracle compiled with an operation-counting double on the benchmark's CPU sample)."""
+    out = {}
+    for line in open(path):
+        p = line.split()
+        if len(p) == 3 and p[0] == "#define" and p[1].startswith("LMFF_"):
+            out[p[1][5:]] = float(p[2])
+    return out
+
+
+FLOPS = read_flops()
+
+
+def alg_flops_pair_kernel(pairs: int, entries: int) -> float:
+    """The reference's arithmetic for one pair-kernel launch: every list candidate's
+    displacement and r^2, and per directed pair in the cutoff the repulsion term with
+    the normal of i and its share of the vdW term (calc_FRep / calc_FvdW).  calc_FRep's
+    normal-derivative terms (dn_i/dx_i and the intralayer neighbours k) are counted with
+    the normal-derivative kernel, which applies them once per atom."""
+    per_pair = FLOPS["FLOPS_ILP_PAIR"] + FLOPS["VDW_PER_PAIR"] * FLOPS["FLOPS_ILP_VDW"]
+    return entries * FLOPS["FLOPS_ILP_CAND"] + pairs * per_pair
+
+
+def alg_flops_nderiv(n_ilp_atoms: int) -> float:
+    """calc_normal's Jacobians and their application to dE/dn_i: the dn_i/dx_i term and
+    one term per intralayer neighbour, once per atom (reverse-accumulated, as LMFF's
+    dprodni)."""
+    return n_ilp_atoms * (FLOPS["FLOPS_NORMAL"] + (1.0 + FLOPS["KTERMS_PER_PAIR"]) * FLOPS["FLOPS_ILP_KTERM"])
+
+
+def alg_flops_tersoff(natoms: int) -> float:
+    """Tersoff arithmetic of sp2 carbon (3 bonds, 6 triplets per atom), per atom as
+    counted on the graphite sample."""
+    return natoms * FLOPS["FLOPS_TERSOFF_ATOM"]
 
 
 def workload(name: str):
@@ -293,31 +331,29 @@ def bench_serving(args, local: int) -> dict:
     """Poisson request stream: 200 requests/s, 70 % single points and 30 % 100-step NVE
     runs at 300 K, bilayers of 1k-200k atoms (log-uniform on a 24-value grid), seeded.
     The server (mixed precision, 150 GB admission budget) replays the stream in real time
-    (latency p50/p99) and all at once (capacity); the baseline serves a prefix of the same
-    stream one request at a time in plain FP64, and the server serves the same prefix."""
+    (open loop: latency p50/p99, solves/s) and all at once (closed loop: capacity); the
+    baseline serves the same whole stream one request at a time in plain FP64 (and in
+    mixed precision, for reference)."""
     from lmff_gb300 import capi, serve
     stream = serve.poisson_stream(count=args.serve_requests, rate=200.0, seed=7)
-    prefix = stream[:args.serve_prefix]
     proto = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=capi.MIXED)
     srv = serve.Server(proto, hbm_budget_bytes=150e9, md_chunk_steps=args.serve_chunk)
     serve.replay(srv, stream[:8], realtime=False)          # warm-up: allocations, graphs
     openl = serve.replay(srv, stream, realtime=True)
     closed = serve.replay(srv, stream, realtime=False)
-    closed_prefix = serve.replay(srv, prefix, realtime=False)
     st = srv.stats()
     srv.close()
     seq64 = serve.replay_sequential(capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=capi.FP64),
-                                    prefix, realtime=False)
+                                    stream, realtime=False)
     seqmx = serve.replay_sequential(capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=capi.MIXED),
-                                    prefix, realtime=False)
+                                    stream, realtime=False)
     return {"metric": "solves/s, Poisson 200 req/s stream", "value": openl["solves_per_s"], "unit": "solves/s",
             "n_gpus": 1, "higher_is_better": True, "data": "synthetic", "dtype": "f32",
             "config": {"workload": f"{len(stream)} requests, 200 req/s, 30% 100-step NVE, 1k-200k atom bilayers",
-                       "precision": "mixed", "md_chunk_steps": args.serve_chunk, "budget_gb": 150,
-                       "prefix_requests": len(prefix)},
-            "open_loop": openl, "closed_loop": closed, "closed_loop_prefix": closed_prefix,
-            "one_at_a_time_fp64_prefix": seq64, "one_at_a_time_mixed_prefix": seqmx,
-            "capacity_vs_one_at_a_time_fp64": closed_prefix["solves_per_s"] / seq64["solves_per_s"],
+                       "precision": "mixed", "md_chunk_steps": args.serve_chunk, "budget_gb": 150},
+            "open_loop": openl, "closed_loop": closed,
+            "one_at_a_time_fp64": seq64, "one_at_a_time_mixed": seqmx,
+            "capacity_vs_one_at_a_time_fp64": closed["solves_per_s"] / seq64["solves_per_s"],
             "server_stats": st}
 
 
@@ -366,8 +402,12 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-peak", action="store_true", help="skip the cuBLAS peak measurement")
-    ap.add_argument("--serve-requests", type=int, default=400)
-    ap.add_argument("--serve-prefix", type=int, default=40)
+    ap.add_argument("--kernel-steps", type=int, default=200,
+                    help="steps of the per-kernel timing run (also gives the rebuild interval)")
+    ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the plain FP64 sub-record")
+    ap.add_argument("--no-north-star", action="store_true",
+                    help="skip the plain-FP64, batched and served sub-records")
+    ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-chunk", type=int, default=20)
     ap.add_argument("--drift-steps-mixed", type=int, default=1000000)
     ap.add_argument("--drift-steps-fp64", type=int, default=100000)
@@ -424,93 +464,22 @@ def main():
         args.tpa = args.tpa or tuned["tpa"]
         args.block = args.block or tuned["block"]
         args.skin = args.skin or tuned["skin"]
-    eng = capi.Engine(TERSOFF_FILE, ILP_FILE, elements=elements, device=local, precision=prec)
-    eng.set_option("tpa", args.tpa)
-    eng.set_option("block", args.block)
-    eng.set_option("skin", args.skin)
-    eng.upload(s)
-    eng.run_nve(args.warmup, 0.001)
-    eng.set_option("count_pairs", 1)
-    # timed region: the production loop (steps replayed as CUDA graphs, no host sync)
-    clocks = ClockSampler(local)
-    clocks.start()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    eng.run_nve(args.steps, 0.001)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    if dist:
-        dist.barrier()
-    clk = clocks.stop()
-    st = eng.stats()
-    graph_steps = st["graph_steps"]
-    dev_s = st["ms_last_run"] / 1e3
-    tmax = max_over_ranks(dev_s, dist)
-    value = replica_throughput(world, s.n, args.steps, tmax)
-    ms_per_step = tmax / args.steps * 1e3
-
-    # dominant kernel: the ILP pair kernel; live per-launch device time from CUDA events
-    # around each launch on the engine's stream, over a second run of the same length
-    # through the host-driven loop (the graph replay runs the same kernels)
-    eng.set_option("kernel_timing", 1)
-    eng.set_option("reset_timing", 1)
-    eng.run_nve(args.steps, 0.001)
-    eng.set_option("kernel_timing", 0)
-    st = eng.stats()
-    k_ms = st["kernel_ms"]["pair_ilp"]
-    k_n = max(1, st["kernel_launches"]["pair_ilp"])
-    k_avg = k_ms / k_n / 1e3
-    pairs = st["pairs_in_cutoff"]
-    cands = st["list_entries"]
-    flops = pairs * ALG_FLOPS_PER_PAIR + (cands - pairs) * ALG_FLOPS_PER_REJECTED
-    exec_flops = pairs * EXEC_FLOPS_PER_PAIR + (cands - pairs) * EXEC_FLOPS_PER_REJECTED
-    launches_total = sum(st["kernel_launches"].values()) + args.steps   # + the graph condition kernel per step
+    m = run_md(s, prec, elements, local, args.tpa, args.block, args.skin, args.warmup, args.steps,
+               args.kernel_steps, dist, clocks=True)
+    value = replica_throughput(world, s.n, args.steps, m["tmax"])
+    ms_per_step = m["tmax"] / args.steps * 1e3
+    launches_total = sum(m["launches_per_step"].values()) * args.steps
 
     # e2e through the drop-in call (lmff_compute) with pinned host buffers
     e2e = None
     if args.e2e_steps > 0:
-        xa = torch.empty((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
-        xb = torch.empty((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
-        fb = torch.empty((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
-        xa[:] = s.x
-        xb[:] = s.x + np.random.default_rng(1).normal(0.0, 0.01, s.x.shape)
-        eng2 = capi.Engine(TERSOFF_FILE, ILP_FILE, elements=elements, device=local, precision=prec)
-        eng2.set_option("tpa", args.tpa)
-        eng2.set_option("block", args.block)
-        eng2.set_option("skin", args.skin)
-        eng2.set_box(s.box_lo, s.box_hi, s.periodic)
-        eng2.compute(xa, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb, overwrite=True)
-        eng2.compute(xb, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb, overwrite=True, same_atoms=True)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for k in range(args.e2e_steps):
-            eng2.compute(xa if k % 2 == 0 else xb, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb,
-                         overwrite=True, same_atoms=True)
-        torch.cuda.synchronize()
-        te = time.perf_counter() - t0
-        e2e = {"value": world * s.n * args.e2e_steps / te, "unit": UNIT, "h2d_bytes_per_step": int(xa.nbytes),
-               "d2h_bytes_per_step": int(fb.nbytes),
-               "path": "lmff_compute: pinned host x in, host f out, per force evaluation"}
-        del eng2
+        e2e = bench_e2e(s, prec, elements, local, args, world)
 
     peaks = measured_peaks()
-    peak_name = "fp32" if prec == capi.MIXED else "fp64"
-    peak = fp_peak_tflops(peak_name) if (rank == 0 and not args.no_peak) else 0.0
-    achieved = flops / k_avg / 1e12
-    roofline = {"bound": peak_name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak if peak else None,
-                "traffic": K_ILP_DRAM_BYTES_PER_ENTRY * cands if prec == capi.MIXED else None,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_ilp launch on the "
-                                  "331,200-atom slab (1.322 GB for 310.3 M list entries), scaled by list entries",
-                "kernel": "k_ilp (pair kernel)", "kernel_ms_avg": k_avg * 1e3,
-                "peak_source": f"cuBLAS {peak_name.upper()} GEMM measured in this run (SIMT; MEASURED_PEAKS.json has "
-                               f"HBM {peaks.get('hbm_gbs')} GB/s and bf16 tensor only)",
-                "pairs_in_cutoff": pairs, "list_entries": cands,
-                "alg_flops_per_pair": ALG_FLOPS_PER_PAIR, "alg_flops_per_rejected": ALG_FLOPS_PER_REJECTED,
-                "executed_tflops": exec_flops / k_avg / 1e12,
-                "hbm_gbs_of_list_stream": cands * 4 / k_avg / 1e9, "hbm_peak_gbs": peaks.get("hbm_gbs")}
+    pk = {"fp32": 0.0, "fp64": 0.0}
+    if rank == 0 and not args.no_peak:
+        pk = {"fp32": fp_peak_tflops("fp32"), "fp64": fp_peak_tflops("fp64")}
+    rl = rooflines(m, s, prec, pk, peaks)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -520,9 +489,16 @@ def main():
                "sample": f"{cn}-atom 98x98 A patch of the same slab, {args.cpu_steps} NVE steps, "
                          f"oracle restatement, {cdt:.1f} s"}
 
+    # the chosen forms' targets, on one GPU: plain FP64 on the same system, batched
+    # replicas and the served Poisson stream against one-at-a-time FP64
+    north = None
+    if rank == 0 and world == 1 and not args.no_north_star and args.workload == "graphite_2p7m":
+        north = north_star(args, s, elements, local, value, pk)
+
     if rank == 0:
         # the pair list is what every step streams from HBM; say whether it fits in the
         # 129 MB L2 (no flush between steps either way: the steps of an MD run re-read it)
+        st = m["stats"]
         list_bytes = 4.0 * st["list_per_atom"] * s.n
         l2_note = (f"inputs larger than L2 (pair list {list_bytes / 1e9:.1f} GB), no flush"
                    if list_bytes > L2_BYTES else
@@ -539,15 +515,180 @@ def main():
                                "probe_atoms": tuned["probe_atoms"], "picked": [tuned["tpa"], tuned["block"], tuned["skin"]],
                                "score_ms_probe": tuned["score_ms"]},
                            "l2": l2_note,
-                           "parallelism": f"replicas x{world}", "wall_s": wall},
-                "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": launches_total, "graph_steps_timed": graph_steps,
-                "kernel_ms": st["kernel_ms"], "kernel_launches": st["kernel_launches"],
-                "rebuilds": st["rebuilds"], "list_per_atom": st["list_per_atom"]}
+                           "parallelism": f"replicas x{world}", "wall_s": m["wall"]},
+                "clocks": m["clocks"], "roofline": rl["k_ilp"],
+                "rooflines_other": {k: v for k, v in rl.items() if k != "k_ilp"},
+                "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches_total, "graph_steps_timed": m["graph_steps"],
+                "rebuilds_in_timed_region": m["rebuilds_timed"], "rebuild": m["rebuild"],
+                "kernel_ms_avg": m["kernel_ms_avg"], "list_per_atom": st["list_per_atom"]}
+        if north is not None:
+            line.update(north)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def run_md(s, prec, elements, local, tpa, block, skin, warmup, steps, kernel_steps, dist=None, clocks=False):
+    """Device-resident NVE of system s: `warmup` untimed steps, `steps` timed steps (the
+    production loop: steps replayed as CUDA graphs, device time from CUDA events on the
+    engine's stream), then a host-driven run of max(steps, kernel_steps) steps with CUDA
+    events around every kernel launch: per-kernel averages, launches per step and the
+    neighbour-rebuild statistics."""
+    import torch
+    from lmff_gb300 import capi
+    eng = capi.Engine(TERSOFF_FILE, ILP_FILE, elements=elements, device=local, precision=prec)
+    eng.set_option("tpa", tpa)
+    eng.set_option("block", block)
+    eng.set_option("skin", skin)
+    eng.upload(s)
+    eng.run_nve(warmup, 0.001)
+    eng.set_option("count_pairs", 1)
+    sampler = ClockSampler(local) if clocks else None
+    if sampler:
+        sampler.start()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    r0 = eng.stats()["rebuilds"]
+    t0 = time.perf_counter()
+    eng.run_nve(steps, 0.001)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    clk = sampler.stop() if sampler else None
+    st = eng.stats()
+    out = {"wall": wall, "clocks": clk, "graph_steps": st["graph_steps"], "rebuilds_timed": st["rebuilds"] - r0,
+           "tmax": max_over_ranks(st["ms_last_run"] / 1e3, dist)}
+    nk = max(steps, kernel_steps)
+    r1 = st["rebuilds"]
+    eng.set_option("kernel_timing", 1)
+    eng.set_option("reset_timing", 1)
+    eng.run_nve(nk, 0.001)
+    eng.set_option("kernel_timing", 0)
+    st = eng.stats()
+    kms, kn = st["kernel_ms"], st["kernel_launches"]
+    out["stats"] = st
+    out["kernel_ms_avg"] = {k: (kms[k] / kn[k] if kn[k] else None) for k in kms}
+    out["launches_per_step"] = {k: kn[k] / nk for k in kn}
+    rb = st["rebuilds"] - r1
+    rb_ms = kms["neighbor_build"] / kn["neighbor_build"] if kn["neighbor_build"] else None
+    out["rebuild"] = {"steps_observed": nk, "rebuilds_observed": rb, "ms_per_rebuild": rb_ms,
+                      "steps_per_rebuild": nk / rb if rb else None,
+                      "amortised_ms_per_step": rb_ms * rb / nk if rb else 0.0}
+    eng.close()
+    return out
+
+
+def rooflines(m, s, prec, pk, peaks) -> dict:
+    """Roofline entries of the pair kernel (the dominant one) and of the two FP64-bound
+    per-atom kernels; algorithmic flops from bench/flops.h over the CUDA-event average."""
+    from lmff_gb300 import capi
+    st = m["stats"]
+    ka = m["kernel_ms_avg"]
+    pairs, cands = st["pairs_in_cutoff"], st["list_entries"]
+    name = "fp32" if prec == capi.MIXED else "fp64"
+    k_s = ka["pair_ilp"] / 1e3
+    achieved = alg_flops_pair_kernel(pairs, cands) / k_s / 1e12
+    out = {"k_ilp": {
+        "bound": name, "achieved": achieved, "peak": pk[name], "unit": "TFLOP/s",
+        "frac": achieved / pk[name] if pk[name] else None,
+        "traffic": K_ILP_DRAM_BYTES_PER_ENTRY * cands if prec == capi.MIXED else None,
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_ilp launch on the "
+                          "331,200-atom slab (1.322 GB for 310.3 M list entries), scaled by list entries",
+        "kernel": "k_ilp (pair kernel)", "kernel_ms_avg": ka["pair_ilp"],
+        "peak_source": f"cuBLAS {name.upper()} GEMM measured in this run (SIMT; MEASURED_PEAKS.json has HBM "
+                       f"{peaks.get('hbm_gbs')} GB/s and bf16 tensor only)",
+        "pairs_in_cutoff": pairs, "list_entries": cands,
+        "alg_flops_source": "bench/flops.h (op count of the oracle)",
+        "alg_flops_per_pair": FLOPS["FLOPS_ILP_CAND"] + FLOPS["FLOPS_ILP_PAIR"]
+        + FLOPS["VDW_PER_PAIR"] * FLOPS["FLOPS_ILP_VDW"],
+        "alg_flops_per_rejected": FLOPS["FLOPS_ILP_CAND"],
+        "hbm_gbs_of_list_stream": cands * 4 / k_s / 1e9, "hbm_peak_gbs": peaks.get("hbm_gbs")}}
+    for kern, key, flops in (("k_tersoff", "tersoff", alg_flops_tersoff(s.n)),
+                             ("k_nderiv", "normal_deriv", alg_flops_nderiv(s.n))):
+        t = ka.get(key)
+        if not t:
+            continue
+        a = flops / (t / 1e3) / 1e12
+        e = {"bound": "fp64", "kernel_ms_avg": t, "alg_flops": flops, "achieved_alg": a, "unit": "TFLOP/s",
+             "peak_fp64": pk["fp64"], "peak_fp32": pk["fp32"]}
+        if prec == capi.FP64:
+            e["frac"] = a / pk["fp64"] if pk["fp64"] else None
+            e["frac_source"] = "algorithmic flops over the measured DGEMM peak"
+        else:
+            # the mixed kernels do the reference's FP64 arithmetic partly in FP32 and in
+            # fewer FP64 operations, so their position on the FP64 roofline is the
+            # measured FP64-pipe activity
+            e["frac"] = FP64_PIPE_ACTIVE_NCU[kern]
+            e["frac_source"] = "ncu sm__pipe_fp64_cycles_active, 331,200-atom slab (profiles/)"
+            e["alg_frac_of_fp32_peak"] = a / pk["fp32"] if pk["fp32"] else None
+        out[kern] = e
+    return out
+
+
+def bench_e2e(s, prec, elements, local, args, world) -> dict:
+    """The same force evaluation through lmff_compute with pinned host x in and host f
+    out per step (host<->device copies inside the timed region)."""
+    import torch
+    from lmff_gb300 import capi
+    xa = torch.empty((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    xb = torch.empty((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    fb = torch.empty((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    xa[:] = s.x
+    xb[:] = s.x + np.random.default_rng(1).normal(0.0, 0.01, s.x.shape)
+    eng2 = capi.Engine(TERSOFF_FILE, ILP_FILE, elements=elements, device=local, precision=prec)
+    eng2.set_option("tpa", args.tpa)
+    eng2.set_option("block", args.block)
+    eng2.set_option("skin", args.skin)
+    eng2.set_box(s.box_lo, s.box_hi, s.periodic)
+    eng2.compute(xa, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb, overwrite=True)
+    eng2.compute(xb, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb, overwrite=True, same_atoms=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.e2e_steps):
+        eng2.compute(xa if k % 2 == 0 else xb, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb,
+                     overwrite=True, same_atoms=True)
+    torch.cuda.synchronize()
+    te = time.perf_counter() - t0
+    eng2.close()
+    return {"value": world * s.n * args.e2e_steps / te, "unit": UNIT, "h2d_bytes_per_step": int(xa.nbytes),
+            "d2h_bytes_per_step": int(fb.nbytes),
+            "path": "lmff_compute: pinned host x in, host f out, per force evaluation"}
+
+
+def north_star(args, s, elements, local, mixed_value, pk) -> dict:
+    """Sub-records for the chosen forms' targets, measured in the same run:
+    plain_fp64 -- the all-FP64 drop-in on the same slab (tpa 16, block 128, skin 1 A);
+    batched -- 256 bilayer replicas, E+F+W, batched mixed vs one-at-a-time FP64;
+    served -- the Poisson stream, server (mixed) vs one-at-a-time FP64, whole stream."""
+    from lmff_gb300 import capi
+    out = {}
+    m = run_md(s, capi.FP64, elements, local, 16, 128, 1.0, 1, args.fp64_steps, 0)
+    v64 = s.n * args.fp64_steps / m["tmax"]
+    rl = rooflines(m, s, capi.FP64, pk, measured_peaks())
+    out["plain_fp64"] = {"value": v64, "unit": UNIT, "steps": args.fp64_steps,
+                         "ms_per_step": m["tmax"] / args.fp64_steps * 1e3, "tpa": 16, "block": 128, "skin": 1.0,
+                         "roofline": rl["k_ilp"], "roofline_tersoff": rl.get("k_tersoff"),
+                         "roofline_nderiv": rl.get("k_nderiv"), "kernel_ms_avg": m["kernel_ms_avg"],
+                         "rebuilds_in_timed_region": m["rebuilds_timed"]}
+    rep = bench_replicas(args, local)
+    out["batched"] = {"value": rep["value"], "unit": rep["unit"], "config": rep["config"],
+                      "one_at_a_time_fp64_replicas_per_s": rep["detail"]["fp64"]["one_at_a_time_replicas_per_s"],
+                      "batched_fp64_replicas_per_s": rep["detail"]["fp64"]["batched_replicas_per_s"],
+                      "resident_mixed_replicas_per_s": 256 / rep["detail"]["mixed"]["resident_s"],
+                      "ratio_vs_one_at_a_time_fp64": rep["batched_mixed_vs_one_at_a_time_fp64"]}
+    srv = bench_serving(args, local)
+    out["served"] = {"open_loop": srv["open_loop"], "closed_loop": srv["closed_loop"],
+                     "one_at_a_time_fp64": srv["one_at_a_time_fp64"], "config": srv["config"],
+                     "capacity_vs_one_at_a_time_fp64": srv["capacity_vs_one_at_a_time_fp64"]}
+    out["north_star"] = {"mixed_vs_plain_fp64": mixed_value / v64, "target_mixed_vs_plain": 1.8,
+                         "batched_vs_one_at_a_time_fp64": rep["batched_mixed_vs_one_at_a_time_fp64"],
+                         "served_capacity_vs_one_at_a_time_fp64": srv["capacity_vs_one_at_a_time_fp64"],
+                         "target_batched_served": 5.0}
+    return out
 
 
 if __name__ == "__main__":

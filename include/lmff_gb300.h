@@ -153,10 +153,10 @@ typedef struct lmff_stats {
   double ms_last_run;
   /* with option "kernel_timing" = 1: summed device time and launch count per kernel
    * since the last "reset_timing": [0] pair (ILP) kernel, [1] Tersoff, [2] intralayer
-   * lists, normals and normal-derivative assembly, [3] gather, [4] integrator,
-   * [5] neighbour build */
-  double kernel_ms[6];
-  int64_t kernel_launches[6];
+   * lists and normals, [3] gather, [4] integrator, [5] neighbour build (one per
+   * rebuild), [6] normal-derivative assembly */
+  double kernel_ms[7];
+  int64_t kernel_launches[7];
   /* interlayer pairs within the ILP cutoff in the current configuration (option
    * "count_pairs" = 1 counts them once, outside any timed region) */
   int64_t pairs_in_cutoff;

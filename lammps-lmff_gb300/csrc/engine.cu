@@ -512,8 +512,8 @@ struct Engine {
   int64_t pairs_in_cut = 0;
   // per-kernel device timing (option "kernel_timing"): events around each launch
   bool ktiming = false;
-  double kms[6] = {0, 0, 0, 0, 0, 0};
-  int64_t klaunch[6] = {0, 0, 0, 0, 0, 0};
+  double kms[7] = {0, 0, 0, 0, 0, 0, 0};
+  int64_t klaunch[7] = {0, 0, 0, 0, 0, 0, 0};
   struct Pend {
     cudaEvent_t a, b;
     int k;
@@ -1350,7 +1350,7 @@ struct Engine {
     }
     if (a.do_ilp) {
       timed(0, [&] { fi(a, ev, eatom, tpa, block, i_one, stream); });
-      timed(2, [&] { fn(a, ev, stream); });
+      timed(6, [&] { fn(a, ev, stream); });
     }
     else if (ev) cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)n, stream);
     if (eatom && !a.do_ters) cudaMemsetAsync(eatom_ters, 0, sizeof(double) * (size_t)n, stream);
@@ -2844,7 +2844,7 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
   } else if (k == "kernel_timing") {
     e->e.ktiming = value != 0.0;
   } else if (k == "reset_timing") {
-    for (int q = 0; q < 6; q++) {
+    for (int q = 0; q < 7; q++) {
       e->e.kms[q] = 0.0;
       e->e.klaunch[q] = 0;
     }
@@ -2981,7 +2981,7 @@ int lmff_get_stats(lmff_engine *e, lmff_stats *out) {
   out->ms_last_run = g.ms_run;
   out->graph_steps = g.graph_steps;
   out->graph_redos = g.graph_redos;
-  for (int q = 0; q < 6; q++) {
+  for (int q = 0; q < 7; q++) {
     out->kernel_ms[q] = g.kms[q];
     out->kernel_launches[q] = g.klaunch[q];
   }

@@ -57,7 +57,7 @@ class Stats(C.Structure):
                 ("list_capacity", C.c_int64), ("rebuilds", C.c_int64), ("steps", C.c_int64),
                 ("list_per_atom", C.c_double), ("bytes_device", C.c_double), ("ms_last_build", C.c_double),
                 ("ms_last_forces", C.c_double), ("precision", C.c_int), ("tpa", C.c_int), ("block", C.c_int),
-                ("ms_last_run", C.c_double), ("kernel_ms", C.c_double * 6), ("kernel_launches", C.c_int64 * 6),
+                ("ms_last_run", C.c_double), ("kernel_ms", C.c_double * 7), ("kernel_launches", C.c_int64 * 7),
                 ("pairs_in_cutoff", C.c_int64), ("graph_steps", C.c_int64), ("graph_redos", C.c_int64),
                 ("bytes_per_atom_need", C.c_double)]
 class MinResult(C.Structure):
@@ -66,7 +66,7 @@ class MinResult(C.Structure):
                 ("fnorm2_final", C.c_double), ("fnorminf_final", C.c_double), ("alpha_final", C.c_double)]
 
 
-KERNELS = ["pair_ilp", "tersoff", "intralayer_normals", "gather", "integrate", "neighbor_build"]
+KERNELS = ["pair_ilp", "tersoff", "intralayer_normals", "gather", "integrate", "neighbor_build", "normal_deriv"]
 
 
 class SystemDesc(C.Structure):

@@ -1350,14 +1350,16 @@ __device__ __forceinline__ void pair_body(const ForceArgs<R> &a, const AtomI<R> 
 #endif
 }
 
-// FP32: at least 5 blocks of 256 threads per SM (48 registers) -- the kernel is
-// issue-bound with long-scoreboard stalls on j's data, and 40 resident warps hide them
-// better than 36 (measured: -8 % at 2.7M atoms, -16 % at 490k).  The two-pair body of
-// the single-element path needs 76 registers without spills; 4 blocks (64 registers)
-// measured 3 % faster than 3 blocks at 2.7M atoms.  FP64 keeps its registers.
+// FP32: the generic force-only loops at least 5 blocks of 256 threads per SM (48
+// registers) -- issue-bound with long-scoreboard stalls on j's data, and 40 resident
+// warps hide them better than 36 (measured: -8 % at 2.7M atoms, -16 % at 490k).  The
+// two-pair body of the single-element path needs 76 registers without spills; 4 blocks
+// (64 registers) measured 3 % faster than 3 blocks at 2.7M atoms.  The energy/virial
+// loops with their FP64 flushes: 4 blocks (64 registers), 26 % faster than 5 on the
+// 256-replica batch, 12 % on the 331k slab.  FP64 keeps its registers.
 template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC, bool TWO>
 constexpr int ilp_min_blocks() {
-  return sizeof(R) == 8 ? 1 : TWO ? 4 : 5;
+  return sizeof(R) == 8 ? 1 : (TWO || EV) ? 4 : 5;
 }
 
 // TWO: the two-pair loop alone (mixed precision, forces only, interlayer list, C >= 0

@@ -218,8 +218,7 @@ int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double 
  * list there, so it equals the uninterrupted run up to summation order).
  * "ters_concurrent" 1 (default) = the Tersoff kernel runs on a second stream beside
  * the interlayer pair kernel (they write disjoint arrays; joined before the gather);
- * 0 = one after the other.  "ilp_prefetch" 1 = software-pipelined multi-element pair
- * loop (j's data one entry ahead). */
+ * 0 = one after the other. */
 int lmff_set_option(lmff_engine *e, const char *key, double value);
 
 /* ---- one-shot evaluation on host buffers (the pair-style drop-in) ------------------ */
@@ -229,6 +228,26 @@ int lmff_set_option(lmff_engine *e, const char *key, double value);
 int lmff_compute(lmff_engine *e, int natoms, const double *x, const int *type, const int64_t *mol,
                  const int64_t *tag, int which, int eflag, int vflag, double *f, double *eatom,
                  lmff_result *res);
+
+/* Subdomain form of lmff_compute for a LAMMPS rank of a domain decomposition: what
+ * PairTersoff::compute (pair_tersoff.cpp:86-265) and PairILPGrapheneHBN::compute
+ * (pair_ilp_graphene_hbn.cpp:428-675) do on the owned atoms [0, nlocal) and the ghost
+ * atoms [nlocal, nall) of the full+ghost list (npair_full_bin_ghost.cpp:36-140), with
+ * newton on.  x[nall*3], type, mol, tag[nall] (tags required: a ghost carries its
+ * owner's tag).  The engine bins all nall atoms in a non-periodic box of its own (the
+ * ghosts carry the periodic images; lmff_set_box is not used).  Evaluated: two-body
+ * terms whose end kept by the tag-parity half of the full list is owned (equal tags:
+ * the coordinate tie-break of pair_tersoff.cpp:150-158), ILP repulsion terms and
+ * Tersoff bond-order terms whose centre is owned.  f[nall*3] and eatom[nall] receive
+ * every atom's share, ghosts included, for LAMMPS's reverse communication to fold
+ * (verlet.cpp:307-332, Comm::reverse_comm); energies and virials in res are those of
+ * the evaluated interactions, equal to the fdotr virial over nall.  which may add
+ * LMFF_SAME_ATOMS when the atoms (order, identity, nlocal) are those of the previous
+ * call; OVERWRITE as in lmff_compute.  The engine stays in this mode until
+ * lmff_set_box; until then the periodic-system calls return LMFF_EINVAL. */
+int lmff_compute_ghost(lmff_engine *e, int nlocal, int nall, const double *x, const int *type,
+                       const int64_t *mol, const int64_t *tag, int which, int eflag, int vflag,
+                       double *f, double *eatom, lmff_result *res);
 
 /* Same on device pointers (d_x[natoms*3] double, d_type int32, d_mol int64, d_tag int64
  * or NULL, d_f double accumulated), ordered on the engine's stream. */

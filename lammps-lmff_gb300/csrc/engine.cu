@@ -452,7 +452,9 @@ struct Engine {
   int precision = LMFF_FP64;
   int tpa = 16, block = 128;
   int list_full = 0;
-  int ilp_prefetch = 0;   // option "ilp_prefetch": software-pipelined pair kernel
+  // subdomain mode (lmff_compute_ghost): the number of owned atoms among the caller's
+  // nall (owned first, then ghosts); -1 for the ordinary periodic-system mode
+  int ghost_nlocal = -1;
   double skin = 2.0;
   int ntypes = 0;
   HostTersoff ht;
@@ -1323,7 +1325,8 @@ struct Engine {
     a.f_out = d.f;
     a.status = d.status;
     a.list_full = list_full;
-    a.ilp_prefetch = ilp_prefetch;
+    a.own_perm = ghost_nlocal >= 0 ? d.perm : nullptr;
+    a.nown = ghost_nlocal;
     a.kc = i_on && hi.model == LMFF_INTERLAYER_KC;
     return a;
   }
@@ -1539,6 +1542,41 @@ struct Engine {
     }
     CK(cudaStreamSynchronize(stream));
     return LMFF_OK;
+  }
+
+  // Subdomain mode: x[nall*3] holds the caller's owned atoms [0, nlocal) followed by
+  // ghost atoms, in a box the engine chooses itself (non-periodic, around all nall atoms
+  // with room for the skin; the ghosts carry the periodic images).  Only interactions
+  // owned by owned atoms are evaluated; every atom receives its share of their forces
+  // (f[nall*3]) and per-atom energy, and the energies and virial are those of the owned
+  // interactions, so that summing over subdomains after the ghost forces are folded back
+  // gives the whole system's.
+  int compute_ghost(int nlocal, int nall, const double *x, const int *type, const int64_t *mol, const int64_t *tag,
+                    int which, int eflag, int vflag, double *f, double *eatom, lmff_result *res) {
+    if (nlocal < 0 || nall < nlocal) return fail(LMFF_EINVAL, "lmff_compute_ghost: need 0 <= nlocal <= nall");
+    const bool same = (which & LMFF_SAME_ATOMS) && ghost_nlocal == nlocal && have_box && loaded && built && n == nall;
+    if (!same) {
+      double lo[3] = {0.0, 0.0, 0.0}, hi[3] = {1.0, 1.0, 1.0};
+      for (int p = 0; p < nall; p++)
+        for (int k = 0; k < 3; k++) {
+          const double c = x[3 * p + k];
+          if (!std::isfinite(c)) return fail(LMFF_EINVAL, "lmff_compute_ghost: non-finite coordinate");
+          if (p == 0 || c < lo[k]) lo[k] = c;
+          if (p == 0 || c > hi[k]) hi[k] = c;
+        }
+      const double pad = skin + 1.0;
+      for (int k = 0; k < 3; k++) {
+        blo[k] = lo[k] - pad;
+        bhi[k] = hi[k] + pad;
+        bper[k] = 0;
+      }
+      have_box = true;
+      loaded = false;
+      built = false;
+      which &= ~LMFF_SAME_ATOMS;
+    }
+    ghost_nlocal = nlocal;
+    return compute_host(nall, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
   }
 
   int compute_device(int nn, const double *dx, const int *dtype, const int64_t *dmol, const int64_t *dtag, int which,
@@ -2803,11 +2841,21 @@ int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double 
     e->e.bper[k] = periodic[k] != 0;
   }
   e->e.have_box = true;
+  if (e->e.ghost_nlocal >= 0) {   // leaving subdomain mode
+    e->e.ghost_nlocal = -1;
+    changed = true;
+  }
   if (changed) {
     e->e.built = false;
     e->e.loaded = false;
   }
   return LMFF_OK;
+}
+
+// calls that evaluate the periodic-system form refuse an engine left in subdomain mode
+static int refuse_ghost_mode(lmff_engine *e) {
+  if (e->e.ghost_nlocal < 0) return LMFF_OK;
+  return e->e.fail(LMFF_EINVAL, "the engine is in subdomain mode (lmff_compute_ghost): call lmff_set_box to leave it");
 }
 
 int lmff_set_option(lmff_engine *e, const char *key, double value) {
@@ -2829,9 +2877,6 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
     e->e.skin = value;
     e->e.build_consts();
     e->e.loaded = false;
-  } else if (k == "ilp_prefetch") {
-    e->e.ilp_prefetch = value != 0.0;
-    e->e.drop_graph();
   } else if (k == "ters_concurrent") {
     e->e.ters_concurrent = value != 0.0;
     e->e.drop_graph();
@@ -2860,13 +2905,23 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
 int lmff_compute(lmff_engine *e, int natoms, const double *x, const int *type, const int64_t *mol, const int64_t *tag,
                  int which, int eflag, int vflag, double *f, double *eatom, lmff_result *res) {
   if (!e || natoms < 0 || (natoms > 0 && (!x || !type))) return LMFF_EINVAL;
+  if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
   return e->e.compute_host(natoms, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
+}
+
+int lmff_compute_ghost(lmff_engine *e, int nlocal, int nall, const double *x, const int *type, const int64_t *mol,
+                       const int64_t *tag, int which, int eflag, int vflag, double *f, double *eatom,
+                       lmff_result *res) {
+  if (!e || nlocal < 0 || nall < nlocal || (nall > 0 && (!x || !type || !tag))) return LMFF_EINVAL;
+  DeviceCall dc(e->e);
+  return e->e.compute_ghost(nlocal, nall, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
 }
 
 int lmff_compute_device(lmff_engine *e, int natoms, const double *d_x, const int *d_type, const int64_t *d_mol,
                         const int64_t *d_tag, int which, int eflag, int vflag, double *d_f, lmff_result *res) {
   if (!e || natoms < 0 || (natoms > 0 && (!d_x || !d_type))) return LMFF_EINVAL;
+  if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
   return e->e.compute_device(natoms, d_x, d_type, d_mol, d_tag, which, eflag, vflag, d_f, res);
 }
@@ -2875,6 +2930,7 @@ int lmff_compute_device_noalloc(lmff_engine *e, int natoms, const double *d_x, c
                                 const int64_t *d_mol, int which, int eflag, int vflag, double *d_f, lmff_result *res) {
   if (!e || natoms < 0 || (natoms > 0 && (!d_x || !d_type || !d_f))) return LMFF_EINVAL;
   if (natoms > 0 && !d_mol) return e->e.fail(LMFF_EINVAL, "lmff_compute_device_noalloc: d_mol is required");
+  if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
   return lmff::noalloc_compute(e->e, natoms, d_x, d_type, d_mol, which, eflag, vflag, d_f, res);
 }
@@ -2882,6 +2938,7 @@ int lmff_compute_device_noalloc(lmff_engine *e, int natoms, const double *d_x, c
 int lmff_upload(lmff_engine *e, int natoms, const double *x, const double *v, const int *type, const int64_t *mol,
                 const int64_t *tag, const double *mass) {
   if (!e || natoms < 0 || (natoms > 0 && (!x || !type))) return LMFF_EINVAL;
+  if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
   return e->e.upload(natoms, x, v, type, mol, tag, mass);
 }
@@ -2889,6 +2946,7 @@ int lmff_upload(lmff_engine *e, int natoms, const double *x, const double *v, co
 int lmff_compute_resident(lmff_engine *e, int which, int eflag, int vflag, lmff_result *res) {
   if (!e) return LMFF_EINVAL;
   if (!e->e.loaded) return e->e.fail(LMFF_EINVAL, "no resident system");
+  if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
   int rc = e->e.maybe_rebuild();
   if (rc) return rc;
@@ -2901,6 +2959,7 @@ int lmff_compute_resident(lmff_engine *e, int which, int eflag, int vflag, lmff_
 
 int lmff_run_nve(lmff_engine *e, int nsteps, double dt, int thermo_every, lmff_thermo *thermo) {
   if (!e || nsteps < 0 || thermo_every < 0) return LMFF_EINVAL;
+  if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
   return e->e.run_nve(nsteps, dt, thermo_every, thermo);
 }
@@ -2913,12 +2972,14 @@ int lmff_download(lmff_engine *e, double *x, double *v, double *f) {
 
 int lmff_batch_set(lmff_engine *e, int nsys, const lmff_system_desc *sys) {
   if (!e || !sys) return LMFF_EINVAL;
+  if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
   return e->e.batch_set(nsys, sys);
 }
 
 int lmff_batch_compute(lmff_engine *e, double *f_out, lmff_result *res) {
   if (!e) return LMFF_EINVAL;
+  if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
   return e->e.batch_compute(f_out, res);
 }
@@ -2926,6 +2987,7 @@ int lmff_batch_compute(lmff_engine *e, double *f_out, lmff_result *res) {
 int lmff_minimize(lmff_engine *e, double etol, double ftol, int maxiter, int maxeval, double dmax,
                   const int *frozen, lmff_min_result *out) {
   if (!e || !out) return LMFF_EINVAL;
+  if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
   return e->e.minimize(etol, ftol, maxiter, maxeval, dmax, frozen, out);
 }

@@ -245,7 +245,13 @@ struct ForceArgs {
   int *status;
   int do_ters, do_ilp;
   int list_full;       // the pair list also holds same-molecule / non-ILP pairs
-  int ilp_prefetch;    // pair kernel loads the next pair's data one iteration ahead
+  // subdomain (ghost-atom) mode: non-null when the caller passes owned atoms followed by
+  // ghost atoms; sorted atom s is owned when own_perm[s] < nown.  Only interactions owned
+  // by owned atoms are evaluated (two-body terms by the reference's tag-parity half of
+  // the full list, three-body and normal terms by their centre atom); every atom, ghosts
+  // included, receives its share of their forces.
+  const int *own_perm;
+  int nown;
   int kc;              // interlayer style is kolmogorov/crespi/full
 };
 

@@ -289,6 +289,18 @@ __device__ __forceinline__ bool keep_half(long long itag, long long jtag, int sx
   if (sy != 0) return sy > 0;
   return sx > 0;
 }
+// the same selection with the reference's own tie-break for equal tags (a ghost copy of
+// an atom's owner): compare the coordinates of j against i on (z, y, x), r = x_j - x_i
+template <class T>
+__device__ __forceinline__ bool keep_half_r(long long itag, long long jtag, T rx, T ry, T rz) {
+  if (itag > jtag) return ((itag + jtag) & 1) != 0;
+  if (itag < jtag) return ((itag + jtag) & 1) == 0;
+  if (rz != T(0)) return rz > T(0);
+  if (ry != T(0)) return ry > T(0);
+  return rx > T(0);
+}
+// subdomain mode: whether sorted atom s is owned
+__device__ __forceinline__ bool owned(const ForceArgs<R> &a, int s) { return a.own_perm[s] < a.nown; }
 
 // ============================================================ k_tersoff ==========
 // One thread per centre atom i: the bonds i-j it centres (zeta over k, force_zeta,
@@ -418,7 +430,9 @@ __device__ __forceinline__ void df_dot3(const float *ah, const float *al, const 
 // on FP32 bond lengths (every term vanishes continuously at its cut-off), h - cos(theta)
 // is formed in FP64 once per bond pair, and the three-body forces on each partner are
 // summed in FP32 before one FP64 addition.
-template <int NB, bool EV>
+// GH (subdomain mode): a bond's repulsion counts when the end the tag-parity half keeps
+// is owned, the bond-order terms when the centre i is owned.
+template <int NB, bool EV, bool GH>
 __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int ie, int cnt) {
   constexpr bool F32 = sizeof(R) == 4;
   constexpr int UNR = NB <= 4 ? NB : 1;
@@ -506,7 +520,8 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
       }
     }
   }
-  const long long itag = c_pot.rep_sym ? 0 : a.tag[i];
+  const long long itag = (c_pot.rep_sym && !GH) ? 0 : a.tag[i];
+  const bool iown = !GH || owned(a, i);
 #pragma unroll UNR
   for (int s = 0; s < NB; s++) {
     if (s >= cnt) continue;
@@ -521,12 +536,15 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
     // of the end the reference's half list keeps
     {
       const TersP<R> *pr = &pij;
-      if (!c_pot.rep_sym) {
+      bool rep_on = true;
+      if (!c_pot.rep_sym || GH) {
         int j, sx, sy, sz;
         decode_entry(ev_[s], a.lc, j, sx, sy, sz);
-        if (!keep_half(itag, a.tag[j], sx, sy, sz)) pr = &c_pot.ters[(je * MAXELEM + ie) * MAXELEM + ie];
+        const bool keep = GH ? keep_half_r(itag, a.tag[j], dxd[s], dyd[s], dzd[s]) : keep_half(itag, a.tag[j], sx, sy, sz);
+        if (!keep && !c_pot.rep_sym) pr = &c_pot.ters[(je * MAXELEM + ie) * MAXELEM + ie];
+        if (GH) rep_on = keep ? iown : owned(a, j);
       }
-      if (F32 ? rR < pr->rhi : rs64[s] < pr->cutsq64) {
+      if (rep_on && (F32 ? rR < pr->rhi : rs64[s] < pr->cutsq64)) {
         double tmp_exp, fpair, fc;
         if constexpr (F32) {
           tmp_exp = exp_x32f(rR, rl[s], pr->nl1h, pr->nl1l);
@@ -553,7 +571,7 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
         }
       }
     }
-    if (!(F32 ? rR < pij.rhi : rs64[s] < pij.cutsq64)) {
+    if (!iown || !(F32 ? rR < pij.rhi : rs64[s] < pij.cutsq64)) {
       fx += dxd[s] * fr; fy += dyd[s] * fr; fz += dzd[s] * fr;
       continue;
     }
@@ -694,15 +712,15 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
 }
 
 // sp2 layers give 3 bonds per atom: those atoms run with their bonds in registers
-template <bool EV, bool EATOM>
+template <bool EV, bool EATOM, bool GH>
 __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const long long iinfo = __double_as_longlong(a.A.xq[i].w);
   const int ie = c_pot.t_map[info_type(iinfo)];
   const int cnt = ie < 0 ? 0 : a.ters_cnt[i];
-  if (cnt <= 3) tersoff_atom<3, EV>(a, i, ie, cnt);
-  else tersoff_atom<MAXTERS, EV>(a, i, ie, cnt);
+  if (cnt <= 3) tersoff_atom<3, EV, GH>(a, i, ie, cnt);
+  else tersoff_atom<MAXTERS, EV, GH>(a, i, ie, cnt);
 }
 
 // ============================================================== k_ilp ============
@@ -914,10 +932,12 @@ __shared__ IlpP<R> s_ilp[MAXELEM * MAXELEM];
 
 // IMG: the entry may carry a periodic image shift (false: every entry of i's list is
 // unshifted, and the image decode and shift are left out)
-template <bool EV, bool ONE, bool KC, bool IMG>
+// GH (subdomain mode, iown: whether i is owned): term (i,j) counts when i is owned,
+// term (j,i) when j is, the vdW pair when the end the tag-parity half keeps is.
+template <bool EV, bool ONE, bool KC, bool IMG, bool GH>
 __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &ai, const SysDesc &sdl, uint32_t e,
                                          const typename AtomI<R>::J &J, const NrmJ<R> &N, R nix, R niy, R niz,
-                                         int ie, long long mi, long long itag, bool check, IlpAcc &acc) {
+                                         int ie, long long mi, long long itag, bool check, bool iown, IlpAcc &acc) {
   int j, sx = 0, sy = 0, sz = 0;
   if (IMG) decode_entry(e, a.lc, j, sx, sy, sz);
   else j = (int)(e & a.lc.imask);
@@ -949,7 +969,18 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
     dTap = (y * y) * (y * (R(140) * c_pot.i_inv_rcut));
   }
   // ---- vdW (both ends evaluate the pair force; energy halved)
-  const IlpP<R> &pv = (c_pot.vdw_sym || keep_half(itag, a.tag[j], sx, sy, sz)) ? pij : pji;
+  R wi = 1, wj = 1, wv = 1;
+  bool keep;
+  if constexpr (GH) {
+    keep = keep_half_r(itag, a.tag[j], -dx, -dy, -dz);
+    const bool jown = owned(a, j);
+    wi = iown ? R(1) : R(0);
+    wj = jown ? R(1) : R(0);
+    wv = (keep ? iown : jown) ? R(1) : R(0);
+  } else {
+    keep = c_pot.vdw_sym || keep_half(itag, a.tag[j], sx, sy, sz);
+  }
+  const IlpP<R> &pv = (c_pot.vdw_sym || keep) ? pij : pji;
   R r2inv = rinv * rinv;
   R r6inv = r2inv * r2inv * r2inv;
   R r8inv = r6inv * r2inv;
@@ -974,6 +1005,10 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
       fpv = pv.C6 * r8inv * TSinv * (R(-6) + pv.d_over_seff * (TSvdw - R(1)) * TSinv * r);
     }
   }
+  if constexpr (GH) {
+    Vvdw *= wv;
+    fpv *= wv;
+  }
   R fsum_v = fpv * Tap - Vvdw * dTap * rinv;
   // ---- repulsion of term (i,j) with n_i and of term (j,i) with n_j (del' = -del, prod' = -q)
   R p = nix * dx + niy * dy + niz * dz;
@@ -992,6 +1027,10 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
     V2 = fma(exp0b, pji.eps_half, F2);
     fpair1 = R(2) * (F1 * pij.delta2inv);
     fpair1b = R(2) * (F2 * pji.delta2inv);
+    if constexpr (GH) {
+      V *= wi; fpair1 *= wi;
+      V2 *= wj; fpair1b *= wj;
+    }
     const R Tr = Tap * rinv, dTr = dTap * rinv;
     crad = fsum_v + Tap * (fpair1 + fpair1b) + fma(Tr, pij.lambda, -dTr) * V + fma(Tr, pji.lambda, -dTr) * V2;
     if (EV) fsum = pij.lambda * rinv * V + fpair1;
@@ -1014,6 +1053,10 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
       exp1b = Math<R>::exp_rep1(pji, rhosq2);
     }
     rep_term<KC>(pji, exp0b, exp1b, rhosq2, rinv, V2, fpair1b, fsum2);
+    if constexpr (GH) {
+      V *= wi; fpair1 *= wi; fsum *= wi;
+      V2 *= wj; fpair1b *= wj; fsum2 *= wj;
+    }
     crad = fsum_v + (fsum + fsum2) * Tap - (V + V2) * dTap * rinv;
   }
   // ---- force on i
@@ -1026,7 +1069,7 @@ __device__ __forceinline__ void ilp_pair(const ForceArgs<R> &a, const AtomI<R> &
   if (EV) {
     acc.evdw += R(0.5) * Vvdw * Tap;
     // Kolmogorov-Crespi without the taper tallies V - offset per directed term
-    const R eoff = (KC && !c_pot.tap) ? pij.kc_off + pji.kc_off : R(0);
+    const R eoff = (KC && !c_pot.tap) ? pij.kc_off * wi + pji.kc_off * wj : R(0);
     acc.erep += R(0.5) * ((V + V2) * Tap - eoff);
     // term (i,j): del (x) fkc_ij;  vdW: half of del (x) fsum_v del
     R cr1 = fsum * Tap - V * dTap * rinv + R(0.5) * fsum_v;
@@ -1075,11 +1118,11 @@ __device__ float2 g_x2m[X2M_ROWS * X2M_N];
 __shared__ float2 s_x2m[X2M_ROWS * X2M_N];
 
 
-template <bool EV, bool ONE, bool KC, bool IMG>
+template <bool EV, bool ONE, bool KC, bool IMG, bool GH>
 __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const AtomI<float> &ai, const SysDesc &sdl,
                                             uint32_t e, const AtomI<float>::J &J, const NrmJ<float> &N, float nix,
                                             float niy, float niz, int ie, long long mi, long long itag, bool check,
-                                            IlpAcc &acc) {
+                                            bool iown, IlpAcc &acc) {
   // del = x_i - x_j(image), x and y packed: ((h_i - h_j) - s Lhi) + ((l_i - l_j) - s Llo)
   int j, sx = 0, sy = 0, sz = 0;
   float2 hxy = add2(p2(ai.hx, ai.hy), p2(-J.h.x, -J.h.y));
@@ -1132,7 +1175,18 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
     dTap = t.y * c_pot.i_inv_rcut;
   }
   // ---- vdW (both ends evaluate the pair force; energy halved)
-  const IlpP<float> &pv = (c_pot.vdw_sym || keep_half(itag, a.tag[j], sx, sy, sz)) ? pij : pji;
+  float wi = 1.f, wj = 1.f, wv = 1.f;
+  bool keep;
+  if constexpr (GH) {
+    keep = keep_half_r(itag, a.tag[j], -dx, -dy, -dz);
+    const bool jown = owned(a, j);
+    wi = iown ? 1.f : 0.f;
+    wj = jown ? 1.f : 0.f;
+    wv = (keep ? iown : jown) ? 1.f : 0.f;
+  } else {
+    keep = c_pot.vdw_sym || keep_half(itag, a.tag[j], sx, sy, sz);
+  }
+  const IlpP<float> &pv = (c_pot.vdw_sym || keep) ? pij : pji;
   const float r2inv = rinv * rinv;
   const float r6inv = r2inv * r2inv * r2inv;
   const float r8inv = r6inv * r2inv;
@@ -1146,6 +1200,10 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
     const float c6t = pv.C6 * TSinv;
     Vvdw = -c6t * r6inv;
     fpv = c6t * r8inv * (-6.f + pv.d_over_seff * (TSvdw - 1.f) * TSinv * r);
+  }
+  if constexpr (GH) {
+    Vvdw *= wv;
+    fpv *= wv;
   }
   const float fsum_v = fpv * Tap - Vvdw * dTap * rinv;
   // ---- the two repulsion terms packed: .x = (i,j) with n_i, .y = (j,i) with n_j.  The
@@ -1176,6 +1234,10 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
     V = mul2(E0, ER);
     FP1 = mul2(mul2(E0, FR), ONE ? c_x2.d2x2 : p2(2.f * pij.delta2inv, 2.f * pji.delta2inv));
   }
+  if constexpr (GH) {
+    V = mul2(V, p2(wi, wj));
+    FP1 = mul2(FP1, p2(wi, wj));
+  }
   const float2 FS = fma2(mul2(ONE ? c_x2.lambda : p2(pij.lambda, pji.lambda), V), p2(rinv, rinv), FP1);
   const float2 TPQ = mul2(mul2(p2(Tap, Tap), PQ), FP1);   // (tp1, tq1)
   const float Vsum = V.x + V.y;
@@ -1202,7 +1264,7 @@ __device__ __forceinline__ void ilp_pair_x2(const ForceArgs<float> &a, const Ato
   }
   if (EV) {
     acc.evdw += 0.5f * Vvdw * Tap;
-    const float eoff = (KC && !c_pot.tap) ? pij.kc_off + pji.kc_off : 0.f;
+    const float eoff = (KC && !c_pot.tap) ? pij.kc_off * wi + pji.kc_off * wj : 0.f;
     acc.erep += 0.5f * (Vsum * Tap - eoff);
     const float cr1 = FS.x * Tap - V.x * dTap * rinv + 0.5f * fsum_v;
     const float kx = cr1 * dx - TPQ.x * nix, ky = cr1 * dy - TPQ.x * niy, kz = cr1 * dz - TPQ.x * niz;
@@ -1339,14 +1401,14 @@ __device__ __forceinline__ void ilp_pair2(const ForceArgs<float> &a, const AtomI
 #endif  // LMFF_PACKED_X2
 
 // the pair body of this precision: packed FP32x2 for the mixed path, scalar FP64
-template <bool EV, bool ONE, bool KC, bool IMG>
+template <bool EV, bool ONE, bool KC, bool IMG, bool GH>
 __device__ __forceinline__ void pair_body(const ForceArgs<R> &a, const AtomI<R> &ai, const SysDesc &sdl, uint32_t e,
                                           const typename AtomI<R>::J &J, const NrmJ<R> &N, R nix, R niy, R niz, int ie,
-                                          long long mi, long long itag, bool check, IlpAcc &acc) {
+                                          long long mi, long long itag, bool check, bool iown, IlpAcc &acc) {
 #ifdef LMFF_PACKED_X2
-  ilp_pair_x2<EV, ONE, KC, IMG>(a, ai, sdl, e, J, N, nix, niy, niz, ie, mi, itag, check, acc);
+  ilp_pair_x2<EV, ONE, KC, IMG, GH>(a, ai, sdl, e, J, N, nix, niy, niz, ie, mi, itag, check, iown, acc);
 #else
-  ilp_pair<EV, ONE, KC, IMG>(a, ai, sdl, e, J, N, nix, niy, niz, ie, mi, itag, check, acc);
+  ilp_pair<EV, ONE, KC, IMG, GH>(a, ai, sdl, e, J, N, nix, niy, niz, ie, mi, itag, check, iown, acc);
 #endif
 }
 
@@ -1357,7 +1419,7 @@ __device__ __forceinline__ void pair_body(const ForceArgs<R> &a, const AtomI<R> 
 // (64 registers) measured 3 % faster than 3 blocks at 2.7M atoms.  The energy/virial
 // loops with their FP64 flushes: 4 blocks (64 registers), 26 % faster than 5 on the
 // 256-replica batch, 12 % on the 331k slab.  FP64 keeps its registers.
-template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC, bool TWO>
+template <int TPA, bool EV, bool EATOM, bool ONE, bool GH, bool KC, bool TWO>
 constexpr int ilp_min_blocks() {
   return sizeof(R) == 8 ? 1 : (TWO || EV) ? 4 : 5;
 }
@@ -1365,8 +1427,9 @@ constexpr int ilp_min_blocks() {
 // TWO: the two-pair loop alone (mixed precision, forces only, interlayer list, C >= 0
 // and symmetric element-pair constants: the host checks these), in a kernel of its own
 // so that the generic loops do not share its register allocation
-template <int TPA, bool EV, bool EATOM, bool ONE, bool PF, bool KC, bool TWO>
-__global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, KC, TWO>())) k_ilp(ForceArgs<R> a) {
+// GH: subdomain mode (owned + ghost atoms, see ForceArgs::own_perm)
+template <int TPA, bool EV, bool EATOM, bool ONE, bool GH, bool KC, bool TWO>
+__global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, GH, KC, TWO>())) k_ilp(ForceArgs<R> a) {
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gtid / TPA;
   const int lane = threadIdx.x & (TPA - 1);
@@ -1381,7 +1444,8 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
   R nix, niy, niz;
   if constexpr (sizeof(R) == 8) { d4 q = a.nrm64[ii]; nix = q.x; niy = q.y; niz = q.z; }
   else { float4 q = a.nrm32[ii]; nix = q.x; niy = q.y; niz = q.z; }
-  const long long itag = c_pot.vdw_sym ? 0 : a.tag[ii];
+  const long long itag = (c_pot.vdw_sym && !GH) ? 0 : a.tag[ii];
+  const bool iown = !GH || owned(a, ii);
   IlpAcc acc;
   __shared__ double s_tot[ILP_TOT_SPLIT ? LaneTot<TPA, EV, EATOM>::HOLD : 1][256];
   LaneTot<TPA, EV, EATOM> tot;
@@ -1461,49 +1525,22 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, PF, 
           const uint32_t e = e_next;
           if (k + TPA < cnt) e_next = __ldg(&lst[k + TPA]);
           const int j = (int)(e & a.lc.imask);
-          pair_body<EV, ONE, KC, IMG>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi,
-                                      itag, check, acc);
+          pair_body<EV, ONE, KC, IMG, GH>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie,
+                                          mi, itag, check, iown, acc);
           ILP_FLUSH_AT(k, TPA, 0)
         }
       } else {
         for (int k = lane; k < cnt; k += TPA) {
           const uint32_t e = __ldg(&lst[k]);
           const int j = (int)(e & a.lc.imask);
-          pair_body<EV, ONE, KC, IMG>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie, mi,
-                                      itag, check, acc);
+          pair_body<EV, ONE, KC, IMG, GH>(a, ai, sdl, e, ai.fetch(a.A, j), NrmJ<R>::load(a, j), nix, niy, niz, ie,
+                                          mi, itag, check, iown, acc);
           ILP_FLUSH_AT(k, TPA, 0)
         }
       }
     };
-    if constexpr (!PF) {
-      if (a.list_img[i]) run(std::true_type{});
-      else run(std::false_type{});
-    } else {
-      // software pipeline: the next entry's position and normal are in flight while
-      // the current pair is evaluated
-      uint32_t e = 0;
-      typename AtomI<R>::J J{};
-      NrmJ<R> N{};
-      if (lane < cnt) {
-        e = __ldg(&lst[lane]);
-        const int j = (int)(e & a.lc.imask);
-        J = ai.fetch(a.A, j);
-        N = NrmJ<R>::load(a, j);
-      }
-      for (int k = lane; k < cnt; k += TPA) {
-        const uint32_t ec = e;
-        const typename AtomI<R>::J Jc = J;
-        const NrmJ<R> Nc = N;
-        if (k + TPA < cnt) {
-          e = __ldg(&lst[k + TPA]);
-          const int j = (int)(e & a.lc.imask);
-          J = ai.fetch(a.A, j);
-          N = NrmJ<R>::load(a, j);
-        }
-        pair_body<EV, ONE, KC, true>(a, ai, sdl, ec, Jc, Nc, nix, niy, niz, ie, mi, itag, check, acc);
-        ILP_FLUSH_AT(k, TPA, 0)
-      }
-    }
+    if (a.list_img[i]) run(std::true_type{});
+    else run(std::false_type{});
   }
 #undef ILP_FLUSH_AT
   if constexpr (ILP_TOT_SPLIT) {
@@ -1833,8 +1870,14 @@ void launch_short(const ForceArgs<R> &a, const double *cutILPsq64, double tcutma
 void launch_tersoff(const ForceArgs<R> &a, bool ev, bool eatom, cudaStream_t s) {
   if (a.n == 0) return;
   int g = (a.n + 127) / 128;
-  if (ev) k_tersoff<true, false><<<g, 128, 0, s>>>(a);
-  else k_tersoff<false, false><<<g, 128, 0, s>>>(a);
+  if (a.own_perm) {
+    if (ev) k_tersoff<true, false, true><<<g, 128, 0, s>>>(a);
+    else k_tersoff<false, false, true><<<g, 128, 0, s>>>(a);
+  } else if (ev) {
+    k_tersoff<true, false, false><<<g, 128, 0, s>>>(a);
+  } else {
+    k_tersoff<false, false, false><<<g, 128, 0, s>>>(a);
+  }
   if (ev && eatom) k_ters_eatom_own<<<g, 128, 0, s>>>(a);
 }
 
@@ -1852,7 +1895,6 @@ static void launch_ilp_t(const ForceArgs<R> &a, bool ev, bool eatom, int block, 
   else if (ev) k_ilp<TPA, true, false, ONE, false, false, false><<<g, block, 0, s>>>(a);
   else if (TWO_PAIR_BODY && !a.list_full && (ONE ? h_two_one : h_two_multi))
     k_ilp<TPA, false, false, ONE, false, false, TWO_PAIR_BODY><<<g, block, 0, s>>>(a);
-  else if (a.ilp_prefetch) k_ilp<TPA, false, false, ONE, true, false, false><<<g, block, 0, s>>>(a);
   else k_ilp<TPA, false, false, ONE, false, false, false><<<g, block, 0, s>>>(a);
 }
 
@@ -1866,8 +1908,32 @@ static void launch_ilp_one(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, 
   }
 }
 
+// subdomain mode: the generic loops at 8 lanes per atom
+template <bool ONE>
+static void launch_ilp_ghost(const ForceArgs<R> &a, bool ev, bool eatom, int block, cudaStream_t s) {
+  constexpr int TPA = 8;
+  long long threads = (long long)a.n * TPA;
+  int g = (int)((threads + block - 1) / block);
+  if (a.kc) {
+    if (ev && eatom) k_ilp<TPA, true, true, ONE, true, true, false><<<g, block, 0, s>>>(a);
+    else if (ev) k_ilp<TPA, true, false, ONE, true, true, false><<<g, block, 0, s>>>(a);
+    else k_ilp<TPA, false, false, ONE, true, true, false><<<g, block, 0, s>>>(a);
+  } else if (ev && eatom) {
+    k_ilp<TPA, true, true, ONE, true, false, false><<<g, block, 0, s>>>(a);
+  } else if (ev) {
+    k_ilp<TPA, true, false, ONE, true, false, false><<<g, block, 0, s>>>(a);
+  } else {
+    k_ilp<TPA, false, false, ONE, true, false, false><<<g, block, 0, s>>>(a);
+  }
+}
+
 void launch_ilp(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, bool one_element, cudaStream_t s) {
   if (a.n == 0) return;
+  if (a.own_perm) {
+    if (one_element) launch_ilp_ghost<true>(a, ev, eatom, block, s);
+    else launch_ilp_ghost<false>(a, ev, eatom, block, s);
+    return;
+  }
   if (one_element) launch_ilp_one<true>(a, ev, eatom, tpa, block, s);
   else launch_ilp_one<false>(a, ev, eatom, tpa, block, s);
 }

@@ -103,6 +103,7 @@ def load_library(path: str = LIB_PATH):
         "lmff_set_option": ([P, C.c_char_p, D], I),
         "lmff_compute": ([P, I, P, P, P, P, I, I, I, P, P, C.POINTER(Result)], I),
         "lmff_compute_device": ([P, I, P, P, P, P, I, I, I, P, C.POINTER(Result)], I),
+        "lmff_compute_ghost": ([P, I, I, P, P, P, P, I, I, I, P, P, C.POINTER(Result)], I),
         "lmff_compute_device_noalloc": ([P, I, P, P, P, I, I, I, P, C.POINTER(Result)], I),
         "lmff_upload": ([P, I, P, P, P, P, P, P], I),
         "lmff_compute_resident": ([P, I, I, I, C.POINTER(Result)], I),
@@ -233,6 +234,28 @@ class Engine:
     def compute_system(self, s, **kw) -> Dict:
         self.set_box(s.box_lo, s.box_hi, s.periodic)
         return self.compute(s.x, s.type, s.mol, s.tag, **kw)
+
+    def compute_ghost(self, nlocal: int, x, type_, mol, tag, which: int = TERSOFF | ILP, eflag=True, vflag=True,
+                      eatom=False, same_atoms=False) -> Dict:
+        """Subdomain evaluation (lmff_compute_ghost): x[nall,3] holds the owned atoms
+        [0, nlocal) then the ghost atoms; returns f[nall,3] (ghost shares included),
+        eatom[nall] if asked, and the energies/virials of the owned interactions."""
+        x = _f64(x).reshape(-1, 3)
+        nall = x.shape[0]
+        t = np.ascontiguousarray(type_, dtype=np.int32)
+        m = np.ascontiguousarray(mol, dtype=np.int64)
+        g = np.ascontiguousarray(tag, dtype=np.int64)
+        f = np.zeros((nall, 3))
+        ea = np.zeros(nall) if eatom else None
+        r = Result()
+        flags = which | (SAME_ATOMS if same_atoms else 0)
+        self._ck(_lib.lmff_compute_ghost(self._h, int(nlocal), nall, _p(x), _p(t), _p(m), _p(g), flags, int(eflag),
+                                         int(vflag), _p(f), _p(ea), C.byref(r)))
+        out = r.to_dict()
+        out["f"] = f
+        if eatom:
+            out["eatom"] = ea
+        return out
 
     def compute_device(self, x, type_, mol, tag, f, which: int = TERSOFF | ILP, eflag=True, vflag=True,
                        same_atoms=False, overwrite=True) -> Dict:

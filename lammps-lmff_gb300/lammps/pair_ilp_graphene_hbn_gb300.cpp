@@ -5,12 +5,8 @@
 #include "pair_ilp_graphene_hbn_gb300.h"
 
 #include <cstring>
-#include <string>
-#include <vector>
 
 #include "atom.h"
-#include "comm.h"
-#include "domain.h"
 #include "error.h"
 #include "force.h"
 #include "neighbor.h"
@@ -25,7 +21,7 @@ PairILPGrapheneHBNGB300::PairILPGrapheneHBNGB300(LAMMPS *lmp) : PairILPGrapheneH
 
 /* ----------------------------------------------------------------------
    checks of PairILPGrapheneHBN::init_style (pair_ilp_graphene_hbn.cpp:393-398);
-   no neighbour request and no ILP pages (the engine builds its own lists)
+   no neighbour request and no intralayer pages (the engine builds its own lists)
 ------------------------------------------------------------------------- */
 
 void PairILPGrapheneHBNGB300::init_style()
@@ -34,11 +30,25 @@ void PairILPGrapheneHBNGB300::init_style()
     error->all(FLERR,"Pair style ilp/graphene/hbn requires newton pair on");
   if (!atom->molecule_flag)
     error->all(FLERR,"Pair style ilp/graphene/hbn requires atom attribute molecule");
+  gb300::setup(lmp,this,this,1,"ilp/graphene/hbn/gb300");
+}
 
-  std::vector<lmff_ilp_param> ip(nparams);
+/* ----------------------------------------------------------------------
+   the parameters after coeff(): Param[] as read, elem2param[ne^2], the intralayer
+   cutoffs, type -> element, cut_global and tap_flag
+------------------------------------------------------------------------- */
+
+void PairILPGrapheneHBNGB300::fill_params(lmff_lammps::StyleParams &sp)
+{
+  sp.ntypes = atom->ntypes;
+  sp.skin = neighbor->skin;
+  sp.interlayer = true;
+  sp.model = LMFF_INTERLAYER_ILP;
+  sp.ilp_params.resize(nparams);
+  lmff_ilp_param *dst = sp.ilp_params.data();
   for (int m = 0; m < nparams; m++) {
     const Param &q = params[m];
-    lmff_ilp_param &o = ip[m];
+    lmff_ilp_param &o = dst[m];
     memset(&o,0,sizeof(o));
     o.z0 = q.z0; o.alpha = q.alpha; o.epsilon = q.epsilon; o.C = q.C; o.delta = q.delta;
     o.d = q.d; o.sR = q.sR; o.reff = q.reff; o.C6 = q.C6; o.S = q.S;
@@ -46,62 +56,31 @@ void PairILPGrapheneHBNGB300::init_style()
     o.ielement = q.ielement; o.jelement = q.jelement;
   }
   int ne = nelements;
-  std::vector<int> e2p(ne*ne);
-  std::vector<double> cut2(ne*ne);
+  sp.i_nelements = ne;
+  sp.i_elem2param.resize(ne*ne);
+  sp.i_cutsq.resize(ne*ne);
   for (int i = 0; i < ne; i++)
     for (int j = 0; j < ne; j++) {
-      e2p[i*ne+j] = elem2param[i][j];
-      cut2[i*ne+j] = cutILPsq[i][j];
+      sp.i_elem2param[i*ne+j] = elem2param[i][j];
+      sp.i_cutsq[i*ne+j] = cutILPsq[i][j];
     }
-  std::vector<int> tmap(atom->ntypes+1);
-  for (int t = 0; t <= atom->ntypes; t++) tmap[t] = t ? map[t] : -1;
-
-  lmff_params p;
-  memset(&p,0,sizeof(p));
-  p.ntypes = atom->ntypes;
-  p.ilp_nelements = ne;
-  p.ilp_nparams = nparams;
-  p.ilp_params = ip.data();
-  p.ilp_elem2param = e2p.data();
-  p.ilp_map = tmap.data();
-  p.ilp_cutILPsq = cut2.data();
-  p.ilp_cut_global = cut_global;
-  p.ilp_tap_flag = tap_flag;
-  p.skin = neighbor->skin;
-  std::string err;
-  if (gb.create(p,lmff_lammps::device_from_env(),lmff_lammps::precision_from_env(),err) != LMFF_OK)
-    error->all(FLERR,(std::string("ilp/graphene/hbn/gb300: ") + err).c_str());
+  sp.i_map.resize(atom->ntypes+1);
+  for (int t = 0; t <= atom->ntypes; t++) sp.i_map[t] = t ? map[t] : -1;
+  sp.cut_global = cut_global;
+  sp.tap_flag = tap_flag;
 }
 
 /* ----------------------------------------------------------------------
-   PairILPGrapheneHBN::compute replaced by one engine evaluation
+   PairILPGrapheneHBN::compute replaced by one engine evaluation (shared with tersoff/gb300
+   under hybrid/overlay)
 ------------------------------------------------------------------------- */
 
 void PairILPGrapheneHBNGB300::compute(int eflag, int vflag)
 {
   ev_init(eflag,vflag);
   pvector[0] = pvector[1] = 0.0;
-  if (comm->nprocs > 1)
-    error->all(FLERR,"Pair style ilp/graphene/hbn/gb300 evaluates the whole periodic system on one GPU: "
-               "run it on one MPI rank");
-  if (domain->triclinic)
-    error->all(FLERR,"Pair style ilp/graphene/hbn/gb300 requires an orthogonal box");
-  if (vflag_atom)
-    error->all(FLERR,"Pair style ilp/graphene/hbn/gb300 does not compute per-atom virials");
-
-  int nlocal = atom->nlocal;
-  int periodic[3] = {domain->xperiodic, domain->yperiodic, domain->zperiodic};
-  const bool big = sizeof(tagint) == 8;
   lmff_lammps::StyleOut out;
-  std::string err;
-  int rc = gb.compute(LMFF_ILP, nlocal, nlocal ? &atom->x[0][0] : NULL, atom->type,
-                      big ? NULL : (const int32_t *) atom->molecule,
-                      big ? (const int64_t *) atom->molecule : NULL,
-                      big ? NULL : (const int32_t *) atom->tag, big ? (const int64_t *) atom->tag : NULL,
-                      neighbor->ago == 0, domain->boxlo, domain->boxhi, periodic,
-                      nlocal ? &atom->f[0][0] : NULL, eflag_atom ? eatom : NULL,
-                      eflag, vflag, out, err);
-  if (rc != LMFF_OK) error->one(FLERR,(std::string("ilp/graphene/hbn/gb300: ") + err).c_str());
+  gb300::compute(lmp,this,this,1,eflag,vflag,eflag_atom,vflag_atom,"ilp/graphene/hbn/gb300",out);
   if (eflag_global) eng_vdwl += out.eng_vdwl;
   if (vflag_global)
     for (int k = 0; k < 6; k++) virial[k] += out.virial[k];

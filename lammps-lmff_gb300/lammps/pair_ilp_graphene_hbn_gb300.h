@@ -11,23 +11,21 @@ PairStyle(ilp/graphene/hbn/gb300,PairILPGrapheneHBNGB300)
 
 #else
 
-#ifndef LMP_PAIR_ILP_GRAPHENE_HBN_GB300_H
-#define LMP_PAIR_ILP_GRAPHENE_HBN_GB300_H
+#ifndef LMP_PAIRILPGRAPHENEHBNGB300_H
+#define LMP_PAIRILPGRAPHENEHBNGB300_H
 
 #include "pair_ilp_graphene_hbn.h"
-#include "lmff_lammps_adapter.h"
+#include "gb300_common.h"
 
 namespace LAMMPS_NS {
 
-class PairILPGrapheneHBNGB300 : public PairILPGrapheneHBN {
+class PairILPGrapheneHBNGB300 : public PairILPGrapheneHBN, public GB300Style {
  public:
   PairILPGrapheneHBNGB300(class LAMMPS *);
   virtual ~PairILPGrapheneHBNGB300() {}
   virtual void compute(int, int);
   void init_style();
-
- protected:
-  lmff_lammps::Adapter gb;
+  virtual void fill_params(lmff_lammps::StyleParams &);
 };
 
 }

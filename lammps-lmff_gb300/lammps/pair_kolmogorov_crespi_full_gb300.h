@@ -11,23 +11,21 @@ PairStyle(kolmogorov/crespi/full/gb300,PairKolmogorovCrespiFullGB300)
 
 #else
 
-#ifndef LMP_PAIR_KOLMOGOROV_CRESPI_FULL_GB300_H
-#define LMP_PAIR_KOLMOGOROV_CRESPI_FULL_GB300_H
+#ifndef LMP_PAIRKOLMOGOROVCRESPIFULLGB300_H
+#define LMP_PAIRKOLMOGOROVCRESPIFULLGB300_H
 
 #include "pair_kolmogorov_crespi_full.h"
-#include "lmff_lammps_adapter.h"
+#include "gb300_common.h"
 
 namespace LAMMPS_NS {
 
-class PairKolmogorovCrespiFullGB300 : public PairKolmogorovCrespiFull {
+class PairKolmogorovCrespiFullGB300 : public PairKolmogorovCrespiFull, public GB300Style {
  public:
   PairKolmogorovCrespiFullGB300(class LAMMPS *);
   virtual ~PairKolmogorovCrespiFullGB300() {}
   virtual void compute(int, int);
   void init_style();
-
- protected:
-  lmff_lammps::Adapter gb;
+  virtual void fill_params(lmff_lammps::StyleParams &);
 };
 
 }

@@ -5,12 +5,8 @@
 #include "pair_tersoff_gb300.h"
 
 #include <cstring>
-#include <string>
-#include <vector>
 
 #include "atom.h"
-#include "comm.h"
-#include "domain.h"
 #include "error.h"
 #include "force.h"
 #include "neighbor.h"
@@ -19,14 +15,14 @@ using namespace LAMMPS_NS;
 
 PairTersoffGB300::PairTersoffGB300(LAMMPS *lmp) : PairTersoff(lmp)
 {
-  // the engine returns each style's exact global virial; ghost forces stay zero, so
-  // a hybrid fdotr sum over owned+ghost atoms would be wrong (pair_hybrid.cpp:97-102)
+  // the engine returns each style's exact global virial (in the periodic form ghost
+  // forces stay zero), so no fdotr sum over owned+ghost atoms (pair_hybrid.cpp:97-102)
   no_virial_fdotr_compute = 1;
 }
 
 /* ----------------------------------------------------------------------
    same checks as PairTersoff::init_style (pair_tersoff.cpp:365-377), no neighbour
-   request (the engine builds its own lists), then the engine from the parameters
+   request (the engine builds its own lists), then the engine
 ------------------------------------------------------------------------- */
 
 void PairTersoffGB300::init_style()
@@ -35,11 +31,22 @@ void PairTersoffGB300::init_style()
     error->all(FLERR,"Pair style Tersoff requires atom IDs");
   if (force->newton_pair == 0)
     error->all(FLERR,"Pair style Tersoff requires newton pair on");
+  gb300::setup(lmp,this,this,0,"tersoff/gb300");
+}
 
-  std::vector<lmff_tersoff_param> tp(nparams);
+/* ----------------------------------------------------------------------
+   the parameters after coeff(): Param[] as read, elem2param[ne^3], type -> element
+------------------------------------------------------------------------- */
+
+void PairTersoffGB300::fill_params(lmff_lammps::StyleParams &sp)
+{
+  sp.ntypes = atom->ntypes;
+  sp.skin = neighbor->skin;
+  sp.tersoff = true;
+  sp.t_params.resize(nparams);
   for (int m = 0; m < nparams; m++) {
     const Param &q = params[m];
-    lmff_tersoff_param &o = tp[m];
+    lmff_tersoff_param &o = sp.t_params[m];
     memset(&o,0,sizeof(o));
     o.lam1 = q.lam1; o.lam2 = q.lam2; o.lam3 = q.lam3;
     o.c = q.c; o.d = q.d; o.h = q.h; o.gamma = q.gamma; o.powerm = q.powerm;
@@ -50,55 +57,26 @@ void PairTersoffGB300::init_style()
     o.powermint = q.powermint;
   }
   int ne = nelements;
-  std::vector<int> e2p(ne*ne*ne);
+  sp.t_nelements = ne;
+  sp.t_elem2param.resize(ne*ne*ne);
   for (int i = 0; i < ne; i++)
     for (int j = 0; j < ne; j++)
-      for (int k = 0; k < ne; k++) e2p[(i*ne+j)*ne+k] = elem2param[i][j][k];
-  std::vector<int> tmap(atom->ntypes+1);
-  for (int t = 0; t <= atom->ntypes; t++) tmap[t] = t ? map[t] : -1;
-
-  lmff_params p;
-  memset(&p,0,sizeof(p));
-  p.ntypes = atom->ntypes;
-  p.tersoff_nelements = ne;
-  p.tersoff_nparams = nparams;
-  p.tersoff_params = tp.data();
-  p.tersoff_elem2param = e2p.data();
-  p.tersoff_map = tmap.data();
-  p.tersoff_cutmax = cutmax;
-  p.skin = neighbor->skin;
-  std::string err;
-  if (gb.create(p,lmff_lammps::device_from_env(),lmff_lammps::precision_from_env(),err) != LMFF_OK)
-    error->all(FLERR,(std::string("tersoff/gb300: ") + err).c_str());
+      for (int k = 0; k < ne; k++) sp.t_elem2param[(i*ne+j)*ne+k] = elem2param[i][j][k];
+  sp.t_map.resize(atom->ntypes+1);
+  for (int t = 0; t <= atom->ntypes; t++) sp.t_map[t] = t ? map[t] : -1;
+  sp.t_cutmax = cutmax;
 }
 
 /* ----------------------------------------------------------------------
-   PairTersoff::compute replaced by one engine evaluation of the periodic system
+   PairTersoff::compute replaced by one engine evaluation (shared with the interlayer
+   gb300 style under hybrid/overlay)
 ------------------------------------------------------------------------- */
 
 void PairTersoffGB300::compute(int eflag, int vflag)
 {
   ev_init(eflag,vflag);
-  if (comm->nprocs > 1)
-    error->all(FLERR,"Pair style tersoff/gb300 evaluates the whole periodic system on one GPU: "
-               "run it on one MPI rank");
-  if (domain->triclinic)
-    error->all(FLERR,"Pair style tersoff/gb300 requires an orthogonal box");
-  if (vflag_atom)
-    error->all(FLERR,"Pair style tersoff/gb300 does not compute per-atom virials");
-
-  int nlocal = atom->nlocal;
-  int periodic[3] = {domain->xperiodic, domain->yperiodic, domain->zperiodic};
-  const bool big = sizeof(tagint) == 8;
   lmff_lammps::StyleOut out;
-  std::string err;
-  int rc = gb.compute(LMFF_TERSOFF, nlocal, nlocal ? &atom->x[0][0] : NULL, atom->type,
-                      NULL, NULL,
-                      big ? NULL : (const int32_t *) atom->tag, big ? (const int64_t *) atom->tag : NULL,
-                      neighbor->ago == 0, domain->boxlo, domain->boxhi, periodic,
-                      nlocal ? &atom->f[0][0] : NULL, eflag_atom ? eatom : NULL,
-                      eflag, vflag, out, err);
-  if (rc != LMFF_OK) error->one(FLERR,(std::string("tersoff/gb300: ") + err).c_str());
+  gb300::compute(lmp,this,this,0,eflag,vflag,eflag_atom,vflag_atom,"tersoff/gb300",out);
   if (eflag_global) eng_vdwl += out.eng_vdwl;
   if (vflag_global)
     for (int k = 0; k < 6; k++) virial[k] += out.virial[k];

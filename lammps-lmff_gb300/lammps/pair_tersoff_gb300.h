@@ -15,19 +15,17 @@ PairStyle(tersoff/gb300,PairTersoffGB300)
 #define LMP_PAIR_TERSOFF_GB300_H
 
 #include "pair_tersoff.h"
-#include "lmff_lammps_adapter.h"
+#include "gb300_common.h"
 
 namespace LAMMPS_NS {
 
-class PairTersoffGB300 : public PairTersoff {
+class PairTersoffGB300 : public PairTersoff, public GB300Style {
  public:
   PairTersoffGB300(class LAMMPS *);
   virtual ~PairTersoffGB300() {}
   virtual void compute(int, int);
   virtual void init_style();
-
- protected:
-  lmff_lammps::Adapter gb;
+  virtual void fill_params(lmff_lammps::StyleParams &);
 };
 
 }

@@ -91,7 +91,8 @@ GEN2 := $(OUT)/gen_gb300
 OBJ2 := $(OUT)/obj_gb300
 LIBDIR := lammps-lmff_gb300/lmff_gb300
 PKG_SRC := $(PKGDIR)/pair_tersoff_gb300.cpp $(PKGDIR)/pair_ilp_graphene_hbn_gb300.cpp \
-           $(PKGDIR)/pair_kolmogorov_crespi_full_gb300.cpp $(PKGDIR)/lmff_lammps_adapter.cpp
+           $(PKGDIR)/pair_kolmogorov_crespi_full_gb300.cpp $(PKGDIR)/lmff_lammps_adapter.cpp \
+           $(PKGDIR)/gb300_common.cpp
 CXXFLAGS2 := -O2 -std=c++11 -w -ffp-contract=off -DLAMMPS_MEMALIGN=64 -DLAMMPS_SMALLBIG \
              -I$(GEN2) -I$(GEN) -I$(SRC) -I$(SRC)/STUBS -I$(SRC)/MOLECULE -I$(SRC)/MANYBODY -I$(SRC)/USER-MISC \
              -I$(PKGDIR) -Iinclude

@@ -1072,7 +1072,7 @@ struct Engine {
       sys_geometry(sd, lo, L, per, cutneigh_max, R);
       sd.bin_begin = bin_begin;
       long long nbins = (long long)sd.nb[0] * sd.nb[1] * sd.nb[2];
-      if (bin_begin + nbins > (1LL << 30)) return fail(LMFF_EOVERFLOW, "too many bins");
+      if (bin_begin + nbins > MAX_GLOBAL_BINS) return fail(LMFF_EOVERFLOW, "too many bins");
       bin_begin += (int)nbins;
       out.push_back(sd);
     }

@@ -44,7 +44,9 @@ __global__ void k_wrap_bin(int n, d4 *xq, const SysDesc *sys, const int *sysid, 
     b[d] = bin_coord(c[d], sd.lo[d], sd.binv[d], sd.nb[d]);
   }
   xq[p] = make_d4(c[0], c[1], c[2], q.w);
-  key[p] = (uint32_t)(sd.bin_begin + (b[2] * sd.nb[1] + b[1]) * sd.nb[0] + b[0]);
+  const uint32_t bin = (uint32_t)(sd.bin_begin + (b[2] * sd.nb[1] + b[1]) * sd.nb[0] + b[0]);
+  const uint32_t molbits = (uint32_t)(__double_as_longlong(q.w) >> 8) & ((1u << KEY_MOL_BITS) - 1u);
+  key[p] = (bin << KEY_MOL_BITS) | molbits;
   idx[p] = p;
 }
 
@@ -71,15 +73,15 @@ __global__ void k_bin_ranges(int n, const uint32_t *key, int *bin_start, int *bi
                              const int *sysid, int *rowocc) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
-  uint32_t k = key[q];
-  if (q == 0 || key[q - 1] != k) {
+  const uint32_t k = key[q] >> KEY_MOL_BITS;
+  if (q == 0 || (key[q - 1] >> KEY_MOL_BITS) != k) {
     bin_start[k] = q;
     if (rowocc) {
       const SysDesc &sd = sys[sysid[q]];
       rowocc[k - (uint32_t)((int)k - sd.bin_begin) % (uint32_t)sd.nb[0]] = 1;
     }
   }
-  if (q == n - 1 || key[q + 1] != k) bin_end[k] = q + 1;
+  if (q == n - 1 || (key[q + 1] >> KEY_MOL_BITS) != k) bin_end[k] = q + 1;
 }
 
 // double-float split of each position: X = x - lo + 32 + base lies in [base, 2 base) for
@@ -152,7 +154,7 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
   if (act) {
     sys = a.sysid[i];
     const SysDesc &sd = a.sys[sys];
-    const int lb = (int)a.bin_key[i] - sd.bin_begin;
+    const int lb = (int)(a.bin_key[i] >> KEY_MOL_BITS) - sd.bin_begin;
     bx = lb % sd.nb[0];
     by = (lb / sd.nb[0]) % sd.nb[1];
     bz = lb / (sd.nb[0] * sd.nb[1]);
@@ -207,12 +209,28 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
           const float shx = (float)sx * sd.Lhi[0], shy = (float)sy * sd.Lhi[1], shz = (float)sz * sd.Lhi[2];
           const float slx = (float)sx * sd.Llo[0], sly = (float)sy * sd.Llo[1], slz = (float)sz * sd.Llo[2];
           const bool self_image = (sx | sy | sz) == 0;
-          for (int jt0 = jstart; jt0 < jend; jt0 += 32) {
-            const int nj = min(32, jend - jt0);
+          // a tile whose candidates all share the molecule of every lane using this bin
+          // holds no interlayer partner; beyond the adjacent bins it holds no short-list
+          // candidate either (the short cutoff is below the bin size), so it is passed over
+          const bool far_bin = !use || dz > 1 || dz < -1 || dy > 1 || dy < -1 || xu > bx + 1 || xu < bx - 1;
+          const bool may_skip = !a.full && (MODE == 1 || __all_sync(FULL, far_bin));
+          for (int jt0 = jstart, nj = 0; jt0 < jend; jt0 += nj) {
+            nj = min(32, jend - jt0);
             __syncwarp();
+            float4 hl = make_float4(0.f, 0.f, 0.f, 0.f);
             if (lane < nj) {
-              th[wl][lane] = a.xh[jt0 + lane];
+              hl = a.xh[jt0 + lane];
+              th[wl][lane] = hl;
               tl[wl][lane] = a.xl[jt0 + lane];
+            }
+            if (may_skip) {
+              // the tile ends where the bin's run of its first candidate's molecule ends
+              // (atoms are sorted by molecule within a bin)
+              const int mt = __float_as_int(hl.w) >> 8;
+              const int m0 = __shfl_sync(FULL, mt, 0);
+              const unsigned chg = __ballot_sync(FULL, lane < nj && mt != m0);
+              if (chg) nj = __ffs(chg) - 1;
+              if (__all_sync(FULL, !use || m0 == mi)) continue;
             }
             __syncwarp();
             if (!use) continue;
@@ -327,9 +345,10 @@ size_t nb_sort_tmp_bytes(int n, int nbits) {
   return a > b ? a : b;
 }
 
+// nbits: bits of the global bin index; the key's molecule bits come below them
 cudaError_t nb_sort(void *tmp, size_t tmp_bytes, const uint32_t *k, uint32_t *k2, const int *v, int *v2, int n, int nbits,
                     cudaStream_t s) {
-  return cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, k, k2, v, v2, n, 0, nbits, s);
+  return cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, k, k2, v, v2, n, 0, nbits + KEY_MOL_BITS, s);
 }
 
 cudaError_t nb_scan(void *tmp, size_t tmp_bytes, const int64_t *cnt, int64_t *off, int n, cudaStream_t s) {

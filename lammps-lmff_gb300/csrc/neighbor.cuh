@@ -5,6 +5,13 @@
 
 namespace lmff {
 
+// Sort key of an atom: its global bin above KEY_MOL_BITS low bits of its molecule id, so
+// that within a bin the atoms of one molecule (layer) are contiguous and the list build
+// can pass over whole tiles of same-molecule candidates (never interlayer partners).
+// Equal low bits of different molecules only make fewer tiles skippable.
+constexpr int KEY_MOL_BITS = 4;
+constexpr int64_t MAX_GLOBAL_BINS = 1LL << (32 - KEY_MOL_BITS);
+
 // per type-pair cutoffs of the pair list and the short-candidate cutoff
 struct NbConst {
   float cutnsq_f[(MAXTYPE + 1) * (MAXTYPE + 1)];
@@ -26,7 +33,7 @@ struct NbArgs {
   const int *bin_end;
   const int *rowocc;  // 1 at the first bin of every bin row (fixed y, z) holding atoms, or null
   int nbins;          // global bins
-  const uint32_t *bin_key;   // global bin of each atom (sorted order)
+  const uint32_t *bin_key;   // sort key of each atom (sorted order): global bin << KEY_MOL_BITS | mol bits
   const int64_t *list_off;
   uint32_t *list;
   int64_t list_cap;

@@ -1375,19 +1375,42 @@ struct Engine {
     cudaEventCreate(&e1);
     cudaEventRecord(e0, stream);
     if (n > 0) {
-      if (precision == LMFF_FP64) {
-        run_kernels(args<double>(), which, ev, eatom, f64::launch_short, f64::launch_tersoff, f64::launch_ilp,
-                    f64::launch_nderiv, f64::launch_finish);
+      if (precision == LMFF_MIXED && !hilo_fresh) hilo_all();
+      const bool cap = use_graphs && !ktiming && !kick_on;
+      std::vector<unsigned char> key;
+      if (cap) {
+        if (ters_concurrent && ensure_stream2() != LMFF_OK) return LMFF_ECUDA;   // before any capture
+        key = force_key(which, ev, eatom);
+      }
+      if (cap && fexec && key == fkey) {
+        CK(cudaGraphLaunch(fexec, stream));
       } else {
-        if (!hilo_fresh) hilo_all();
-        run_kernels(args<float>(), which, ev, eatom, f32::launch_short, f32::launch_tersoff, f32::launch_ilp,
-                    f32::launch_nderiv, f32::launch_finish);
+        if (cap) {
+          drop_fgraph();
+          CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        }
+        if (precision == LMFF_FP64) {
+          run_kernels(args<double>(), which, ev, eatom, f64::launch_short, f64::launch_tersoff, f64::launch_ilp,
+                      f64::launch_nderiv, f64::launch_finish);
+        } else {
+          run_kernels(args<float>(), which, ev, eatom, f32::launch_short, f32::launch_tersoff, f32::launch_ilp,
+                      f32::launch_nderiv, f32::launch_finish);
+        }
+        if (ev) k_reduce<<<(int)hsys.size() * 16, 256, 0, stream>>>(n, 16, (const double *const *)d_arrs, d.sys, d.red_out);
+        if (cap) {
+          cudaGraph_t g = nullptr;
+          cudaError_t e = cudaStreamEndCapture(stream, &g);
+          if (e == cudaSuccess) e = cudaGraphInstantiate(&fexec, g, 0);
+          if (g) cudaGraphDestroy(g);
+          if (e != cudaSuccess) {
+            fexec = nullptr;
+            return fail(LMFF_ECUDA, std::string("force graph: ") + cudaGetErrorString(e));
+          }
+          fkey = key;
+          CK(cudaGraphLaunch(fexec, stream));
+        }
       }
       CK(cudaGetLastError());
-      if (ev) {
-        k_reduce<<<(int)hsys.size() * 16, 256, 0, stream>>>(n, 16, (const double *const *)d_arrs, d.sys, d.red_out);
-        CK(cudaGetLastError());
-      }
     }
     cudaEventRecord(e1, stream);
     int st = 0;
@@ -1736,6 +1759,33 @@ struct Engine {
   void drop_graph() {
     if (step_exec) cudaGraphExecDestroy(step_exec);
     step_exec = nullptr;
+    drop_fgraph();
+  }
+
+  // One force evaluation's device work (the kernels of run_kernels and the reduction)
+  // as a CUDA graph, replayed while its arguments and launch shapes stay the same:
+  // repeated single points, batch re-evaluations, the LAMMPS styles' per-step calls.
+  cudaGraphExec_t fexec = nullptr;
+  std::vector<unsigned char> fkey;
+  void drop_fgraph() {
+    if (fexec) cudaGraphExecDestroy(fexec);
+    fexec = nullptr;
+    fkey.clear();
+  }
+  template <class T>
+  static void key_put(std::vector<unsigned char> &k, const T &v) {
+    const unsigned char *b = reinterpret_cast<const unsigned char *>(&v);
+    k.insert(k.end(), b, b + sizeof(T));
+  }
+  std::vector<unsigned char> force_key(int which, bool ev, bool eatom) {
+    std::vector<unsigned char> k;
+    if (precision == LMFF_FP64) key_put(k, args<double>());
+    else key_put(k, args<float>());
+    const int ints[] = {precision, which, (int)ev, (int)eatom, tpa, block, (int)ters_concurrent, (int)hsys.size()};
+    key_put(k, ints);
+    const void *ptrs[] = {d_arrs, d.sys, d.red_out, stat_ilp, stat_ters, eatom_ters};
+    key_put(k, ptrs);
+    return k;
   }
 
   // NVE steps: the gather kernel applies the second half-kick (k_nve2's arithmetic)

@@ -283,14 +283,15 @@ def bench_replicas(args, local: int) -> dict:
     each displaced by N(0, 0.02 A): energies, forces and virial of every replica.
     Batched = one launch per kernel over all replicas (lmff_batch_set +
     lmff_batch_compute: host arrays in, forces and per-replica energies/virials out).
-    Baseline = the same evaluations one replica at a time through lmff_compute."""
+    Baseline = the same evaluations one replica at a time through lmff_compute.  Single
+    points reuse no list, so both build theirs without a skin (skin 0)."""
     from lmff_gb300 import capi
     from lmff_gb300 import structures as S
     systems = [S.displace(s, 0.02, seed=k) for k, s in enumerate(S.replica_set(256, 500, 20000, seed=4))]
     ntot = sum(s.n for s in systems)
     out = {}
     for name, prec in (("mixed", capi.MIXED), ("fp64", capi.FP64)):
-        eng = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=prec)
+        eng = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=prec, skin=0.0)
         eng.batch_set(systems)
         eng.batch_compute()
 
@@ -304,7 +305,7 @@ def bench_replicas(args, local: int) -> dict:
         st = eng.stats()
         # device-resident re-evaluation of the loaded batch (no host copies, no rebuild)
         t_r = _sync_wall(lambda: eng.compute_resident(eflag=True, vflag=True), max(3, args.steps // 4))
-        seq = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=prec)
+        seq = capi.Engine(TERSOFF_FILE, ILP_FILE, device=local, precision=prec, skin=0.0)
         for s_ in systems[:8]:
             seq.compute_system(s_)
         t0 = time.perf_counter()
@@ -320,7 +321,7 @@ def bench_replicas(args, local: int) -> dict:
     return {"metric": "replica evaluations/s (E+F+W), 256 bilayer replicas", "value": value,
             "unit": "replicas/s", "n_gpus": 1, "higher_is_better": True, "data": "synthetic",
             "dtype": "f32", "config": {"workload": "256 bilayer replicas, 500-20000 atoms log-uniform",
-                                       "atoms_total": ntot, "precision": "mixed"},
+                                       "atoms_total": ntot, "precision": "mixed", "skin": 0.0},
             "batched_mixed_vs_one_at_a_time_fp64": value / out["fp64"]["one_at_a_time_replicas_per_s"],
             "atom_evals_per_s_batched_mixed": ntot / out["mixed"]["batched_s"],
             "atom_evals_per_s_resident_mixed": ntot / out["mixed"]["resident_s"],
@@ -398,6 +399,8 @@ def main():
     ap.add_argument("--tpa", type=int, default=0, help="threads per atom (0: autotune)")
     ap.add_argument("--block", type=int, default=0, help="threads per block (0: autotune)")
     ap.add_argument("--skin", type=float, default=0.0, help="neighbour skin in A (0: autotune)")
+    ap.add_argument("--tile", type=int, default=0, help="pair-loop tile, list entries per lane and iteration "
+                                                         "(1 or 2; 0: autotune)")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
@@ -452,7 +455,7 @@ def main():
     # pure carbon: one atom type mapped to C (pair_coeff * * <style> <file> C)
     elements = ("C",) if set(np.unique(s.type)) == {1} else ("C", "B", "N")
     tuned = None
-    if not (args.tpa and args.block and args.skin):
+    if not (args.tpa and args.block and args.skin and args.tile):
         from lmff_gb300 import tune
         # tuned on the workload itself: a smaller patch of the same slab ranks the launch
         # shapes differently (measured: 16 threads per atom best at 331k, 8 at 2.7M)
@@ -460,12 +463,13 @@ def main():
         # thread's walk over its share of the list
         tuned = tune.tune(s, TERSOFF_FILE, ILP_FILE, elements=elements, precision=prec, device=local,
                           tpas=(8, 16, 32) if s.n < 100_000 else (8, 16), blocks=(128, 256), skins=(1.0, 2.0),
-                          use_cache=False, n_full=s.n)
+                          use_cache=False, n_full=s.n, tiles=(2, 1))
         args.tpa = args.tpa or tuned["tpa"]
         args.block = args.block or tuned["block"]
         args.skin = args.skin or tuned["skin"]
+        args.tile = args.tile or tuned.get("tile", 2)
     m = run_md(s, prec, elements, local, args.tpa, args.block, args.skin, args.warmup, args.steps,
-               args.kernel_steps, dist, clocks=True)
+               args.kernel_steps, dist, clocks=True, tile=args.tile)
     value = replica_throughput(world, s.n, args.steps, m["tmax"])
     ms_per_step = m["tmax"] / args.steps * 1e3
     launches_total = sum(m["launches_per_step"].values()) * args.steps
@@ -510,9 +514,10 @@ def main():
                 "config": {"workload": "10-layer AB graphite slab, 2,694,960 atoms, 300 K NVE dt 1 fs"
                            if args.workload == "graphite_2p7m" else args.workload,
                            "natoms": s.n, "precision": args.precision, "tpa": args.tpa, "block": args.block,
-                           "skin": args.skin, "elements": list(elements),
+                           "skin": args.skin, "pair_tile": args.tile, "elements": list(elements),
                            "autotune": None if tuned is None else {
-                               "probe_atoms": tuned["probe_atoms"], "picked": [tuned["tpa"], tuned["block"], tuned["skin"]],
+                               "probe_atoms": tuned["probe_atoms"],
+                               "picked": [tuned["tpa"], tuned["block"], tuned["skin"], tuned.get("tile", 2)],
                                "score_ms_probe": tuned["score_ms"]},
                            "l2": l2_note,
                            "parallelism": f"replicas x{world}", "wall_s": m["wall"]},
@@ -530,7 +535,8 @@ def main():
         dist.destroy_process_group()
 
 
-def run_md(s, prec, elements, local, tpa, block, skin, warmup, steps, kernel_steps, dist=None, clocks=False):
+def run_md(s, prec, elements, local, tpa, block, skin, warmup, steps, kernel_steps, dist=None, clocks=False,
+           tile=2):
     """Device-resident NVE of system s: `warmup` untimed steps, `steps` timed steps (the
     production loop: steps replayed as CUDA graphs, device time from CUDA events on the
     engine's stream), then a host-driven run of max(steps, kernel_steps) steps with CUDA
@@ -542,6 +548,7 @@ def run_md(s, prec, elements, local, tpa, block, skin, warmup, steps, kernel_ste
     eng.set_option("tpa", tpa)
     eng.set_option("block", block)
     eng.set_option("skin", skin)
+    eng.set_option("pair_tile", tile)
     eng.upload(s)
     eng.run_nve(warmup, 0.001)
     eng.set_option("count_pairs", 1)
@@ -643,6 +650,7 @@ def bench_e2e(s, prec, elements, local, args, world) -> dict:
     eng2.set_option("tpa", args.tpa)
     eng2.set_option("block", args.block)
     eng2.set_option("skin", args.skin)
+    eng2.set_option("pair_tile", args.tile)
     eng2.set_box(s.box_lo, s.box_hi, s.periodic)
     eng2.compute(xa, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb, overwrite=True)
     eng2.compute(xb, s.type, s.mol, s.tag, eflag=False, vflag=False, f=fb, overwrite=True, same_atoms=True)

@@ -218,7 +218,9 @@ int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double 
  * list there, so it equals the uninterrupted run up to summation order).
  * "ters_concurrent" 1 (default) = the Tersoff kernel runs on a second stream beside
  * the interlayer pair kernel (they write disjoint arrays; joined before the gather);
- * 0 = one after the other. */
+ * 0 = one after the other.  "pair_tile" 2 (default) = the mixed force-only pair kernel
+ * takes two list entries per lane and iteration (FP32x2 lanes across the pair), 1 = one
+ * entry (the neighbour-tile shape the tuner chooses). */
 int lmff_set_option(lmff_engine *e, const char *key, double value);
 
 /* ---- one-shot evaluation on host buffers (the pair-style drop-in) ------------------ */

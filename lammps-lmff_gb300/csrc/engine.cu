@@ -455,6 +455,7 @@ struct Engine {
   // subdomain mode (lmff_compute_ghost): the number of owned atoms among the caller's
   // nall (owned first, then ghosts); -1 for the ordinary periodic-system mode
   int ghost_nlocal = -1;
+  int pair_tile = 2;   // option "pair_tile": list entries per pair-loop iteration (1 or 2)
   double skin = 2.0;
   int ntypes = 0;
   HostTersoff ht;
@@ -1327,6 +1328,7 @@ struct Engine {
     a.list_full = list_full;
     a.own_perm = ghost_nlocal >= 0 ? d.perm : nullptr;
     a.nown = ghost_nlocal;
+    a.pair_tile = pair_tile;
     a.kc = i_on && hi.model == LMFF_INTERLAYER_KC;
     return a;
   }
@@ -2927,6 +2929,11 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
     e->e.skin = value;
     e->e.build_consts();
     e->e.loaded = false;
+  } else if (k == "pair_tile") {
+    const int v = (int)value;
+    if (v != 1 && v != 2) return e->e.fail(LMFF_EINVAL, "pair_tile must be 1 or 2");
+    e->e.pair_tile = v;
+    e->e.drop_graph();
   } else if (k == "ters_concurrent") {
     e->e.ters_concurrent = value != 0.0;
     e->e.drop_graph();

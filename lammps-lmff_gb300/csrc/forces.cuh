@@ -252,6 +252,9 @@ struct ForceArgs {
   // included, receives its share of their forces.
   const int *own_perm;
   int nown;
+  // list entries a lane of the mixed force-only pair kernel takes per loop iteration:
+  // 2 (the two-entry loop, where it applies) or 1 (the one-entry loop); a tuning knob
+  int pair_tile;
   int kc;              // interlayer style is kolmogorov/crespi/full
 };
 

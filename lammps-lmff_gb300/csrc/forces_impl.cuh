@@ -1893,7 +1893,7 @@ static void launch_ilp_t(const ForceArgs<R> &a, bool ev, bool eatom, int block, 
   }
   if (ev && eatom) k_ilp<TPA, true, true, ONE, false, false, false><<<g, block, 0, s>>>(a);
   else if (ev) k_ilp<TPA, true, false, ONE, false, false, false><<<g, block, 0, s>>>(a);
-  else if (TWO_PAIR_BODY && !a.list_full && (ONE ? h_two_one : h_two_multi))
+  else if (TWO_PAIR_BODY && !a.list_full && a.pair_tile != 1 && (ONE ? h_two_one : h_two_multi))
     k_ilp<TPA, false, false, ONE, false, false, TWO_PAIR_BODY><<<g, block, 0, s>>>(a);
   else k_ilp<TPA, false, false, ONE, false, false, false><<<g, block, 0, s>>>(a);
 }

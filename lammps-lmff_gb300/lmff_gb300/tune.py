@@ -1,7 +1,8 @@
 """Launch-shape autotuner for the pair kernel and the neighbour list.
 
-Picks threads per atom (4, 8, 16, 32), threads per block (128, 256) and the neighbour
-skin (1.0, 1.5, 2.0 A) by timing short device-resident NVE runs of a representative
+Picks threads per atom (4, 8, 16, 32), threads per block (128, 256), the pair-kernel
+tile (list entries a lane takes per iteration: 1, or 2 packed in FP32x2 lanes) and the
+neighbour skin (1.0, 1.5, 2.0 A) by timing short device-resident NVE runs of a representative
 system with per-kernel CUDA-event timing on the engine's stream.  The score of a
 candidate is the device time of one step plus the amortised cost of a list rebuild
 (rebuild time / expected steps between rebuilds, estimated from the largest
@@ -62,7 +63,7 @@ def save_cache(c: Dict) -> None:
 def tune(system, tersoff_file: str, ilp_file: str, elements=("C", "B", "N"), precision: int = capi.MIXED,
          device: int = 0, tpas: Iterable[int] = (8, 16, 32), blocks: Iterable[int] = (128, 256),
          skins: Iterable[float] = (1.0, 1.5, 2.0), steps: int = 4, use_cache: bool = True,
-         n_full: Optional[int] = None) -> Dict:
+         n_full: Optional[int] = None, tiles: Iterable[int] = (2, 1)) -> Dict:
     """Time the candidates on `system` and return the best {"tpa", "block", "skin", ...}.
     `n_full` (the production system size) selects the cache bucket when `system` is a
     smaller stand-in with the same density."""
@@ -76,34 +77,38 @@ def tune(system, tersoff_file: str, ilp_file: str, elements=("C", "B", "N"), pre
     for skin in skins:
         for tpa in tpas:
             for block in blocks:
-                eng = capi.Engine(tersoff_file, ilp_file, elements=elements, precision=precision, skin=skin,
-                                  device=device)
-                eng.set_option("tpa", tpa)
-                eng.set_option("block", block)
-                eng.upload(system)
-                eng.run_nve(2, 0.001)
-                eng.set_option("kernel_timing", 1)
-                eng.set_option("reset_timing", 1)
-                x0, _, _ = eng.download()
-                eng.run_nve(steps, 0.001)
-                x1, _, _ = eng.download()
-                st = eng.stats()
-                step_ms = st["ms_last_run"] / steps
-                # amortised rebuild: steps until the fastest atom moves skin/2 at the probe's rate
-                L = system.box_hi - system.box_lo
-                d = x1 - x0
-                for c in range(3):
-                    if system.periodic[c]:
-                        d[:, c] -= L[c] * np.rint(d[:, c] / L[c])
-                vmax = float(np.sqrt((d * d).sum(1)).max()) / steps
-                steps_between = (0.5 * skin / vmax) if vmax > 0 else 1e9
-                build_ms = st["ms_last_build"]
-                score = step_ms + build_ms / max(steps_between, 1.0)
-                results.append({"tpa": tpa, "block": block, "skin": skin, "step_ms": step_ms, "build_ms": build_ms,
-                                "steps_between_rebuilds": steps_between, "score_ms": score})
-                eng.close()
+                for tile in (tiles if precision == capi.MIXED else (2,)):
+                    eng = capi.Engine(tersoff_file, ilp_file, elements=elements, precision=precision, skin=skin,
+                                      device=device)
+                    eng.set_option("tpa", tpa)
+                    eng.set_option("block", block)
+                    eng.set_option("pair_tile", tile)
+                    eng.upload(system)
+                    eng.run_nve(2, 0.001)
+                    eng.set_option("kernel_timing", 1)
+                    eng.set_option("reset_timing", 1)
+                    x0, _, _ = eng.download()
+                    eng.run_nve(steps, 0.001)
+                    x1, _, _ = eng.download()
+                    st = eng.stats()
+                    step_ms = st["ms_last_run"] / steps
+                    # amortised rebuild: steps until the fastest atom moves skin/2 at the probe's rate
+                    L = system.box_hi - system.box_lo
+                    d = x1 - x0
+                    for c in range(3):
+                        if system.periodic[c]:
+                            d[:, c] -= L[c] * np.rint(d[:, c] / L[c])
+                    vmax = float(np.sqrt((d * d).sum(1)).max()) / steps
+                    steps_between = (0.5 * skin / vmax) if vmax > 0 else 1e9
+                    build_ms = st["ms_last_build"]
+                    score = step_ms + build_ms / max(steps_between, 1.0)
+                    results.append({"tpa": tpa, "block": block, "skin": skin, "tile": tile, "step_ms": step_ms,
+                                    "build_ms": build_ms,
+                                    "steps_between_rebuilds": steps_between, "score_ms": score})
+                    eng.close()
     best = min(results, key=lambda r: r["score_ms"])
-    out = {"tpa": best["tpa"], "block": best["block"], "skin": best["skin"], "score_ms": best["score_ms"],
+    out = {"tpa": best["tpa"], "block": best["block"], "skin": best["skin"], "tile": best["tile"],
+           "score_ms": best["score_ms"],
            "probe_atoms": system.n, "key": key, "candidates": results, "when": time.time()}
     if use_cache:
         cache[key] = {k: v for k, v in out.items() if k != "candidates"}

@@ -220,7 +220,15 @@ int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double 
  * the interlayer pair kernel (they write disjoint arrays; joined before the gather);
  * 0 = one after the other.  "pair_tile" 2 (default) = the mixed force-only pair kernel
  * takes two list entries per lane and iteration (FP32x2 lanes across the pair), 1 = one
- * entry (the neighbour-tile shape the tuner chooses). */
+ * entry (the neighbour-tile shape the tuner chooses).  "check_every" = how often
+ * lmff_run_nve tests the pair list: 1 = every step, for displacement alone (LAMMPS's
+ * neigh_modify every 1 delay 0 check yes); k > 1 = at steps whose index is a multiple
+ * of k, rebuilding when an atom may move more than skin/2 before the next test (its
+ * displacement plus a look-ahead from its velocity and force); a step between tests
+ * that finds an atom past skin/2 rebuilds at once (the step graphs redo their chunk on
+ * the host-driven loop).  0 (default) = 1 above 65,536 atoms, else the largest of 8, 4,
+ * 2 whose look-ahead from the run's starting motion stays within skin/4.  Forces do
+ * not depend on when the list is rebuilt, only the order of some sums does. */
 int lmff_set_option(lmff_engine *e, const char *key, double value);
 
 /* ---- one-shot evaluation on host buffers (the pair-style drop-in) ------------------ */

@@ -210,25 +210,47 @@ struct DtfmTab {
   double v[MAXTYPE + 1];
 };
 
+// The rebuild test of a step when the list is checked only every k-th step (small
+// systems, where a step costs a few tens of microseconds and the test's conditional graph
+// node a sizeable part of it).  A check step looks ahead: it rebuilds when any atom may
+// move more than skin/2 from its position at the last build before the next check,
+// taking the reach as d + hv |v| + ha dtfm |f| (d: displacement so far; the velocity and
+// acceleration terms of k-1 steps with a 25 % margin) into *pred.  A step between checks
+// raises ST_SKIN_TRIP into *status when an atom did move more than skin/2 (the list may
+// then miss a pair: the host redoes the chunk with a test at every step of it).
+struct Lookahead {
+  unsigned long long *pred;
+  double hv, ha;
+  int *status;
+  double trig2;
+};
+
 // velocity Verlet halves (fix_nve.cpp:64-111); the first also moves x, refreshes the
 // double-float split and tracks the displacement since the last build
 __global__ void k_nve1(int n, d4 *xq, double *v, const double *f, DtfmTab tab, double dtv,
                        const double *xhold, unsigned long long *maxdisp, const SysDesc *sys, const int *sysid,
                        float4 *xh, float4 *xl, int do_hilo, cudaGraphConditionalHandle h = 0, double trig2 = 0.0,
-                       unsigned *ticket = nullptr) {
+                       unsigned *ticket = nullptr, Lookahead la = Lookahead{}) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
-  double d2 = 0.0;
+  double d2 = 0.0, p2 = 0.0;
   if (q < n) {
     d4 w = xq[q];
     double dtfm = tab.v[__double_as_longlong(w.w) & 255];
-    double vx = v[q] + dtfm * f[q];
-    double vy = v[n + q] + dtfm * f[n + q];
-    double vz = v[2 * n + q] + dtfm * f[2 * n + q];
+    const double fx = f[q], fy = f[n + q], fz = f[2 * n + q];
+    double vx = v[q] + dtfm * fx;
+    double vy = v[n + q] + dtfm * fy;
+    double vz = v[2 * n + q] + dtfm * fz;
     v[q] = vx; v[n + q] = vy; v[2 * n + q] = vz;
     double x = w.x + dtv * vx, y = w.y + dtv * vy, z = w.z + dtv * vz;
     xq[q] = make_d4(x, y, z, w.w);
     double dx = x - xhold[3 * q], dy = y - xhold[3 * q + 1], dz = z - xhold[3 * q + 2];
     d2 = dx * dx + dy * dy + dz * dz;
+    if (la.pred) {
+      const double p = sqrt(d2) + la.hv * sqrt(vx * vx + vy * vy + vz * vz) +
+                       la.ha * fabs(dtfm) * sqrt(fx * fx + fy * fy + fz * fz);
+      p2 = p * p;
+    }
+    if (la.status && d2 > la.trig2) atomicOr(la.status, ST_SKIN_TRIP);
     if (do_hilo) {
       const SysDesc &sd = sys[sysid[q]];
       double X = x - sd.lo[0] + 32.0 + sd.base;
@@ -241,9 +263,14 @@ __global__ void k_nve1(int n, d4 *xq, double *v, const double *f, DtfmTab tab, d
     }
   }
   block_max_disp(d2, maxdisp);
+  if (la.pred) {
+    __syncthreads();   // block_max_disp's shared words are reused
+    block_max_disp(p2, la.pred);
+  }
   if (ticket) {
     // in the step graph: the last block to finish sets the rebuild condition, any atom
-    // moved more than skin/2 since the last build (neighbor.cpp:1947-1976 check_distance)
+    // moved more than skin/2 since the last build (neighbor.cpp:1947-1976 check_distance),
+    // or may before the next check
     __shared__ bool last;
     if (threadIdx.x == 0) {
       __threadfence();
@@ -252,7 +279,8 @@ __global__ void k_nve1(int n, d4 *xq, double *v, const double *f, DtfmTab tab, d
     __syncthreads();
     if (last && threadIdx.x == 0) {
       *ticket = 0;
-      const double dmax = __longlong_as_double((long long)atomicMax(maxdisp, 0ull));
+      double dmax = __longlong_as_double((long long)atomicMax(maxdisp, 0ull));
+      if (la.pred) dmax = fmax(dmax, __longlong_as_double((long long)atomicExch(la.pred, 0ull)));
       cudaGraphSetConditional(h, dmax > trig2 ? 1u : 0u);
     }
   }
@@ -268,6 +296,22 @@ __global__ void k_nve2(int n, double *v, const double *f, const d4 *xq, const do
   double vz = v[2 * n + q] + dtfm * f[2 * n + q];
   v[q] = vx; v[n + q] = vy; v[2 * n + q] = vz;
   if (ke) ke[q] = 0.5 * MVV2E * mass[q] * (vx * vx + vy * vy + vz * vz);
+}
+
+// largest |v| and dtfm |f| over the atoms (squared, into out[0], out[1]): the motion
+// bound the look-ahead rebuild test sizes its check interval with
+__global__ void k_motion_max(int n, const double *v, const double *f, const d4 *xq, DtfmTab tab,
+                             unsigned long long *out) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  double v2 = 0.0, a2 = 0.0;
+  if (q < n) {
+    const double dtfm = tab.v[__double_as_longlong(xq[q].w) & 255];
+    v2 = v[q] * v[q] + v[n + q] * v[n + q] + v[2 * n + q] * v[2 * n + q];
+    a2 = dtfm * dtfm * (f[q] * f[q] + f[n + q] * f[n + q] + f[2 * n + q] * f[2 * n + q]);
+  }
+  block_max_disp(v2, out);
+  __syncthreads();
+  block_max_disp(a2, out + 1);
 }
 
 // ---------------------------------------------------------------- minimiser kernels
@@ -589,7 +633,7 @@ struct Engine {
                     d.short_cnt, d.short_nb, d.list_img, d.nin_tmp, d.list_tmp, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.rowocc, d.cub_tmp,
                     d.cnt_tmp, d.sys, d.red_out, d.status, d.maxdisp, d_xin, d_fin, d_vin, d_ein, d_tin, d_sysin,
                     d_min, d_gin, d_massT, xq2, v2, mass2, tag2, perm2, sysid2, stat_ilp, stat_ters, eatom_ilp,
-                    eatom_ters, ke, d_arrs, d_karrs, d_kout, d_cutILPsq};
+                    eatom_ters, ke, d_arrs, d_karrs, d_kout, d_cutILPsq, d_maxpred};
     for (void *p : ptrs)
       if (p) cudaFree(p);
     d = DevState();
@@ -606,6 +650,7 @@ struct Engine {
     d_karrs = nullptr;
     d_kout = nullptr;
     d_cutILPsq = nullptr;
+    d_maxpred = nullptr;
     if (h_pinned) cudaFreeHost(h_pinned);
     h_pinned = nullptr;
     h_pinned_bytes = 0;
@@ -891,6 +936,8 @@ struct Engine {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaMalloc(&d.status, sizeof(int)));
     CK(cudaMalloc(&d.maxdisp, sizeof(unsigned long long)));
+    CK(cudaMalloc(&d_maxpred, 3 * sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(d_maxpred, 0, 3 * sizeof(unsigned long long), stream));
     CK(cudaMalloc(&d_cutILPsq, sizeof(double) * MAXELEM * MAXELEM));
     CK(cudaMalloc(&d_arrs, sizeof(double *) * 2));
     CK(cudaMalloc(&d_karrs, sizeof(double *) * 2));
@@ -1275,14 +1322,72 @@ struct Engine {
     return fail(LMFF_ECUDA, "kernel status " + std::to_string(st));
   }
 
-  // rebuild when any atom moved more than skin/2 since the last build
-  int maybe_rebuild() {
-    unsigned long long bits = 0;
-    CK(cudaMemcpyAsync(&bits, d.maxdisp, sizeof bits, cudaMemcpyDeviceToHost, stream));
+  // rebuild when any atom moved more than skin/2 since the last build; ahead: also when
+  // one may before the next check (the look-ahead reach k_nve1 left in d_maxpred)
+  int maybe_rebuild(bool ahead = false) {
+    unsigned long long bits[2] = {0, 0};
+    CK(cudaMemcpyAsync(&bits[0], d.maxdisp, sizeof bits[0], cudaMemcpyDeviceToHost, stream));
+    if (ahead) {
+      CK(cudaMemcpyAsync(&bits[1], d_maxpred, sizeof bits[1], cudaMemcpyDeviceToHost, stream));
+      CK(cudaMemsetAsync(d_maxpred, 0, sizeof bits[1], stream));
+    }
     CK(cudaStreamSynchronize(stream));
-    double d2;
-    memcpy(&d2, &bits, sizeof d2);
-    if (!built || d2 > 0.25 * skin * skin) return rebuild();
+    double d2[2];
+    memcpy(d2, bits, sizeof d2);
+    if (!built || d2[0] > 0.25 * skin * skin || (ahead && d2[1] > 0.25 * skin * skin)) return rebuild();
+    return LMFF_OK;
+  }
+
+  // ---------------------------------------------------------------- rebuild checks
+  // The list is tested every ck-th step of an NVE run (steps whose index is a multiple of
+  // ck) with the look-ahead; ck = 1 tests every step for displacement alone, as LAMMPS's
+  // neigh_modify every 1 delay 0 check yes.  Forces do not depend on when the list is
+  // rebuilt (the cutoff tests are exact), only the order of some sums does.
+  static constexpr int LOOKAHEAD_MAX_ATOMS = 65536;
+  static constexpr int LOOKAHEAD_MAX_EVERY = 8;
+  int check_every_opt = 0;   // option "check_every": 0 = chosen per run, k >= 1 = every k steps
+  int ck = 1;                // the interval of the current run
+  unsigned long long *d_maxpred = nullptr;   // [0] look-ahead reach, [1..2] motion bound
+
+  bool check_step(int64_t step) const { return ck <= 1 || step % ck == 0; }
+  Lookahead lookahead_for(bool check, bool graph, double dt) const {
+    Lookahead la{};
+    if (ck <= 1) return la;
+    if (check) {
+      la.pred = d_maxpred;
+      la.hv = 1.25 * (ck - 1) * dt;
+      la.ha = 1.25 * (double)(ck - 1) * (ck - 1) * dt;
+    } else if (graph) {
+      la.status = d.status;
+      la.trig2 = 0.25 * skin * skin;
+    }
+    return la;
+  }
+  // the run's check interval: the largest of 8, 4, 2 whose look-ahead reach from the
+  // current motion stays within skin/4 (half the margin, so that a check rarely finds
+  // a rebuild needed right after the last one), else 1
+  int choose_check_every(double dt) {
+    ck = 1;
+    if (check_every_opt >= 1) {
+      ck = check_every_opt;
+      return LMFF_OK;
+    }
+    if (n == 0 || n > LOOKAHEAD_MAX_ATOMS || !(skin > 0.0)) return LMFF_OK;
+    CK(cudaMemsetAsync(d_maxpred + 1, 0, 2 * sizeof(unsigned long long), stream));
+    k_motion_max<<<(n + 255) / 256, 256, 0, stream>>>(n, d.v, d.f, d.xq, dtfm_table(0.5 * dt * FTM2V), d_maxpred + 1);
+    CK(cudaGetLastError());
+    unsigned long long bits[2] = {0, 0};
+    CK(cudaMemcpyAsync(bits, d_maxpred + 1, sizeof bits, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    double m2[2];
+    memcpy(m2, bits, sizeof m2);
+    const double vmax = sqrt(m2[0]), amax = sqrt(m2[1]);
+    for (int k = LOOKAHEAD_MAX_EVERY; k >= 2; k /= 2) {
+      if (1.25 * ((k - 1) * dt * vmax + (double)(k - 1) * (k - 1) * dt * amax) <= 0.25 * skin) {
+        ck = k;
+        break;
+      }
+    }
     return LMFF_OK;
   }
 
@@ -1683,11 +1788,13 @@ struct Engine {
   // (an overflow raises ST_LIST_OVERFLOW; the chunk is then redone on the eager path
   // from a checkpoint of its first step, equal to the uninterrupted run up to the
   // summation order of a list built at a different step).
+  // With a check interval ck > 1 there are three graphs: a check step, a step between
+  // checks, and ck steps from a check step on (one launch, one conditional node).
   bool use_graphs = true;
-  cudaGraphExec_t step_exec = nullptr;
+  cudaGraphExec_t step_exec = nullptr, between_exec = nullptr, block_exec = nullptr;
   cudaStream_t cap_stream = nullptr;
   struct StepKey {
-    int n, prec, tpa, block, full;
+    int n, prec, tpa, block, full, ck;
     double dt, skin;
     const void *list, *xq;
     int64_t cap;
@@ -1760,7 +1867,9 @@ struct Engine {
 
   void drop_graph() {
     if (step_exec) cudaGraphExecDestroy(step_exec);
-    step_exec = nullptr;
+    if (between_exec) cudaGraphExecDestroy(between_exec);
+    if (block_exec) cudaGraphExecDestroy(block_exec);
+    step_exec = between_exec = block_exec = nullptr;
     drop_fgraph();
   }
 
@@ -1845,55 +1954,75 @@ struct Engine {
     }
     graph_cap = d.list_cap;
     if (graph_cap_limit > 0 && graph_cap_limit < graph_cap) graph_cap = graph_cap_limit;
-    double dtf = 0.5 * dt * FTM2V;
-    bool mixed = precision == LMFF_MIXED;
-    cudaGraph_t g = nullptr;
-    CK(cudaGraphCreate(&g, 0));
-    cudaGraphConditionalHandle h;
-    CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
-    CK(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
-                                                d.sysid, d.xh, d.xl, mixed ? 1 : 0, h, 0.25 * skin * skin,
-                                                d_cond_ticket);
-    cudaStreamCaptureStatus cs;
-    const cudaGraphNode_t *deps = nullptr;
-    size_t nd = 0;
-    CK(cudaStreamGetCaptureInfo(stream, &cs, nullptr, nullptr, &deps, nullptr, &nd));
-    cudaGraphNodeParams cp = {};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = h;
-    cp.conditional.type = cudaGraphCondTypeIf;
-    cp.conditional.size = 1;
-    cudaGraphNode_t cn;
-    CK(cudaGraphAddNode(&cn, g, deps, nullptr, nd, &cp));
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    CK(cudaStreamBeginCaptureToGraph(cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    cudaError_t eb = enqueue_rebuild_fixed(cap_stream);
-    CK(cudaStreamEndCapture(cap_stream, &body));
-    if (eb != cudaSuccess) return cuda_fail(eb, "capturing the rebuild body");
-    CK(cudaStreamUpdateCaptureDependencies(stream, &cn, nullptr, 1, cudaStreamSetCaptureDependencies));
+    const double dtf = 0.5 * dt * FTM2V;
     bool kt = ktiming;
     ktiming = false;
     set_kick(dtf);   // the graph's rebuild copies back, so d.v stays fixed
     kick_on = true;
-    if (precision == LMFF_FP64)
-      run_kernels(args<double>(), LMFF_TERSOFF | LMFF_ILP, false, false, f64::launch_short, f64::launch_tersoff,
-                  f64::launch_ilp, f64::launch_nderiv, f64::launch_finish);
-    else
-      run_kernels(args<float>(), LMFF_TERSOFF | LMFF_ILP, false, false, f32::launch_short, f32::launch_tersoff,
-                  f32::launch_ilp, f32::launch_nderiv, f32::launch_finish);
+    int rc = capture_steps(dt, dtf, 1, true, &step_exec);
+    if (!rc && ck > 1) rc = capture_steps(dt, dtf, 1, false, &between_exec);
+    if (!rc && ck > 1) rc = capture_steps(dt, dtf, ck, true, &block_exec);
     ktiming = kt;
     kick_on = false;
-    cudaGraph_t gout = nullptr;
-    CK(cudaStreamEndCapture(stream, &gout));
-    cudaError_t ei = cudaGraphInstantiate(&step_exec, gout, 0);
-    cudaGraphDestroy(gout);
-    if (ei != cudaSuccess) {
-      step_exec = nullptr;
-      return cuda_fail(ei, "cudaGraphInstantiate(step graph)");
+    if (rc) {
+      drop_graph();
+      return rc;
     }
     memset(&step_key, 0, sizeof step_key);
-    step_key = StepKey{n, precision, tpa, block, list_full, dt, skin, d.list, d.xq, d.list_cap};
+    step_key = StepKey{n, precision, tpa, block, list_full, ck, dt, skin, d.list, d.xq, d.list_cap};
+    return LMFF_OK;
+  }
+
+  // Captures nsteps NVE steps into one graph: the first a check step (its rebuild test
+  // sets the condition of an IF node holding the rebuild) when check, the others steps
+  // between checks.
+  int capture_steps(double dt, double dtf, int nsteps, bool check, cudaGraphExec_t *out) {
+    const bool mixed = precision == LMFF_MIXED;
+    const double trig2 = 0.25 * skin * skin;
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h = 0;
+    if (check) CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+    CK(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    for (int s = 0; s < nsteps; s++) {
+      const bool chk = check && s == 0;
+      k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
+                                                  d.sysid, d.xh, d.xl, mixed ? 1 : 0, h, trig2,
+                                                  chk ? d_cond_ticket : nullptr, lookahead_for(chk, true, dt));
+      if (chk) {
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t nd = 0;
+        CK(cudaStreamGetCaptureInfo(stream, &cs, nullptr, nullptr, &deps, nullptr, &nd));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cn;
+        CK(cudaGraphAddNode(&cn, g, deps, nullptr, nd, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        CK(cudaStreamBeginCaptureToGraph(cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+        cudaError_t eb = enqueue_rebuild_fixed(cap_stream);
+        CK(cudaStreamEndCapture(cap_stream, &body));
+        if (eb != cudaSuccess) return cuda_fail(eb, "capturing the rebuild body");
+        CK(cudaStreamUpdateCaptureDependencies(stream, &cn, nullptr, 1, cudaStreamSetCaptureDependencies));
+      }
+      if (precision == LMFF_FP64)
+        run_kernels(args<double>(), LMFF_TERSOFF | LMFF_ILP, false, false, f64::launch_short, f64::launch_tersoff,
+                    f64::launch_ilp, f64::launch_nderiv, f64::launch_finish);
+      else
+        run_kernels(args<float>(), LMFF_TERSOFF | LMFF_ILP, false, false, f32::launch_short, f32::launch_tersoff,
+                    f32::launch_ilp, f32::launch_nderiv, f32::launch_finish);
+    }
+    cudaGraph_t gout = nullptr;
+    CK(cudaStreamEndCapture(stream, &gout));
+    cudaError_t ei = cudaGraphInstantiate(out, gout, 0);
+    cudaGraphDestroy(gout);
+    if (ei != cudaSuccess) {
+      *out = nullptr;
+      return cuda_fail(ei, "cudaGraphInstantiate(step graph)");
+    }
     return LMFF_OK;
   }
 
@@ -1918,14 +2047,27 @@ struct Engine {
 
   // nsteps NVE steps through the step graph; falls back to the eager loop on overflow
   int run_steps_graph(int nsteps, double dt) {
-    StepKey want{n, precision, tpa, block, list_full, dt, skin, d.list, d.xq, d.list_cap};
+    StepKey want;
+    memset(&want, 0, sizeof want);
+    want = StepKey{n, precision, tpa, block, list_full, ck, dt, skin, d.list, d.xq, d.list_cap};
     if (!step_exec || !(step_key == want)) {
       int rc = build_step_graph(dt);
       if (rc) return rc;
     }
     int rc = checkpoint(false);
     if (rc) return rc;
-    for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(step_exec, stream));
+    int64_t s = steps;
+    for (int left = nsteps; left > 0;) {
+      if (ck > 1 && s % ck == 0 && left >= ck) {
+        CK(cudaGraphLaunch(block_exec, stream));
+        s += ck;
+        left -= ck;
+      } else {
+        CK(cudaGraphLaunch(check_step(s) ? step_exec : between_exec, stream));
+        s++;
+        left--;
+      }
+    }
     int st = 0;
     unsigned long long nrb = 0;
     CK(cudaMemcpyAsync(&st, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -1933,8 +2075,9 @@ struct Engine {
     CK(cudaMemsetAsync(d_graph_rebuilds, 0, sizeof nrb, stream));
     CK(cudaStreamSynchronize(stream));
     hilo_fresh = precision == LMFF_MIXED;
-    if (st & (ST_LIST_OVERFLOW | ST_SHORT_OVERFLOW)) {
-      // redo the chunk on the eager path, which grows the list as needed
+    if (st & (ST_LIST_OVERFLOW | ST_SHORT_OVERFLOW | ST_SKIN_TRIP)) {
+      // redo the chunk on the eager path, which grows the list as needed and rebuilds at
+      // any step an atom moved more than skin/2
       CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
       rc = checkpoint(true);
       if (rc) return rc;
@@ -1961,13 +2104,15 @@ struct Engine {
     double dtf = 0.5 * dt * FTM2V;
     for (int s = 1; s <= nsteps; s++) {
       bool mixed = precision == LMFF_MIXED;
+      const bool chk = check_step(steps);
       timed(4, [&] {
         k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
-                                                    d.sysid, d.xh, d.xl, mixed ? 1 : 0);
+                                                    d.sysid, d.xh, d.xl, mixed ? 1 : 0, 0, 0.0, nullptr,
+                                                    lookahead_for(chk, false, dt));
       });
       CK(cudaGetLastError());
       hilo_fresh = mixed;
-      int rc = maybe_rebuild();
+      int rc = maybe_rebuild(chk && ck > 1);
       if (rc) return rc;
       set_kick(dtf);   // after any rebuild: it may have moved d.v
       kick_on = true;
@@ -2022,6 +2167,8 @@ struct Engine {
       rc = sample(steps, hr);
       if (rc) return rc;
     }
+    rc = choose_check_every(dt);
+    if (rc) return rc;
     cudaEvent_t r0, r1;
     cudaEventCreate(&r0);
     cudaEventCreate(&r1);
@@ -2047,11 +2194,13 @@ struct Engine {
       }
       if (th_at_end) {
         bool mixed = precision == LMFF_MIXED;
+        const bool chk = check_step(steps);
         k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dtv, d.xhold, d.maxdisp, d.sys,
-                                                    d.sysid, d.xh, d.xl, mixed ? 1 : 0);
+                                                    d.sysid, d.xh, d.xl, mixed ? 1 : 0, 0, 0.0, nullptr,
+                                                    lookahead_for(chk, false, dt));
         CK(cudaGetLastError());
         hilo_fresh = mixed;
-        rc = maybe_rebuild();
+        rc = maybe_rebuild(chk && ck > 1);
         if (rc) return rc;
         rc = forces(LMFF_TERSOFF | LMFF_ILP, true, false, &hr);
         if (rc) return rc;
@@ -2933,6 +3082,10 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
     const int v = (int)value;
     if (v != 1 && v != 2) return e->e.fail(LMFF_EINVAL, "pair_tile must be 1 or 2");
     e->e.pair_tile = v;
+    e->e.drop_graph();
+  } else if (k == "check_every") {
+    if (!(value >= 0.0 && value <= 64.0)) return e->e.fail(LMFF_EINVAL, "check_every must be in 0..64");
+    e->e.check_every_opt = (int)value;
     e->e.drop_graph();
   } else if (k == "ters_concurrent") {
     e->e.ters_concurrent = value != 0.0;

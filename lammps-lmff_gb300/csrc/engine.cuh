@@ -31,6 +31,7 @@ enum : int {
   ST_LIST_OVERFLOW = 16,
   ST_NONFINITE = 32,
   ST_STRIDE_OVERFLOW = 64,   // internal: an atom's list outgrew the strided build's stride
+  ST_SKIN_TRIP = 128,        // internal: an atom moved more than skin/2 between rebuild checks
 };
 
 // ILP parameters of one ordered element pair (pair_ilp_graphene_hbn.h:53-57 after

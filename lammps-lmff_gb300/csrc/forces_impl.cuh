@@ -72,10 +72,12 @@ __device__ __forceinline__ bool lt_exact(R rsq, R thr, const d4 *xq, const SysDe
 // SG lanes per atom share its short candidates.  Each round the lanes test one
 // candidate each; ballots over the atom's lanes give every accepted entry its position
 // in candidate order, so the lists equal a one-lane walk's, and the bond vectors of the
-// first three intralayer neighbours reach every lane by shuffles.  SG = 4 for small
-// systems, whose few threads cannot hide the candidate loop's chain of dependent loads
-// (7,200 atoms: 82.4 -> 79.4 us per step); SG = 1 for large ones, where the ballots
-// only add work (2.7M atoms: 0.87 vs 1.09 ms with the normal-derivative kernel).
+// first three intralayer neighbours reach every lane by shuffles.  SG = 16 up to 16,384
+// atoms and 4 up to 65,536, whose few threads cannot hide the candidate loop's chain of
+// dependent loads (7,200 atoms, per step: SG 1 82.4 us, SG 4 66.7, SG 16 63.7); SG = 1
+// for large ones, where the ballots only add work (2.7M atoms: 0.87 vs 1.09 ms with the
+// normal-derivative kernel).
+constexpr int SHORT_SG16_MAX_ATOMS = 16384;
 constexpr int SHORT_SG_MAX_ATOMS = 65536;
 template <int SG>
 __global__ void k_short(ForceArgs<R> a, const double *cutILPsq64, double tcutmaxsq64) {
@@ -1767,6 +1769,97 @@ __global__ void k_finish(ForceArgs<R> a, KickArgs kick) {
   }
 }
 
+// k_finish with FINISH_LANES lanes per atom, for small systems whose few threads cannot
+// hide k_finish's chains of dependent loads (the reverse search of each partner's list).
+// The atom's gather items (its Tersoff partners, then its intralayer candidates) are
+// dealt out to the lanes, one item per lane and round; lane 0 adds the items' values in
+// item order, so the forces are the one-lane kernel's to the bit.
+constexpr int FINISH_LANES = 8;
+constexpr int FINISH_LANES_MAX_ATOMS = 65536;
+template <bool EATOM, bool KICK>
+__global__ void k_finish_lanes(ForceArgs<R> a, KickArgs kick) {
+  constexpr int L = FINISH_LANES;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gtid / L;
+  if (i >= a.n) return;   // whole groups: blockDim is a multiple of L
+  const int wl = threadIdx.x & 31, l = wl & (L - 1), gbase = wl & ~(L - 1);
+  const unsigned gmask = ((1u << L) - 1) << gbase;
+  const bool sym = c_pot.ilp_cut_sym != 0;
+  const int nt = a.do_ters ? a.ters_cnt[i] : 0;
+  const int ni = a.do_ilp ? (sym ? a.ilp_cnt[i] : a.short_cnt[i]) : 0;
+  const uint32_t *cand = sym ? a.ilp_nb + (size_t)i * MAXILP : a.short_nb + (size_t)i * MAXSHORT;
+  const long long mi = (sym || !a.do_ilp) ? 0 : info_mol(__double_as_longlong(a.A.xq[i].w));
+  double Fx = 0, Fy = 0, Fz = 0, ea = 0;
+  if (l == 0) {
+    if (a.do_ilp) {
+      Fx += a.ilp_f[i]; Fy += a.ilp_f[a.n + i]; Fz += a.ilp_f[2 * a.n + i];
+    }
+    if (a.do_ters) {
+      Fx += a.ters_f[i]; Fy += a.ters_f[a.n + i]; Fz += a.ters_f[2 * a.n + i];
+    }
+  }
+  const int tot = nt + ni;
+  for (int q0 = 0; q0 < tot; q0 += L) {
+    const int q = q0 + l;
+    int found = 0;
+    d4 g = make_d4(0.0, 0.0, 0.0, 0.0);
+    if (q < nt) {
+      int j, sx, sy, sz;
+      decode_entry(a.ters_nb[(size_t)i * MAXTERS + q], a.lc, j, sx, sy, sz);
+      const uint32_t want = encode_entry(i, -sx, -sy, -sz, a.lc);
+      const int cj = a.ters_cnt[j];
+      for (int t = 0; t < cj; t++) {
+        if (a.ters_nb[(size_t)j * MAXTERS + t] == want) {
+          g = a.ters_g[(size_t)j * MAXTERS + t];
+          found = 1;
+          break;
+        }
+      }
+    } else if (q < tot) {
+      int j, sx, sy, sz;
+      decode_entry(cand[q - nt], a.lc, j, sx, sy, sz);
+      const int cj = a.ilp_cnt[j];
+      if (cj > 0 && (sym || info_mol(__double_as_longlong(a.A.xq[j].w)) == mi)) {
+        const uint32_t want = encode_entry(i, -sx, -sy, -sz, a.lc);
+        for (int t = 0; t < cj; t++) {
+          if (a.ilp_nb[(size_t)j * MAXILP + t] == want) {
+            g = a.ilp_c[(size_t)j * MAXILP + t];
+            found = 1;
+            break;
+          }
+        }
+      }
+    }
+    const int nr = min(L, tot - q0);
+    for (int k = 0; k < nr; k++) {
+      const int fk = __shfl_sync(gmask, found, gbase + k);
+      const double gx = __shfl_sync(gmask, g.x, gbase + k);
+      const double gy = __shfl_sync(gmask, g.y, gbase + k);
+      const double gz = __shfl_sync(gmask, g.z, gbase + k);
+      const double gw = EATOM ? __shfl_sync(gmask, g.w, gbase + k) : 0.0;
+      if (l == 0 && fk) {
+        Fx += gx; Fy += gy; Fz += gz;
+        if (EATOM && q0 + k < nt) ea += 0.5 * gw;
+      }
+    }
+  }
+  if (l != 0) return;
+  a.f_out[i] = Fx;
+  a.f_out[a.n + i] = Fy;
+  a.f_out[2 * a.n + i] = Fz;
+  if constexpr (KICK) {
+    const double dtfm = kick.dtfm[__double_as_longlong(a.A.xq[i].w) & 255];
+    kick.v[i] = kick.v[i] + dtfm * Fx;
+    kick.v[a.n + i] = kick.v[a.n + i] + dtfm * Fy;
+    kick.v[2 * a.n + i] = kick.v[2 * a.n + i] + dtfm * Fz;
+  }
+  if (EATOM) {
+    double e = a.do_ters ? a.eatom_ters[i] + ea : 0.0;
+    if (a.do_ilp) e += a.eatom_ilp[i];
+    a.eatom_ters[i] = e;
+  }
+}
+
 // Tersoff per-atom energy, own share (half of each bond energy centred here and half of
 // each repulsion from this end), written before k_finish adds the partners' halves.
 __global__ void k_ters_eatom_own(ForceArgs<R> a) {
@@ -1863,7 +1956,9 @@ void upload_pot(const PotConst<R> &p, cudaStream_t s) {
 
 void launch_short(const ForceArgs<R> &a, const double *cutILPsq64, double tcutmaxsq64, cudaStream_t s) {
   if (a.n == 0) return;
-  if (a.n <= SHORT_SG_MAX_ATOMS) k_short<4><<<(int)(((long long)a.n * 4 + 127) / 128), 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
+  if (a.n <= SHORT_SG16_MAX_ATOMS)
+    k_short<16><<<(int)(((long long)a.n * 16 + 127) / 128), 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
+  else if (a.n <= SHORT_SG_MAX_ATOMS) k_short<4><<<(int)(((long long)a.n * 4 + 127) / 128), 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
   else k_short<1><<<(a.n + 127) / 128, 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
 }
 
@@ -1950,6 +2045,14 @@ void launch_finish(const ForceArgs<R> &a, bool eatom, const KickArgs *kick, cuda
   int g = (a.n + 127) / 128;
   KickArgs k{};
   if (kick) k = *kick;
+  if (a.n <= FINISH_LANES_MAX_ATOMS) {
+    const int gl = (int)(((long long)a.n * FINISH_LANES + 127) / 128);
+    if (kick && !eatom) k_finish_lanes<false, true><<<gl, 128, 0, s>>>(a, k);
+    else if (kick) k_finish_lanes<true, true><<<gl, 128, 0, s>>>(a, k);
+    else if (eatom) k_finish_lanes<true, false><<<gl, 128, 0, s>>>(a, k);
+    else k_finish_lanes<false, false><<<gl, 128, 0, s>>>(a, k);
+    return;
+  }
   if (kick && !eatom) k_finish<false, true><<<g, 128, 0, s>>>(a, k);
   else if (kick) k_finish<true, true><<<g, 128, 0, s>>>(a, k);
   else if (eatom) k_finish<true, false><<<g, 128, 0, s>>>(a, k);

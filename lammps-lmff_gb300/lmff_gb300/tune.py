@@ -3,7 +3,10 @@
 Picks threads per atom (4, 8, 16, 32), threads per block (128, 256), the pair-kernel
 tile (list entries a lane takes per iteration: 1, or 2 packed in FP32x2 lanes) and the
 neighbour skin (1.0, 1.5, 2.0 A) by timing short device-resident NVE runs of a representative
-system with per-kernel CUDA-event timing on the engine's stream.  The score of a
+system as production runs them (steps replayed as CUDA graphs; CUDA events on the
+engine's stream around the run).  Timing kernels one by one instead adds a launch gap
+per kernel, which ranks the shapes of small systems wrongly (7,200 atoms: host-driven
+timing picked 8 threads per atom, the graph replay is fastest at 32).  The score of a
 candidate is the device time of one step plus the amortised cost of a list rebuild
 (rebuild time / expected steps between rebuilds, estimated from the largest
 displacement seen during the probe).  Forces do not depend on any of these knobs: the
@@ -62,12 +65,15 @@ def save_cache(c: Dict) -> None:
 
 def tune(system, tersoff_file: str, ilp_file: str, elements=("C", "B", "N"), precision: int = capi.MIXED,
          device: int = 0, tpas: Iterable[int] = (8, 16, 32), blocks: Iterable[int] = (128, 256),
-         skins: Iterable[float] = (1.0, 1.5, 2.0), steps: int = 4, use_cache: bool = True,
+         skins: Iterable[float] = (1.0, 1.5, 2.0), steps: Optional[int] = None, use_cache: bool = True,
          n_full: Optional[int] = None, tiles: Iterable[int] = (2, 1)) -> Dict:
     """Time the candidates on `system` and return the best {"tpa", "block", "skin", ...}.
     `n_full` (the production system size) selects the cache bucket when `system` is a
-    smaller stand-in with the same density."""
+    smaller stand-in with the same density.  `steps` (timed steps per candidate) defaults
+    to about 2 M atom-steps, 4 to 200 steps."""
     key = _key(precision, n_full or system.n, len(elements))
+    if steps is None:
+        steps = max(4, min(200, 2_000_000 // max(system.n, 1)))
     cache = load_cache() if use_cache else {}
     if key in cache:
         out = dict(cache[key])
@@ -84,9 +90,7 @@ def tune(system, tersoff_file: str, ilp_file: str, elements=("C", "B", "N"), pre
                     eng.set_option("block", block)
                     eng.set_option("pair_tile", tile)
                     eng.upload(system)
-                    eng.run_nve(2, 0.001)
-                    eng.set_option("kernel_timing", 1)
-                    eng.set_option("reset_timing", 1)
+                    eng.run_nve(2, 0.001)   # captures the step graph
                     x0, _, _ = eng.download()
                     eng.run_nve(steps, 0.001)
                     x1, _, _ = eng.download()
@@ -109,7 +113,7 @@ def tune(system, tersoff_file: str, ilp_file: str, elements=("C", "B", "N"), pre
     best = min(results, key=lambda r: r["score_ms"])
     out = {"tpa": best["tpa"], "block": best["block"], "skin": best["skin"], "tile": best["tile"],
            "score_ms": best["score_ms"],
-           "probe_atoms": system.n, "key": key, "candidates": results, "when": time.time()}
+           "probe_atoms": system.n, "steps": steps, "key": key, "candidates": results, "when": time.time()}
     if use_cache:
         cache[key] = {k: v for k, v in out.items() if k != "candidates"}
         save_cache(cache)

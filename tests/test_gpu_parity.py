@@ -313,13 +313,15 @@ def test_two_engines_interleaved_share_constant_memory_safely():
         assert rel_max(rt["f"] + ri["f"], g["f"]) <= F64_TOL, call
 
 
-def _graph_vs_host_loop(prec, graph_list_cap=0, steps=60, thermo_every=20):
+def _graph_vs_host_loop(prec, graph_list_cap=0, steps=60, thermo_every=20, check_every=0, temp=1500.0):
     """The same NVE run through the step graph and through the host-driven loop."""
-    s = S.thermalize(S.twisted_bilayer(8, 8, 3.0, top="hbn"), 1500.0, seed=11)
+    s = S.thermalize(S.twisted_bilayer(8, 8, 3.0, top="hbn"), temp, seed=11)
     out = []
     for graphs in (1, 0):
         eng = capi.Engine(TERSOFF, ILP, precision=prec, skin=0.4)
         eng.set_option("graphs", graphs)
+        if check_every:
+            eng.set_option("check_every", check_every)
         if graph_list_cap:
             eng.set_option("graph_list_cap", graph_list_cap)
         eng.upload(s)
@@ -341,6 +343,42 @@ def test_step_graph_bitwise_equals_host_loop(prec):
     assert np.array_equal(xg, xe) and np.array_equal(vg, ve) and np.array_equal(fg, fe)
     assert [t["etotal"] for t in thg] == [t["etotal"] for t in the]
     assert len(thg) == 60 // 20 + 1
+
+
+@pytest.mark.parametrize("check_every", [1, 4])
+def test_step_graph_with_check_interval_bitwise_equals_host_loop(check_every):
+    """A fixed rebuild-check interval (every step; every 4th with the look-ahead, one
+    conditional node per 4-step graph) gives the same trajectory and rebuild count
+    through the graphs as through the host-driven loop; forces equal a fresh FP64
+    evaluation of the final positions (no pair was missed)."""
+    (xg, vg, fg, thg, sg), (xe, ve, fe, the, se), s = _graph_vs_host_loop(capi.FP64, check_every=check_every,
+                                                                          temp=300.0, steps=80)
+    assert sg["graph_steps"] > 0 and sg["graph_redos"] == 0
+    assert se["rebuilds"] >= 2 and sg["rebuilds"] == se["rebuilds"]
+    assert np.array_equal(xg, xe) and np.array_equal(vg, ve) and np.array_equal(fg, fe)
+    assert [t["etotal"] for t in thg] == [t["etotal"] for t in the]
+    s1 = s.copy()
+    s1.x = xg
+    r = capi.Engine(TERSOFF, ILP).compute_system(s1, eflag=False, vflag=False)
+    assert rel_max(fg, r["f"]) < 1e-10
+
+
+def test_step_graph_skin_trip_redo():
+    """A check interval far too long for the motion (16 steps at 1500 K, skin 0.4 A):
+    atoms move more than skin/2 between checks, the graph raises the trip and the chunk
+    is redone on the host-driven loop, which rebuilds at such steps.  The result agrees
+    with the host-driven run to FP64 rounding and its forces with a fresh evaluation."""
+    (xg, vg, fg, thg, sg), (xe, ve, fe, the, se), s = _graph_vs_host_loop(capi.FP64, check_every=16)
+    assert sg["graph_redos"] > 0
+    assert sg["steps"] == se["steps"]
+    assert np.abs(min_image(xg - xe, s.box_lo, s.box_hi, s.periodic)).max() < 1e-9
+    assert rel_max(vg, ve) < 1e-7 and rel_max(fg, fe) < 1e-7
+    for a, b in zip(thg, the):
+        assert abs(a["etotal"] - b["etotal"]) <= 1e-10 * abs(b["etotal"])
+    s1 = s.copy()
+    s1.x = xg
+    r = capi.Engine(TERSOFF, ILP).compute_system(s1, eflag=False, vflag=False)
+    assert rel_max(fg, r["f"]) < 1e-10
 
 
 def test_step_graph_overflow_redo():

@@ -241,26 +241,13 @@ __global__ void k_nve1(int n, d4 *xq, double *v, const double *f, DtfmTab tab, d
     double vy = v[n + q] + dtfm * fy;
     double vz = v[2 * n + q] + dtfm * fz;
     v[q] = vx; v[n + q] = vy; v[2 * n + q] = vz;
-    double x = w.x + dtv * vx, y = w.y + dtv * vy, z = w.z + dtv * vz;
-    xq[q] = make_d4(x, y, z, w.w);
-    double dx = x - xhold[3 * q], dy = y - xhold[3 * q + 1], dz = z - xhold[3 * q + 2];
-    d2 = dx * dx + dy * dy + dz * dz;
+    d2 = nve_drift(q, vx, vy, vz, dtv, xq, xhold, xh, xl, sys, sysid, do_hilo);
     if (la.pred) {
       const double p = sqrt(d2) + la.hv * sqrt(vx * vx + vy * vy + vz * vz) +
                        la.ha * fabs(dtfm) * sqrt(fx * fx + fy * fy + fz * fz);
       p2 = p * p;
     }
     if (la.status && d2 > la.trig2) atomicOr(la.status, ST_SKIN_TRIP);
-    if (do_hilo) {
-      const SysDesc &sd = sys[sysid[q]];
-      double X = x - sd.lo[0] + 32.0 + sd.base;
-      double Y = y - sd.lo[1] + 32.0 + sd.base;
-      double Z = z - sd.lo[2] + 32.0 + sd.base;
-      float hx = (float)X, hy = (float)Y, hz = (float)Z;
-      float4 h = xh[q];
-      xh[q] = make_float4(hx, hy, hz, h.w);
-      xl[q] = make_float4((float)(X - (double)hx), (float)(Y - (double)hy), (float)(Z - (double)hz), 0.f);
-    }
   }
   block_max_disp(d2, maxdisp);
   if (la.pred) {
@@ -1902,10 +1889,21 @@ struct Engine {
   // NVE steps: the gather kernel applies the second half-kick (k_nve2's arithmetic)
   KickArgs kick_args{};
   bool kick_on = false;
-  void set_kick(double dtf) {
+  void set_kick(double dtf, double dt = 0.0) {
     kick_args.v = d.v;
     DtfmTab t = dtfm_table(dtf);
     for (int k = 0; k <= MAXTYPE; k++) kick_args.dtfm[k] = t.v[k];
+    kick_args.drift = 0;
+    kick_args.do_hilo = precision == LMFF_MIXED;
+    kick_args.dtv = dt;
+    kick_args.trig2 = 0.25 * skin * skin;
+    kick_args.xq = d.xq;
+    kick_args.xhold = d.xhold;
+    kick_args.xh = d.xh;
+    kick_args.xl = d.xl;
+    kick_args.sys = d.sys;
+    kick_args.sysid = d.sysid;
+    kick_args.status = d.status;
   }
 
   DtfmTab dtfm_table(double dtf) const {
@@ -1957,7 +1955,7 @@ struct Engine {
     const double dtf = 0.5 * dt * FTM2V;
     bool kt = ktiming;
     ktiming = false;
-    set_kick(dtf);   // the graph's rebuild copies back, so d.v stays fixed
+    set_kick(dtf, dt);   // the graph's rebuild copies back, so d.v stays fixed
     kick_on = true;
     int rc = capture_steps(dt, dtf, 1, true, &step_exec);
     if (!rc && ck > 1) rc = capture_steps(dt, dtf, 1, false, &between_exec);
@@ -1975,7 +1973,7 @@ struct Engine {
 
   // Captures nsteps NVE steps into one graph: the first a check step (its rebuild test
   // sets the condition of an IF node holding the rebuild) when check, the others steps
-  // between checks.
+  // between checks, whose first half the previous step's gather makes (no k_nve1).
   int capture_steps(double dt, double dtf, int nsteps, bool check, cudaGraphExec_t *out) {
     const bool mixed = precision == LMFF_MIXED;
     const double trig2 = 0.25 * skin * skin;
@@ -1986,9 +1984,11 @@ struct Engine {
     CK(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     for (int s = 0; s < nsteps; s++) {
       const bool chk = check && s == 0;
-      k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
-                                                  d.sysid, d.xh, d.xl, mixed ? 1 : 0, h, trig2,
-                                                  chk ? d_cond_ticket : nullptr, lookahead_for(chk, true, dt));
+      if (s == 0)
+        k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
+                                                    d.sysid, d.xh, d.xl, mixed ? 1 : 0, h, trig2,
+                                                    chk ? d_cond_ticket : nullptr, lookahead_for(chk, true, dt));
+      kick_args.drift = s + 1 < nsteps;
       if (chk) {
         cudaStreamCaptureStatus cs;
         const cudaGraphNode_t *deps = nullptr;
@@ -2015,6 +2015,7 @@ struct Engine {
         run_kernels(args<float>(), LMFF_TERSOFF | LMFF_ILP, false, false, f32::launch_short, f32::launch_tersoff,
                     f32::launch_ilp, f32::launch_nderiv, f32::launch_finish);
     }
+    kick_args.drift = 0;
     cudaGraph_t gout = nullptr;
     CK(cudaStreamEndCapture(stream, &gout));
     cudaError_t ei = cudaGraphInstantiate(out, gout, 0);

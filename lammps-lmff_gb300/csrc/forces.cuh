@@ -211,7 +211,44 @@ __device__ __forceinline__ void disp64(const d4 *xq, const SysDesc &sd, int i, i
 struct KickArgs {
   double *v;
   double dtfm[MAXTYPE + 1];
+  // drift != 0: the gather also makes the next step's first half (velocity half-kick and
+  // position drift, k_nve1's arithmetic) -- steps between rebuild tests inside one step
+  // graph; an atom moved more than skin/2 since the last build raises ST_SKIN_TRIP
+  int drift;
+  int do_hilo;
+  double dtv, trig2;
+  d4 *xq;
+  const double *xhold;
+  float4 *xh, *xl;
+  const SysDesc *sys;
+  const int *sysid;
+  int *status;
 };
+
+// Velocity Verlet's position drift of atom q (fix_nve.cpp:89-91) on its half-kicked
+// velocity, with the double-float split of the mixed kernels refreshed; returns the
+// squared displacement since the last build.  k_nve1 and the gather's drift share it.
+__device__ __forceinline__ double nve_drift(int q, double vx, double vy, double vz, double dtv, d4 *xq,
+                                            const double *xhold, float4 *xh, float4 *xl, const SysDesc *sys,
+                                            const int *sysid, int do_hilo) {
+  const d4 w = xq[q];
+  const double x = w.x + dtv * vx, y = w.y + dtv * vy, z = w.z + dtv * vz;
+  xq[q].x = x;
+  xq[q].y = y;
+  xq[q].z = z;
+  const double dx = x - xhold[3 * q], dy = y - xhold[3 * q + 1], dz = z - xhold[3 * q + 2];
+  if (do_hilo) {
+    const SysDesc &sd = sys[sysid[q]];
+    const double X = x - sd.lo[0] + 32.0 + sd.base;
+    const double Y = y - sd.lo[1] + 32.0 + sd.base;
+    const double Z = z - sd.lo[2] + 32.0 + sd.base;
+    const float hx = (float)X, hy = (float)Y, hz = (float)Z;
+    const float4 h = xh[q];
+    xh[q] = make_float4(hx, hy, hz, h.w);
+    xl[q] = make_float4((float)(X - (double)hx), (float)(Y - (double)hy), (float)(Z - (double)hz), 0.f);
+  }
+  return dx * dx + dy * dy + dz * dz;
+}
 
 template <class R>
 struct ForceArgs {

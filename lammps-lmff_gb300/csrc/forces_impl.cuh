@@ -1701,6 +1701,30 @@ __global__ void k_nderiv(ForceArgs<R> a) {
 // Per atom a: its own ILP and Tersoff forces + the slots its neighbours left for it:
 // Tersoff bond/three-body forces from every j with a in N_ters(j) and ILP normal-
 // derivative forces from every j with a in N_ilp(j).  Fixed summation order.
+// The gather's velocity half-kick of atom i (k_nve2's arithmetic on the force just
+// stored) and, with kick.drift, the next step's first half (k_nve1's: a second
+// half-kick on the same force, then the drift).
+__device__ __forceinline__ void kick_atom(const KickArgs &kick, const ForceArgs<R> &a, int i, double Fx, double Fy,
+                                          double Fz) {
+  const double dtfm = kick.dtfm[__double_as_longlong(a.A.xq[i].w) & 255];
+  double vx = kick.v[i] + dtfm * Fx;
+  double vy = kick.v[a.n + i] + dtfm * Fy;
+  double vz = kick.v[2 * a.n + i] + dtfm * Fz;
+  if (kick.drift) {
+    vx = vx + dtfm * Fx;
+    vy = vy + dtfm * Fy;
+    vz = vz + dtfm * Fz;
+  }
+  kick.v[i] = vx;
+  kick.v[a.n + i] = vy;
+  kick.v[2 * a.n + i] = vz;
+  if (kick.drift) {
+    const double d2 = nve_drift(i, vx, vy, vz, kick.dtv, kick.xq, kick.xhold, kick.xh, kick.xl, kick.sys, kick.sysid,
+                                kick.do_hilo);
+    if (d2 > kick.trig2) atomicOr(kick.status, ST_SKIN_TRIP);
+  }
+}
+
 template <bool EATOM, bool KICK>
 __global__ void k_finish(ForceArgs<R> a, KickArgs kick) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1754,12 +1778,7 @@ __global__ void k_finish(ForceArgs<R> a, KickArgs kick) {
   a.f_out[i] = Fx;
   a.f_out[a.n + i] = Fy;
   a.f_out[2 * a.n + i] = Fz;
-  if constexpr (KICK) {   // the same arithmetic as k_nve2 on the force just stored
-    const double dtfm = kick.dtfm[__double_as_longlong(a.A.xq[i].w) & 255];
-    kick.v[i] = kick.v[i] + dtfm * Fx;
-    kick.v[a.n + i] = kick.v[a.n + i] + dtfm * Fy;
-    kick.v[2 * a.n + i] = kick.v[2 * a.n + i] + dtfm * Fz;
-  }
+  if constexpr (KICK) kick_atom(kick, a, i, Fx, Fy, Fz);
   if (EATOM) {
     // per-atom energy as the reference's ev_tally splits it: the Tersoff own share was
     // written by k_ters_eatom_own, the partners' halves are gathered above
@@ -1847,12 +1866,7 @@ __global__ void k_finish_lanes(ForceArgs<R> a, KickArgs kick) {
   a.f_out[i] = Fx;
   a.f_out[a.n + i] = Fy;
   a.f_out[2 * a.n + i] = Fz;
-  if constexpr (KICK) {
-    const double dtfm = kick.dtfm[__double_as_longlong(a.A.xq[i].w) & 255];
-    kick.v[i] = kick.v[i] + dtfm * Fx;
-    kick.v[a.n + i] = kick.v[a.n + i] + dtfm * Fy;
-    kick.v[2 * a.n + i] = kick.v[2 * a.n + i] + dtfm * Fz;
-  }
+  if constexpr (KICK) kick_atom(kick, a, i, Fx, Fy, Fz);
   if (EATOM) {
     double e = a.do_ters ? a.eatom_ters[i] + ea : 0.0;
     if (a.do_ilp) e += a.eatom_ilp[i];

@@ -1612,10 +1612,15 @@ __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, GH, 
 // intralayer neighbour m is -(dn1/dv_m)^T h and on i -(dn1/dx_i)^T h; dn1/dv of a cross
 // product is a skew matrix, so each term is one cross product with h.  The neighbour
 // forces go to ilp_c slots, gathered by k_finish.
+// nderiv_eval: the assembly of atom i without writes -- the neighbour forces c[m] (zero
+// past the atom's intralayer count), the force F on i and, with EV, the virial W.
+struct NDeriv {
+  double c[3][3];
+  double F[3];
+  double W[6];
+};
 template <bool EV>
-__global__ void k_nderiv(ForceArgs<R> a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+__device__ __forceinline__ void nderiv_eval(const ForceArgs<R> &a, int i, NDeriv &o) {
   const SysDesc &sd = a.A.sys[a.A.sysid[i]];
   const int ie = c_pot.i_map[info_type(__double_as_longlong(a.A.xq[i].w))];
   const int cont = ie >= 0 ? a.ilp_cnt[i] : 0;
@@ -1683,24 +1688,35 @@ __global__ void k_nderiv(ForceArgs<R> a) {
       }
     }
   }
-  d4 *cs = a.ilp_c + (size_t)i * MAXILP;
-  cs[0] = make_d4(c0x, c0y, c0z, 0.0);
-  cs[1] = make_d4(c1x, c1y, c1z, 0.0);
-  cs[2] = make_d4(c2x, c2y, c2z, 0.0);
-  a.ilp_f[i] += Fx;
-  a.ilp_f[a.n + i] += Fy;
-  a.ilp_f[2 * a.n + i] += Fz;
+  o.c[0][0] = c0x; o.c[0][1] = c0y; o.c[0][2] = c0z;
+  o.c[1][0] = c1x; o.c[1][1] = c1y; o.c[1][2] = c1z;
+  o.c[2][0] = c2x; o.c[2][1] = c2y; o.c[2][2] = c2z;
+  o.F[0] = Fx; o.F[1] = Fy; o.F[2] = Fz;
   if (EV) {
-    double *st = a.stat_ilp;
-    st[(size_t)2 * a.n + i] += W0; st[(size_t)3 * a.n + i] += W1; st[(size_t)4 * a.n + i] += W2;
-    st[(size_t)5 * a.n + i] += W3; st[(size_t)6 * a.n + i] += W4; st[(size_t)7 * a.n + i] += W5;
+    o.W[0] = W0; o.W[1] = W1; o.W[2] = W2; o.W[3] = W3; o.W[4] = W4; o.W[5] = W5;
   }
 }
 
-// ============================================================== k_finish =========
-// Per atom a: its own ILP and Tersoff forces + the slots its neighbours left for it:
-// Tersoff bond/three-body forces from every j with a in N_ters(j) and ILP normal-
-// derivative forces from every j with a in N_ilp(j).  Fixed summation order.
+template <bool EV>
+__global__ void k_nderiv(ForceArgs<R> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  NDeriv o;
+  nderiv_eval<EV>(a, i, o);
+  d4 *cs = a.ilp_c + (size_t)i * MAXILP;
+  cs[0] = make_d4(o.c[0][0], o.c[0][1], o.c[0][2], 0.0);
+  cs[1] = make_d4(o.c[1][0], o.c[1][1], o.c[1][2], 0.0);
+  cs[2] = make_d4(o.c[2][0], o.c[2][1], o.c[2][2], 0.0);
+  a.ilp_f[i] += o.F[0];
+  a.ilp_f[a.n + i] += o.F[1];
+  a.ilp_f[2 * a.n + i] += o.F[2];
+  if (EV) {
+    double *st = a.stat_ilp;
+    st[(size_t)2 * a.n + i] += o.W[0]; st[(size_t)3 * a.n + i] += o.W[1]; st[(size_t)4 * a.n + i] += o.W[2];
+    st[(size_t)5 * a.n + i] += o.W[3]; st[(size_t)6 * a.n + i] += o.W[4]; st[(size_t)7 * a.n + i] += o.W[5];
+  }
+}
+
 // The gather's velocity half-kick of atom i (k_nve2's arithmetic on the force just
 // stored) and, with kick.drift, the next step's first half (k_nve1's: a second
 // half-kick on the same force, then the drift).
@@ -1725,6 +1741,10 @@ __device__ __forceinline__ void kick_atom(const KickArgs &kick, const ForceArgs<
   }
 }
 
+// ============================================================== k_finish =========
+// Per atom a: its own ILP and Tersoff forces + the slots its neighbours left for it:
+// Tersoff bond/three-body forces from every j with a in N_ters(j) and ILP normal-
+// derivative forces from every j with a in N_ilp(j).  Fixed summation order.
 template <bool EATOM, bool KICK>
 __global__ void k_finish(ForceArgs<R> a, KickArgs kick) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;

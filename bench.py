@@ -54,12 +54,12 @@ TERSOFF_FILE = os.path.join(ROOT, "lammps-lmff_gb300", "potentials", "BNC.tersof
 ILP_FILE = os.path.join(ROOT, "lammps-lmff_gb300", "potentials", "BNCH.ILP")
 
 # DRAM bytes per pair-list entry of the mixed pair kernel, from one ncu capture of the
-# 331,200-atom graphite slab (k_ilp<8,0,0,1,0,0>: 1.303 GB read + 19.7 MB written for
+# 331,200-atom graphite slab (k_ilp<16,0,0,1,0,0,1>: 1.297 GB read + 20.1 MB written for
 # 310,301,280 entries; the list is larger than L2, so traffic grows with the entries)
-K_ILP_DRAM_BYTES_PER_ENTRY = (1.302568e9 + 19.73888e6) / 310301280
+K_ILP_DRAM_BYTES_PER_ENTRY = (1.297430e9 + 20.068096e6) / 310301280
 # FP64-pipe activity of the two FP64-bound per-atom kernels of the mixed step (ncu
 # sm__pipe_fp64_cycles_active on the 331,200-atom slab, profiles/)
-FP64_PIPE_ACTIVE_NCU = {"k_tersoff": 0.628, "k_nderiv": 0.821}
+FP64_PIPE_ACTIVE_NCU = {"k_tersoff": 0.624, "k_nderiv": 0.824}
 L2_BYTES = 129e6   # GB300 L2
 FLOPS_H = os.path.join(ROOT, "bench", "flops.h")
 
@@ -604,7 +604,7 @@ def rooflines(m, s, prec, pk, peaks) -> dict:
         "frac": achieved / pk[name] if pk[name] else None,
         "traffic": K_ILP_DRAM_BYTES_PER_ENTRY * cands if prec == capi.MIXED else None,
         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_ilp launch on the "
-                          "331,200-atom slab (1.322 GB for 310.3 M list entries), scaled by list entries",
+                          "331,200-atom slab (1.317 GB for 310.3 M list entries), scaled by list entries",
         "kernel": "k_ilp (pair kernel)", "kernel_ms_avg": ka["pair_ilp"],
         "peak_source": f"cuBLAS {name.upper()} GEMM measured in this run (SIMT; MEASURED_PEAKS.json has HBM "
                        f"{peaks.get('hbm_gbs')} GB/s and bf16 tensor only)",

@@ -2562,10 +2562,38 @@ struct Engine {
     for (size_t s = 0; s < hr.size() && res; s++) res[s] = hr[s];
     if (f_out && n > 0) {
       k_scatter_add<<<(n + 255) / 256, 256, 0, stream>>>(n, d.perm, d.f, d_fin, 1);
-      CK(cudaMemcpyAsync(f_out, d_fin, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, stream));
+      const size_t bf = sizeof(double) * 3 * (size_t)n;
+      if (n >= (1 << 17) && ensure_pinned(bf) == LMFF_OK) {
+        // a large batch comes back through the pinned staging block (a pageable copy is
+        // staged by the driver at a fraction of the link's rate), then into the caller's
+        // array on several host threads
+        CK(cudaMemcpyAsync(h_pinned, d_fin, bf, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        parallel_copy(f_out, h_pinned, bf);
+        return LMFF_OK;
+      }
+      CK(cudaMemcpyAsync(f_out, d_fin, bf, cudaMemcpyDeviceToHost, stream));
     }
     CK(cudaStreamSynchronize(stream));
     return LMFF_OK;
+  }
+
+  // memcpy on up to 8 host threads, in 64-byte aligned pieces
+  static void parallel_copy(void *dst, const void *src, size_t bytes) {
+    const int nth = (int)std::min<size_t>(8, std::max(1u, std::thread::hardware_concurrency()));
+    if (nth <= 1 || bytes < ((size_t)4 << 20)) {
+      memcpy(dst, src, bytes);
+      return;
+    }
+    const size_t piece = ((bytes / nth) + 63) & ~(size_t)63;
+    std::vector<std::thread> pool;
+    for (int k = 0; k < nth; k++) {
+      const size_t b = (size_t)k * piece;
+      if (b >= bytes) break;
+      const size_t e = std::min(bytes, b + piece);
+      pool.emplace_back([=] { memcpy((char *)dst + b, (const char *)src + b, e - b); });
+    }
+    for (auto &t : pool) t.join();
   }
 
   // ---------------------------------------------------------------- lists export

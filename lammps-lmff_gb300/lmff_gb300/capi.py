@@ -47,6 +47,16 @@ class Result(C.Structure):
                 "e_pair": self.e_tersoff + self.e_ilp}
 
 
+def _results(res, n: int) -> List[Dict]:
+    """Result.to_dict of each of the n entries of a Result array, by columns (a batch has
+    hundreds of systems)."""
+    a = np.frombuffer(res, dtype=np.float64, count=16 * n).reshape(n, 16).copy()
+    et, ei, pv, vt, vi = a[:, 0], a[:, 1], a[:, 2:4], a[:, 4:10], a[:, 10:16]
+    vs, ep = vt + vi, et + ei
+    return [{"e_tersoff": float(et[k]), "e_ilp": float(ei[k]), "pvector": pv[k], "virial_tersoff": vt[k],
+             "virial_ilp": vi[k], "virial": vs[k], "e_pair": float(ep[k])} for k in range(n)]
+
+
 class Thermo(C.Structure):
     _fields_ = [("step", C.c_int64), ("pe", C.c_double), ("ke", C.c_double), ("etotal", C.c_double),
                 ("temp", C.c_double), ("virial", C.c_double * 6)]
@@ -72,6 +82,19 @@ KERNELS = ["pair_ilp", "tersoff", "intralayer_normals", "gather", "integrate", "
 class SystemDesc(C.Structure):
     _fields_ = [("natoms", C.c_int), ("x", C.c_void_p), ("type", C.c_void_p), ("mol", C.c_void_p),
                 ("lo", C.c_double * 3), ("hi", C.c_double * 3), ("periodic", C.c_int * 3), ("v", C.c_void_p)]
+
+
+# a numpy view of a SystemDesc array, so a large batch's descriptors are filled by column
+_DESC_DTYPE = np.dtype({"names": ["natoms", "x", "type", "mol", "lo", "hi", "periodic", "v"],
+                        "formats": ["<i4", "<u8", "<u8", "<u8", ("<f8", 3), ("<f8", 3), ("<i4", 3), "<u8"],
+                        "offsets": [SystemDesc.natoms.offset, SystemDesc.x.offset, SystemDesc.type.offset,
+                                    SystemDesc.mol.offset, SystemDesc.lo.offset, SystemDesc.hi.offset,
+                                    SystemDesc.periodic.offset, SystemDesc.v.offset],
+                        "itemsize": C.sizeof(SystemDesc)})
+
+
+def _addr(a: np.ndarray) -> int:
+    return a.__array_interface__["data"][0]
 
 
 _lib = None
@@ -331,25 +354,21 @@ class Engine:
     def batch_set(self, systems, velocities: bool = False) -> None:
         """Load many systems as one resident batch; with velocities=True each system's
         v (or zeros) is loaded too, for run_nve on the whole batch."""
-        self._batch_keep = []
+        xs = [_f64(s.x) for s in systems]
+        ts = [np.ascontiguousarray(s.type, dtype=np.int32) for s in systems]
+        ms = [np.ascontiguousarray(s.mol, dtype=np.int64) for s in systems]
+        vs = [_f64(s.v) if velocities and s.v is not None else None for s in systems]
+        self._batch_keep = [xs, ts, ms, vs]
         descs = (SystemDesc * len(systems))()
-        for k, s in enumerate(systems):
-            x = _f64(s.x)
-            t = np.ascontiguousarray(s.type, dtype=np.int32)
-            m = np.ascontiguousarray(s.mol, dtype=np.int64)
-            self._batch_keep += [x, t, m]
-            descs[k].natoms = s.n
-            descs[k].x = x.ctypes.data
-            descs[k].type = t.ctypes.data
-            descs[k].mol = m.ctypes.data
-            if velocities and s.v is not None:
-                v = _f64(s.v)
-                self._batch_keep.append(v)
-                descs[k].v = v.ctypes.data
-            for c in range(3):
-                descs[k].lo[c] = float(s.box_lo[c])
-                descs[k].hi[c] = float(s.box_hi[c])
-                descs[k].periodic[c] = int(bool(s.periodic[c]))
+        d = np.frombuffer(descs, dtype=_DESC_DTYPE)
+        d["natoms"] = [s.n for s in systems]
+        d["x"] = [_addr(x) for x in xs]
+        d["type"] = [_addr(t) for t in ts]
+        d["mol"] = [_addr(m) for m in ms]
+        d["v"] = [0 if v is None else _addr(v) for v in vs]
+        d["lo"] = [s.box_lo for s in systems]
+        d["hi"] = [s.box_hi for s in systems]
+        d["periodic"] = [[int(bool(p)) for p in s.periodic] for s in systems]
         self._batch_n = [s.n for s in systems]
         self._n = sum(self._batch_n)
         self._ck(_lib.lmff_batch_set(self._h, len(systems), C.cast(descs, C.c_void_p)))
@@ -358,7 +377,7 @@ class Engine:
         """Per-system energies and virials of the last evaluation that computed them."""
         res = (Result * len(self._batch_n))()
         self._ck(_lib.lmff_batch_results(self._h, len(self._batch_n), C.cast(res, C.c_void_p)))
-        return [r.to_dict() for r in res]
+        return _results(res, len(self._batch_n))
 
     def split(self, a: np.ndarray) -> List[np.ndarray]:
         """Split a batch-ordered per-atom array into the systems of the batch."""
@@ -366,16 +385,14 @@ class Engine:
 
     def batch_compute(self):
         ntot = sum(self._batch_n)
-        f = np.zeros((ntot, 3))
+        f = np.empty((ntot, 3))   # lmff_batch_compute writes every element
         res = (Result * len(self._batch_n))()
         self._ck(_lib.lmff_batch_compute(self._h, _p(f), C.cast(res, C.c_void_p)))
-        out = []
+        out = _results(res, len(self._batch_n))
         o = 0
-        for k, n in enumerate(self._batch_n):
-            d = res[k].to_dict()
+        for d, n in zip(out, self._batch_n):
             d["f"] = f[o:o + n]
             o += n
-            out.append(d)
         return out
 
     # -------------------------------------------------------------- diagnostics

@@ -1985,7 +1985,7 @@ struct Engine {
     for (int s = 0; s < nsteps; s++) {
       const bool chk = check && s == 0;
       if (s == 0)
-        k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
+        k_nve1<<<(n + per_atom_block(n) - 1) / per_atom_block(n), per_atom_block(n), 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
                                                     d.sysid, d.xh, d.xl, mixed ? 1 : 0, h, trig2,
                                                     chk ? d_cond_ticket : nullptr, lookahead_for(chk, true, dt));
       kick_args.drift = s + 1 < nsteps;
@@ -2107,7 +2107,7 @@ struct Engine {
       bool mixed = precision == LMFF_MIXED;
       const bool chk = check_step(steps);
       timed(4, [&] {
-        k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
+        k_nve1<<<(n + per_atom_block(n) - 1) / per_atom_block(n), per_atom_block(n), 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dt, d.xhold, d.maxdisp, d.sys,
                                                     d.sysid, d.xh, d.xl, mixed ? 1 : 0, 0, 0.0, nullptr,
                                                     lookahead_for(chk, false, dt));
       });
@@ -2196,7 +2196,7 @@ struct Engine {
       if (th_at_end) {
         bool mixed = precision == LMFF_MIXED;
         const bool chk = check_step(steps);
-        k_nve1<<<(n + 255) / 256, 256, 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dtv, d.xhold, d.maxdisp, d.sys,
+        k_nve1<<<(n + per_atom_block(n) - 1) / per_atom_block(n), per_atom_block(n), 0, stream>>>(n, d.xq, d.v, d.f, dtfm_table(dtf), dtv, d.xhold, d.maxdisp, d.sys,
                                                     d.sysid, d.xh, d.xl, mixed ? 1 : 0, 0, 0.0, nullptr,
                                                     lookahead_for(chk, false, dt));
         CK(cudaGetLastError());

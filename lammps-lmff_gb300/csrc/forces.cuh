@@ -225,6 +225,23 @@ struct KickArgs {
   int *status;
 };
 
+// Threads per block of the one-thread-per-atom kernels: 128, halved (down to 32) while
+// the grid would give fewer than two blocks per SM.  A small system then spreads over
+// every SM instead of filling a few with four warps each: the FP64-bound kernels
+// (Tersoff, the normal-derivative assembly, the integrator) take their time from the
+// FP64 pipe of the SMs they occupy (7,200 atoms: 57 blocks of 128 on 152 SMs).
+inline int per_atom_block(int n) {
+  static const int sms = [] {
+    int d = 0, v = 0;
+    cudaGetDevice(&d);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, d);
+    return v > 0 ? v : 1;
+  }();
+  int b = 128;
+  while (b > 32 && (n + b - 1) / b < 2 * sms) b >>= 1;
+  return b;
+}
+
 // Velocity Verlet's position drift of atom q (fix_nve.cpp:89-91) on its half-kicked
 // velocity, with the double-float split of the mixed kernels refreshed; returns the
 // squared displacement since the last build.  k_nve1 and the gather's drift share it.

@@ -1998,16 +1998,17 @@ void launch_short(const ForceArgs<R> &a, const double *cutILPsq64, double tcutma
 
 void launch_tersoff(const ForceArgs<R> &a, bool ev, bool eatom, cudaStream_t s) {
   if (a.n == 0) return;
-  int g = (a.n + 127) / 128;
+  const int b = per_atom_block(a.n);
+  const int g = (a.n + b - 1) / b;
   if (a.own_perm) {
-    if (ev) k_tersoff<true, false, true><<<g, 128, 0, s>>>(a);
-    else k_tersoff<false, false, true><<<g, 128, 0, s>>>(a);
+    if (ev) k_tersoff<true, false, true><<<g, b, 0, s>>>(a);
+    else k_tersoff<false, false, true><<<g, b, 0, s>>>(a);
   } else if (ev) {
-    k_tersoff<true, false, false><<<g, 128, 0, s>>>(a);
+    k_tersoff<true, false, false><<<g, b, 0, s>>>(a);
   } else {
-    k_tersoff<false, false, false><<<g, 128, 0, s>>>(a);
+    k_tersoff<false, false, false><<<g, b, 0, s>>>(a);
   }
-  if (ev && eatom) k_ters_eatom_own<<<g, 128, 0, s>>>(a);
+  if (ev && eatom) k_ters_eatom_own<<<g, b, 0, s>>>(a);
 }
 
 template <int TPA, bool ONE>
@@ -2069,9 +2070,10 @@ void launch_ilp(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, 
 
 void launch_nderiv(const ForceArgs<R> &a, bool ev, cudaStream_t s) {
   if (a.n == 0) return;
-  int g = (a.n + 127) / 128;
-  if (ev) k_nderiv<true><<<g, 128, 0, s>>>(a);
-  else k_nderiv<false><<<g, 128, 0, s>>>(a);
+  const int b = per_atom_block(a.n);
+  const int g = (a.n + b - 1) / b;
+  if (ev) k_nderiv<true><<<g, b, 0, s>>>(a);
+  else k_nderiv<false><<<g, b, 0, s>>>(a);
 }
 
 void launch_finish(const ForceArgs<R> &a, bool eatom, const KickArgs *kick, cudaStream_t s) {

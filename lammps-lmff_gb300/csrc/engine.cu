@@ -1435,6 +1435,7 @@ struct Engine {
     // the two share the SMs and overlap; joined before the gather.  Serial when the
     // kernels are timed one by one.
     const bool fork = a.do_ters && a.do_ilp && ters_concurrent && !ktiming && ensure_stream2() == LMFF_OK;
+    a.ters_alone = !fork;
     if (fork) {
       cudaEventRecord(ev_fork, stream);
       cudaStreamWaitEvent(stream2, ev_fork, 0);

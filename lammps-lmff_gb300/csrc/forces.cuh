@@ -309,6 +309,11 @@ struct ForceArgs {
   // list entries a lane of the mixed force-only pair kernel takes per loop iteration:
   // 2 (the two-entry loop, where it applies) or 1 (the one-entry loop); a tuning knob
   int pair_tile;
+  // Tersoff runs with no pair kernel beside it (no interlayer style, or the two kernels
+  // serialised): small systems then take one lane per bond (k_tersoff_lanes); beside
+  // the pair kernel the one-thread kernel is kept, whose fewer instructions take fewer
+  // issue slots from it
+  int ters_alone;
   int kc;              // interlayer style is kolmogorov/crespi/full
 };
 

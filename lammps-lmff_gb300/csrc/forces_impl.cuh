@@ -725,6 +725,327 @@ __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
   else tersoff_atom<MAXTERS, EV, GH>(a, i, ie, cnt);
 }
 
+// ---- Tersoff with one lane per bond (small systems) ---------------------------------
+// TERS_LANES lanes per centre atom i, lane l taking bond l (an atom with more bonds runs
+// the one-thread routine on its group's first lane).  Every lane builds the geometry of
+// all of i's bonds, which the zeta and three-body loops need, then evaluates its own
+// bond: repulsion, zeta_ij, b_ij and the three-body forces on the other partners.  The
+// per-partner three-body sums and the force on i are then formed by shuffles in bond
+// order on their owner lanes, the order of the one-thread routine.  For small systems,
+// where one thread's walk over three bonds is the kernel's time, when Tersoff runs alone:
+// beside the pair kernel its four times as many threads take issue slots from it (7,200
+// atoms, per NVE step: Tersoff alone 30.3 -> 26.8 us, the two styles one after the other
+// 56.1 -> 52.5 us, side by side 41.2 -> 43.1 us).  Force-only evaluations in periodic
+// mode (the energy/virial and subdomain evaluations run k_tersoff).
+constexpr int TERS_LANES = 4;
+constexpr int TERS_LANES_MAX_ATOMS = 65536;
+__global__ void __launch_bounds__(128) k_tersoff_lanes(ForceArgs<R> a) {
+  constexpr int NB = TERS_LANES;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gtid / NB;
+  if (i >= a.n) return;   // whole groups: blockDim is a multiple of NB
+  const int wl = threadIdx.x & 31, l = wl & (NB - 1), gbase = wl & ~(NB - 1);
+  const unsigned gmask = ((1u << NB) - 1) << gbase;
+  const int ie = c_pot.t_map[info_type(__double_as_longlong(a.A.xq[i].w))];
+  const int cnt = ie < 0 ? 0 : a.ters_cnt[i];
+  if (cnt > NB) {   // the same in every lane of the group
+    if (l == 0) tersoff_atom<MAXTERS, false, false>(a, i, ie, cnt);
+    return;
+  }
+  constexpr bool F32 = sizeof(R) == 4;
+  const SysDesc &sd = a.A.sys[a.A.sysid[i]];
+  double dxd[NB], dyd[NB], dzd[NB], r64[NB], ri64[NB], rs64[NB];
+  R dx[NB], dy[NB], dz[NB], rf[NB], rl[NB];
+  float vh[NB][3], vl[NB][3];   // FP32 mode: delr as hi + lo parts
+  int el[NB];
+  uint32_t ev_[NB];
+  float cq0[NB][NB], cq1[NB][NB];   // FP32 mode: cos(theta_jik) of each bond pair as hi + lo
+#pragma unroll
+  for (int s = 0; s < NB; s++) {
+    if (s < cnt) {
+      const uint32_t e = a.ters_nb[(size_t)i * MAXTERS + s];
+      int j, sx, sy, sz;
+      decode_entry(e, a.lc, j, sx, sy, sz);
+      if constexpr (F32) {
+        // delr = x_j(image) - x_i from the double-float position parts: the hi sum is
+        // exact (a small multiple of the hi parts' ulp, one FMA), the lo sum carries the
+        // rest; |delr| as an FP32 pair from a double-float dot and one Newton step
+        const float4 hi4 = a.A.xh[i], lo4 = a.A.xl[i];
+        const float4 hj = __ldg(&a.A.xh[j]), lj = __ldg(&a.A.xl[j]);
+        const float fsx = (float)sx, fsy = (float)sy, fsz = (float)sz;
+        vh[s][0] = __fmaf_rn(fsx, sd.Lhi[0], __fsub_rn(hj.x, hi4.x));
+        vh[s][1] = __fmaf_rn(fsy, sd.Lhi[1], __fsub_rn(hj.y, hi4.y));
+        vh[s][2] = __fmaf_rn(fsz, sd.Lhi[2], __fsub_rn(hj.z, hi4.z));
+        vl[s][0] = __fmaf_rn(fsx, sd.Llo[0], __fsub_rn(lj.x, lo4.x));
+        vl[s][1] = __fmaf_rn(fsy, sd.Llo[1], __fsub_rn(lj.y, lo4.y));
+        vl[s][2] = __fmaf_rn(fsz, sd.Llo[2], __fsub_rn(lj.z, lo4.z));
+        float sh, sl;
+        df_dot3(vh[s], vl[s], vh[s], vl[s], sh, sl);
+        const float ri0 = rsqrt_ftz(sh);
+        const float r0 = __fmul_rn(sh, ri0);
+        const float corr = __fmul_rn(__fadd_rn(__fmaf_rn(-r0, r0, sh), sl), __fmul_rn(0.5f, ri0));
+        const float rh = __fadd_rn(r0, corr);
+        rf[s] = rh;
+        rl[s] = __fsub_rn(corr, __fsub_rn(rh, r0));
+        ri64[s] = (double)__fmaf_rn(__fmul_rn(-corr, ri0), ri0, ri0);
+        dx[s] = __fadd_rn(vh[s][0], vl[s][0]);
+        dy[s] = __fadd_rn(vh[s][1], vl[s][1]);
+        dz[s] = __fadd_rn(vh[s][2], vl[s][2]);
+        dxd[s] = (double)dx[s]; dyd[s] = (double)dy[s]; dzd[s] = (double)dz[s];
+        el[s] = c_pot.t_map[info_type((long long)__float_as_int(hj.w))];
+      } else {
+        double ddx, ddy, ddz;
+        disp64(a.A.xq, sd, i, j, sx, sy, sz, ddx, ddy, ddz);
+        dxd[s] = -ddx; dyd[s] = -ddy; dzd[s] = -ddz;  // delr = x_j - x_i
+        const double rs = rsq_rn(ddx, ddy, ddz);
+        rs64[s] = rs;
+        r64[s] = sqrt(rs);
+        ri64[s] = 0.0;
+        rf[s] = r64[s];
+        rl[s] = 0.0;
+        dx[s] = (R)dxd[s]; dy[s] = (R)dyd[s]; dz[s] = (R)dzd[s];
+        el[s] = c_pot.t_map[info_type(__double_as_longlong(a.A.xq[j].w))];
+      }
+      ev_[s] = e;
+    }
+  }
+  if constexpr (F32) {
+#pragma unroll
+    for (int s = 0; s < NB; s++) {
+#pragma unroll
+      for (int k = s + 1; k < NB; k++) {
+        if (k < cnt) {
+          // cos = delr_s . delr_k / (r_s r_k) in double-float: q0 + q1
+          float Dh, Dl;
+          df_dot3(vh[s], vl[s], vh[k], vl[k], Dh, Dl);
+          const float nh = __fmul_rn(rf[s], rf[k]);
+          const float nl = __fmaf_rn(rf[s], rl[k], __fmaf_rn(rl[s], rf[k], __fmaf_rn(rf[s], rf[k], -nh)));
+          const float inv = rcp_ftz(nh);
+          const float q0 = __fmul_rn(Dh, inv);
+          const float q1 = __fmul_rn(__fadd_rn(__fmaf_rn(-q0, nh, Dh), __fmaf_rn(-q0, nl, Dl)), inv);
+          cq0[s][k] = cq0[k][s] = q0;
+          cq1[s][k] = cq1[k][s] = q1;
+        }
+      }
+    }
+  }
+  // this lane's bond, in scalars (a runtime index into the bond arrays would put them in
+  // local memory)
+  double mdx = 0, mdy = 0, mdz = 0, mr64 = 0, mri64 = 0, mrs64 = 0;
+  R mxr = 0, myr = 0, mzr = 0, mrf = 1, mrl = 0;
+  int mel = 0;
+  uint32_t mev = 0;
+  float mq0[NB], mq1[NB];
+#pragma unroll
+  for (int q = 0; q < NB; q++) {
+    mq0[q] = 0.f;
+    mq1[q] = 0.f;
+  }
+#pragma unroll
+  for (int q = 0; q < NB; q++) {
+    if (q == l && q < cnt) {
+      mdx = dxd[q]; mdy = dyd[q]; mdz = dzd[q];
+      mri64 = ri64[q];
+      if constexpr (!F32) {
+        mr64 = r64[q];
+        mrs64 = rs64[q];
+      }
+      mxr = dx[q]; myr = dy[q]; mzr = dz[q];
+      mrf = rf[q]; mrl = rl[q];
+      mel = el[q];
+      mev = ev_[q];
+      if constexpr (F32) {
+#pragma unroll
+        for (int k = 0; k < NB; k++) {
+          if (k != q) {
+            mq0[k] = cq0[q][k];
+            mq1[k] = cq1[q][k];
+          }
+        }
+      }
+    }
+  }
+  const long long itag = c_pot.rep_sym ? 0 : a.tag[i];
+  double fr = 0.0, fjx = 0.0, fjy = 0.0, fjz = 0.0;
+  R fkx[NB], fky[NB], fkz[NB];   // three-body force of this bond on partner k (k != l)
+  R ajx = 0, ajy = 0, ajz = 0;   // ... on partner l
+#pragma unroll
+  for (int k = 0; k < NB; k++) fkx[k] = fky[k] = fkz[k] = R(0);
+  if (l < cnt) {
+    const int je = mel;
+    const TersP<R> &pij = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + je];
+    const R rR = mrf;
+    const double r = F32 ? (double)mrf + (double)mrl : mr64;
+    // ---- repulsion, from both ends of the bond, with the parameters of the end the
+    // reference's half list keeps
+    {
+      const TersP<R> *pr = &pij;
+      if (!c_pot.rep_sym) {
+        int j, sx, sy, sz;
+        decode_entry(mev, a.lc, j, sx, sy, sz);
+        if (!keep_half(itag, a.tag[j], sx, sy, sz)) pr = &c_pot.ters[(je * MAXELEM + ie) * MAXELEM + ie];
+      }
+      if (F32 ? rR < pr->rhi : mrs64 < pr->cutsq64) {
+        double tmp_exp, fpair, fc;
+        if constexpr (F32) {
+          tmp_exp = exp_x32f(rR, mrl, pr->nl1h, pr->nl1l);
+          if (rR < pr->rlo) {
+            fc = 1.0;
+            fpair = pr->Al1_64 * tmp_exp * mri64;
+          } else {
+            double fcd;
+            ters_fc_both64(r, *pr, fc, fcd);
+            fpair = -pr->A64 * tmp_exp * (fcd - fc * pr->lam1_64) * mri64;
+          }
+        } else {
+          double fcd;
+          ters_fc_both64(r, *pr, fc, fcd);
+          tmp_exp = exp(-pr->lam1_64 * r);
+          fpair = -pr->A64 * tmp_exp * (fcd - fc * pr->lam1_64) / r;
+        }
+        fr -= fpair;
+      }
+    }
+    if (F32 ? rR < pij.rhi : mrs64 < pij.cutsq64) {
+      // ---- zeta_ij over k
+      R zeta = 0;
+      R ufk[NB];
+#pragma unroll
+      for (int k = 0; k < NB; k++) {
+        ufk[k] = R(0);
+        if (k == l || k >= cnt) continue;
+        const TersP<R> &pk = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + el[k]];
+        const R rik = rf[k];
+        if (!(F32 ? rik < pk.rhi : rs64[k] < pk.cutsq64)) continue;
+        R ex = pk.lam3 == R(0) ? R(1) : ters_exdelr(rR, rik, pk);
+        R g;
+        if constexpr (F32) {
+          ufk[k] = __fadd_rn(__fsub_rn(pk.hhi, mq0[k]), __fsub_rn(pk.hlo, mq1[k]));
+          g = ters_g_u(ufk[k], pk);
+        } else {
+          R cost = (mxr * dx[k] + myr * dy[k] + mzr * dz[k]) / (rR * rik);
+          g = ters_gijk(cost, pk);
+        }
+        zeta += ters_fc(rik, pk) * g * ex;
+      }
+      // ---- force_zeta: radial part in FP64
+      double fa = 0.0, fa_d = 0.0;
+      if constexpr (F32) {
+        const double ex2 = exp_x32f(rR, mrl, pij.nl2h, pij.nl2l);
+        if (rR < pij.rlo) {
+          fa = -pij.B64 * ex2;
+          fa_d = pij.Bl2_64 * ex2;
+        } else {
+          double fc, fcd;
+          ters_fc_both64(r, pij, fc, fcd);
+          fa = -pij.B64 * ex2 * fc;
+          fa_d = pij.B64 * ex2 * (pij.lam2_64 * fc - fcd);
+        }
+      } else {
+        double fc, fcd;
+        ters_fc_both64(r, pij, fc, fcd);
+        if (!(r > pij.rhi64)) {
+          double ex2 = exp(-pij.lam2_64 * r);
+          fa = -pij.B64 * ex2 * fc;
+          fa_d = pij.B64 * ex2 * (pij.lam2_64 * fc - fcd);
+        }
+      }
+      double bm1;
+      R bd;
+      ters_bij_delta(zeta, pij, bm1, bd);
+      const double bij = 1.0 + bm1;
+      const double fpair = F32 ? 0.5 * bij * fa_d * mri64 : 0.5 * bij * fa_d / r;
+      const R prefactor = (R)(-0.5 * fa) * bd;
+      fr += fpair;
+      fjx = -mdx * fpair; fjy = -mdy * fpair; fjz = -mdz * fpair;
+      // ---- attractive over k -> ters_zetaterm_d, in R
+      if (prefactor != R(0)) {
+        R rinv = R(1) / rR;
+        R rhx = mxr * rinv, rhy = myr * rinv, rhz = mzr * rinv;
+#pragma unroll
+        for (int k = 0; k < NB; k++) {
+          if (k == l || k >= cnt) continue;
+          const TersP<R> &pk = c_pot.ters[(ie * MAXELEM + je) * MAXELEM + el[k]];
+          const R rik = rf[k];
+          if (!(F32 ? rik < pk.rhi : rs64[k] < pk.cutsq64)) continue;
+          R rikinv = R(1) / rik;
+          R khx = dx[k] * rikinv, khy = dy[k] * rikinv, khz = dz[k] * rikinv;
+          R fck, dfck;
+          ters_fc_both(rik, pk, fck, dfck);
+          R exd, exd_d;
+          if (pk.lam3 == R(0)) {
+            exd = R(1);
+            exd_d = R(0);
+          } else {
+            exd = ters_exdelr(rR, rik, pk);
+            exd_d = pk.powermint == 3 ? R(3) * pk.lam3 * pk.lam3 * pk.lam3 * (rR - rik) * (rR - rik) * exd
+                                      : pk.lam3 * exd;
+          }
+          R cs = rhx * khx + rhy * khy + rhz * khz;
+          R g, gd;
+          if constexpr (F32) {
+            g = ters_g_u(ufk[k], pk);
+            gd = ters_gd_u(ufk[k], pk);
+          } else {
+            g = ters_gijk(cs, pk);
+            gd = ters_gijk_d(cs, pk);
+          }
+          R djx = (-cs * rhx + khx) * rinv, djy = (-cs * rhy + khy) * rinv, djz = (-cs * rhz + khz) * rinv;
+          R dkx = (-cs * khx + rhx) * rikinv, dky = (-cs * khy + rhy) * rikinv, dkz = (-cs * khz + rhz) * rikinv;
+          R A1 = fck * gd * exd, A2 = fck * g * exd_d, A3 = dfck * g * exd;
+          fkx[k] = prefactor * (A3 * khx + A1 * dkx - A2 * khx);
+          fky[k] = prefactor * (A3 * khy + A1 * dky - A2 * khy);
+          fkz[k] = prefactor * (A3 * khz + A1 * dkz - A2 * khz);
+          ajx += prefactor * (A1 * djx + A2 * rhx);
+          ajy += prefactor * (A1 * djy + A2 * rhy);
+          ajz += prefactor * (A1 * djz + A2 * rhz);
+        }
+      }
+    }
+  }
+  // ---- per-partner three-body sums on the partner's lane, in bond order: bond s gives
+  // partner k (k != s) its fk and partner s its aj
+  R tx = 0, ty = 0, tz = 0;
+#pragma unroll
+  for (int k = 0; k < NB; k++) {
+#pragma unroll
+    for (int s = 0; s < NB; s++) {
+      const R vx = __shfl_sync(gmask, k == l ? ajx : fkx[k], gbase + s);
+      const R vy = __shfl_sync(gmask, k == l ? ajy : fky[k], gbase + s);
+      const R vz = __shfl_sync(gmask, k == l ? ajz : fkz[k], gbase + s);
+      if (l == k && s < cnt) {
+        tx += vx; ty += vy; tz += vz;
+      }
+    }
+  }
+  const double ux = (double)tx, uy = (double)ty, uz = (double)tz;
+  if (l < cnt) a.ters_g[(size_t)i * MAXTERS + l] = make_d4(fjx + ux, fjy + uy, fjz + uz, 0.0);
+  // ---- the force on i on lane 0: the radial terms, then minus the three-body totals
+  double fx = 0, fy = 0, fz = 0;
+#pragma unroll
+  for (int s = 0; s < NB; s++) {
+    const double frs = __shfl_sync(gmask, fr, gbase + s);
+    if (s < cnt) {
+      fx += dxd[s] * frs; fy += dyd[s] * frs; fz += dzd[s] * frs;
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < NB; s++) {
+    const double vx = __shfl_sync(gmask, ux, gbase + s);
+    const double vy = __shfl_sync(gmask, uy, gbase + s);
+    const double vz = __shfl_sync(gmask, uz, gbase + s);
+    if (s < cnt) {
+      fx -= vx; fy -= vy; fz -= vz;
+    }
+  }
+  if (l == 0) {
+    a.ters_f[i] = fx;
+    a.ters_f[a.n + i] = fy;
+    a.ters_f[2 * a.n + i] = fz;
+  }
+}
+
+
 // ============================================================== k_ilp ============
 // TPA lanes per atom i stride over i's interlayer list.  Per pair (del = x_i - x_j):
 //   vdW (calc_FvdW :509-533) from both ends; repulsion of term (i,j) with n_i and of
@@ -2005,6 +2326,8 @@ void launch_tersoff(const ForceArgs<R> &a, bool ev, bool eatom, cudaStream_t s) 
     else k_tersoff<false, false, true><<<g, b, 0, s>>>(a);
   } else if (ev) {
     k_tersoff<true, false, false><<<g, b, 0, s>>>(a);
+  } else if (a.ters_alone && a.n <= TERS_LANES_MAX_ATOMS) {
+    k_tersoff_lanes<<<(int)(((long long)a.n * TERS_LANES + 127) / 128), 128, 0, s>>>(a);
   } else {
     k_tersoff<false, false, false><<<g, b, 0, s>>>(a);
   }

@@ -422,6 +422,21 @@ def test_moved_atoms_rebuild_the_list(prec):
         assert abs(r["e_tersoff"] - fresh["e_tersoff"]) <= e_tol * abs(fresh["e_tersoff"])
 
 
+@pytest.mark.parametrize("prec", [capi.FP64, capi.MIXED])
+@pytest.mark.parametrize("name", ["bilayer_small", "hetero_small", "edges"])
+def test_force_only_tersoff_lanes_equal_one_thread_routine(name, prec):
+    """Small systems evaluate force-only Tersoff with one lane per bond (k_tersoff_lanes)
+    and energy/virial evaluations with one thread per atom (k_tersoff): the lanes add the
+    per-partner sums in the one-thread routine's order, so the forces agree to rounding."""
+    g = load_golden(name)
+    eng = engine_for(g, precision=prec)
+    r_ev = eng.compute(g["x"], g["type"], g["mol"], g["tag"], which=capi.TERSOFF)
+    r_f = eng.compute(g["x"], g["type"], g["mol"], g["tag"], which=capi.TERSOFF, eflag=False, vflag=False,
+                      same_atoms=True)
+    d = np.abs(r_f["f"] - r_ev["f"]).max()
+    assert d <= 1e-13 * np.abs(r_ev["f"]).max(), d
+
+
 def test_host_positions_in_another_periodic_image_need_no_rebuild():
     """A caller may pass unwrapped coordinates, or wrap some atoms between calls (LAMMPS
     does at reneighbouring): the engine takes each position in the image its list was

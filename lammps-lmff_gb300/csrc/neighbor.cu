@@ -234,11 +234,24 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
             }
             __syncwarp();
             if (!use) continue;
+            // the prefilter over the whole tile first, into a bit mask: a uniform loop, and
+            // the candidates that pass are then taken in order by each lane on its own
+            // (testing and accepting inside one loop would run the accepting path for the
+            // warp whenever any of its lanes accepts; 2.7M-atom rebuild 39.4 -> 36.0 ms.
+            // The prefilter in FP32x2 lanes, two candidates per iteration, measured slower:
+            // 37.9 ms)
+            unsigned pass = 0u;
             for (int jj = 0; jj < nj; jj++) {
+              const float4 hj = th[wl][jj];
+              const float hx = (hi.x - hj.x) - shx, hy = (hi.y - hj.y) - shy, hz = (hi.z - hj.z) - shz;
+              pass |= (hx * hx + hy * hy + hz * hz > prefilt ? 0u : 1u) << jj;   // most candidates fail
+            }
+            while (pass) {
+              const int jj = __ffs(pass) - 1;
+              pass &= pass - 1u;
               const int j = jt0 + jj;
               const float4 hj = th[wl][jj];
               const float hx = (hi.x - hj.x) - shx, hy = (hi.y - hj.y) - shy, hz = (hi.z - hj.z) - shz;
-              if (hx * hx + hy * hy + hz * hz > prefilt) continue;   // most candidates
               const float4 lj = tl[wl][jj];
               float ddx = hx + ((lo.x - lj.x) - slx);
               float ddy = hy + ((lo.y - lj.y) - sly);

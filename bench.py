@@ -23,7 +23,7 @@ With one GPU the line also carries the chosen forms' targets, measured in the sa
 plain_fp64 (the all-FP64 drop-in on the same slab), batched (256 bilayer replicas,
 batched mixed vs one-at-a-time FP64), served (the Poisson stream, the server's
 closed-loop capacity vs one-at-a-time FP64 over the whole stream, and open-loop
-p50/p99), and the benchmark spec (the ratios).  --no-north-star skips them.
+p50/p99), and form_ratios (the ratios and their targets).  --no-forms skips them.
 
 Multi-GPU: the path is run as independent replicas (one system per GPU, no data-path
 collective): value = total atom-steps of all ranks / max rank time, scaling "weak".
@@ -408,7 +408,7 @@ def main():
     ap.add_argument("--kernel-steps", type=int, default=200,
                     help="steps of the per-kernel timing run (also gives the rebuild interval)")
     ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the plain FP64 sub-record")
-    ap.add_argument("--no-north-star", action="store_true",
+    ap.add_argument("--no-forms", action="store_true",
                     help="skip the plain-FP64, batched and served sub-records")
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-chunk", type=int, default=20)
@@ -495,9 +495,9 @@ def main():
 
     # the chosen forms' targets, on one GPU: plain FP64 on the same system, batched
     # replicas and the served Poisson stream against one-at-a-time FP64
-    north = None
-    if rank == 0 and world == 1 and not args.no_north_star and args.workload == "graphite_2p7m":
-        north = north_star(args, s, elements, local, value, pk)
+    forms = None
+    if rank == 0 and world == 1 and not args.no_forms and args.workload == "graphite_2p7m":
+        forms = form_records(args, s, elements, local, value, pk)
 
     if rank == 0:
         # the pair list is what every step streams from HBM; say whether it fits in the
@@ -527,8 +527,8 @@ def main():
                 "gpu_launches": launches_total, "graph_steps_timed": m["graph_steps"],
                 "rebuilds_in_timed_region": m["rebuilds_timed"], "rebuild": m["rebuild"],
                 "kernel_ms_avg": m["kernel_ms_avg"], "list_per_atom": st["list_per_atom"]}
-        if north is not None:
-            line.update(north)
+        if forms is not None:
+            line.update(forms)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
@@ -667,7 +667,7 @@ def bench_e2e(s, prec, elements, local, args, world) -> dict:
             "path": "lmff_compute: pinned host x in, host f out, per force evaluation"}
 
 
-def north_star(args, s, elements, local, mixed_value, pk) -> dict:
+def form_records(args, s, elements, local, mixed_value, pk) -> dict:
     """Sub-records for the chosen forms' targets, measured in the same run:
     plain_fp64 -- the all-FP64 drop-in on the same slab (tpa 16, block 128, skin 1 A);
     batched -- 256 bilayer replicas, E+F+W, batched mixed vs one-at-a-time FP64;
@@ -692,7 +692,7 @@ def north_star(args, s, elements, local, mixed_value, pk) -> dict:
     out["served"] = {"open_loop": srv["open_loop"], "closed_loop": srv["closed_loop"],
                      "one_at_a_time_fp64": srv["one_at_a_time_fp64"], "config": srv["config"],
                      "capacity_vs_one_at_a_time_fp64": srv["capacity_vs_one_at_a_time_fp64"]}
-    out["north_star"] = {"mixed_vs_plain_fp64": mixed_value / v64, "target_mixed_vs_plain": 1.8,
+    out["form_ratios"] = {"mixed_vs_plain_fp64": mixed_value / v64, "target_mixed_vs_plain": 1.8,
                          "batched_vs_one_at_a_time_fp64": rep["batched_mixed_vs_one_at_a_time_fp64"],
                          "served_capacity_vs_one_at_a_time_fp64": srv["capacity_vs_one_at_a_time_fp64"],
                          "target_batched_served": 5.0}

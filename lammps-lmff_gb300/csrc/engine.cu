@@ -2566,7 +2566,7 @@ struct Engine {
       const size_t bf = sizeof(double) * 3 * (size_t)n;
       if (n >= (1 << 17) && ensure_pinned(bf) == LMFF_OK) {
         // a large batch comes back through the pinned staging block (a pageable copy is
-        // staged by the driver at a fraction of the link's rate), then into the caller's
+        // staged by the CUDA runtime at a fraction of the link's rate), then into the caller's
         // array on several host threads
         CK(cudaMemcpyAsync(h_pinned, d_fin, bf, cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));

@@ -9,7 +9,7 @@
  *   npair_full_bin_ghost.cpp:36-140    (full list incl. ghosts, rsq <= cutneighsq)
  *   pair.cpp:1554 virial_fdotr_compute, pair.cpp:913/1060 ev_tally(_xyz) per-atom energy
  *
- * TEST INFRASTRUCTURE ONLY.  This code is the checker for the CUDA engine: the parity
+ * TEST INFRASTRUCTURE ONLY.  This code is the oracle for the CUDA engine: the parity
  * tests, the smoke check and the CPU-baseline leg of the benchmark may call it; the
  * engine never does.  Its own correctness is pinned against the reference binary built
  * from the reference sources (oracle/ref.mk) through the fixtures in tests/golden/.

@@ -1,6 +1,6 @@
 """The oracle restatement against the reference's own outputs (tests/golden/*.npz, made by
 tests/golden/make_golden.py from the reference sources).  This pins the oracle: every GPU
-parity test uses it as the checker."""
+parity test compares the engine with it."""
 import numpy as np
 import pytest
 from conftest import GOLDEN_LISTS, GOLDEN_SINGLE, ILP, TERSOFF, load_golden, min_image, rel_max, rel_rms

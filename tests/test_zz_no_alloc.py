@@ -76,7 +76,7 @@ def test_noalloc_matches_compute_device_on_two_calls(name, precision):
 @pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
 def test_noalloc_leaves_free_device_memory_unchanged(precision):
     """After a first call (which looks the static array up and loads the kernels), further
-    calls change neither the driver's free-memory figure nor torch's allocator."""
+    calls change neither cudaMemGetInfo's free-memory figure nor torch's allocator."""
     import torch
     g = load_golden("hetero_small")
     eng = capi.Engine(TERSOFF, ILP, tap_flag=int(g["tap_flag"]), precision=precision)

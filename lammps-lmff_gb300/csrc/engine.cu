@@ -143,6 +143,18 @@ __global__ void k_scatter_add(int n, const int *perm, const double *fs, double *
   }
 }
 
+// fout = fin + fs in the caller's order (fout = fs without fin): k_scatter_add's sums into
+// a separate output, so that fin stays the caller's input
+__global__ void k_scatter_sum(int n, const int *perm, const double *fs, const double *fin, double *fout) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int o = perm[q];
+  for (int c = 0; c < 3; c++) {
+    double v = fs[(size_t)c * n + q];
+    fout[3 * o + c] = fin ? fin[3 * o + c] + v : v;
+  }
+}
+
 __global__ void k_scatter_add1(int n, const int *perm, const double *es, double *ein, int overwrite) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -513,6 +525,11 @@ struct Engine {
   int n = 0;
   // staging (caller order)
   double *d_xin = nullptr, *d_fin = nullptr, *d_vin = nullptr, *d_ein = nullptr;
+  double *d_fo = nullptr;   // lmff_compute's force output, d_fin keeping the caller's input
+  // pinned words the device writes back without a host wait: [0] status, [1] largest
+  // squared displacement since the build
+  unsigned long long *h_words = nullptr;
+  cudaEvent_t pend_e0 = nullptr, pend_e1 = nullptr;   // a force evaluation not waited for
   int *d_tin = nullptr, *d_sysin = nullptr;
   int64_t *d_min = nullptr, *d_gin = nullptr;
   double *d_massT = nullptr;
@@ -618,13 +635,15 @@ struct Engine {
     void *ptrs[] = {d.xq, d.xh, d.xl, d.v, d.f, d.xhold, d.tag, d.perm, d.sysid, d.mass, d.nrm64, d.nrm32, d.jrec, d.ilp_cnt,
                     d.ilp_nb, d.ters_cnt, d.ters_nb, d.ters_g, d.ters_f, d.ilp_f, d.ilp_c, d.ilp_g, d.list_off, d.list,
                     d.short_cnt, d.short_nb, d.list_img, d.nin_tmp, d.list_tmp, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.rowocc, d.cub_tmp,
-                    d.cnt_tmp, d.sys, d.red_out, d.status, d.maxdisp, d_xin, d_fin, d_vin, d_ein, d_tin, d_sysin,
+                    d.cnt_tmp, d.sys, d.red_out, d.status, d.maxdisp, d_xin, d_fin, d_fo, d_vin, d_ein, d_tin, d_sysin,
                     d_min, d_gin, d_massT, xq2, v2, mass2, tag2, perm2, sysid2, stat_ilp, stat_ters, eatom_ilp,
                     eatom_ters, ke, d_arrs, d_karrs, d_kout, d_cutILPsq, d_maxpred};
     for (void *p : ptrs)
       if (p) cudaFree(p);
     d = DevState();
-    d_xin = d_fin = d_vin = d_ein = nullptr;
+    d_xin = d_fin = d_fo = d_vin = d_ein = nullptr;
+    if (h_words) cudaFreeHost(h_words);
+    h_words = nullptr;
     d_tin = d_sysin = nullptr;
     d_min = d_gin = nullptr;
     d_massT = nullptr;
@@ -923,6 +942,7 @@ struct Engine {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaMalloc(&d.status, sizeof(int)));
     CK(cudaMalloc(&d.maxdisp, sizeof(unsigned long long)));
+    CK(cudaMallocHost(&h_words, 8 * sizeof(unsigned long long)));
     CK(cudaMalloc(&d_maxpred, 3 * sizeof(unsigned long long)));
     CK(cudaMemsetAsync(d_maxpred, 0, 3 * sizeof(unsigned long long), stream));
     CK(cudaMalloc(&d_cutILPsq, sizeof(double) * MAXELEM * MAXELEM));
@@ -998,6 +1018,7 @@ struct Engine {
     CK(dalloc(d.bin_key, c)); CK(dalloc(d.bin_key2, c)); CK(dalloc(d.idx, c)); CK(dalloc(d.idx2, c));
     CK(dalloc(d.cnt_tmp, (size_t)c + 1));
     CK(dalloc(d_xin, 3 * (size_t)c)); CK(dalloc(d_fin, 3 * (size_t)c)); CK(dalloc(d_vin, 3 * (size_t)c));
+    CK(dalloc(d_fo, 3 * (size_t)c));
     CK(dalloc(d_ein, c)); CK(dalloc(d_tin, c)); CK(dalloc(d_sysin, c)); CK(dalloc(d_min, c)); CK(dalloc(d_gin, c));
     // CUB temporary storage for the sort (32 key bits) and the scan
     size_t tb = nb_sort_tmp_bytes(c, 32);
@@ -1457,7 +1478,9 @@ struct Engine {
   }
 
   // forces (+ energies/virials per system into hres when ev) on the resident state
-  int forces(int which, bool ev, bool eatom, std::vector<lmff_result> *hres) {
+  // wait = false (force-only evaluations): the status word comes back into a pinned word
+  // and the caller waits once for everything it queued, then calls forces_done
+  int forces(int which, bool ev, bool eatom, std::vector<lmff_result> *hres, bool wait = true) {
     int rc = push_consts();
     if (rc) return rc;
     if (!built) {
@@ -1508,6 +1531,12 @@ struct Engine {
       CK(cudaGetLastError());
     }
     cudaEventRecord(e1, stream);
+    if (!wait && !ev && !hres) {
+      pend_e0 = e0;
+      pend_e1 = e1;
+      CK(cudaMemcpyAsync(h_words, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      return LMFF_OK;
+    }
     int st = 0;
     CK(cudaMemcpyAsync(&st, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
     std::vector<double> red;
@@ -1541,6 +1570,20 @@ struct Engine {
       }
       if (ev) last_res = *hres;
     }
+    return LMFF_OK;
+  }
+  // the end of a force evaluation queued with wait = false, after the caller's wait
+  int forces_done() {
+    harvest();
+    float ms = 0;
+    cudaEventElapsedTime(&ms, pend_e0, pend_e1);
+    cudaEventDestroy(pend_e0);
+    cudaEventDestroy(pend_e1);
+    pend_e0 = pend_e1 = nullptr;
+    ms_forces = ms;
+    const int st = (int)*reinterpret_cast<const int *>(h_words);
+    if (st) return status_error(st);
+    forces_valid = true;
     return LMFF_OK;
   }
   bool hilo_fresh = false;
@@ -1612,7 +1655,8 @@ struct Engine {
     return LMFF_OK;
   }
 
-  int apply_positions(int nn, bool reload) {
+  // test: rebuild now if an atom moved more than skin/2 (else the caller tests later)
+  int apply_positions(int nn, bool reload, bool test = true) {
     if (reload) {
       if (!mass_type.empty()) {
         if (!d_massT) CK(cudaMalloc(&d_massT, sizeof(double) * (MAXTYPE + 1)));
@@ -1632,7 +1676,7 @@ struct Engine {
       hilo_all();
       hilo_fresh = true;
     }
-    return maybe_rebuild();
+    return test ? maybe_rebuild() : LMFF_OK;
   }
 
   int compute_host(int nn, const double *x, const int *type, const int64_t *mol, const int64_t *tag, int which,
@@ -1640,6 +1684,7 @@ struct Engine {
     bool reload = false;
     int rc = stage_host(nn, x, type, mol, tag, (which & LMFF_SAME_ATOMS) != 0, reload);
     if (rc) return rc;
+    if (!reload && nn > 0 && f && !eatom && !eflag && !vflag) return compute_forces_one_wait(nn, which, f, res);
     rc = apply_positions(nn, reload);
     if (rc) return rc;
     std::vector<lmff_result> hr;
@@ -1659,6 +1704,47 @@ struct Engine {
       CK(cudaMemcpyAsync(eatom, d_ein, sizeof(double) * nn, cudaMemcpyDeviceToHost, stream));
     }
     CK(cudaStreamSynchronize(stream));
+    return LMFF_OK;
+  }
+
+  // Forces only, on loaded atoms (a pair style's call on most steps), with one host wait.
+  // The list test comes after the evaluation: the forces run on the current list at once
+  // and the largest displacement since the build comes back with them.  In the rare call
+  // where an atom moved more than skin/2 the list is rebuilt and the evaluation repeated
+  // (the first result is discarded; the caller's input forces stay in d_fin meanwhile).
+  int compute_forces_one_wait(int nn, int which, double *f, lmff_result *res) {
+    int rc = apply_positions(nn, false, false);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h_words + 1, d.maxdisp, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
+    rc = forces(which, false, false, nullptr, false);
+    if (rc) return rc;
+    const bool overwrite = (which & LMFF_OVERWRITE) != 0;
+    if (!overwrite) CK(cudaMemcpyAsync(d_fin, f, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, stream));
+    k_scatter_sum<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, d.f, overwrite ? nullptr : d_fin, d_fo);
+    CK(cudaMemcpyAsync(f, d_fo, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    double d2;
+    memcpy(&d2, h_words + 1, sizeof d2);
+    if (!(d2 > 0.25 * skin * skin)) {
+      rc = forces_done();
+      if (rc) return rc;
+    } else {
+      // the list did not cover these positions: the evaluation (and any status it
+      // raised) is discarded
+      harvest();
+      cudaEventDestroy(pend_e0);
+      cudaEventDestroy(pend_e1);
+      pend_e0 = pend_e1 = nullptr;
+      CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
+      rc = rebuild();
+      if (rc) return rc;
+      rc = forces(which, false, false, nullptr);
+      if (rc) return rc;
+      k_scatter_sum<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, d.f, overwrite ? nullptr : d_fin, d_fo);
+      CK(cudaMemcpyAsync(f, d_fo, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost, stream));
+      CK(cudaStreamSynchronize(stream));
+    }
+    if (res) memset(res, 0, sizeof *res);
     return LMFF_OK;
   }
 

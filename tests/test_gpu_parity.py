@@ -395,10 +395,12 @@ def test_step_graph_overflow_redo():
         assert abs(a["etotal"] - b["etotal"]) <= 1e-10 * abs(b["etotal"])
 
 
+@pytest.mark.parametrize("ev", [True, False])
 @pytest.mark.parametrize("prec", [capi.FP64, capi.MIXED])
-def test_moved_atoms_rebuild_the_list(prec):
+def test_moved_atoms_rebuild_the_list(prec, ev):
     """lmff_compute on already loaded atoms (LMFF_SAME_ATOMS) rebuilds the list when an
-    atom moved past skin/2 since the last build and only then.  Either way the
+    atom moved past skin/2 since the last build and only then (force-only calls test the
+    displacement after the evaluation and redo it on a rebuilt list).  Either way the
     accumulated forces (input f + forces) equal a fresh engine's, energies too."""
     g = load_golden("bilayer_small")
     eng = engine_for(g, precision=prec)
@@ -408,18 +410,21 @@ def test_moved_atoms_rebuild_the_list(prec):
     x1 = np.array(g["x"])
     x1[5, 2] += 0.25 * skin                            # out of plane, |d| = skin / 4: no rebuild
     f_in = np.random.default_rng(3).normal(0.0, 1.0, x1.shape)
-    r1 = eng.compute(x1, g["type"], g["mol"], g["tag"], f=f_in.copy(), same_atoms=True)
+    r1 = eng.compute(x1, g["type"], g["mol"], g["tag"], f=f_in.copy(), same_atoms=True, eflag=ev, vflag=ev)
     assert eng.stats()["rebuilds"] == rb
     x2 = x1 + [0.6 * skin, 0.25 * skin, 0.0]           # rigid shift, |d| > skin / 2: rebuild
-    r2 = eng.compute(x2, g["type"], g["mol"], g["tag"], f=f_in.copy(), same_atoms=True)
+    r2 = eng.compute(x2, g["type"], g["mol"], g["tag"], f=f_in.copy(), same_atoms=True, eflag=ev, vflag=ev)
     assert eng.stats()["rebuilds"] == rb + 1
     f_tol = F64_TOL * 10.0 if prec == capi.FP64 else MIX_F_ABS   # eV/A; the sums run in another order
     e_tol = 1e-12 if prec == capi.FP64 else MIX_E_REL
     for x, r in ((x1, r1), (x2, r2)):
         fresh = engine_for(g, precision=prec).compute(x, g["type"], g["mol"], g["tag"])
         assert np.abs(r["f"] - f_in - fresh["f"]).max() <= f_tol
-        assert abs(r["e_ilp"] - fresh["e_ilp"]) <= e_tol * abs(fresh["e_ilp"])
-        assert abs(r["e_tersoff"] - fresh["e_tersoff"]) <= e_tol * abs(fresh["e_tersoff"])
+        if ev:
+            assert abs(r["e_ilp"] - fresh["e_ilp"]) <= e_tol * abs(fresh["e_ilp"])
+            assert abs(r["e_tersoff"] - fresh["e_tersoff"]) <= e_tol * abs(fresh["e_tersoff"])
+        else:
+            assert r["e_ilp"] == 0.0 and r["e_tersoff"] == 0.0
 
 
 @pytest.mark.parametrize("prec", [capi.FP64, capi.MIXED])

@@ -304,6 +304,121 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
   }
 }
 
+
+// One warp per atom, for small systems: the lanes take 32 consecutive candidates of the
+// atom's stencil at a time (the bins and the order of k_list's walk for that atom), and
+// ballots give every accepted entry its place -- inner entries from the front, the skin
+// shell from the back, short candidates in order -- so the lists equal k_list's entry for
+// entry.  k_list's warp walks its 32 atoms' stencils one candidate at a time, a serial
+// chain that the few warps of a small system cannot hide (7,200 atoms: 225 warps, about
+// 0.5 ms per build).
+constexpr int LIST_ATOM_MAX_ATOMS = 16384;
+template <int MODE>
+__global__ void __launch_bounds__(128) k_list_atom(NbArgs a) {
+  constexpr bool FILL = MODE != 0;
+  const int i = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= a.n) return;   // whole warps
+  const unsigned FULL = 0xffffffffu, below = (1u << lane) - 1u;
+  const SysDesc &sd = a.sys[a.sysid[i]];
+  const int lb = (int)(a.bin_key[i] >> KEY_MOL_BITS) - sd.bin_begin;
+  const int bx = lb % sd.nb[0], by = (lb / sd.nb[0]) % sd.nb[1], bz = lb / (sd.nb[0] * sd.nb[1]);
+  const float4 hi = a.xh[i], lo = a.xl[i];
+  const int infoi = __float_as_int(hi.w);
+  const int ti = infoi & 255;
+  const int mi = infoi >> 8;
+  const int ilp_i = c_nb.ilp_mapped[ti];
+  const float prefilt = sd.prefilt_sq;
+  int nlong = 0, nin = 0, nsh = 0, nshort = 0;
+  bool img = false;
+  const int64_t base = MODE == 1 ? a.list_off[i] : MODE == 2 ? (int64_t)i * a.stride : 0;
+  const int64_t lend = MODE == 1 ? a.list_off[i + 1] : MODE == 2 ? base + a.stride : 0;
+  uint32_t *const dst = MODE == 2 ? a.tmp : a.list;
+  const int64_t dcap = MODE == 2 ? (int64_t)a.n * a.stride : a.list_cap;
+  for (int dz = -sd.reach[2]; dz <= sd.reach[2]; dz++) {
+    int jz = bz + dz, sz = 0;
+    if (sd.per[2]) {
+      sz = jz >= 0 ? jz / sd.nb[2] : -((-jz + sd.nb[2] - 1) / sd.nb[2]);
+      jz -= sz * sd.nb[2];
+    } else if (jz < 0 || jz >= sd.nb[2]) continue;
+    for (int dy = -sd.reach[1]; dy <= sd.reach[1]; dy++) {
+      int jy = by + dy, sy = 0;
+      if (sd.per[1]) {
+        sy = jy >= 0 ? jy / sd.nb[1] : -((-jy + sd.nb[1] - 1) / sd.nb[1]);
+        jy -= sy * sd.nb[1];
+      } else if (jy < 0 || jy >= sd.nb[1]) continue;
+      if (a.rowocc && !a.rowocc[sd.bin_begin + (jz * sd.nb[1] + jy) * sd.nb[0]]) continue;   // empty row
+      for (int xu = bx - sd.reach[0]; xu <= bx + sd.reach[0]; xu++) {
+        int jx = xu, sx = 0;
+        if (sd.per[0]) {
+          sx = jx >= 0 ? jx / sd.nb[0] : -((-jx + sd.nb[0] - 1) / sd.nb[0]);
+          jx -= sx * sd.nb[0];
+        } else if (jx < 0 || jx >= sd.nb[0]) continue;
+        const int gbj = sd.bin_begin + (jz * sd.nb[1] + jy) * sd.nb[0] + jx;
+        const int jstart = a.bin_start[gbj], jend = a.bin_end[gbj];
+        const float shx = (float)sx * sd.Lhi[0], shy = (float)sy * sd.Lhi[1], shz = (float)sz * sd.Lhi[2];
+        const float slx = (float)sx * sd.Llo[0], sly = (float)sy * sd.Llo[1], slz = (float)sz * sd.Llo[2];
+        const bool self_image = (sx | sy | sz) == 0;
+        for (int j0 = jstart; j0 < jend; j0 += 32) {
+          const int j = j0 + lane;
+          bool take_long = false, inner = false, take_short = false;
+          if (j < jend) {
+            const float4 hj = a.xh[j];
+            const float hx = (hi.x - hj.x) - shx, hy = (hi.y - hj.y) - shy, hz = (hi.z - hj.z) - shz;
+            if (!(hx * hx + hy * hy + hz * hz > prefilt)) {
+              const float4 lj = a.xl[j];
+              float ddx = hx + ((lo.x - lj.x) - slx);
+              float ddy = hy + ((lo.y - lj.y) - sly);
+              float ddz = hz + ((lo.z - lj.z) - slz);
+              float rsq = ddx * ddx + ddy * ddy + ddz * ddz;
+              const int infoj = __float_as_int(hj.w);
+              const int tj = infoj & 255;
+              const int mj = infoj >> 8;
+              const int tt = ti * (MAXTYPE + 1) + tj;
+              if ((a.full || (mj != mi && ilp_i && c_nb.ilp_mapped[tj])) && !(self_image && j == i))
+                take_long = le_exact(rsq, c_nb.cutnsq_f[tt], c_nb.cutnsq_d[tt], a.xq, sd, i, j, sx, sy, sz);
+              inner = rsq < c_nb.innersq_f;
+              if (MODE != 1 && !(self_image && j == i))
+                take_short = le_exact(rsq, c_nb.rshortsq_f, c_nb.rshortsq_d, a.xq, sd, i, j, sx, sy, sz);
+            }
+          }
+          const unsigned bin_ = __ballot_sync(FULL, take_long && inner);
+          const unsigned bsh_ = __ballot_sync(FULL, take_long && !inner);
+          if (FILL && take_long) {
+            const int64_t pos = inner ? base + nin + __popc(bin_ & below) : lend - 1 - (nsh + __popc(bsh_ & below));
+            if (pos >= base && pos < lend && pos < dcap) dst[pos] = encode_entry(j, sx, sy, sz, a.lc);
+          }
+          if (MODE != 1) {
+            const unsigned bs = __ballot_sync(FULL, take_short);
+            if (take_short) {
+              const int q = nshort + __popc(bs & below);
+              if (q < MAXSHORT) a.short_nb[(size_t)i * MAXSHORT + q] = encode_entry(j, sx, sy, sz, a.lc);
+            }
+            nshort += __popc(bs);
+          }
+          nin += __popc(bin_);
+          nsh += __popc(bsh_);
+          nlong += __popc(bin_ | bsh_);
+          if ((bin_ | bsh_) && !self_image) img = true;
+        }
+      }
+    }
+  }
+  if (lane != 0) return;
+  if (MODE != 1) {
+    a.cnt[i] = nlong;
+    a.short_cnt[i] = nshort < MAXSHORT ? nshort : MAXSHORT;
+    if (nshort > MAXSHORT) atomicOr(a.status, ST_SHORT_OVERFLOW);
+    if (a.maxcnt) atomicMax(a.maxcnt, nlong);
+  }
+  if (MODE != 0) a.img[i] = img;
+  if (MODE == 1 && base + nlong > a.list_cap) atomicOr(a.status, ST_LIST_OVERFLOW);
+  if (MODE == 2) {
+    a.nin[i] = nin;
+    if (nlong > a.stride) atomicOr(a.status, ST_STRIDE_OVERFLOW | ST_LIST_OVERFLOW);
+  }
+}
+
 // Strided buffer -> CSR list, one warp per atom: the entries inside the cutoff, then the
 // shell (kept at the end of the atom's slice, in the order MODE 1 writes them), so the
 // list equals MODE 1's.  Does nothing after a stride overflow (the host then fills).
@@ -385,6 +500,13 @@ void nb_hilo(int n, const d4 *xq, const SysDesc *sys, const int *sysid, float4 *
 
 void nb_list(const NbArgs &a, int mode, cudaStream_t s) {
   if (!a.n) return;
+  if (a.n <= LIST_ATOM_MAX_ATOMS) {
+    const int ga = (int)(((int64_t)a.n * 32 + 127) / 128);
+    if (mode == 1) k_list_atom<1><<<ga, 128, 0, s>>>(a);
+    else if (mode == 2) k_list_atom<2><<<ga, 128, 0, s>>>(a);
+    else k_list_atom<0><<<ga, 128, 0, s>>>(a);
+    return;
+  }
   const int g = (a.n + 32 * LW - 1) / (32 * LW);
   if (mode == 1) k_list<1><<<g, 32 * LW, 0, s>>>(a);
   else if (mode == 2) k_list<2><<<g, 32 * LW, 0, s>>>(a);

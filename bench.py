@@ -462,7 +462,8 @@ def main():
         # small systems also try 32 threads per atom: the pair kernel's time there is one
         # thread's walk over its share of the list
         tuned = tune.tune(s, TERSOFF_FILE, ILP_FILE, elements=elements, precision=prec, device=local,
-                          tpas=(8, 16, 32) if s.n < 100_000 else (8, 16), blocks=(128, 256), skins=(1.0, 2.0),
+                          tpas=(8, 16, 32) if s.n < 100_000 else (8, 16), blocks=(128, 256),
+                          skins=(1.0, 1.5, 2.0) if s.n < 100_000 else (1.0, 2.0),
                           use_cache=False, n_full=s.n, tiles=(2, 1))
         args.tpa = args.tpa or tuned["tpa"]
         args.block = args.block or tuned["block"]

@@ -311,8 +311,10 @@ __global__ void __launch_bounds__(32 * LW) k_list(NbArgs a) {
 // shell from the back, short candidates in order -- so the lists equal k_list's entry for
 // entry.  k_list's warp walks its 32 atoms' stencils one candidate at a time, a serial
 // chain that the few warps of a small system cannot hide (7,200 atoms: 225 warps, about
-// 0.5 ms per build).
-constexpr int LIST_ATOM_MAX_ATOMS = 16384;
+// 0.5 ms per build).  Per build, this kernel against k_list: 7,200-atom bilayer 0.26 vs
+// 0.62 ms, 36,800-atom graphite 1.61 vs 1.94 ms, 331,200-atom graphite 12.8 vs 5.2 ms
+// (there k_list's shared tiles save most candidate loads).
+constexpr int LIST_ATOM_MAX_ATOMS = 40000;
 template <int MODE>
 __global__ void __launch_bounds__(128) k_list_atom(NbArgs a) {
   constexpr bool FILL = MODE != 0;

@@ -2131,87 +2131,123 @@ __global__ void k_finish(ForceArgs<R> a, KickArgs kick) {
 
 // k_finish with FINISH_LANES lanes per atom, for small systems whose few threads cannot
 // hide k_finish's chains of dependent loads (the reverse search of each partner's list).
-// The atom's gather items (its Tersoff partners, then its intralayer candidates) are
-// dealt out to the lanes, one item per lane and round; lane 0 adds the items' values in
-// item order, so the forces are the one-lane kernel's to the bit.
+// A block takes FINISH_ATOMS atoms.  The atom's gather items (its Tersoff partners, then
+// its intralayer candidates) are dealt out to its lanes, one item per lane and round, and
+// staged in shared memory; then one thread per atom -- a full warp for the block's atoms,
+// since GB300 issues an FP64 instruction for the whole warp whatever lanes are active --
+// adds them in item order and applies the kick, so the forces are the one-lane
+// kernel's to the bit.
 constexpr int FINISH_LANES = 8;
+constexpr int FINISH_ATOMS = 32;
 constexpr int FINISH_LANES_MAX_ATOMS = 65536;
 template <bool EATOM, bool KICK>
-__global__ void k_finish_lanes(ForceArgs<R> a, KickArgs kick) {
-  constexpr int L = FINISH_LANES;
-  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = gtid / L;
-  if (i >= a.n) return;   // whole groups: blockDim is a multiple of L
-  const int wl = threadIdx.x & 31, l = wl & (L - 1), gbase = wl & ~(L - 1);
-  const unsigned gmask = ((1u << L) - 1) << gbase;
+__global__ void __launch_bounds__(FINISH_LANES * FINISH_ATOMS) k_finish_lanes(ForceArgs<R> a, KickArgs kick) {
+  constexpr int L = FINISH_LANES, NA = FINISH_ATOMS, NV = EATOM ? 4 : 3;
+  __shared__ double sv[NA][L][NV];
+  __shared__ int sf[NA][L];
+  __shared__ int stot[NA], snt[NA];
+  __shared__ int srounds;
+  const int t = threadIdx.x, al = t / L, l = t % L;
+  const int i = blockIdx.x * NA + al;
+  const bool act = i < a.n;
   const bool sym = c_pot.ilp_cut_sym != 0;
-  const int nt = a.do_ters ? a.ters_cnt[i] : 0;
-  const int ni = a.do_ilp ? (sym ? a.ilp_cnt[i] : a.short_cnt[i]) : 0;
-  const uint32_t *cand = sym ? a.ilp_nb + (size_t)i * MAXILP : a.short_nb + (size_t)i * MAXSHORT;
-  const long long mi = (sym || !a.do_ilp) ? 0 : info_mol(__double_as_longlong(a.A.xq[i].w));
-  double Fx = 0, Fy = 0, Fz = 0, ea = 0;
-  if (l == 0) {
-    if (a.do_ilp) {
-      Fx += a.ilp_f[i]; Fy += a.ilp_f[a.n + i]; Fz += a.ilp_f[2 * a.n + i];
-    }
-    if (a.do_ters) {
-      Fx += a.ters_f[i]; Fy += a.ters_f[a.n + i]; Fz += a.ters_f[2 * a.n + i];
-    }
+  int nt = 0, ni = 0;
+  const uint32_t *cand = nullptr;
+  long long mi = 0;
+  if (act) {
+    nt = a.do_ters ? a.ters_cnt[i] : 0;
+    ni = a.do_ilp ? (sym ? a.ilp_cnt[i] : a.short_cnt[i]) : 0;
+    cand = sym ? a.ilp_nb + (size_t)i * MAXILP : a.short_nb + (size_t)i * MAXSHORT;
+    mi = (sym || !a.do_ilp) ? 0 : info_mol(__double_as_longlong(a.A.xq[i].w));
   }
   const int tot = nt + ni;
-  for (int q0 = 0; q0 < tot; q0 += L) {
-    const int q = q0 + l;
+  if (l == 0) {
+    stot[al] = tot;
+    snt[al] = nt;
+  }
+  __syncthreads();
+  if (t < 32) {   // the block's rounds: its largest item count
+    int m = t < NA ? stot[t] : 0;
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (t == 0) srounds = (m + L - 1) / L;
+  }
+  // the adding thread of atom i2 (threads t < NA)
+  const int i2 = blockIdx.x * NA + t;
+  const bool adder = t < NA && i2 < a.n;
+  double Fx = 0, Fy = 0, Fz = 0, ea = 0;
+  int tot2 = 0, nt2 = 0;
+  if (adder) {
+    if (a.do_ilp) {
+      Fx += a.ilp_f[i2]; Fy += a.ilp_f[a.n + i2]; Fz += a.ilp_f[2 * a.n + i2];
+    }
+    if (a.do_ters) {
+      Fx += a.ters_f[i2]; Fy += a.ters_f[a.n + i2]; Fz += a.ters_f[2 * a.n + i2];
+    }
+  }
+  __syncthreads();
+  if (adder) {
+    tot2 = stot[t];
+    nt2 = snt[t];
+  }
+  const int rounds = srounds;
+  for (int r = 0; r < rounds; r++) {
+    const int q = r * L + l;
     int found = 0;
     d4 g = make_d4(0.0, 0.0, 0.0, 0.0);
-    if (q < nt) {
+    if (act && q < nt) {
       int j, sx, sy, sz;
       decode_entry(a.ters_nb[(size_t)i * MAXTERS + q], a.lc, j, sx, sy, sz);
       const uint32_t want = encode_entry(i, -sx, -sy, -sz, a.lc);
       const int cj = a.ters_cnt[j];
-      for (int t = 0; t < cj; t++) {
-        if (a.ters_nb[(size_t)j * MAXTERS + t] == want) {
-          g = a.ters_g[(size_t)j * MAXTERS + t];
+      for (int u = 0; u < cj; u++) {
+        if (a.ters_nb[(size_t)j * MAXTERS + u] == want) {
+          g = a.ters_g[(size_t)j * MAXTERS + u];
           found = 1;
           break;
         }
       }
-    } else if (q < tot) {
+    } else if (act && q < tot) {
       int j, sx, sy, sz;
       decode_entry(cand[q - nt], a.lc, j, sx, sy, sz);
       const int cj = a.ilp_cnt[j];
       if (cj > 0 && (sym || info_mol(__double_as_longlong(a.A.xq[j].w)) == mi)) {
         const uint32_t want = encode_entry(i, -sx, -sy, -sz, a.lc);
-        for (int t = 0; t < cj; t++) {
-          if (a.ilp_nb[(size_t)j * MAXILP + t] == want) {
-            g = a.ilp_c[(size_t)j * MAXILP + t];
+        for (int u = 0; u < cj; u++) {
+          if (a.ilp_nb[(size_t)j * MAXILP + u] == want) {
+            g = a.ilp_c[(size_t)j * MAXILP + u];
             found = 1;
             break;
           }
         }
       }
     }
-    const int nr = min(L, tot - q0);
-    for (int k = 0; k < nr; k++) {
-      const int fk = __shfl_sync(gmask, found, gbase + k);
-      const double gx = __shfl_sync(gmask, g.x, gbase + k);
-      const double gy = __shfl_sync(gmask, g.y, gbase + k);
-      const double gz = __shfl_sync(gmask, g.z, gbase + k);
-      const double gw = EATOM ? __shfl_sync(gmask, g.w, gbase + k) : 0.0;
-      if (l == 0 && fk) {
-        Fx += gx; Fy += gy; Fz += gz;
-        if (EATOM && q0 + k < nt) ea += 0.5 * gw;
+    sv[al][l][0] = g.x;
+    sv[al][l][1] = g.y;
+    sv[al][l][2] = g.z;
+    if (EATOM) sv[al][l][NV - 1] = g.w;
+    sf[al][l] = found;
+    __syncthreads();
+    if (adder) {
+#pragma unroll
+      for (int k = 0; k < L; k++) {
+        const int qq = r * L + k;
+        if (qq < tot2 && sf[t][k]) {
+          Fx += sv[t][k][0]; Fy += sv[t][k][1]; Fz += sv[t][k][2];
+          if (EATOM && qq < nt2) ea += 0.5 * sv[t][k][NV - 1];
+        }
       }
     }
+    __syncthreads();
   }
-  if (l != 0) return;
-  a.f_out[i] = Fx;
-  a.f_out[a.n + i] = Fy;
-  a.f_out[2 * a.n + i] = Fz;
-  if constexpr (KICK) kick_atom(kick, a, i, Fx, Fy, Fz);
+  if (!adder) return;
+  a.f_out[i2] = Fx;
+  a.f_out[a.n + i2] = Fy;
+  a.f_out[2 * a.n + i2] = Fz;
+  if constexpr (KICK) kick_atom(kick, a, i2, Fx, Fy, Fz);
   if (EATOM) {
-    double e = a.do_ters ? a.eatom_ters[i] + ea : 0.0;
-    if (a.do_ilp) e += a.eatom_ilp[i];
-    a.eatom_ters[i] = e;
+    double e = a.do_ters ? a.eatom_ters[i2] + ea : 0.0;
+    if (a.do_ilp) e += a.eatom_ilp[i2];
+    a.eatom_ters[i2] = e;
   }
 }
 
@@ -2405,11 +2441,11 @@ void launch_finish(const ForceArgs<R> &a, bool eatom, const KickArgs *kick, cuda
   KickArgs k{};
   if (kick) k = *kick;
   if (a.n <= FINISH_LANES_MAX_ATOMS) {
-    const int gl = (int)(((long long)a.n * FINISH_LANES + 127) / 128);
-    if (kick && !eatom) k_finish_lanes<false, true><<<gl, 128, 0, s>>>(a, k);
-    else if (kick) k_finish_lanes<true, true><<<gl, 128, 0, s>>>(a, k);
-    else if (eatom) k_finish_lanes<true, false><<<gl, 128, 0, s>>>(a, k);
-    else k_finish_lanes<false, false><<<gl, 128, 0, s>>>(a, k);
+    const int gl = (a.n + FINISH_ATOMS - 1) / FINISH_ATOMS, bl = FINISH_LANES * FINISH_ATOMS;
+    if (kick && !eatom) k_finish_lanes<false, true><<<gl, bl, 0, s>>>(a, k);
+    else if (kick) k_finish_lanes<true, true><<<gl, bl, 0, s>>>(a, k);
+    else if (eatom) k_finish_lanes<true, false><<<gl, bl, 0, s>>>(a, k);
+    else k_finish_lanes<false, false><<<gl, bl, 0, s>>>(a, k);
     return;
   }
   if (kick && !eatom) k_finish<false, true><<<g, 128, 0, s>>>(a, k);

@@ -38,6 +38,7 @@ namespace lmff {
   void launch_tersoff(const ForceArgs<R> &a, bool ev, bool eatom, cudaStream_t s);                        \
   void launch_ilp(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, bool one_element,       \
                   cudaStream_t s);                                                                         \
+  void launch_nframe(const ForceArgs<R> &a, cudaStream_t s);                                               \
   void launch_nderiv(const ForceArgs<R> &a, bool ev, cudaStream_t s);                                      \
   void launch_finish(const ForceArgs<R> &a, bool eatom, const KickArgs *kick, cudaStream_t s);             \
   }
@@ -547,7 +548,8 @@ struct Engine {
   int stride = 0;
   int *d_maxcnt = nullptr;
   cudaStream_t stream2 = nullptr;   // Tersoff beside the pair kernel
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t stream3 = nullptr;   // the normal frames beside both
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_frame = nullptr;
   bool ters_concurrent = true;      // option "ters_concurrent"
   double *h_pinned = nullptr;   // batch staging (lmff_batch_set)
   size_t h_pinned_bytes = 0;
@@ -633,7 +635,7 @@ struct Engine {
   void release() {
     if (device >= 0) cudaSetDevice(device);
     void *ptrs[] = {d.xq, d.xh, d.xl, d.v, d.f, d.xhold, d.tag, d.perm, d.sysid, d.mass, d.nrm64, d.nrm32, d.jrec, d.ilp_cnt,
-                    d.ilp_nb, d.ters_cnt, d.ters_nb, d.ters_g, d.ters_f, d.ilp_f, d.ilp_c, d.ilp_g, d.list_off, d.list,
+                    d.ilp_nb, d.ters_cnt, d.ters_nb, d.ters_g, d.ters_f, d.ilp_f, d.ilp_c, d.ilp_g, d.nframe, d.list_off, d.list,
                     d.short_cnt, d.short_nb, d.list_img, d.nin_tmp, d.list_tmp, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.rowocc, d.cub_tmp,
                     d.cnt_tmp, d.sys, d.red_out, d.status, d.maxdisp, d_xin, d_fin, d_fo, d_vin, d_ein, d_tin, d_sysin,
                     d_min, d_gin, d_massT, xq2, v2, mass2, tag2, perm2, sysid2, stat_ilp, stat_ters, eatom_ilp,
@@ -689,9 +691,12 @@ struct Engine {
     m_cap = 0;
     if (stream2) cudaStreamDestroy(stream2);
     stream2 = nullptr;
+    if (stream3) cudaStreamDestroy(stream3);
+    stream3 = nullptr;
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
-    ev_fork = ev_join = nullptr;
+    if (ev_frame) cudaEventDestroy(ev_frame);
+    ev_fork = ev_join = ev_frame = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
   }
@@ -1011,6 +1016,7 @@ struct Engine {
     CK(dalloc(d.ters_cnt, c)); CK(dalloc(d.ters_nb, (size_t)c * MAXTERS));
     CK(dalloc(d.ters_g, (size_t)c * MAXTERS)); CK(dalloc(d.ters_f, 3 * (size_t)c));
     CK(dalloc(d.ilp_f, 3 * (size_t)c)); CK(dalloc(d.ilp_c, (size_t)c * MAXILP)); CK(dalloc(d.ilp_g, c));
+    CK(dalloc(d.nframe, 4 * (size_t)c));
     CK(dalloc(stat_ilp, 8 * (size_t)c)); CK(dalloc(stat_ters, 8 * (size_t)c));
     CK(dalloc(eatom_ilp, c)); CK(dalloc(eatom_ters, c)); CK(dalloc(ke, c));
     CK(dalloc(d.list_off, (size_t)c + 1)); CK(dalloc(d.short_cnt, c)); CK(dalloc(d.short_nb, (size_t)c * MAXSHORT));
@@ -1092,8 +1098,10 @@ struct Engine {
   int ensure_stream2() {
     if (stream2) return LMFF_OK;
     CK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&stream3, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_frame, cudaEventDisableTiming));
     return LMFF_OK;
   }
 
@@ -1432,6 +1440,7 @@ struct Engine {
     a.ilp_f = d.ilp_f;
     a.ilp_c = d.ilp_c;
     a.ilp_g = d.ilp_g;
+    a.nframe = d.nframe;
     a.stat_ilp = stat_ilp;
     a.stat_ters = stat_ters;
     a.eatom_ilp = eatom_ilp;
@@ -1446,9 +1455,9 @@ struct Engine {
     return a;
   }
 
-  template <class R, class NS_SHORT, class NS_TERS, class NS_ILP, class NS_ND, class NS_FIN>
-  void run_kernels(ForceArgs<R> a, int which, bool ev, bool eatom, NS_SHORT fs, NS_TERS ft, NS_ILP fi, NS_ND fn,
-                   NS_FIN ff) {
+  template <class R, class NS_SHORT, class NS_TERS, class NS_ILP, class NS_FR, class NS_ND, class NS_FIN>
+  void run_kernels(ForceArgs<R> a, int which, bool ev, bool eatom, NS_SHORT fs, NS_TERS ft, NS_ILP fi, NS_FR fr,
+                   NS_ND fn, NS_FIN ff) {
     a.do_ters = t_on && (which & LMFF_TERSOFF);
     a.do_ilp = i_on && (which & LMFF_ILP);
     timed(2, [&] { fs(a, d_cutILPsq, ht.cutmax * ht.cutmax, stream); });
@@ -1457,9 +1466,14 @@ struct Engine {
     // kernels are timed one by one.
     const bool fork = a.do_ters && a.do_ilp && ters_concurrent && !ktiming && ensure_stream2() == LMFF_OK;
     a.ters_alone = !fork;
+    // the normal frames (the g-independent part of the normal-derivative assembly) on a
+    // third stream, beside both
     if (fork) {
       cudaEventRecord(ev_fork, stream);
       cudaStreamWaitEvent(stream2, ev_fork, 0);
+      cudaStreamWaitEvent(stream3, ev_fork, 0);
+      fr(a, stream3);
+      cudaEventRecord(ev_frame, stream3);
       ft(a, ev, eatom, stream2);
       cudaEventRecord(ev_join, stream2);
     } else if (a.do_ters) {
@@ -1468,7 +1482,9 @@ struct Engine {
       cudaMemsetAsync(stat_ters, 0, sizeof(double) * 8 * (size_t)n, stream);
     }
     if (a.do_ilp) {
+      if (!fork) timed(6, [&] { fr(a, stream); });
       timed(0, [&] { fi(a, ev, eatom, tpa, block, i_one, stream); });
+      if (fork) cudaStreamWaitEvent(stream, ev_frame, 0);
       timed(6, [&] { fn(a, ev, stream); });
     }
     else if (ev) cudaMemsetAsync(stat_ilp, 0, sizeof(double) * 8 * (size_t)n, stream);
@@ -1509,10 +1525,10 @@ struct Engine {
         }
         if (precision == LMFF_FP64) {
           run_kernels(args<double>(), which, ev, eatom, f64::launch_short, f64::launch_tersoff, f64::launch_ilp,
-                      f64::launch_nderiv, f64::launch_finish);
+                      f64::launch_nframe, f64::launch_nderiv, f64::launch_finish);
         } else {
           run_kernels(args<float>(), which, ev, eatom, f32::launch_short, f32::launch_tersoff, f32::launch_ilp,
-                      f32::launch_nderiv, f32::launch_finish);
+                      f32::launch_nframe, f32::launch_nderiv, f32::launch_finish);
         }
         if (ev) k_reduce<<<(int)hsys.size() * 16, 256, 0, stream>>>(n, 16, (const double *const *)d_arrs, d.sys, d.red_out);
         if (cap) {
@@ -2097,10 +2113,10 @@ struct Engine {
       }
       if (precision == LMFF_FP64)
         run_kernels(args<double>(), LMFF_TERSOFF | LMFF_ILP, false, false, f64::launch_short, f64::launch_tersoff,
-                    f64::launch_ilp, f64::launch_nderiv, f64::launch_finish);
+                    f64::launch_ilp, f64::launch_nframe, f64::launch_nderiv, f64::launch_finish);
       else
         run_kernels(args<float>(), LMFF_TERSOFF | LMFF_ILP, false, false, f32::launch_short, f32::launch_tersoff,
-                    f32::launch_ilp, f32::launch_nderiv, f32::launch_finish);
+                    f32::launch_ilp, f32::launch_nframe, f32::launch_nderiv, f32::launch_finish);
     }
     kick_args.drift = 0;
     cudaGraph_t gout = nullptr;

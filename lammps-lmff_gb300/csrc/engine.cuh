@@ -156,6 +156,7 @@ struct DevState {
   double *ilp_f = nullptr;    // 3*n: ILP direct force (+ normal term on the atom itself)
   d4 *ilp_c = nullptr;   // n * MAXILP: normal-derivative force on each intralayer neighbour
   d4 *ilp_g = nullptr;   // n: dE/dn_i accumulated by the pair kernel
+  d4 *nframe = nullptr;  // 4n: normal frames (k_nframe -> k_nderiv)
   double *eatom = nullptr;    // per-atom energy (when requested)
   double *ters_eatom = nullptr;
   // lists

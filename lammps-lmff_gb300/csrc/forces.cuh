@@ -291,6 +291,8 @@ struct ForceArgs {
   double *ilp_f;
   d4 *ilp_c;
   d4 *ilp_g;           // reverse-accumulated dE/dn_i of the terms owned by i (k_ilp -> k_nderiv)
+  d4 *nframe;          // 4 per atom: the normal frame k_nframe leaves for k_nderiv, or null
+                       // (k_nderiv then assembles in one piece)
   double *stat_ilp;    // 8 * n SoA: e_vdw/2, e_rep/2, virial[6]    (EV only)
   double *stat_ters;   // 8 * n SoA: e, 0, virial[6]
   double *eatom_ilp;   // n (EATOM only)

@@ -1940,17 +1940,27 @@ struct NDeriv {
   double F[3];
   double W[6];
 };
-template <bool EV>
-__device__ __forceinline__ void nderiv_eval(const ForceArgs<R> &a, int i, NDeriv &o) {
+// The normal frame of atom i: the part of the assembly that does not depend on g_i -- the
+// bond vectors to its intralayer neighbours, the unit normal and 1/|n1|.  With a frame
+// array (ForceArgs::nframe) k_nframe computes it beside the pair kernel, on the Tersoff
+// stream, and k_nderiv only applies g_i to it: about half of the assembly's FP64 work
+// leaves the step's critical path.  The arithmetic is that of the assembly done in one
+// piece, so the results are the same to the bit.
+struct NFrame {
+  int cont;   // intralayer neighbours (0 when i is not ILP-mapped)
+  bool ok;    // cont >= 2 and |n1| > 0
+  double v[MAXILP][3];
+  double nx, ny, nz, inn;
+};
+__device__ __forceinline__ void nframe_eval(const ForceArgs<R> &a, int i, NFrame &fr) {
   const SysDesc &sd = a.A.sys[a.A.sysid[i]];
   const int ie = c_pot.i_map[info_type(__double_as_longlong(a.A.xq[i].w))];
-  const int cont = ie >= 0 ? a.ilp_cnt[i] : 0;
-  const d4 g = a.ilp_g[i];
-  const double Gx = g.x, Gy = g.y, Gz = g.z;
-  double Fx = 0, Fy = 0, Fz = 0;
-  double W0 = 0, W1 = 0, W2 = 0, W3 = 0, W4 = 0, W5 = 0;
-  double c0x = 0, c0y = 0, c0z = 0, c1x = 0, c1y = 0, c1z = 0, c2x = 0, c2y = 0, c2z = 0;
-  double v[MAXILP][3];
+  fr.cont = ie >= 0 ? a.ilp_cnt[i] : 0;
+  fr.ok = false;
+  fr.nx = fr.ny = fr.nz = fr.inn = 0.0;
+#pragma unroll
+  for (int m = 0; m < MAXILP; m++) fr.v[m][0] = fr.v[m][1] = fr.v[m][2] = 0.0;
+  const int cont = fr.cont;
   if (cont >= 2) {
 #pragma unroll
     for (int m = 0; m < MAXILP; m++) {
@@ -1959,18 +1969,18 @@ __device__ __forceinline__ void nderiv_eval(const ForceArgs<R> &a, int i, NDeriv
       decode_entry(a.ilp_nb[(size_t)i * MAXILP + m], a.lc, j, sx, sy, sz);
       double ddx, ddy, ddz;
       disp64(a.A.xq, sd, i, j, sx, sy, sz, ddx, ddy, ddz);
-      v[m][0] = -ddx; v[m][1] = -ddy; v[m][2] = -ddz;
+      fr.v[m][0] = -ddx; fr.v[m][1] = -ddy; fr.v[m][2] = -ddz;
     }
     // three neighbours: v1 x v2 + v3 x v1 + v2 x v3 = (v2 - v1) x (v3 - v1), one product
     // instead of three.  The reference averages the three products (n1 / 3); the
     // unnormalised sum gives the same n, and h / 3 absorbs the 1/3 of each product's
     // derivative.
-    const double ax = cont == 3 ? v[1][0] - v[0][0] : v[0][0];
-    const double ay = cont == 3 ? v[1][1] - v[0][1] : v[0][1];
-    const double az = cont == 3 ? v[1][2] - v[0][2] : v[0][2];
-    const double bx = cont == 3 ? v[2][0] - v[0][0] : v[1][0];
-    const double by = cont == 3 ? v[2][1] - v[0][1] : v[1][1];
-    const double bz = cont == 3 ? v[2][2] - v[0][2] : v[1][2];
+    const double ax = cont == 3 ? fr.v[1][0] - fr.v[0][0] : fr.v[0][0];
+    const double ay = cont == 3 ? fr.v[1][1] - fr.v[0][1] : fr.v[0][1];
+    const double az = cont == 3 ? fr.v[1][2] - fr.v[0][2] : fr.v[0][2];
+    const double bx = cont == 3 ? fr.v[2][0] - fr.v[0][0] : fr.v[1][0];
+    const double by = cont == 3 ? fr.v[2][1] - fr.v[0][1] : fr.v[1][1];
+    const double bz = cont == 3 ? fr.v[2][2] - fr.v[0][2] : fr.v[1][2];
     const double n1x = ay * bz - by * az;
     const double n1y = az * bx - bz * ax;
     const double n1z = ax * by - bx * ay;
@@ -1979,33 +1989,57 @@ __device__ __forceinline__ void nderiv_eval(const ForceArgs<R> &a, int i, NDeriv
       double inn;
       if constexpr (sizeof(R) == 4) inn = nn2 > 1e-30 ? rsqrt_nr(nn2) : 1.0 / sqrt(nn2);
       else inn = 1.0 / sqrt(nn2);
-      double nx = n1x * inn, ny = n1y * inn, nz = n1z * inn;
-      double ng = nx * Gx + ny * Gy + nz * Gz;
-      double hx = (Gx - nx * ng) * inn, hy = (Gy - ny * ng) * inn, hz = (Gz - nz * ng) * inn;
-      auto crs = [](double ax, double ay, double az, double bx, double by, double bz, double &ox, double &oy, double &oz) {
-        ox = ay * bz - az * by; oy = az * bx - ax * bz; oz = ax * by - ay * bx;
-      };
-      if (cont == 2) {
-        // -(dn1/dv1)^T h = -(v2 x h); -(dn1/dv2)^T h = v1 x h; on i: (v2 - v1) x h
-        crs(v[1][0], v[1][1], v[1][2], hx, hy, hz, c0x, c0y, c0z);
-        c0x = -c0x; c0y = -c0y; c0z = -c0z;
-        crs(v[0][0], v[0][1], v[0][2], hx, hy, hz, c1x, c1y, c1z);
-        Fx = -(c0x + c1x); Fy = -(c0y + c1y); Fz = -(c0z + c1z);
-      } else {
-        // -(dn1/dv_m)^T h for m = 1, 2, 3: (v3 - v2) x h, (v1 - v3) x h, (v2 - v1) x h; the
-        // three sum to zero (no force on i), so the first is minus the other two
-        crs(-bx, -by, -bz, hx, hy, hz, c1x, c1y, c1z);
-        crs(ax, ay, az, hx, hy, hz, c2x, c2y, c2z);
-        c0x = -(c1x + c2x); c0y = -(c1y + c2y); c0z = -(c1z + c2z);
-      }
-      if (EV) {
-        // virial of the neighbour forces relative to i (the term's forces sum to zero)
-        W0 = v[0][0] * c0x + v[1][0] * c1x; W1 = v[0][1] * c0y + v[1][1] * c1y; W2 = v[0][2] * c0z + v[1][2] * c1z;
-        W3 = v[0][0] * c0y + v[1][0] * c1y; W4 = v[0][0] * c0z + v[1][0] * c1z; W5 = v[0][1] * c0z + v[1][1] * c1z;
-        if (cont == 3) {
-          W0 += v[2][0] * c2x; W1 += v[2][1] * c2y; W2 += v[2][2] * c2z;
-          W3 += v[2][0] * c2y; W4 += v[2][0] * c2z; W5 += v[2][1] * c2z;
-        }
+      fr.ok = true;
+      fr.inn = inn;
+      fr.nx = n1x * inn; fr.ny = n1y * inn; fr.nz = n1z * inn;
+    }
+  }
+}
+
+// g_i applied to the frame: the forces on the intralayer neighbours and on i, and with EV
+// their virial
+template <bool EV>
+__device__ __forceinline__ void nderiv_apply(const NFrame &fr, const d4 &g, NDeriv &o) {
+  const double Gx = g.x, Gy = g.y, Gz = g.z;
+  double Fx = 0, Fy = 0, Fz = 0;
+  double W0 = 0, W1 = 0, W2 = 0, W3 = 0, W4 = 0, W5 = 0;
+  double c0x = 0, c0y = 0, c0z = 0, c1x = 0, c1y = 0, c1z = 0, c2x = 0, c2y = 0, c2z = 0;
+  const int cont = fr.cont;
+  if (fr.ok) {
+    const double(&v)[MAXILP][3] = fr.v;
+    const double ax = cont == 3 ? v[1][0] - v[0][0] : v[0][0];
+    const double ay = cont == 3 ? v[1][1] - v[0][1] : v[0][1];
+    const double az = cont == 3 ? v[1][2] - v[0][2] : v[0][2];
+    const double bx = cont == 3 ? v[2][0] - v[0][0] : v[1][0];
+    const double by = cont == 3 ? v[2][1] - v[0][1] : v[1][1];
+    const double bz = cont == 3 ? v[2][2] - v[0][2] : v[1][2];
+    const double inn = fr.inn;
+    const double nx = fr.nx, ny = fr.ny, nz = fr.nz;
+    double ng = nx * Gx + ny * Gy + nz * Gz;
+    double hx = (Gx - nx * ng) * inn, hy = (Gy - ny * ng) * inn, hz = (Gz - nz * ng) * inn;
+    auto crs = [](double ax, double ay, double az, double bx, double by, double bz, double &ox, double &oy, double &oz) {
+      ox = ay * bz - az * by; oy = az * bx - ax * bz; oz = ax * by - ay * bx;
+    };
+    if (cont == 2) {
+      // -(dn1/dv1)^T h = -(v2 x h); -(dn1/dv2)^T h = v1 x h; on i: (v2 - v1) x h
+      crs(v[1][0], v[1][1], v[1][2], hx, hy, hz, c0x, c0y, c0z);
+      c0x = -c0x; c0y = -c0y; c0z = -c0z;
+      crs(v[0][0], v[0][1], v[0][2], hx, hy, hz, c1x, c1y, c1z);
+      Fx = -(c0x + c1x); Fy = -(c0y + c1y); Fz = -(c0z + c1z);
+    } else {
+      // -(dn1/dv_m)^T h for m = 1, 2, 3: (v3 - v2) x h, (v1 - v3) x h, (v2 - v1) x h; the
+      // three sum to zero (no force on i), so the first is minus the other two
+      crs(-bx, -by, -bz, hx, hy, hz, c1x, c1y, c1z);
+      crs(ax, ay, az, hx, hy, hz, c2x, c2y, c2z);
+      c0x = -(c1x + c2x); c0y = -(c1y + c2y); c0z = -(c1z + c2z);
+    }
+    if (EV) {
+      // virial of the neighbour forces relative to i (the term's forces sum to zero)
+      W0 = v[0][0] * c0x + v[1][0] * c1x; W1 = v[0][1] * c0y + v[1][1] * c1y; W2 = v[0][2] * c0z + v[1][2] * c1z;
+      W3 = v[0][0] * c0y + v[1][0] * c1y; W4 = v[0][0] * c0z + v[1][0] * c1z; W5 = v[0][1] * c0z + v[1][1] * c1z;
+      if (cont == 3) {
+        W0 += v[2][0] * c2x; W1 += v[2][1] * c2y; W2 += v[2][2] * c2z;
+        W3 += v[2][0] * c2y; W4 += v[2][0] * c2z; W5 += v[2][1] * c2z;
       }
     }
   }
@@ -2016,6 +2050,35 @@ __device__ __forceinline__ void nderiv_eval(const ForceArgs<R> &a, int i, NDeriv
   if (EV) {
     o.W[0] = W0; o.W[1] = W1; o.W[2] = W2; o.W[3] = W3; o.W[4] = W4; o.W[5] = W5;
   }
+}
+
+// the assembly of atom i from its stored frame, or in one piece without a frame array
+template <bool EV>
+__device__ __forceinline__ void nderiv_eval(const ForceArgs<R> &a, int i, NDeriv &o) {
+  NFrame fr;
+  if (a.nframe) {
+    const d4 f0 = a.nframe[4 * (size_t)i], f1 = a.nframe[4 * (size_t)i + 1], f2 = a.nframe[4 * (size_t)i + 2],
+             f3 = a.nframe[4 * (size_t)i + 3];
+    fr.nx = f0.x; fr.ny = f0.y; fr.nz = f0.z; fr.inn = f0.w;
+    fr.v[0][0] = f1.x; fr.v[0][1] = f1.y; fr.v[0][2] = f1.z; fr.cont = (int)f1.w;
+    fr.v[1][0] = f2.x; fr.v[1][1] = f2.y; fr.v[1][2] = f2.z; fr.ok = f2.w != 0.0;
+    fr.v[2][0] = f3.x; fr.v[2][1] = f3.y; fr.v[2][2] = f3.z;
+  } else {
+    nframe_eval(a, i, fr);
+  }
+  nderiv_apply<EV>(fr, a.ilp_g[i], o);
+}
+
+__global__ void k_nframe(ForceArgs<R> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  NFrame fr;
+  nframe_eval(a, i, fr);
+  d4 *q = a.nframe + 4 * (size_t)i;
+  q[0] = make_d4(fr.nx, fr.ny, fr.nz, fr.inn);
+  q[1] = make_d4(fr.v[0][0], fr.v[0][1], fr.v[0][2], (double)fr.cont);
+  q[2] = make_d4(fr.v[1][0], fr.v[1][1], fr.v[1][2], fr.ok ? 1.0 : 0.0);
+  q[3] = make_d4(fr.v[2][0], fr.v[2][1], fr.v[2][2], 0.0);
 }
 
 template <bool EV>
@@ -2425,6 +2488,12 @@ void launch_ilp(const ForceArgs<R> &a, bool ev, bool eatom, int tpa, int block, 
   }
   if (one_element) launch_ilp_one<true>(a, ev, eatom, tpa, block, s);
   else launch_ilp_one<false>(a, ev, eatom, tpa, block, s);
+}
+
+void launch_nframe(const ForceArgs<R> &a, cudaStream_t s) {
+  if (a.n == 0 || !a.nframe) return;
+  const int b = per_atom_block(a.n);
+  k_nframe<<<(a.n + b - 1) / b, b, 0, s>>>(a);
 }
 
 void launch_nderiv(const ForceArgs<R> &a, bool ev, cudaStream_t s) {

@@ -220,7 +220,12 @@ int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double 
  * the interlayer pair kernel (they write disjoint arrays; joined before the gather);
  * 0 = one after the other.  "pair_tile" 2 (default) = the mixed force-only pair kernel
  * takes two list entries per lane and iteration (FP32x2 lanes across the pair), 1 = one
- * entry (the neighbour-tile shape the tuner chooses).  "check_every" = how often
+ * entry (the neighbour-tile shape the tuner chooses).  "small_variants" 1 (default) = small
+ * systems run the kernel variants made for them (one warp per atom in the list build, 16
+ * or 4 lanes per atom in the intralayer lists, 8 in the gather, one lane per bond in
+ * Tersoff when it runs alone), 0 = the large-system kernels at every size; the lists and
+ * results are the same to the bit either way, except Tersoff run alone, which agrees to
+ * rounding.  "check_every" = how often
  * lmff_run_nve tests the pair list: 1 = every step, for displacement alone (LAMMPS's
  * neigh_modify every 1 delay 0 check yes); k > 1 = at steps whose index is a multiple
  * of k, rebuilding when an atom may move more than skin/2 before the next test (its

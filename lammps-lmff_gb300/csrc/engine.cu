@@ -500,6 +500,7 @@ struct Engine {
   // nall (owned first, then ghosts); -1 for the ordinary periodic-system mode
   int ghost_nlocal = -1;
   int pair_tile = 2;   // option "pair_tile": list entries per pair-loop iteration (1 or 2)
+  bool small_variants = true;   // option "small_variants": the small-system kernel variants
   double skin = 2.0;
   int ntypes = 0;
   HostTersoff ht;
@@ -1228,6 +1229,7 @@ struct Engine {
     NbArgs a;
     memset(&a, 0, sizeof a);
     a.n = n;
+    a.no_small = !small_variants;
     a.xq = d.xq;
     a.xh = d.xh;
     a.xl = d.xl;
@@ -1451,6 +1453,7 @@ struct Engine {
     a.own_perm = ghost_nlocal >= 0 ? d.perm : nullptr;
     a.nown = ghost_nlocal;
     a.pair_tile = pair_tile;
+    a.no_small = !small_variants;
     a.kc = i_on && hi.model == LMFF_INTERLAYER_KC;
     return a;
   }
@@ -1916,6 +1919,7 @@ struct Engine {
     NbArgs a;
     memset(&a, 0, sizeof a);
     a.n = n;
+    a.no_small = !small_variants;
     a.xq = d.xq;
     a.xh = d.xh;
     a.xl = d.xl;
@@ -3219,6 +3223,10 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
     if (!(value >= 0.0 && value <= 64.0)) return e->e.fail(LMFF_EINVAL, "check_every must be in 0..64");
     e->e.check_every_opt = (int)value;
     e->e.drop_graph();
+  } else if (k == "small_variants") {
+    e->e.small_variants = value != 0.0;
+    e->e.drop_graph();
+    e->e.built = false;
   } else if (k == "ters_concurrent") {
     e->e.ters_concurrent = value != 0.0;
     e->e.drop_graph();

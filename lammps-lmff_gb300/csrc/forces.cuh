@@ -316,6 +316,9 @@ struct ForceArgs {
   // the pair kernel the one-thread kernel is kept, whose fewer instructions take fewer
   // issue slots from it
   int ters_alone;
+  // 1: the large-system kernels at every size (option small_variants 0: the lanes-per-atom
+  // variants of the short lists, the gather and Tersoff are not used)
+  int no_small;
   int kc;              // interlayer style is kolmogorov/crespi/full
 };
 

@@ -2410,7 +2410,9 @@ void upload_pot(const PotConst<R> &p, cudaStream_t s) {
 
 void launch_short(const ForceArgs<R> &a, const double *cutILPsq64, double tcutmaxsq64, cudaStream_t s) {
   if (a.n == 0) return;
-  if (a.n <= SHORT_SG16_MAX_ATOMS)
+  if (a.no_small)
+    k_short<1><<<(a.n + 127) / 128, 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
+  else if (a.n <= SHORT_SG16_MAX_ATOMS)
     k_short<16><<<(int)(((long long)a.n * 16 + 127) / 128), 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
   else if (a.n <= SHORT_SG_MAX_ATOMS) k_short<4><<<(int)(((long long)a.n * 4 + 127) / 128), 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
   else k_short<1><<<(a.n + 127) / 128, 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
@@ -2425,7 +2427,7 @@ void launch_tersoff(const ForceArgs<R> &a, bool ev, bool eatom, cudaStream_t s) 
     else k_tersoff<false, false, true><<<g, b, 0, s>>>(a);
   } else if (ev) {
     k_tersoff<true, false, false><<<g, b, 0, s>>>(a);
-  } else if (a.ters_alone && a.n <= TERS_LANES_MAX_ATOMS) {
+  } else if (a.ters_alone && a.n <= TERS_LANES_MAX_ATOMS && !a.no_small) {
     k_tersoff_lanes<<<(int)(((long long)a.n * TERS_LANES + 127) / 128), 128, 0, s>>>(a);
   } else {
     k_tersoff<false, false, false><<<g, b, 0, s>>>(a);
@@ -2509,7 +2511,7 @@ void launch_finish(const ForceArgs<R> &a, bool eatom, const KickArgs *kick, cuda
   int g = (a.n + 127) / 128;
   KickArgs k{};
   if (kick) k = *kick;
-  if (a.n <= FINISH_LANES_MAX_ATOMS) {
+  if (a.n <= FINISH_LANES_MAX_ATOMS && !a.no_small) {
     const int gl = (a.n + FINISH_ATOMS - 1) / FINISH_ATOMS, bl = FINISH_LANES * FINISH_ATOMS;
     if (kick && !eatom) k_finish_lanes<false, true><<<gl, bl, 0, s>>>(a, k);
     else if (kick) k_finish_lanes<true, true><<<gl, bl, 0, s>>>(a, k);

@@ -502,7 +502,7 @@ void nb_hilo(int n, const d4 *xq, const SysDesc *sys, const int *sysid, float4 *
 
 void nb_list(const NbArgs &a, int mode, cudaStream_t s) {
   if (!a.n) return;
-  if (a.n <= LIST_ATOM_MAX_ATOMS) {
+  if (a.n <= LIST_ATOM_MAX_ATOMS && !a.no_small) {
     const int ga = (int)(((int64_t)a.n * 32 + 127) / 128);
     if (mode == 1) k_list_atom<1><<<ga, 128, 0, s>>>(a);
     else if (mode == 2) k_list_atom<2><<<ga, 128, 0, s>>>(a);

@@ -48,6 +48,7 @@ struct NbArgs {
   ListCode lc;
   int full;
   int *status;
+  int no_small;       // 1: the warp-per-32-atoms build at every size (option small_variants 0)
 };
 
 void nb_upload_const(const NbConst &c, cudaStream_t s);

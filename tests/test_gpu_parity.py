@@ -442,6 +442,39 @@ def test_force_only_tersoff_lanes_equal_one_thread_routine(name, prec):
     assert d <= 1e-13 * np.abs(r_ev["f"]).max(), d
 
 
+@pytest.mark.parametrize("prec", [capi.FP64, capi.MIXED])
+@pytest.mark.parametrize("name", ["bilayer_small", "hetero_small", "edges", "tiny_images"])
+def test_small_system_variants_equal_large_system_kernels(name, prec):
+    """The kernel variants small systems run (one warp per atom in the list build, 16
+    lanes per atom in the intralayer lists, 8 in the gather, one lane per bond in
+    Tersoff alone) against the large-system kernels (option small_variants 0): the same
+    lists entry for entry and the same forces, energies and per-atom energies to the bit;
+    Tersoff alone with one lane per bond agrees with the one-thread kernel to rounding: the
+    one-thread force-only kernel adds each three-body product into its partner's sum in
+    one FMA, the lanes (like the one-thread energy/virial kernel, which uses the product
+    twice) round it first (FP64 ~1e-15, the FP32 sums of the mixed mode ~1e-8 relative)."""
+    g = load_golden(name)
+    out = {}
+    for sv in (1, 0):
+        eng = engine_for(g, precision=prec, small_variants=sv)
+        args = (g["x"], g["type"], g["mol"], g["tag"])
+        rf = eng.compute(*args, eflag=False, vflag=False)
+        lists = (eng.export_list(0), eng.export_list(1))
+        rt = eng.compute(*args, which=capi.TERSOFF, eflag=False, vflag=False, same_atoms=True)
+        re = eng.compute(*args, eatom=True, same_atoms=True)
+        out[sv] = (rf, lists, rt, re)
+        eng.close()
+    (rf1, l1, rt1, re1), (rf0, l0, rt0, re0) = out[1], out[0]
+    assert np.array_equal(l1[0], l0[0]) and np.array_equal(l1[1], l0[1])
+    assert np.array_equal(rf1["f"], rf0["f"])
+    rel = 1e-13 if prec == capi.FP64 else 1e-6
+    assert np.abs(rt1["f"] - rt0["f"]).max() <= rel * np.abs(rt0["f"]).max()
+    assert np.array_equal(re1["f"], re0["f"]) and np.array_equal(re1["eatom"], re0["eatom"])
+    for k in ("e_tersoff", "e_ilp"):
+        assert re1[k] == re0[k]
+    assert np.array_equal(re1["virial"], re0["virial"])
+
+
 def test_host_positions_in_another_periodic_image_need_no_rebuild():
     """A caller may pass unwrapped coordinates, or wrap some atoms between calls (LAMMPS
     does at reneighbouring): the engine takes each position in the image its list was

@@ -354,6 +354,7 @@ struct orc_ctx {
   double *dnormal;    /* nlocal*27  [(m*3+id)*3+ip] d n[id] / d x_m[ip] */
   double *fthr;       /* nthreads * nall*3 (Tersoff) then ILP */
   double *ethr;       /* nthreads * nall */
+  double *vthr;       /* nthreads * nall*6 (per-atom virial) */
   int64_t nrebuild;
   int have_lists;
   char err[256];
@@ -381,7 +382,7 @@ void orc_free(orc_ctx *c) {
   if (!c) return;
   free(c->x); free(c->type); free(c->mol); free(c->tag); free(c->owner); free(c->shift);
   free(c->xhold); free(c->nb_off); free(c->nb); free(c->ilpn); free(c->ilpnb);
-  free(c->normal); free(c->dnormdri); free(c->dnormal); free(c->fthr); free(c->ethr);
+  free(c->normal); free(c->dnormdri); free(c->dnormal); free(c->fthr); free(c->ethr); free(c->vthr);
   free(c);
 }
 
@@ -796,8 +797,39 @@ static inline int skip_half(const orc_ctx *c, int i, int j) {
   return 0;
 }
 
-/* calc_FvdW (:471-540) and calc_FRep (:577-674) for owned atom i */
-static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *evdw, double *erep) {
+/* Per-atom virial tallies (pair.cpp): ev_tally (:913-1058) with a scalar pair force
+ * fpair along del, ev_tally_xyz (:1060-1153) with a force vector, each half to both
+ * atoms with newton on; v_tally3 (:1435-1453) a third to each of three atoms. */
+static inline void va_pair(double *va, int i, int j, double fpair, double dx, double dy, double dz) {
+  double v[6] = {dx * dx * fpair, dy * dy * fpair, dz * dz * fpair,
+                 dx * dy * fpair, dx * dz * fpair, dy * dz * fpair};
+  for (int c = 0; c < 6; c++) va[6 * i + c] += 0.5 * v[c];
+  for (int c = 0; c < 6; c++) va[6 * j + c] += 0.5 * v[c];
+}
+static inline void va_xyz(double *va, int i, int j, const double fv[3], double dx, double dy, double dz) {
+  double v[6] = {dx * fv[0], dy * fv[1], dz * fv[2], dx * fv[1], dx * fv[2], dy * fv[2]};
+  for (int c = 0; c < 6; c++) va[6 * i + c] += 0.5 * v[c];
+  for (int c = 0; c < 6; c++) va[6 * j + c] += 0.5 * v[c];
+}
+static inline void va_three(double *va, int i, int j, int k, const double fj[3], const double fk[3],
+                            const double drij[3], const double drik[3]) {
+  const double third = 1.0 / 3.0;
+  double v[6] = {third * (drij[0] * fj[0] + drik[0] * fk[0]), third * (drij[1] * fj[1] + drik[1] * fk[1]),
+                 third * (drij[2] * fj[2] + drik[2] * fk[2]), third * (drij[0] * fj[1] + drik[0] * fk[1]),
+                 third * (drij[0] * fj[2] + drik[0] * fk[2]), third * (drij[1] * fj[2] + drik[1] * fk[2])};
+  for (int c = 0; c < 6; c++) {
+    va[6 * i + c] += v[c];
+    va[6 * j + c] += v[c];
+    va[6 * k + c] += v[c];
+  }
+}
+
+/* calc_FvdW (:471-540) and calc_FRep (:577-674) for owned atom i; vatom (nall*6, may be
+ * NULL) receives the per-atom virial as the reference tallies it: ev_tally of the vdW
+ * pair (:536), ev_tally_xyz of each normal-derivative force on k against x_k - x_j
+ * (:667) and of the repulsion's pair force (:671) */
+static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *vatom, double *evdw,
+                     double *erep) {
   const orc_pot *p = &c->p;
   int ie = p->i_map[c->type[i]];
   if (ie < 0) return;
@@ -862,6 +894,7 @@ static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *
         eatom[i] += 0.5 * evdwl;
         eatom[j] += 0.5 * evdwl;
       }
+      if (vatom) va_pair(vatom, i, j, fsum, delx, dely, delz);
       ORC_OPCAT(ORC_CAT_ILP_PAIR);
     }
     /* repulsion with the normal of i, every directed pair */
@@ -912,11 +945,16 @@ static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *
       if (k == i) continue;
       ORC_OPCAT(ORC_CAT_ILP_KTERM);
       ORC_OPUNIT(ORC_CAT_ILP_KTERM);
+      double fk[3];
       for (int ip = 0; ip < 3; ip++) {
         double dp = dk[(kk * 3 + 0) * 3 + ip] * delx + dk[(kk * 3 + 1) * 3 + ip] * dely +
                     dk[(kk * 3 + 2) * 3 + ip] * delz;
-        f[3 * k + ip] += (-prodnorm1 * dp * fpair1) * Tap;
+        fk[ip] = (-prodnorm1 * dp * fpair1) * Tap;
+        f[3 * k + ip] += fk[ip];
       }
+      if (vatom)
+        va_xyz(vatom, k, j, fk, c->x[3 * k] - c->x[3 * j], c->x[3 * k + 1] - c->x[3 * j + 1],
+               c->x[3 * k + 2] - c->x[3 * j + 2]);
       ORC_OPCAT(ORC_CAT_ILP_PAIR);
     }
     /* KC without the taper tallies V - offset, offset = -A (z0/cut)^6 (init_one :235) */
@@ -926,6 +964,7 @@ static void ilp_atom(const orc_ctx *c, int i, double *f, double *eatom, double *
       eatom[i] += 0.5 * ev;
       eatom[j] += 0.5 * ev;
     }
+    if (vatom) va_xyz(vatom, i, j, fkc, delx, dely, delz);
   }
   ORC_OPCAT(ORC_CAT_OTHER);
 }
@@ -1030,8 +1069,10 @@ static void ters_attractive(const orc_ters_param *q, double prefactor, double rs
   }
 }
 
-/* PairTersoff::compute body for owned atom i, pair_tersoff.cpp:117-262 */
-static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, double *eng) {
+/* PairTersoff::compute body for owned atom i, pair_tersoff.cpp:117-262; vatom (nall*6,
+ * may be NULL) receives the per-atom virial of its ev_tally (:173, :223) and v_tally3
+ * (:253) calls */
+static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, double *vatom, double *eng) {
   const orc_pot *p = &c->p;
   int itype = p->t_map[c->type[i]];
   if (itype < 0) return 0;
@@ -1076,6 +1117,7 @@ static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, doubl
       eatom[i] += 0.5 * evdwl;
       eatom[j] += 0.5 * evdwl;
     }
+    if (vatom) va_pair(vatom, i, j, fpair, delx, dely, delz);
   }
   for (int jj = 0; jj < numshort; jj++) {
     int j = neighshort[jj];
@@ -1119,6 +1161,7 @@ static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, doubl
       eatom[i] += 0.5 * evdwl;
       eatom[j] += 0.5 * evdwl;
     }
+    if (vatom) va_pair(vatom, i, j, -fpair, -delr1[0], -delr1[1], -delr1[2]);
     ORC_OPCAT(ORC_CAT_TERS_ATTR);
     for (int kk = 0; kk < numshort; kk++) {
       if (jj == kk) continue;
@@ -1140,6 +1183,7 @@ static int tersoff_atom(const orc_ctx *c, int i, double *f, double *eatom, doubl
       f[3 * k] += fk[0];
       f[3 * k + 1] += fk[1];
       f[3 * k + 2] += fk[2];
+      if (vatom) va_three(vatom, i, j, k, fj, fk, delr1, delr2);
     }
     f[3 * j] += fjx;
     f[3 * j + 1] += fjy;
@@ -1167,14 +1211,19 @@ static void fdotr(const orc_ctx *c, const double *f, double *v) {
   }
 }
 
-static int style_pass(orc_ctx *c, int style, double *ftot, double *eatom, double *eng, double *pv, double *vir) {
+static int style_pass(orc_ctx *c, int style, double *ftot, double *eatom, double *vatom, double *eng, double *pv,
+                      double *vir) {
   int nall = c->nall, nt = c->nthreads;
-  size_t fsz = (size_t)nall * 3;
+  size_t fsz = (size_t)nall * 3, vsz = (size_t)nall * 6;
   c->fthr = (double *)realloc(c->fthr, sizeof(double) * fsz * nt);
   memset(c->fthr, 0, sizeof(double) * fsz * nt);
   if (eatom) {
     c->ethr = (double *)realloc(c->ethr, sizeof(double) * nall * nt);
     memset(c->ethr, 0, sizeof(double) * nall * nt);
+  }
+  if (vatom) {
+    c->vthr = (double *)realloc(c->vthr, sizeof(double) * vsz * nt);
+    memset(c->vthr, 0, sizeof(double) * vsz * nt);
   }
   double e0 = 0.0, e1 = 0.0;
   int err = 0;
@@ -1186,12 +1235,13 @@ static int style_pass(orc_ctx *c, int style, double *ftot, double *eatom, double
 #endif
     double *ft = c->fthr + fsz * tid;
     double *et = eatom ? c->ethr + (size_t)nall * tid : NULL;
+    double *vt = vatom ? c->vthr + vsz * tid : NULL;
 #pragma omp for schedule(dynamic, 32)
     for (int i = 0; i < c->nlocal; i++) {
       if (style == 1) {
-        if (tersoff_atom(c, i, ft, et, &e0)) err = 1;
+        if (tersoff_atom(c, i, ft, et, vt, &e0)) err = 1;
       } else {
-        ilp_atom(c, i, ft, et, &e0, &e1);
+        ilp_atom(c, i, ft, et, vt, &e0, &e1);
       }
     }
   }
@@ -1211,6 +1261,12 @@ static int style_pass(orc_ctx *c, int style, double *ftot, double *eatom, double
       for (int t = 0; t < nt; t++) e += c->ethr[(size_t)nall * t + a];
       eatom[o] += e;
     }
+    if (vatom)
+      for (int k = 0; k < 6; k++) {
+        double v = 0.0;
+        for (int t = 0; t < nt; t++) v += c->vthr[vsz * t + 6 * (size_t)a + k];
+        vatom[6 * o + k] += v;
+      }
   }
   if (style == 1) {
     *eng = e0;
@@ -1223,18 +1279,25 @@ static int style_pass(orc_ctx *c, int style, double *ftot, double *eatom, double
 }
 
 int orc_forces(orc_ctx *c, int which, double *f, double *eatom, orc_result *r) {
+  return orc_forces_va(c, which, f, eatom, NULL, NULL, r);
+}
+
+int orc_forces_va(orc_ctx *c, int which, double *f, double *eatom, double *vatom_ters, double *vatom_ilp,
+                  orc_result *r) {
   memset(r, 0, sizeof *r);
   memset(f, 0, sizeof(double) * 3 * c->nlocal);
   if (eatom) memset(eatom, 0, sizeof(double) * c->nlocal);
+  if (vatom_ters) memset(vatom_ters, 0, sizeof(double) * 6 * c->nlocal);
+  if (vatom_ilp) memset(vatom_ilp, 0, sizeof(double) * 6 * c->nlocal);
   int rc;
   if ((which & 1) && c->p.t_enabled) {
-    rc = style_pass(c, 1, f, eatom, &r->e_tersoff, NULL, r->virial_tersoff);
+    rc = style_pass(c, 1, f, eatom, vatom_ters, &r->e_tersoff, NULL, r->virial_tersoff);
     if (rc) return rc;
   }
   if ((which & 2) && c->p.i_enabled) {
     if ((rc = ilp_neigh(c))) return rc;
     if ((rc = calc_normal(c))) return rc;
-    rc = style_pass(c, 2, f, eatom, &r->e_ilp, r->pvector, r->virial_ilp);
+    rc = style_pass(c, 2, f, eatom, vatom_ilp, &r->e_ilp, r->pvector, r->virial_ilp);
     if (rc) return rc;
   }
   for (int k = 0; k < 6; k++) r->virial[k] = r->virial_tersoff[k] + r->virial_ilp[k];

@@ -92,6 +92,11 @@ int orc_update_x(orc_ctx *c, const double *x);
 /* Forces on owned atoms (overwritten), energies, pvector, fdotr virials, per-atom energy
  * (eatom may be NULL).  which: 1 = Tersoff, 2 = ILP, 3 = both. */
 int orc_forces(orc_ctx *c, int which, double *f, double *eatom, orc_result *r);
+/* The same with each style's per-atom virial (nlocal*6 each, xx yy zz xy xz yz,
+ * overwritten; either may be NULL) as the reference's ev_tally, ev_tally_xyz and
+ * v_tally3 calls split it over atoms, ghost shares folded into their owners. */
+int orc_forces_va(orc_ctx *c, int which, double *f, double *eatom, double *vatom_ters, double *vatom_ilp,
+                  orc_result *r);
 /* Velocity-Verlet NVE (fix_nve.cpp:64-111, metal units) for nsteps; x, v, f in/out,
  * f must hold the forces of x on entry.  mass_of_type[t-1]. */
 int orc_nve(orc_ctx *c, int nsteps, double dt, const double *mass_of_type, double *x, double *v,

@@ -58,6 +58,7 @@ def _load():
         lib.orc_set_atoms.argtypes = [P, C.c_int, P, P, P, P, P, P, P]
         lib.orc_update_x.argtypes = [P, P]
         lib.orc_forces.argtypes = [P, C.c_int, P, P, C.POINTER(_Result)]
+        lib.orc_forces_va.argtypes = [P, C.c_int, P, P, P, P, C.POINTER(_Result)]
         lib.orc_nve.argtypes = [P, C.c_int, C.c_double, P, P, P, P, C.POINTER(_Result)]
         lib.orc_nrebuilds.argtypes = [P]
         lib.orc_nrebuilds.restype = C.c_int64
@@ -133,17 +134,26 @@ class Oracle:
         x = np.ascontiguousarray(x, dtype=np.float64)
         self._check(_lib.orc_update_x(self._ctx, _ptr(x)))
 
-    def forces(self, which: int = 3, eatom: bool = False) -> Dict:
+    def forces(self, which: int = 3, eatom: bool = False, vatom: bool = False) -> Dict:
+        """vatom: also each style's per-atom virial (n x 6, xx yy zz xy xz yz) as
+        "vatom_tersoff" / "vatom_ilp" and their sum "vatom"."""
         f = np.zeros((self.n, 3))
         ea = np.zeros(self.n) if eatom else None
         r = _Result()
-        self._check(_lib.orc_forces(self._ctx, which, _ptr(f), _ptr(ea) if eatom else None, C.byref(r)))
+        if vatom:
+            vt, vi = np.zeros((self.n, 6)), np.zeros((self.n, 6))
+            self._check(_lib.orc_forces_va(self._ctx, which, _ptr(f), _ptr(ea) if eatom else None, _ptr(vt),
+                                           _ptr(vi), C.byref(r)))
+        else:
+            self._check(_lib.orc_forces(self._ctx, which, _ptr(f), _ptr(ea) if eatom else None, C.byref(r)))
         out = {"f": f, "e_tersoff": r.e_tersoff, "e_ilp": r.e_ilp, "pvector": np.array(r.pvector[:]),
                "virial": np.array(r.virial[:]), "virial_tersoff": np.array(r.virial_tersoff[:]),
                "virial_ilp": np.array(r.virial_ilp[:]), "nghost": r.nghost, "nlist": r.nlist}
         out["e_pair"] = out["e_tersoff"] + out["e_ilp"]
         if eatom:
             out["eatom"] = ea
+        if vatom:
+            out["vatom_tersoff"], out["vatom_ilp"], out["vatom"] = vt, vi, vt + vi
         return out
 
     def nve(self, nsteps: int, dt: float, mass_of_type, x, v, f) -> Dict:

@@ -153,6 +153,33 @@ int main(int argc, char **argv) {
     rec("eatom", 'd', ea.size(), ea.data());
   }
 
+  // Per-atom virial of each sub-style (Pair::vatom as its ev_tally / ev_tally_xyz /
+  // v_tally3 calls left it), when the script defines a stress/atom compute named
+  // "satom" that was invoked on the last step (that sets vflag_atom).  Ghost rows are
+  // folded into their owned atoms as Comm::reverse_comm does for compute stress/atom
+  // (Atom::map returns the owned copy of a tag); rows are in tag order, 6 per atom
+  // (xx yy zz xy xz yz).
+  if (lmp->modify->find_compute("satom") >= 0 && strcmp(lmp->force->pair_style, "hybrid/overlay") == 0) {
+    PairHybrid *h = (PairHybrid *)pair;
+    int nall = nlocal + atom->nghost;
+    for (int m = 0; m < h->nstyles; m++) {
+      Pair *ps = h->styles[m];
+      if (!ps->vatom) continue;
+      std::vector<double> fold((size_t)nlocal * 6, 0.0);
+      for (int i = 0; i < nall; i++) {
+        int o = i < nlocal ? i : atom->map(atom->tag[i]);
+        if (o < 0 || o >= nlocal) continue;
+        for (int c = 0; c < 6; c++) fold[(size_t)o * 6 + c] += ps->vatom[i][c];
+      }
+      std::vector<double> va;
+      for (int ii = 0; ii < nlocal; ii++)
+        for (int c = 0; c < 6; c++) va.push_back(fold[(size_t)order[ii] * 6 + c]);
+      std::string kw = h->keywords[m];
+      bool inter = kw == "ilp/graphene/hbn" || kw == "kolmogorov/crespi/full";
+      rec(inter ? "vatom_ilp" : "vatom_tersoff", 'd', va.size(), va.data());
+    }
+  }
+
   if (minstats && lmp->update->minimize) {
     Min *m = lmp->update->minimize;
     int64_t q[3] = {m->niter, m->neval, m->stop_condition};

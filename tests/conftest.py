@@ -52,3 +52,5 @@ def min_image(d, lo, hi, periodic):
 GOLDEN_SINGLE = ["bilayer_small", "bilayer_small_notaper", "hetero_small", "tiny_images", "edges",
                  "trilayer_alt", "c1_t0", "c1_t100"]
 GOLDEN_LISTS = ["bilayer_small", "hetero_small", "tiny_images", "edges", "trilayer_alt"]
+# fixtures that carry each style's per-atom virial (vatom_tersoff, vatom_ilp)
+GOLDEN_VATOM = ["bilayer_small", "bilayer_small_notaper", "hetero_small", "tiny_images", "edges", "trilayer_alt"]

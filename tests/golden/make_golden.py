@@ -13,7 +13,8 @@ that has it:
 
 Every fixture stores the inputs (x, v, type, mol, tag, box, periodicity, potential
 settings) and the reference outputs (forces, per-style energies, ILP pvector, fdotr
-virial, per-atom energy; for list cases the full Verlet list and the ILP intralayer list
+virial, per-atom energy, each sub-style's per-atom virial as its tallies leave it, in
+LAMMPS order xx yy zz xy xz yz; for list cases the full Verlet list and the ILP intralayer list
 as (tag_i, tag_j, image) triples with image = sum_c ((s_c+8)&15) << 4c).
 """
 from __future__ import annotations
@@ -77,7 +78,9 @@ neighbor 2.0 bin
 neigh_modify every 1 delay 0 check yes one 10000 page 200000
 compute peatom all pe/atom pair
 compute pesum all reduce sum c_peatom
-thermo_style custom step pe c_pesum press
+compute satom all stress/atom NULL pair
+compute vsum all reduce sum c_satom[1]
+thermo_style custom step pe c_pesum press c_vsum
 thermo {max(nsteps, 1)}
 timestep {dt}
 """
@@ -152,6 +155,9 @@ def pack(s: S.System, r, tap_flag, extra=None):
         "virial": r["virial"], "eatom": r["eatom"], "tap_flag": tap_flag, "cut_global": 16.0,
         "skin": 2.0, "step": r["step"][0],
     }
+    for k in ("vatom_tersoff", "vatom_ilp"):
+        if k in r:
+            d[k] = r[k].reshape(n, 6)
     if "nlist" in r:
         nl = r["nlist"].reshape(-1, 3)
         nl = nl[np.lexsort((nl[:, 2], nl[:, 1], nl[:, 0]))]

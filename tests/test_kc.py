@@ -37,8 +37,10 @@ def _engine(g, precision=capi.FP64):
 @pytest.mark.parametrize("name", ["kc_bilayer", "kc_bilayer_notaper"])
 def test_kc_oracle_matches_reference(name):
     g = load_golden(name)
-    r = _oracle(g).forces(eatom=True)
+    r = _oracle(g).forces(eatom=True, vatom=True)
     assert rel_max(r["f"], g["f"]) < TOL and rel_rms(r["f"], g["f"]) < TOL
+    assert rel_max(r["vatom_tersoff"], g["vatom_tersoff"]) < TOL
+    assert rel_max(r["vatom_ilp"], g["vatom_ilp"]) < TOL
     assert abs(r["e_tersoff"] - g["e_tersoff"]) <= E_TOL * abs(g["e_tersoff"])
     assert abs(r["e_ilp"] - g["e_ilp"]) <= E_TOL * abs(g["e_ilp"])
     assert rel_max(r["pvector"], g["pvector"]) < E_TOL

@@ -3,7 +3,7 @@ tests/golden/make_golden.py from the reference sources).  This pins the oracle: 
 parity test compares the engine with it."""
 import numpy as np
 import pytest
-from conftest import GOLDEN_LISTS, GOLDEN_SINGLE, ILP, TERSOFF, load_golden, min_image, rel_max, rel_rms
+from conftest import GOLDEN_LISTS, GOLDEN_SINGLE, GOLDEN_VATOM, ILP, TERSOFF, load_golden, min_image, rel_max, rel_rms
 
 from oracle import Oracle
 
@@ -31,6 +31,17 @@ def test_oracle_matches_reference(name):
     assert rel_max(r["pvector"], g["pvector"]) < E_TOL
     assert rel_max(r["virial"], g["virial"]) < TOL
     assert rel_max(r["eatom"], g["eatom"]) < TOL
+
+
+@pytest.mark.parametrize("name", GOLDEN_VATOM)
+def test_oracle_per_atom_virial_matches_reference(name):
+    """Each style's per-atom virial as the reference's ev_tally / ev_tally_xyz / v_tally3
+    calls split it (pair_tersoff.cpp:173,223,253; pair_ilp_graphene_hbn.cpp:536,667,671),
+    ghost shares folded into their owners."""
+    g = load_golden(name)
+    r = _oracle_for(g).forces(vatom=True)
+    assert rel_max(r["vatom_tersoff"], g["vatom_tersoff"]) < TOL
+    assert rel_max(r["vatom_ilp"], g["vatom_ilp"]) < TOL
 
 
 def _set(a):

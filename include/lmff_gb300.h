@@ -25,6 +25,8 @@
  *                          calc_FvdW, calc_FRep) + the neighbour build
  *                          (npair_full_bin_ghost.cpp:36-140) + virial_fdotr_compute
  *                          (pair.cpp:1554) + per-atom energy tallies (pair.cpp:913,1060)
+ *   lmff_compute_vatom     the per-atom virial tallies of both styles (Pair::vatom:
+ *                          pair.cpp ev_tally :913, ev_tally_xyz :1060, v_tally3 :1435)
  *   lmff_upload / lmff_run_nve / lmff_download
  *                          Verlet::run (verlet.cpp:220-339) with FixNVE
  *                          (fix_nve.cpp:64-111) and Neighbor::decide / check_distance
@@ -263,6 +265,22 @@ int lmff_compute(lmff_engine *e, int natoms, const double *x, const int *type, c
 int lmff_compute_ghost(lmff_engine *e, int nlocal, int nall, const double *x, const int *type,
                        const int64_t *mol, const int64_t *tag, int which, int eflag, int vflag,
                        double *f, double *eatom, lmff_result *res);
+
+/* Per-atom virial of the evaluation that the previous call on this engine made
+ * (lmff_compute, lmff_compute_ghost, lmff_compute_device or lmff_compute_resident; a
+ * second lmff_compute_vatom for the other style may follow; after any other call of
+ * the engine that uses the device it returns LMFF_EINVAL): Pair::vatom of
+ * PairTersoff::compute (pair_tersoff.cpp:173, :223, :253) and of PairILPGrapheneHBN /
+ * PairKolmogorovCrespiFull::compute (pair_ilp_graphene_hbn.cpp:536, :667, :671), split
+ * over atoms as their ev_tally, ev_tally_xyz and v_tally3 calls split it (pair.cpp).
+ * which = LMFF_TERSOFF and/or LMFF_ILP selects the styles (each sub-style of
+ * hybrid/overlay has its own vatom); LMFF_OVERWRITE overwrites instead of accumulating.
+ * vatom[natoms*6] in the evaluated call's atom order, rows xx yy zz xy xz yz (LAMMPS
+ * order, energy units, not divided by a volume); natoms = that call's natoms (nall in
+ * subdomain mode, where ghost rows carry the shares LAMMPS's reverse communication
+ * folds into their owners).  Computed in FP64 by a separate pass in either precision
+ * mode, from the evaluated positions; not for batches (LMFF_EUNSUPPORTED). */
+int lmff_compute_vatom(lmff_engine *e, int which, int natoms, double *vatom);
 
 /* Same on device pointers (d_x[natoms*3] double, d_type int32, d_mol int64, d_tag int64
  * or NULL, d_f double accumulated), ordered on the engine's stream. */

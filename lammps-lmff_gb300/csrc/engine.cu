@@ -44,6 +44,9 @@ namespace lmff {
   }
 LMFF_FORCE_API(f64, double)
 LMFF_FORCE_API(f32, float)
+namespace f64 {
+void launch_vatom(const ForceArgs<double> &a, double *out, cudaStream_t s);
+}
 
 static const double LOG2E = 1.4426950408889634;
 static const double FTM2V = 1.0 / 1.0364269e-4;  // units metal (update.cpp)
@@ -153,6 +156,17 @@ __global__ void k_scatter_sum(int n, const int *perm, const double *fs, const do
   for (int c = 0; c < 3; c++) {
     double v = fs[(size_t)c * n + q];
     fout[3 * o + c] = fin ? fin[3 * o + c] + v : v;
+  }
+}
+
+// per-atom rows of 6 (the per-atom virial), sorted order -> the caller's
+__global__ void k_scatter_add6(int n, const int *perm, const double *vs, double *vin, int overwrite) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int o = perm[q];
+  for (int c = 0; c < 6; c++) {
+    double v = vs[6 * (size_t)q + c];
+    vin[6 * (size_t)o + c] = overwrite ? v : vin[6 * (size_t)o + c] + v;
   }
 }
 
@@ -544,6 +558,14 @@ struct Engine {
   double **d_arrs = nullptr;
   double **d_karrs = nullptr;
   double *d_kout = nullptr;
+  // per-atom virial pass (lmff_compute_vatom): own shares, slots, the sorted result and
+  // the result in the caller's order, VA_DOUBLES per atom of capacity va_cap
+  static constexpr int VA_DOUBLES = 6 * (2 + MAXTERS + MAXILP + 2);
+  double *d_va = nullptr;
+  int va_cap = 0;
+  // device calls on this engine (counted by DeviceCall) and the one whose evaluation
+  // lmff_compute_vatom may still use
+  uint64_t calls = 0, va_call = 0;
   // single-pass list build: stride of the scratch slices (0: two passes), only grown, so
   // that a captured rebuild keeps working; largest per-atom count of the last build
   int stride = 0;
@@ -640,7 +662,7 @@ struct Engine {
                     d.short_cnt, d.short_nb, d.list_img, d.nin_tmp, d.list_tmp, d.bin_key, d.bin_key2, d.idx, d.idx2, d.bin_start, d.bin_end, d.rowocc, d.cub_tmp,
                     d.cnt_tmp, d.sys, d.red_out, d.status, d.maxdisp, d_xin, d_fin, d_fo, d_vin, d_ein, d_tin, d_sysin,
                     d_min, d_gin, d_massT, xq2, v2, mass2, tag2, perm2, sysid2, stat_ilp, stat_ters, eatom_ilp,
-                    eatom_ters, ke, d_arrs, d_karrs, d_kout, d_cutILPsq, d_maxpred};
+                    eatom_ters, ke, d_arrs, d_karrs, d_kout, d_cutILPsq, d_maxpred, d_va};
     for (void *p : ptrs)
       if (p) cudaFree(p);
     d = DevState();
@@ -660,6 +682,8 @@ struct Engine {
     d_kout = nullptr;
     d_cutILPsq = nullptr;
     d_maxpred = nullptr;
+    d_va = nullptr;
+    va_cap = 0;
     if (h_pinned) cudaFreeHost(h_pinned);
     h_pinned = nullptr;
     h_pinned_bytes = 0;
@@ -1057,7 +1081,7 @@ struct Engine {
   }
   double device_bytes() const {
     return (double)cap_n * per_atom_bytes() + (double)(d.list_cap + d.tmp_cap) * sizeof(uint32_t) +
-           (double)d.cub_tmp_bytes + (double)d.nbins_cap * 3 * sizeof(int);
+           (double)d.cub_tmp_bytes + (double)d.nbins_cap * 3 * sizeof(int) + (double)va_cap * VA_DOUBLES * sizeof(double);
   }
   // device bytes per atom a batch like the current one needs: the per-atom arrays with
   // their growth margin, the pair list at the current density with the step graph's
@@ -1838,6 +1862,40 @@ struct Engine {
       k_scatter_add<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, d.f, df, (which & LMFF_OVERWRITE) != 0);
       CK(cudaGetLastError());
     }
+    CK(cudaStreamSynchronize(stream));
+    return LMFF_OK;
+  }
+
+  // Per-atom virial of the last evaluation (lmff_compute_vatom): the FP64 pass of
+  // launch_vatom on that evaluation's lists and positions, in either precision mode,
+  // added into out[6 nn] in the caller's atom order.
+  int vatom(int which, int nn, double *out) {
+    if (nn != n) return fail(LMFF_EINVAL, "lmff_compute_vatom: natoms is not the atom count of the last evaluation");
+    if (hsys.size() > 1) return fail(LMFF_EUNSUPPORTED, "lmff_compute_vatom: batches are not supported");
+    if (n == 0) return LMFF_OK;
+    if (va_cap < cap_n) {
+      if (d_va) cudaFree(d_va);
+      d_va = nullptr;
+      va_cap = 0;
+      CK(cudaMalloc(&d_va, sizeof(double) * VA_DOUBLES * (size_t)cap_n));
+      va_cap = cap_n;
+    }
+    ForceArgs<double> a = args<double>();
+    a.do_ters = t_on && (which & LMFF_TERSOFF);
+    a.do_ilp = i_on && (which & LMFF_ILP);
+    const size_t c6 = 6 * (size_t)va_cap;
+    a.va_t = d_va;
+    a.va_i = d_va + c6;
+    a.va_ts = d_va + 2 * c6;
+    a.va_is = a.va_ts + MAXTERS * c6;
+    double *sorted = a.va_is + MAXILP * c6;
+    double *inorder = sorted + c6;
+    f64::launch_vatom(a, sorted, stream);
+    CK(cudaGetLastError());
+    const bool overwrite = (which & LMFF_OVERWRITE) != 0;
+    if (!overwrite) CK(cudaMemcpyAsync(inorder, out, sizeof(double) * 6 * (size_t)nn, cudaMemcpyHostToDevice, stream));
+    k_scatter_add6<<<(nn + 255) / 256, 256, 0, stream>>>(nn, d.perm, sorted, inorder, overwrite);
+    CK(cudaMemcpyAsync(out, inorder, sizeof(double) * 6 * (size_t)nn, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     return LMFF_OK;
   }
@@ -3020,6 +3078,7 @@ using lmff::Engine;
 struct DeviceCall {
   std::shared_lock<std::shared_mutex> lk;
   explicit DeviceCall(Engine &g) {
+    g.calls++;
     int dev = (g.device >= 0 && g.device < 64) ? g.device : 0;
     cudaSetDevice(g.device);
     for (int attempt = 0;; attempt++) {
@@ -3257,7 +3316,9 @@ int lmff_compute(lmff_engine *e, int natoms, const double *x, const int *type, c
   if (!e || natoms < 0 || (natoms > 0 && (!x || !type))) return LMFF_EINVAL;
   if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
-  return e->e.compute_host(natoms, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
+  const int rc = e->e.compute_host(natoms, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
+  if (rc == LMFF_OK) e->e.va_call = e->e.calls;
+  return rc;
 }
 
 int lmff_compute_ghost(lmff_engine *e, int nlocal, int nall, const double *x, const int *type, const int64_t *mol,
@@ -3265,7 +3326,9 @@ int lmff_compute_ghost(lmff_engine *e, int nlocal, int nall, const double *x, co
                        lmff_result *res) {
   if (!e || nlocal < 0 || nall < nlocal || (nall > 0 && (!x || !type || !tag))) return LMFF_EINVAL;
   DeviceCall dc(e->e);
-  return e->e.compute_ghost(nlocal, nall, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
+  const int rc = e->e.compute_ghost(nlocal, nall, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
+  if (rc == LMFF_OK) e->e.va_call = e->e.calls;
+  return rc;
 }
 
 int lmff_compute_device(lmff_engine *e, int natoms, const double *d_x, const int *d_type, const int64_t *d_mol,
@@ -3273,7 +3336,9 @@ int lmff_compute_device(lmff_engine *e, int natoms, const double *d_x, const int
   if (!e || natoms < 0 || (natoms > 0 && (!d_x || !d_type))) return LMFF_EINVAL;
   if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
-  return e->e.compute_device(natoms, d_x, d_type, d_mol, d_tag, which, eflag, vflag, d_f, res);
+  const int rc = e->e.compute_device(natoms, d_x, d_type, d_mol, d_tag, which, eflag, vflag, d_f, res);
+  if (rc == LMFF_OK) e->e.va_call = e->e.calls;
+  return rc;
 }
 
 int lmff_compute_device_noalloc(lmff_engine *e, int natoms, const double *d_x, const int *d_type,
@@ -3304,7 +3369,18 @@ int lmff_compute_resident(lmff_engine *e, int which, int eflag, int vflag, lmff_
   rc = e->e.forces(which, eflag || vflag, false, &hr);
   if (rc) return rc;
   if (res) *res = hr.empty() ? lmff_result() : hr[0];
+  e->e.va_call = e->e.calls;
   return LMFF_OK;
+}
+
+int lmff_compute_vatom(lmff_engine *e, int which, int natoms, double *vatom) {
+  if (!e || natoms < 0 || (natoms > 0 && !vatom)) return LMFF_EINVAL;
+  if (e->e.va_call == 0 || e->e.va_call != e->e.calls)
+    return e->e.fail(LMFF_EINVAL, "lmff_compute_vatom: must directly follow an evaluation on this engine");
+  DeviceCall dc(e->e);
+  const int rc = e->e.vatom(which, natoms, vatom);
+  e->e.va_call = rc == LMFF_OK ? e->e.calls : 0;   // the two styles may be asked one after the other
+  return rc;
 }
 
 int lmff_run_nve(lmff_engine *e, int nsteps, double dt, int thermo_every, lmff_thermo *thermo) {

@@ -298,6 +298,11 @@ struct ForceArgs {
   double *eatom_ilp;   // n (EATOM only)
   double *eatom_ters;  // n
   double *f_out;       // 3*n SoA (k_finish)
+  // per-atom virial pass (FP64 kernels run on request after an evaluation), 6 doubles
+  // per entry in LAMMPS order xx yy zz xy xz yz: each atom's own share per style (va_t,
+  // va_i: n entries) and the shares it leaves for its Tersoff bond partners (va_ts:
+  // MAXTERS per atom, by short-list slot) and intralayer neighbours (va_is: MAXILP per atom)
+  double *va_t, *va_i, *va_ts, *va_is;
   int *status;
   int do_ters, do_ilp;
   int list_full;       // the pair list also holds same-molecule / non-ILP pairs

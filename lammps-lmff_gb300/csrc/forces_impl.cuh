@@ -434,7 +434,12 @@ __device__ __forceinline__ void df_dot3(const float *ah, const float *al, const 
 // summed in FP32 before one FP64 addition.
 // GH (subdomain mode): a bond's repulsion counts when the end the tag-parity half keeps
 // is owned, the bond-order terms when the centre i is owned.
-template <int NB, bool EV, bool GH>
+// VA (per-atom virial, FP64 instantiation only): the virial split over atoms as the
+// reference tallies it -- ev_tally of the repulsion and of force_zeta's pair force, half
+// to each end (pair_tersoff.cpp:173, :223), v_tally3 of each triplet, a third to each of
+// i, j, k (:253).  i's shares go to va_t[i]; its partners' shares to i's per-bond slots
+// va_ts, which the per-atom virial gather collects.
+template <int NB, bool EV, bool GH, bool VA = false>
 __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int ie, int cnt) {
   constexpr bool F32 = sizeof(R) == 4;
   constexpr int UNR = NB <= 4 ? NB : 1;
@@ -451,6 +456,14 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
   R uf[NB][NB];          // FP32 mode: h_ijk - cos(theta_jik)
   double fx = 0, fy = 0, fz = 0, eng = 0;
   double v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
+  double vo[6] = {0, 0, 0, 0, 0, 0};   // VA: i's own share
+  double vs[VA ? NB : 1][6];           // VA: the shares of i's bond partners
+  if constexpr (VA) {
+#pragma unroll UNR
+    for (int s = 0; s < NB; s++)
+#pragma unroll
+      for (int c = 0; c < 6; c++) vs[s][c] = 0.0;
+  }
 #pragma unroll UNR
   for (int s = 0; s < NB; s++) {
     if (s < cnt) {
@@ -565,6 +578,13 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
           fpair = -pr->A64 * tmp_exp * (fcd - fc * pr->lam1_64) / r;
         }
         fr -= fpair;
+        if constexpr (VA) {
+          // ev_tally(i, j, .., fpair, del): del (x) del fpair, half to this end
+          const double w[6] = {dxd[s] * dxd[s] * fpair, dyd[s] * dyd[s] * fpair, dzd[s] * dzd[s] * fpair,
+                               dxd[s] * dyd[s] * fpair, dxd[s] * dzd[s] * fpair, dyd[s] * dzd[s] * fpair};
+#pragma unroll
+          for (int c = 0; c < 6; c++) vo[c] += 0.5 * w[c];
+        }
         if (EV) {
           eng += 0.5 * fc * pr->A64 * tmp_exp;
           double h = 0.5 * fpair;
@@ -628,6 +648,15 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
     fx += dxd[s] * fr; fy += dyd[s] * fr; fz += dzd[s] * fr;
     const double fjx = -dxd[s] * fpair, fjy = -dyd[s] * fpair, fjz = -dzd[s] * fpair;
     gx[s] = fjx; gy[s] = fjy; gz[s] = fjz;   // the only radial contribution to partner s
+    if constexpr (VA) {
+      // ev_tally(i, j, .., -fpair, -delr1): half to i, half to j
+      const double w[6] = {dxd[s] * fjx, dyd[s] * fjy, dzd[s] * fjz, dxd[s] * fjy, dxd[s] * fjz, dyd[s] * fjz};
+#pragma unroll
+      for (int c = 0; c < 6; c++) {
+        vo[c] += 0.5 * w[c];
+        vs[s][c] += 0.5 * w[c];
+      }
+    }
     if (EV) {
       double eb = 0.5 * bij * fa;
       eng += eb;
@@ -681,6 +710,21 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
         ajy += prefactor * (A1 * djy + A2 * rhy);
         ajz += prefactor * (A1 * djz + A2 * rhz);
         tx[k] += fkx_; ty[k] += fky_; tz[k] += fkz_;
+        if constexpr (VA) {
+          // v_tally3(i, j, k, fj, fk, delr1, delr2): a third to each of i, j, k
+          const double third = 1.0 / 3.0;
+          const double fjx_ = prefactor * (A1 * djx + A2 * rhx), fjy_ = prefactor * (A1 * djy + A2 * rhy),
+                       fjz_ = prefactor * (A1 * djz + A2 * rhz);
+          const double w[6] = {third * (dx[s] * fjx_ + dx[k] * fkx_), third * (dy[s] * fjy_ + dy[k] * fky_),
+                               third * (dz[s] * fjz_ + dz[k] * fkz_), third * (dx[s] * fjy_ + dx[k] * fky_),
+                               third * (dx[s] * fjz_ + dx[k] * fkz_), third * (dy[s] * fjz_ + dy[k] * fkz_)};
+#pragma unroll
+          for (int c = 0; c < 6; c++) {
+            vo[c] += w[c];
+            vs[s][c] += w[c];
+            vs[k][c] += w[c];
+          }
+        }
         if (EV) {
           v0 += (double)(dx[k] * fkx_); v1 += (double)(dy[k] * fky_); v2 += (double)(dz[k] * fkz_);
           v3 += (double)(dx[k] * fky_); v4 += (double)(dx[k] * fkz_); v5 += (double)(dy[k] * fkz_);
@@ -704,6 +748,15 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
   a.ters_f[i] = fx;
   a.ters_f[a.n + i] = fy;
   a.ters_f[2 * a.n + i] = fz;
+  if constexpr (VA) {
+#pragma unroll
+    for (int c = 0; c < 6; c++) a.va_t[6 * (size_t)i + c] = vo[c];
+#pragma unroll UNR
+    for (int s = 0; s < NB; s++)
+      if (s < cnt)
+#pragma unroll
+        for (int c = 0; c < 6; c++) a.va_ts[((size_t)i * MAXTERS + s) * 6 + c] = vs[s][c];
+  }
   if (EV) {
     double *st = a.stat_ters;
     st[i] = eng;
@@ -714,15 +767,15 @@ __device__ __forceinline__ void tersoff_atom(const ForceArgs<R> &a, int i, int i
 }
 
 // sp2 layers give 3 bonds per atom: those atoms run with their bonds in registers
-template <bool EV, bool EATOM, bool GH>
+template <bool EV, bool EATOM, bool GH, bool VA = false>
 __global__ void __launch_bounds__(128) k_tersoff(ForceArgs<R> a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const long long iinfo = __double_as_longlong(a.A.xq[i].w);
   const int ie = c_pot.t_map[info_type(iinfo)];
   const int cnt = ie < 0 ? 0 : a.ters_cnt[i];
-  if (cnt <= 3) tersoff_atom<3, EV, GH>(a, i, ie, cnt);
-  else tersoff_atom<MAXTERS, EV, GH>(a, i, ie, cnt);
+  if (cnt <= 3) tersoff_atom<3, EV, GH, VA>(a, i, ie, cnt);
+  else tersoff_atom<MAXTERS, EV, GH, VA>(a, i, ie, cnt);
 }
 
 // ---- Tersoff with one lane per bond (small systems) ---------------------------------
@@ -2328,6 +2381,268 @@ __global__ void k_ters_eatom_own(ForceArgs<R> a) {
   a.eatom_ters[i] = (a.stat_ters[i] - bonds) + e;
 }
 
+#ifndef LMFF_PACKED_X2
+// ===================================================== per-atom virial (FP64) =====
+// Pair::vatom as the reference's tallies split it (pair.cpp ev_tally :913, ev_tally_xyz
+// :1060, v_tally3 :1435), run on request after an evaluation in either precision mode:
+// FP64 kernels from the FP64 positions, lists and constants.  Deterministic like the
+// forces: every atom sums its own shares, and the shares it cannot form itself are left
+// in per-slot arrays by the atom that can and gathered in a fixed order.
+//
+// ILP (pair_ilp_graphene_hbn.cpp:536, :667, :671).  For atom i and each interlayer
+// neighbour j (del = x_i - x_j):
+//   * vdW: ev_tally of fsum along del, half to each end, once per pair;
+//   * the repulsion term with i's normal (i owns it): ev_tally_xyz of its pair force fkc
+//     along del, half to i; and its normal-derivative forces fk on i's intralayer
+//     neighbours m, tallied against x_m - x_j, half to m and half to j.  j's half is
+//     formed by j (below); m's half is summed over j here through
+//       sum_j (x_m - x_j) (x) fk_jm = v_m (x) c_m(g_i) + [c_m(G_i row p)]_pb,
+//     with v_m = x_m - x_i, c_m(g) = -(dn_i/dx_m)^T g the normal-derivative force for a
+//     vector g, g_i = sum_j c_ij del and G_i = sum_j c_ij del (x) del (c_ij = Tap prod
+//     fpair1): the first from the whole of g_i, the second from the three rows of the
+//     symmetric G_i, four applications of i's frame, written to i's slot of m;
+//   * the term with j's normal (i is its partner): half of its pair force's tally, and
+//     i's half of its normal-derivative tallies, sum_m (x_m - x_i) (x) fk_m over j's
+//     intralayer neighbours m, = W_j + del_ji (x) sum_m c_m from one application of j's
+//     frame to g = c_ji del_ji (W_j = sum_m v_m (x) c_m, the assembly's own virial).
+// Subdomain mode: vdW when the end the tag-parity half keeps is owned, each repulsion
+// term when its normal's atom is owned.
+
+// the frame k_nframe left for atom i and the normal it carries: the reference's (0,0,1)
+// for fewer than two intralayer neighbours (calc_normal, pair_ilp_graphene_hbn.cpp:800-806)
+__device__ __forceinline__ void va_frame(const ForceArgs<R> &a, int i, NFrame &fr, double &nx, double &ny,
+                                         double &nz) {
+  const d4 f0 = a.nframe[4 * (size_t)i], f1 = a.nframe[4 * (size_t)i + 1], f2 = a.nframe[4 * (size_t)i + 2],
+           f3 = a.nframe[4 * (size_t)i + 3];
+  fr.nx = f0.x; fr.ny = f0.y; fr.nz = f0.z; fr.inn = f0.w;
+  fr.v[0][0] = f1.x; fr.v[0][1] = f1.y; fr.v[0][2] = f1.z; fr.cont = (int)f1.w;
+  fr.v[1][0] = f2.x; fr.v[1][1] = f2.y; fr.v[1][2] = f2.z; fr.ok = f2.w != 0.0;
+  fr.v[2][0] = f3.x; fr.v[2][1] = f3.y; fr.v[2][2] = f3.z;
+  if (fr.cont >= 2) {
+    nx = fr.nx; ny = fr.ny; nz = fr.nz;
+  } else {
+    nx = 0.0; ny = 0.0; nz = 1.0;
+  }
+}
+
+// one repulsion term (calc_FRep :609-640, kolmogorov/crespi/full :600-645) with normal n
+// along del: its pair force fkc and c = Tap prod fpair1, the weight of its normal-
+// derivative forces
+template <bool KC>
+__device__ __forceinline__ void va_rep(const IlpP<double> &p, double nx, double ny, double nz, double dx, double dy,
+                                       double dz, double rsq, double r, double Tap, double dTap, double fkc[3],
+                                       double &c) {
+  const double prod = nx * dx + ny * dy + nz * dz;
+  const double rhosq = rsq - prod * prod;
+  const double x = rhosq * p.delta2inv;
+  const double exp0 = exp(-p.lambda * (r - p.z0));
+  const double exp1 = exp(-x);
+  double V, fpair, fpair1;
+  if constexpr (KC) {
+    const double sumC1 = p.kc_C0 + p.kc_C2 * x + p.kc_C4 * x * x;
+    const double sumC11 = (p.kc_C2 + 2.0 * p.kc_C4 * x) * p.delta2inv;
+    const double E = p.eps_half + exp1 * sumC1;
+    V = exp0 * E;
+    fpair = p.lambda * exp0 / r * E;
+    fpair1 = 2.0 * exp0 * exp1 * (p.delta2inv * sumC1 - sumC11);
+  } else {
+    const double frho = exp1 * p.C;
+    const double E = p.eps_half + frho;
+    V = exp0 * E;
+    fpair = p.lambda * exp0 / r * E;
+    fpair1 = 2.0 * exp0 * frho * p.delta2inv;
+  }
+  const double fsum = fpair + fpair1;
+  fkc[0] = (dx * fsum - prod * nx * fpair1) * Tap - V * dTap * dx / r;
+  fkc[1] = (dy * fsum - prod * ny * fpair1) * Tap - V * dTap * dy / r;
+  fkc[2] = (dz * fsum - prod * nz * fpair1) * Tap - V * dTap * dz / r;
+  c = Tap * prod * fpair1;
+}
+
+// v += s * (d (x) f) in LAMMPS order (ev_tally_xyz's v[6])
+__device__ __forceinline__ void va_add_xyz(double v[6], double s, double dx, double dy, double dz, const double f[3]) {
+  v[0] += s * (dx * f[0]); v[1] += s * (dy * f[1]); v[2] += s * (dz * f[2]);
+  v[3] += s * (dx * f[1]); v[4] += s * (dx * f[2]); v[5] += s * (dy * f[2]);
+}
+
+template <bool GH, bool KC>
+__global__ void __launch_bounds__(128) k_va_ilp(ForceArgs<R> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  double w[6] = {0, 0, 0, 0, 0, 0};
+  double gx = 0, gy = 0, gz = 0;
+  double G[6] = {0, 0, 0, 0, 0, 0};   // xx yy zz xy xz yz
+  const long long iinfo = __double_as_longlong(a.A.xq[i].w);
+  const int ie = c_pot.i_map[info_type(iinfo)];
+  const bool iown = !GH || owned(a, i);
+  NFrame fri;
+  double nix, niy, niz;
+  va_frame(a, i, fri, nix, niy, niz);
+  if (ie >= 0) {
+    const SysDesc &sd = a.A.sys[a.A.sysid[i]];
+    const long long mi = info_mol(iinfo);
+    const long long itag = a.tag[i];
+    const double cutsq = c_pot.i_cutsq;
+    const int64_t q1 = a.list_off[i + 1];
+    for (int64_t q = a.list_off[i]; q < q1; q++) {
+      int j, sx, sy, sz;
+      decode_entry(a.list[q], a.lc, j, sx, sy, sz);
+      const long long jinfo = __double_as_longlong(a.A.xq[j].w);
+      if (info_mol(jinfo) == mi) continue;
+      const int je = c_pot.i_map[info_type(jinfo)];
+      if (je < 0) continue;
+      double dx, dy, dz;
+      disp64(a.A.xq, sd, i, j, sx, sy, sz, dx, dy, dz);
+      const double rsq = rsq_rn(dx, dy, dz);
+      if (!(rsq < cutsq)) continue;
+      const double r = sqrt(rsq);
+      double Tap = 1.0, dTap = 0.0;
+      if (c_pot.tap) {
+        // Tap = 20x^7 - 70x^6 + 84x^5 - 35x^4 + 1, dTap/dr = 140 x^3 (x - 1)^3 / Rcut
+        const double xr = r * c_pot.i_inv_rcut, x2 = xr * xr;
+        Tap = (((20.0 * xr - 70.0) * xr + 84.0) * xr - 35.0) * (x2 * x2) + 1.0;
+        const double y = x2 - xr;
+        dTap = (y * y) * (y * (140.0 * c_pot.i_inv_rcut));
+      }
+      const bool jown = !GH || owned(a, j);
+      const long long jtag = a.tag[j];
+      const bool keep = GH ? keep_half_r(itag, jtag, -dx, -dy, -dz) : keep_half(itag, jtag, sx, sy, sz);
+      // ---- vdW (calc_FvdW :506-540), the kept end's parameters
+      if (!GH || (keep ? iown : jown)) {
+        const IlpP<double> &pv = c_pot.ilp[(keep || c_pot.vdw_sym) ? ie * MAXELEM + je : je * MAXELEM + ie];
+        const double r2inv = 1.0 / rsq, r6inv = r2inv * r2inv * r2inv, r8inv = r6inv * r2inv;
+        double Vv, fpv;
+        if constexpr (KC) {
+          Vv = -pv.kc_Az06 * r6inv;
+          fpv = -6.0 * pv.kc_Az06 * r8inv;
+        } else {
+          const double TS = 1.0 + exp(-pv.d * (r / pv.seff - 1.0));
+          const double TS2inv = 1.0 / (TS * TS);
+          Vv = -pv.C6 * r6inv / TS;
+          fpv = -6.0 * pv.C6 * r8inv / TS + pv.C6 * pv.d / pv.seff * (TS - 1.0) * TS2inv * r8inv * r;
+        }
+        const double fs = fpv * Tap - Vv * dTap / r;
+        const double f3[3] = {fs * dx, fs * dy, fs * dz};
+        va_add_xyz(w, 0.5, dx, dy, dz, f3);
+      }
+      // ---- the term with i's normal
+      if (iown) {
+        double fkc[3], c;
+        va_rep<KC>(c_pot.ilp[ie * MAXELEM + je], nix, niy, niz, dx, dy, dz, rsq, r, Tap, dTap, fkc, c);
+        va_add_xyz(w, 0.5, dx, dy, dz, fkc);
+        gx += c * dx; gy += c * dy; gz += c * dz;
+        G[0] += c * (dx * dx); G[1] += c * (dy * dy); G[2] += c * (dz * dz);
+        G[3] += c * (dx * dy); G[4] += c * (dx * dz); G[5] += c * (dy * dz);
+      }
+      // ---- the term with j's normal, i its partner: del' = x_j - x_i
+      if (jown) {
+        NFrame frj;
+        double njx, njy, njz;
+        va_frame(a, j, frj, njx, njy, njz);
+        const double ex = -dx, ey = -dy, ez = -dz;
+        double fkc[3], c;
+        va_rep<KC>(c_pot.ilp[je * MAXELEM + ie], njx, njy, njz, ex, ey, ez, rsq, r, Tap, dTap, fkc, c);
+        va_add_xyz(w, 0.5, ex, ey, ez, fkc);
+        if (frj.ok) {
+          NDeriv o;
+          nderiv_apply<true>(frj, make_d4(c * ex, c * ey, c * ez, 0.0), o);
+          const double sc[3] = {o.c[0][0] + o.c[1][0] + o.c[2][0], o.c[0][1] + o.c[1][1] + o.c[2][1],
+                                o.c[0][2] + o.c[1][2] + o.c[2][2]};
+#pragma unroll
+          for (int k = 0; k < 6; k++) w[k] += 0.5 * o.W[k];
+          va_add_xyz(w, 0.5, ex, ey, ez, sc);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 6; k++) a.va_i[6 * (size_t)i + k] = w[k];
+  // ---- i's slots: the halves of its normal-derivative tallies that its intralayer
+  // neighbours receive
+  double s[MAXILP][6];
+#pragma unroll
+  for (int m = 0; m < MAXILP; m++)
+#pragma unroll
+    for (int k = 0; k < 6; k++) s[m][k] = 0.0;
+  if (ie >= 0 && iown && fri.ok) {
+    NDeriv og, o0, o1, o2;
+    nderiv_apply<false>(fri, make_d4(gx, gy, gz, 0.0), og);
+    nderiv_apply<false>(fri, make_d4(G[0], G[3], G[4], 0.0), o0);   // row x of G
+    nderiv_apply<false>(fri, make_d4(G[3], G[1], G[5], 0.0), o1);   // row y
+    nderiv_apply<false>(fri, make_d4(G[4], G[5], G[2], 0.0), o2);   // row z
+#pragma unroll
+    for (int m = 0; m < MAXILP; m++) {
+      if (m >= fri.cont) break;
+      const double *v = fri.v[m];
+      s[m][0] = 0.5 * (v[0] * og.c[m][0] + o0.c[m][0]);
+      s[m][1] = 0.5 * (v[1] * og.c[m][1] + o1.c[m][1]);
+      s[m][2] = 0.5 * (v[2] * og.c[m][2] + o2.c[m][2]);
+      s[m][3] = 0.5 * (v[0] * og.c[m][1] + o0.c[m][1]);
+      s[m][4] = 0.5 * (v[0] * og.c[m][2] + o0.c[m][2]);
+      s[m][5] = 0.5 * (v[1] * og.c[m][2] + o1.c[m][2]);
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < MAXILP; m++)
+#pragma unroll
+    for (int k = 0; k < 6; k++) a.va_is[((size_t)i * MAXILP + m) * 6 + k] = s[m][k];
+}
+
+// Per atom: its own shares plus the slots its Tersoff bond partners and the atoms whose
+// intralayer list holds it left for it (found as k_finish finds its force slots), in a
+// fixed order, into out[6 n] (sorted order).
+__global__ void __launch_bounds__(128) k_va_gather(ForceArgs<R> a, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  double w[6] = {0, 0, 0, 0, 0, 0};
+  if (a.do_ters) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) w[k] += a.va_t[6 * (size_t)i + k];
+    const int cnt = a.ters_cnt[i];
+    for (int s = 0; s < cnt; s++) {
+      int j, sx, sy, sz;
+      decode_entry(a.ters_nb[(size_t)i * MAXTERS + s], a.lc, j, sx, sy, sz);
+      const uint32_t want = encode_entry(i, -sx, -sy, -sz, a.lc);
+      const int cj = a.ters_cnt[j];
+      for (int t = 0; t < cj; t++) {
+        if (a.ters_nb[(size_t)j * MAXTERS + t] == want) {
+          const double *v = a.va_ts + ((size_t)j * MAXTERS + t) * 6;
+#pragma unroll
+          for (int k = 0; k < 6; k++) w[k] += v[k];
+          break;
+        }
+      }
+    }
+  }
+  if (a.do_ilp) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) w[k] += a.va_i[6 * (size_t)i + k];
+    const bool sym = c_pot.ilp_cut_sym != 0;
+    const int cnt = sym ? a.ilp_cnt[i] : a.short_cnt[i];
+    const uint32_t *cand = sym ? a.ilp_nb + (size_t)i * MAXILP : a.short_nb + (size_t)i * MAXSHORT;
+    const long long mi = sym ? 0 : info_mol(__double_as_longlong(a.A.xq[i].w));
+    for (int c = 0; c < cnt; c++) {
+      int j, sx, sy, sz;
+      decode_entry(cand[c], a.lc, j, sx, sy, sz);
+      const int cj = a.ilp_cnt[j];
+      if (cj == 0) continue;
+      if (!sym && info_mol(__double_as_longlong(a.A.xq[j].w)) != mi) continue;
+      const uint32_t want = encode_entry(i, -sx, -sy, -sz, a.lc);
+      for (int t = 0; t < cj; t++) {
+        if (a.ilp_nb[(size_t)j * MAXILP + t] == want) {
+          const double *v = a.va_is + ((size_t)j * MAXILP + t) * 6;
+#pragma unroll
+          for (int k = 0; k < 6; k++) w[k] += v[k];
+          break;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 6; k++) out[6 * (size_t)i + k] = w[k];
+}
+#endif  // !LMFF_PACKED_X2
+
 // ============================================================ host launchers ======
 
 void upload_pot(const PotConst<R> &p, cudaStream_t s) {
@@ -2524,6 +2839,30 @@ void launch_finish(const ForceArgs<R> &a, bool eatom, const KickArgs *kick, cuda
   else if (eatom) k_finish<true, false><<<g, 128, 0, s>>>(a, k);
   else k_finish<false, false><<<g, 128, 0, s>>>(a, k);
 }
+
+#ifndef LMFF_PACKED_X2
+// The per-atom virial pass on the lists and positions of the last evaluation: Tersoff's
+// shares (the one-thread routine with VA; it also rewrites the force scratch arrays,
+// which the evaluation has already gathered), the FP64 normal frames, ILP's shares, and
+// the gather into out[6 n] (sorted order).  a.do_ters / a.do_ilp select the styles.
+void launch_vatom(const ForceArgs<R> &a, double *out, cudaStream_t s) {
+  if (a.n == 0) return;
+  const int g = (a.n + 127) / 128;
+  const bool gh = a.own_perm != nullptr;
+  if (a.do_ters) {
+    if (gh) k_tersoff<false, false, true, true><<<g, 128, 0, s>>>(a);
+    else k_tersoff<false, false, false, true><<<g, 128, 0, s>>>(a);
+  }
+  if (a.do_ilp) {
+    k_nframe<<<g, 128, 0, s>>>(a);
+    if (gh && a.kc) k_va_ilp<true, true><<<g, 128, 0, s>>>(a);
+    else if (gh) k_va_ilp<true, false><<<g, 128, 0, s>>>(a);
+    else if (a.kc) k_va_ilp<false, true><<<g, 128, 0, s>>>(a);
+    else k_va_ilp<false, false><<<g, 128, 0, s>>>(a);
+  }
+  k_va_gather<<<g, 128, 0, s>>>(a, out);
+}
+#endif
 
 }  // namespace LMFF_NS
 }  // namespace lmff

@@ -73,8 +73,6 @@ void gb300::compute(LAMMPS *lmp, Pair *self, GB300Style *me, int slot, int eflag
   Domain *domain = lmp->domain;
   if (domain->triclinic)
     lmp->error->all(FLERR,(std::string("Pair style ") + name + " requires an orthogonal box").c_str());
-  if (vflag_atom)
-    lmp->error->all(FLERR,(std::string("Pair style ") + name + " does not compute per-atom virials").c_str());
   if (!me->gb) lmp->error->all(FLERR,(std::string(name) + ": engine not set up").c_str());
 
   // one MPI rank: the periodic form (owned atoms + box); a domain decomposition: the
@@ -92,6 +90,7 @@ void gb300::compute(LAMMPS *lmp, Pair *self, GB300Style *me, int slot, int eflag
                             big ? NULL : (const int32_t *) mol, big ? (const int64_t *) mol : NULL,
                             big ? NULL : (const int32_t *) atom->tag, big ? (const int64_t *) atom->tag : NULL,
                             lmp->neighbor->ago == 0, domain->boxlo, domain->boxhi, periodic,
-                            n ? &atom->f[0][0] : NULL, eflag_atom ? self->eatom : NULL, eflag, vflag, out, err);
+                            n ? &atom->f[0][0] : NULL, eflag_atom ? self->eatom : NULL,
+                            (vflag_atom && n) ? &self->vatom[0][0] : NULL, eflag, vflag, out, err);
   if (rc != LMFF_OK) lmp->error->one(FLERR,(std::string(name) + ": " + err).c_str());
 }

@@ -88,7 +88,7 @@ int Adapter::create(const StyleParams &sp, int device, int precision, std::strin
 int Adapter::compute(int which, int nlocal, int nall, bool subdomain, const double *x, const int *type,
                      const int32_t *mol32, const int64_t *mol64, const int32_t *tag32, const int64_t *tag64,
                      bool reneighbored, const double boxlo[3], const double boxhi[3], const int periodic[3], double *f,
-                     double *eatom, int eflag, int vflag, StyleOut out[2], std::string &err) {
+                     double *eatom, double *vatom, int eflag, int vflag, StyleOut out[2], std::string &err) {
   out[0] = StyleOut();
   out[1] = StyleOut();
   if (!e_) {
@@ -125,6 +125,8 @@ int Adapter::compute(int which, int nlocal, int nall, bool subdomain, const doub
     rc = lmff_compute_ghost(e_, nlocal, nall, x, type, mol_.data(), tag_.data(), flags, eflag, vflag, f, eatom, &res);
   else
     rc = lmff_compute(e_, nlocal, x, type, mol_.data(), tag_.data(), flags, eflag, vflag, f, eatom, &res);
+  if (rc == LMFF_OK && vatom && n > 0)
+    rc = lmff_compute_vatom(e_, which & (LMFF_TERSOFF | LMFF_ILP), n, vatom);
   if (rc != LMFF_OK) {
     err = lmff_last_error(e_);
     have_identity_ = false;
@@ -146,8 +148,8 @@ int Adapter::compute(int which, int nlocal, int nall, bool subdomain, const doub
 int Shared::evaluate(int slot, bool partner_computes, int nlocal, int nall, bool subdomain, const double *x,
                      const int *type, const int32_t *mol32, const int64_t *mol64, const int32_t *tag32,
                      const int64_t *tag64, bool reneighbored, const double boxlo[3], const double boxhi[3],
-                     const int periodic[3], double *f, double *eatom, int eflag, int vflag, StyleOut &out,
-                     std::string &err) {
+                     const int periodic[3], double *f, double *eatom, double *vatom, int eflag, int vflag,
+                     StyleOut &out, std::string &err) {
   if (pending_[slot]) {   // the partner's call this step evaluated this style too
     pending_[slot] = false;
     out = cache_[slot];
@@ -157,7 +159,7 @@ int Shared::evaluate(int slot, bool partner_computes, int nlocal, int nall, bool
   const int other = slot == 0 ? LMFF_ILP : LMFF_TERSOFF;
   StyleOut o[2];
   int rc = ad.compute(mine | (partner_computes ? other : 0), nlocal, nall, subdomain, x, type, mol32, mol64, tag32,
-                      tag64, reneighbored, boxlo, boxhi, periodic, f, eatom, eflag, vflag, o, err);
+                      tag64, reneighbored, boxlo, boxhi, periodic, f, eatom, vatom, eflag, vflag, o, err);
   if (rc != LMFF_OK) return rc;
   out = o[slot];
   if (partner_computes) {

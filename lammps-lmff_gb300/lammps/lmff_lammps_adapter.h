@@ -14,13 +14,15 @@
 //    forces and per-atom energies for all nall atoms, which LAMMPS's reverse
 //    communication folds onto their owners.
 // Forces are accumulated into f, energies per style into StyleOut::eng_vdwl, the global
-// virial into StyleOut::virial, per-atom energy into eatom.
+// virial into StyleOut::virial, per-atom energy into eatom, per-atom virial (rows of 6,
+// LAMMPS's vatom) into vatom.
 //
 // With pair_style hybrid/overlay of a Tersoff and an interlayer gb300 style, both share
 // one engine (Shared): PairHybrid::compute (pair_hybrid.cpp:93-137) calls the sub-styles
 // one after the other, and the first one called evaluates both in one engine call (one
 // list build, one short-list pass, one launch sequence); the second takes its energies,
-// virial and pvector from that evaluation and adds no force.
+// virial and pvector from that evaluation and adds no force (per-atom energies and
+// virials of both styles go to the first style's arrays, whose sum PairHybrid forms).
 #pragma once
 
 #include <stdint.h>
@@ -83,11 +85,11 @@ class Adapter {
   // (LAMMPS tagint); pass the matching pointer and nullptr for the other.
   // reneighbored: LAMMPS rebuilt its lists this step (atoms may have been reordered or
   // exchanged), so the identity arrays are sent again.  out[0]: Tersoff, out[1]: the
-  // interlayer style.
+  // interlayer style.  eatom, vatom: nullptr when not asked (eflag_atom, vflag_atom).
   int compute(int which, int nlocal, int nall, bool subdomain, const double *x, const int *type, const int32_t *mol32,
               const int64_t *mol64, const int32_t *tag32, const int64_t *tag64, bool reneighbored,
-              const double boxlo[3], const double boxhi[3], const int periodic[3], double *f, double *eatom, int eflag,
-              int vflag, StyleOut out[2], std::string &err);
+              const double boxlo[3], const double boxhi[3], const int periodic[3], double *f, double *eatom,
+              double *vatom, int eflag, int vflag, StyleOut out[2], std::string &err);
 
  private:
   lmff_engine *e_ = nullptr;
@@ -109,7 +111,7 @@ class Shared {
   int evaluate(int slot, bool partner_computes, int nlocal, int nall, bool subdomain, const double *x, const int *type,
                const int32_t *mol32, const int64_t *mol64, const int32_t *tag32, const int64_t *tag64,
                bool reneighbored, const double boxlo[3], const double boxhi[3], const int periodic[3], double *f,
-               double *eatom, int eflag, int vflag, StyleOut &out, std::string &err);
+               double *eatom, double *vatom, int eflag, int vflag, StyleOut &out, std::string &err);
   void reset() { pending_[0] = pending_[1] = false; }
 
  private:

@@ -127,6 +127,7 @@ def load_library(path: str = LIB_PATH):
         "lmff_compute": ([P, I, P, P, P, P, I, I, I, P, P, C.POINTER(Result)], I),
         "lmff_compute_device": ([P, I, P, P, P, P, I, I, I, P, C.POINTER(Result)], I),
         "lmff_compute_ghost": ([P, I, I, P, P, P, P, I, I, I, P, P, C.POINTER(Result)], I),
+        "lmff_compute_vatom": ([P, I, I, P], I),
         "lmff_compute_device_noalloc": ([P, I, P, P, P, I, I, I, P, C.POINTER(Result)], I),
         "lmff_upload": ([P, I, P, P, P, P, P, P], I),
         "lmff_compute_resident": ([P, I, I, I, C.POINTER(Result)], I),
@@ -236,7 +237,9 @@ class Engine:
     # -------------------------------------------------------------- one-shot compute
     def compute(self, x, type_, mol=None, tag=None, which: int = TERSOFF | ILP, eflag: bool = True,
                 vflag: bool = True, eatom: bool = False, same_atoms: bool = False, f=None,
-                overwrite: bool = False) -> Dict:
+                overwrite: bool = False, vatom: bool = False) -> Dict:
+        """vatom: also each style's per-atom virial ("vatom_tersoff", "vatom_ilp" [n, 6]
+        and their sum "vatom"), from lmff_compute_vatom right after the evaluation."""
         x = _f64(x)
         n = x.shape[0]
         t = np.ascontiguousarray(type_, dtype=np.int32)
@@ -248,21 +251,39 @@ class Engine:
         flags = which | (SAME_ATOMS if same_atoms else 0) | (OVERWRITE if overwrite else 0)
         self._ck(_lib.lmff_compute(self._h, n, _p(x), _p(t), _p(m), _p(g), flags, int(eflag), int(vflag),
                                    _p(out_f), _p(ea), C.byref(r)))
+        self._last_n = n
         out = r.to_dict()
         out["f"] = out_f
         if eatom:
             out["eatom"] = ea
+        if vatom:
+            self._add_vatom(out, which)
         return out
+
+    def vatom(self, which: int = TERSOFF | ILP, natoms: Optional[int] = None) -> np.ndarray:
+        """Per-atom virial (lmff_compute_vatom) of the evaluation the previous call on this
+        engine made: [n, 6], rows xx yy zz xy xz yz in that call's atom order (nall rows
+        after compute_ghost), the styles selected by `which`."""
+        n = getattr(self, "_last_n", 0) if natoms is None else int(natoms)
+        v = np.zeros((n, 6))
+        self._ck(_lib.lmff_compute_vatom(self._h, which, n, _p(v)))
+        return v
+
+    def _add_vatom(self, out: Dict, which: int):
+        vt = self.vatom(TERSOFF) if which & TERSOFF else np.zeros((self._last_n, 6))
+        vi = self.vatom(ILP) if which & ILP else np.zeros((self._last_n, 6))
+        out["vatom_tersoff"], out["vatom_ilp"], out["vatom"] = vt, vi, vt + vi
 
     def compute_system(self, s, **kw) -> Dict:
         self.set_box(s.box_lo, s.box_hi, s.periodic)
         return self.compute(s.x, s.type, s.mol, s.tag, **kw)
 
     def compute_ghost(self, nlocal: int, x, type_, mol, tag, which: int = TERSOFF | ILP, eflag=True, vflag=True,
-                      eatom=False, same_atoms=False) -> Dict:
+                      eatom=False, same_atoms=False, vatom=False) -> Dict:
         """Subdomain evaluation (lmff_compute_ghost): x[nall,3] holds the owned atoms
         [0, nlocal) then the ghost atoms; returns f[nall,3] (ghost shares included),
-        eatom[nall] if asked, and the energies/virials of the owned interactions."""
+        eatom[nall] and the per-atom virials [nall, 6] if asked, and the energies/virials
+        of the owned interactions."""
         x = _f64(x).reshape(-1, 3)
         nall = x.shape[0]
         t = np.ascontiguousarray(type_, dtype=np.int32)
@@ -274,10 +295,13 @@ class Engine:
         flags = which | (SAME_ATOMS if same_atoms else 0)
         self._ck(_lib.lmff_compute_ghost(self._h, int(nlocal), nall, _p(x), _p(t), _p(m), _p(g), flags, int(eflag),
                                          int(vflag), _p(f), _p(ea), C.byref(r)))
+        self._last_n = nall
         out = r.to_dict()
         out["f"] = f
         if eatom:
             out["eatom"] = ea
+        if vatom:
+            self._add_vatom(out, which)
         return out
 
     def compute_device(self, x, type_, mol, tag, f, which: int = TERSOFF | ILP, eflag=True, vflag=True,
@@ -290,6 +314,7 @@ class Engine:
                                           mol.data_ptr() if mol is not None else None,
                                           tag.data_ptr() if tag is not None else None, flags, int(eflag),
                                           int(vflag), f.data_ptr(), C.byref(r)))
+        self._last_n = int(x.shape[0])
         return r.to_dict()
 
     def compute_device_noalloc(self, x, type_, mol, f, which: int = TERSOFF | ILP, eflag=True, vflag=True) -> Dict:
@@ -320,6 +345,7 @@ class Engine:
     def compute_resident(self, which: int = TERSOFF | ILP, eflag=True, vflag=True) -> Dict:
         r = Result()
         self._ck(_lib.lmff_compute_resident(self._h, which, int(eflag), int(vflag), C.byref(r)))
+        self._last_n = self._n
         return r.to_dict()
 
     def run_nve(self, nsteps: int, dt: float = 0.001, thermo_every: int = 0) -> List[Dict]:

@@ -11,8 +11,8 @@
 //          k > 0: k subdomains in the subdomain form), double box[6], int32
 //          periodic[3], tap_flag; then per system (one, or nsub): int32 nlocal, nall;
 //          double x[nall*3]; int32 type[nall], mol[nall], tag[nall]
-// out.bin: per call (two) and per system: double f[nall*3], eatom[nall], e_tersoff,
-//          e_ilp, pvector[2], virial[6] (sum of both styles)
+// out.bin: per call (two) and per system: double f[nall*3], eatom[nall], vatom[nall*6],
+//          e_tersoff, e_ilp, pvector[2], virial[6] (sum of both styles)
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -101,14 +101,16 @@ int main(int argc, char **argv) {
     for (int k = 0; k < nsys; k++) {
       Sys &s = sys[k];
       const size_t n = subdomain ? s.nall : s.nlocal;
-      std::vector<double> f(3 * n, 0.0), eatom(n, 0.0);   // force_clear / ev_setup
+      std::vector<double> f(3 * n, 0.0), eatom(n, 0.0), vatom(6 * n, 0.0);   // force_clear / ev_setup
       lmff_lammps::StyleOut ot, oi;
       const bool renei = call == 0;
       const bool partner = shared != 0;
       if (eng_t[k]->evaluate(0, partner, s.nlocal, s.nall, subdomain, s.x.data(), s.type.data(), s.mol.data(), nullptr,
-                             s.tag.data(), nullptr, renei, box, box + 3, per, f.data(), eatom.data(), 1, 1, ot, err) ||
+                             s.tag.data(), nullptr, renei, box, box + 3, per, f.data(), eatom.data(), vatom.data(), 1,
+                             1, ot, err) ||
           eng_i[k]->evaluate(1, partner, s.nlocal, s.nall, subdomain, s.x.data(), s.type.data(), s.mol.data(), nullptr,
-                             s.tag.data(), nullptr, renei, box, box + 3, per, f.data(), eatom.data(), 1, 1, oi, err)) {
+                             s.tag.data(), nullptr, renei, box, box + 3, per, f.data(), eatom.data(), vatom.data(), 1,
+                             1, oi, err)) {
         fprintf(stderr, "%s\n", err.c_str());
         return 6;
       }
@@ -116,6 +118,7 @@ int main(int argc, char **argv) {
       for (int q = 0; q < 6; q++) vir[q] = ot.virial[q] + oi.virial[q];
       fwrite(f.data(), 8, f.size(), fo);
       fwrite(eatom.data(), 8, n, fo);
+      fwrite(vatom.data(), 8, 6 * n, fo);
       fwrite(&ot.eng_vdwl, 8, 1, fo);
       fwrite(&oi.eng_vdwl, 8, 1, fo);
       fwrite(oi.pvector, 8, 2, fo);

@@ -62,7 +62,7 @@ def _oracle(name):
         s = build_fn()
         o = Oracle(TERSOFF, ILP, elements=elements, nthreads=os.cpu_count() or 1)
         o.set_system(s)
-        _REF[name] = (s, o.forces(eatom=True))
+        _REF[name] = (s, o.forces(eatom=True, vatom=True))
     return _REF[name]
 
 
@@ -92,6 +92,20 @@ def test_mixed_matches_oracle_on_benchmark_workloads(name):
     assert abs(got["e_ilp"] - ref["e_ilp"]) <= MIX_E_REL * abs(ref["e_ilp"])
     assert rel_max(got["pvector"], ref["pvector"]) <= MIX_E_REL
     assert rel_max(got["virial"], ref["virial"]) <= MIX_W_REL
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+@pytest.mark.parametrize("name", sorted(_CASES))
+def test_vatom_matches_oracle_on_benchmark_workloads(name, precision):
+    """Per-atom virial (an FP64 pass in either mode) at 1e-10 per style; with three
+    intralayer neighbours for every atom each style's per-atom virials sum to its fdotr
+    virial (the reference leaves out only the dn_i/dx_i term of atoms with two)."""
+    s, ref = _oracle(name)
+    got = _engine(name, precision=precision).compute_system(s, vatom=True)
+    assert rel_max(got["vatom_tersoff"], ref["vatom_tersoff"]) <= F64_TOL
+    assert rel_max(got["vatom_ilp"], ref["vatom_ilp"]) <= F64_TOL
+    assert rel_max(got["vatom_tersoff"].sum(0), ref["virial_tersoff"]) <= 1e-9
+    assert rel_max(got["vatom_ilp"].sum(0), ref["virial_ilp"]) <= 1e-9
 
 
 @pytest.mark.parametrize("name", sorted(_CASES))

@@ -5,7 +5,8 @@ LAMMPS (tests/lammps_adapter_driver.cpp), against the reference's golden outputs
   style's call evaluates both, the second takes its energies from that call);
 - the periodic form (one MPI rank) and the subdomain form (the system split over ranks
   with ghost shells built as LAMMPS's brick decomposition does; the ghost forces and
-  per-atom energies folded onto their owners as LAMMPS's reverse communication does)."""
+  per-atom energies and virials folded onto their owners as LAMMPS's reverse
+  communication does)."""
 import os
 import subprocess
 
@@ -37,8 +38,8 @@ def driver(tmp_path_factory):
 
 
 def run_driver(driver, tmp_path, g, shared, splits=None):
-    """Returns, per call (two), the folded whole-system f, eatom, energies, pvector,
-    virial."""
+    """Returns, per call (two), the folded whole-system f, eatom, vatom, energies,
+    pvector, virial."""
     n = len(g["tag"])
     if splits is None:
         systems = [(np.arange(n), np.asarray(g["x"], float), np.arange(n), n)]
@@ -65,6 +66,7 @@ def run_driver(driver, tmp_path, g, shared, splits=None):
     for call in range(2):
         f = np.zeros((n, 3))
         ea = np.zeros(n)
+        va = np.zeros((n, 6))
         tot = np.zeros(10)   # e_tersoff, e_ilp, pvector[2], virial[6]
         for own, xs, idx, nlocal in systems:
             m = len(idx) if splits is not None else n
@@ -72,17 +74,21 @@ def run_driver(driver, tmp_path, g, shared, splits=None):
             pos += 3 * m
             np.add.at(ea, idx, raw[pos:pos + m])
             pos += m
+            np.add.at(va, idx, raw[pos:pos + 6 * m].reshape(m, 6))
+            pos += 6 * m
             tot += raw[pos:pos + 10]
             pos += 10
-        calls.append((f, ea, tot))
+        calls.append((f, ea, va, tot))
     assert pos == raw.size
     return calls
 
 
 def check(calls, g):
-    for call, (f, ea, tot) in enumerate(calls):
+    for call, (f, ea, va, tot) in enumerate(calls):
         assert rel_max(f, g["f"]) <= TOL, call
         assert rel_max(ea, g["eatom"]) <= TOL, call
+        if "vatom_ilp" in g:   # per-atom virial (vflag_atom) of both styles together
+            assert rel_max(va, g["vatom_tersoff"] + g["vatom_ilp"]) <= TOL, call
         assert abs(tot[0] - g["e_tersoff"]) <= TOL * abs(g["e_tersoff"]), call
         assert abs(tot[1] - g["e_ilp"]) <= TOL * abs(g["e_ilp"]), call
         assert rel_max(tot[2:4], g["pvector"]) <= TOL, call

@@ -201,7 +201,15 @@ void lmff_destroy(lmff_engine *e);
 
 /* ---- configuration ---------------------------------------------------------------- */
 int lmff_set_precision(lmff_engine *e, int mode);
-/* Orthogonal box only (xy = xz = yz = 0); periodic[d] != 0 marks periodic dims. */
+/* Box lo/hi and LAMMPS's tilt factors xy, xz, yz (domain.cpp: the edges (hi-lo)_x,
+ * (xy, (hi-lo)_y, 0), (xz, yz, (hi-lo)_z)); periodic[d] != 0 marks periodic dims.
+ * A triclinic box (any tilt non-zero) is evaluated by lmff_compute and
+ * lmff_compute_vatom only: the engine wraps the atoms into the box by whole lattice
+ * vectors, adds the periodic images within the neighbour cutoff of it as ghosts (the
+ * atoms a LAMMPS rank would hold, comm_brick.cpp borders) and evaluates them in the
+ * subdomain form of lmff_compute_ghost, folding the images' shares into their owners;
+ * LMFF_SAME_ATOMS has no effect there.  The resident, batch, device and subdomain
+ * calls return LMFF_EUNSUPPORTED / LMFF_EINVAL on a triclinic box. */
 int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double xy, double xz,
                  double yz, const int periodic[3]);
 /* Tunables: "tpa" threads per atom in the ILP kernel (4,8,16,32), "block" threads per

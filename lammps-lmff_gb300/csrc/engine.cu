@@ -533,6 +533,14 @@ struct Engine {
   double blo[3] = {0, 0, 0}, bhi[3] = {0, 0, 0};
   int bper[3] = {0, 0, 0};
   bool have_box = false;
+  // triclinic box (lmff_set_box with a tilt): lmff_compute evaluates the owned atoms and
+  // their periodic images, made on the host, through the subdomain form; tri_owner[a] is
+  // the owned atom of each of the last call's atoms (owned first, then images)
+  bool tri = false;
+  double tlo[3] = {0, 0, 0}, thi[3] = {0, 0, 0}, tilt[3] = {0, 0, 0};   // tilt: xy xz yz
+  int tper[3] = {0, 0, 0};
+  std::vector<int> tri_owner;
+  int tri_n = -1;
   // state
   DevState d;
   std::vector<SysDesc> hsys;
@@ -1826,6 +1834,97 @@ struct Engine {
     return compute_host(nall, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
   }
 
+  // A triclinic periodic box (domain.cpp: h = [[lx, xy, xz], [0, ly, yz], [0, 0, lz]],
+  // lamda = h^-1 (x - lo)): the owned atoms are wrapped into the box by whole lattice
+  // vectors (an atom inside keeps its coordinates to the bit), then every periodic image
+  // whose lamda lies within the ghost cutoff of the box, cutneigh in each direction
+  // (lamda_d within cutneigh |row d of h^-1| of [0, 1), the distance between the box's
+  // faces of constant lamda_d being 1 / |row d|), is added as a ghost carrying its
+  // owner's type, molecule and tag -- the atoms a LAMMPS rank holds (comm_brick.cpp
+  // borders, domain.cpp pbc) -- and the subdomain form evaluates them.  The images'
+  // forces and per-atom energies are folded into their owners.
+  int compute_tri(int nn, const double *x, const int *type, const int64_t *mol, const int64_t *tag, int which,
+                  int eflag, int vflag, double *f, double *eatom, lmff_result *res) {
+    const double lx = thi[0] - tlo[0], ly = thi[1] - tlo[1], lz = thi[2] - tlo[2];
+    const double xy = tilt[0], xz = tilt[1], yz = tilt[2];
+    const double col[3][3] = {{lx, 0.0, 0.0}, {xy, ly, 0.0}, {xz, yz, lz}};
+    // rows of h^-1 (domain.cpp h_inv)
+    const double r0[3] = {1.0 / lx, -xy / (lx * ly), (xy * yz - ly * xz) / (lx * ly * lz)};
+    const double r1[3] = {0.0, 1.0 / ly, -yz / (ly * lz)};
+    const double r2[3] = {0.0, 0.0, 1.0 / lz};
+    const double *row[3] = {r0, r1, r2};
+    const double cg = cutneigh_max > 0.0 ? cutneigh_max : skin;
+    double cl[3];
+    int K[3];
+    for (int d = 0; d < 3; d++) {
+      cl[d] = cg * std::sqrt(row[d][0] * row[d][0] + row[d][1] * row[d][1] + row[d][2] * row[d][2]);
+      K[d] = tper[d] ? (int)std::ceil(cl[d]) : 0;
+    }
+    std::vector<double> xw(3 * (size_t)nn), lam(3 * (size_t)nn);
+    for (int p = 0; p < nn; p++) {
+      const double q[3] = {x[3 * p] - tlo[0], x[3 * p + 1] - tlo[1], x[3 * p + 2] - tlo[2]};
+      double l[3], s[3];
+      for (int d = 0; d < 3; d++) {
+        l[d] = row[d][0] * q[0] + row[d][1] * q[1] + row[d][2] * q[2];
+        if (!std::isfinite(l[d])) return fail(LMFF_EINVAL, "lmff_compute: non-finite coordinate");
+        s[d] = tper[d] ? std::floor(l[d]) : 0.0;
+      }
+      for (int c = 0; c < 3; c++) {
+        const double sh = s[0] * col[0][c] + s[1] * col[1][c] + s[2] * col[2][c];
+        xw[3 * p + c] = sh != 0.0 ? x[3 * p + c] - sh : x[3 * p + c];
+      }
+      for (int d = 0; d < 3; d++) lam[3 * p + d] = l[d] - s[d];
+    }
+    std::vector<double> xs(xw);
+    std::vector<int> ts(type, type + nn), own(nn);
+    std::vector<int64_t> ms(nn), gs(nn);
+    for (int p = 0; p < nn; p++) {
+      own[p] = p;
+      ms[p] = mol ? mol[p] : 0;
+      gs[p] = tag ? tag[p] : (int64_t)(p + 1);
+    }
+    for (int a = -K[0]; a <= K[0]; a++)
+      for (int b = -K[1]; b <= K[1]; b++)
+        for (int c = -K[2]; c <= K[2]; c++) {
+          if (a == 0 && b == 0 && c == 0) continue;
+          const int sh[3] = {a, b, c};
+          double dv[3];
+          for (int k = 0; k < 3; k++) dv[k] = a * col[0][k] + b * col[1][k] + c * col[2][k];
+          for (int p = 0; p < nn; p++) {
+            bool in = true;
+            for (int d = 0; d < 3 && in; d++) {
+              if (!tper[d]) continue;   // no images along a non-periodic direction
+              const double l = lam[3 * p + d] + sh[d];
+              in = l >= -cl[d] && l < 1.0 + cl[d];
+            }
+            if (!in) continue;
+            for (int k = 0; k < 3; k++) xs.push_back(xw[3 * p + k] + dv[k]);
+            ts.push_back(type[p]);
+            ms.push_back(ms[p]);
+            gs.push_back(gs[p]);
+            own.push_back(p);
+          }
+        }
+    if (xs.size() / 3 > (size_t)INT32_MAX / 2) return fail(LMFF_EOVERFLOW, "lmff_compute: too many periodic images");
+    const int nall = (int)own.size();
+    std::vector<double> fa(3 * (size_t)nall, 0.0), ea(eatom ? (size_t)nall : 0, 0.0);
+    int rc = compute_ghost(nn, nall, xs.data(), ts.data(), ms.data(), gs.data(), which & (LMFF_TERSOFF | LMFF_ILP),
+                           eflag, vflag, fa.data(), eatom ? ea.data() : nullptr, res);
+    if (rc) return rc;
+    const bool overwrite = (which & LMFF_OVERWRITE) != 0;
+    if (f && overwrite) memset(f, 0, sizeof(double) * 3 * (size_t)nn);
+    if (eatom && overwrite) memset(eatom, 0, sizeof(double) * (size_t)nn);
+    for (int a = 0; a < nall; a++) {
+      const int o = own[a];
+      if (f)
+        for (int c = 0; c < 3; c++) f[3 * (size_t)o + c] += fa[3 * (size_t)a + c];
+      if (eatom) eatom[o] += ea[a];
+    }
+    tri_owner.swap(own);
+    tri_n = nn;
+    return LMFF_OK;
+  }
+
   int compute_device(int nn, const double *dx, const int *dtype, const int64_t *dmol, const int64_t *dtag, int which,
                      int eflag, int vflag, double *df, lmff_result *res) {
     int rc = ensure_atoms(nn);
@@ -1870,6 +1969,18 @@ struct Engine {
   // launch_vatom on that evaluation's lists and positions, in either precision mode,
   // added into out[6 nn] in the caller's atom order.
   int vatom(int which, int nn, double *out) {
+    if (tri && tri_n >= 0) {   // the last evaluation was a triclinic lmff_compute: fold the images
+      if (nn != tri_n) return fail(LMFF_EINVAL, "lmff_compute_vatom: natoms is not the atom count of the last evaluation");
+      std::vector<double> va(6 * (size_t)n, 0.0);
+      tri_n = -1;   // the inner call evaluates the n = owned + image atoms
+      int rc = vatom((which & (LMFF_TERSOFF | LMFF_ILP)) | LMFF_OVERWRITE, n, va.data());
+      tri_n = nn;
+      if (rc) return rc;
+      if (which & LMFF_OVERWRITE) memset(out, 0, sizeof(double) * 6 * (size_t)nn);
+      for (int a = 0; a < n; a++)
+        for (int c = 0; c < 6; c++) out[6 * (size_t)tri_owner[a] + c] += va[6 * (size_t)a + c];
+      return LMFF_OK;
+    }
     if (nn != n) return fail(LMFF_EINVAL, "lmff_compute_vatom: natoms is not the atom count of the last evaluation");
     if (hsys.size() > 1) return fail(LMFF_EUNSUPPORTED, "lmff_compute_vatom: batches are not supported");
     if (n == 0) return LMFF_OK;
@@ -3227,7 +3338,28 @@ int lmff_set_precision(lmff_engine *e, int mode) {
 int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double xy, double xz, double yz,
                  const int periodic[3]) {
   if (!e || !lo || !hi || !periodic) return LMFF_EINVAL;
-  if (xy != 0.0 || xz != 0.0 || yz != 0.0) return e->e.fail(LMFF_EUNSUPPORTED, "triclinic boxes are not supported");
+  if (!std::isfinite(xy) || !std::isfinite(xz) || !std::isfinite(yz)) return e->e.fail(LMFF_EINVAL, "non-finite tilt");
+  if (xy != 0.0 || xz != 0.0 || yz != 0.0) {
+    for (int k = 0; k < 3; k++)
+      if (!(hi[k] > lo[k])) return e->e.fail(LMFF_EINVAL, "box hi must exceed lo");
+    Engine &g = e->e;
+    for (int k = 0; k < 3; k++) {
+      g.tlo[k] = lo[k];
+      g.thi[k] = hi[k];
+      g.tper[k] = periodic[k] != 0;
+    }
+    g.tilt[0] = xy;
+    g.tilt[1] = xz;
+    g.tilt[2] = yz;
+    g.tri = true;
+    g.tri_n = -1;
+    return LMFF_OK;
+  }
+  if (e->e.tri) {   // leaving a triclinic box (and the subdomain form it ran through)
+    e->e.tri = false;
+    e->e.tri_n = -1;
+    e->e.have_box = false;
+  }
   bool changed = false;
   for (int k = 0; k < 3; k++) {
     if (!(hi[k] > lo[k])) return e->e.fail(LMFF_EINVAL, "box hi must exceed lo");
@@ -3248,8 +3380,11 @@ int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double 
   return LMFF_OK;
 }
 
-// calls that evaluate the periodic-system form refuse an engine left in subdomain mode
+// calls that evaluate the periodic-system form refuse an engine left in subdomain mode,
+// and every call but lmff_compute a triclinic box
 static int refuse_ghost_mode(lmff_engine *e) {
+  if (e->e.tri)
+    return e->e.fail(LMFF_EUNSUPPORTED, "triclinic boxes: only lmff_compute and lmff_compute_vatom evaluate them");
   if (e->e.ghost_nlocal < 0) return LMFF_OK;
   return e->e.fail(LMFF_EINVAL, "the engine is in subdomain mode (lmff_compute_ghost): call lmff_set_box to leave it");
 }
@@ -3314,6 +3449,12 @@ int lmff_set_option(lmff_engine *e, const char *key, double value) {
 int lmff_compute(lmff_engine *e, int natoms, const double *x, const int *type, const int64_t *mol, const int64_t *tag,
                  int which, int eflag, int vflag, double *f, double *eatom, lmff_result *res) {
   if (!e || natoms < 0 || (natoms > 0 && (!x || !type))) return LMFF_EINVAL;
+  if (e->e.tri) {
+    DeviceCall dc(e->e);
+    const int rc = e->e.compute_tri(natoms, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
+    if (rc == LMFF_OK) e->e.va_call = e->e.calls;
+    return rc;
+  }
   if (int rc = refuse_ghost_mode(e)) return rc;
   DeviceCall dc(e->e);
   const int rc = e->e.compute_host(natoms, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
@@ -3325,6 +3466,7 @@ int lmff_compute_ghost(lmff_engine *e, int nlocal, int nall, const double *x, co
                        const int64_t *tag, int which, int eflag, int vflag, double *f, double *eatom,
                        lmff_result *res) {
   if (!e || nlocal < 0 || nall < nlocal || (nall > 0 && (!x || !type || !tag))) return LMFF_EINVAL;
+  if (e->e.tri) return e->e.fail(LMFF_EINVAL, "the engine has a triclinic box: call lmff_set_box with an orthogonal one first");
   DeviceCall dc(e->e);
   const int rc = e->e.compute_ghost(nlocal, nall, x, type, mol, tag, which, eflag, vflag, f, eatom, res);
   if (rc == LMFF_OK) e->e.va_call = e->e.calls;

@@ -71,13 +71,12 @@ void gb300::compute(LAMMPS *lmp, Pair *self, GB300Style *me, int slot, int eflag
 {
   Atom *atom = lmp->atom;
   Domain *domain = lmp->domain;
-  if (domain->triclinic)
-    lmp->error->all(FLERR,(std::string("Pair style ") + name + " requires an orthogonal box").c_str());
   if (!me->gb) lmp->error->all(FLERR,(std::string(name) + ": engine not set up").c_str());
 
-  // one MPI rank: the periodic form (owned atoms + box); a domain decomposition: the
-  // subdomain form (owned + ghost atoms)
-  const bool sub = lmp->comm->nprocs > 1 || lmff_lammps::subdomain_from_env();
+  // one MPI rank with an orthogonal box: the periodic form (owned atoms + box); a domain
+  // decomposition or a triclinic box: the subdomain form (owned + ghost atoms, the
+  // ghosts LAMMPS made carrying the periodic images)
+  const bool sub = lmp->comm->nprocs > 1 || domain->triclinic || lmff_lammps::subdomain_from_env();
   const int nlocal = atom->nlocal;
   const int nall = nlocal + atom->nghost;
   const int n = sub ? nall : nlocal;

@@ -225,11 +225,13 @@ class Engine:
     def set_precision(self, mode: int):
         self._ck(_lib.lmff_set_precision(self._h, mode))
 
-    def set_box(self, lo, hi, periodic):
+    def set_box(self, lo, hi, periodic, tilt=None):
+        """tilt: LAMMPS's (xy, xz, yz) of a triclinic box (lmff_compute evaluates it)."""
         lo = _f64(lo)
         hi = _f64(hi)
         per = np.ascontiguousarray(np.asarray(periodic, dtype=bool).astype(np.int32))
-        self._ck(_lib.lmff_set_box(self._h, _p(lo), _p(hi), 0.0, 0.0, 0.0, _p(per)))
+        xy, xz, yz = (0.0, 0.0, 0.0) if tilt is None else (float(t) for t in tilt)
+        self._ck(_lib.lmff_set_box(self._h, _p(lo), _p(hi), xy, xz, yz, _p(per)))
 
     def set_option(self, key: str, value: float):
         self._ck(_lib.lmff_set_option(self._h, key.encode(), float(value)))
@@ -275,7 +277,7 @@ class Engine:
         out["vatom_tersoff"], out["vatom_ilp"], out["vatom"] = vt, vi, vt + vi
 
     def compute_system(self, s, **kw) -> Dict:
-        self.set_box(s.box_lo, s.box_hi, s.periodic)
+        self.set_box(s.box_lo, s.box_hi, s.periodic, getattr(s, "tilt", None))
         return self.compute(s.x, s.type, s.mol, s.tag, **kw)
 
     def compute_ghost(self, nlocal: int, x, type_, mol, tag, which: int = TERSOFF | ILP, eflag=True, vflag=True,

@@ -40,6 +40,9 @@ class System:
     periodic: np.ndarray           # (3,) bool
     v: Optional[np.ndarray] = None  # (N,3) Angstrom/ps
     meta: Dict = dataclasses.field(default_factory=dict)
+    # LAMMPS tilt factors (xy, xz, yz) of a triclinic box, None for an orthogonal one:
+    # the box edges are (hi-lo)_x (1,0,0), (xy, (hi-lo)_y, 0), (xz, yz, (hi-lo)_z)
+    tilt: Optional[np.ndarray] = None
 
     @property
     def n(self) -> int:
@@ -58,7 +61,8 @@ class System:
     def copy(self) -> "System":
         return System(self.x.copy(), self.type.copy(), self.mol.copy(), self.tag.copy(),
                       self.box_lo.copy(), self.box_hi.copy(), self.periodic.copy(),
-                      None if self.v is None else self.v.copy(), dict(self.meta))
+                      None if self.v is None else self.v.copy(), dict(self.meta),
+                      None if self.tilt is None else self.tilt.copy())
 
 
 # --------------------------------------------------------------------------- layers
@@ -215,6 +219,46 @@ def twisted_graphene_hbn_500k(seed: int = 2, theta_deg: float = 0.6) -> System:
     s.x += rng.normal(0.0, 0.02, size=s.x.shape)
     s.meta["displacement_sigma"] = 0.02
     return s
+
+
+def hex_layers(m: int, n: int, nlayers: int = 2, spacing: float = 3.4, species: str = "C",
+               mol_mode: str = "unique", periodic_z: bool = False, xz: float = 0.0, yz: float = 0.0,
+               vacuum: float = 30.0) -> System:
+    """AB-stacked honeycomb layers in a triclinic (hexagonal) cell of m x n primitive
+    cells, C-C 1.42 A: in-plane edges m a (1, 0) and n a (1/2, sqrt(3)/2), a = sqrt(3) d,
+    so LAMMPS's tilt xy = n a / 2 (n < m keeps it below half the x edge, LAMMPS's skew
+    limit).  Primitive-cell basis (0, 0) and (a1 + a2)/3; odd layers shifted by
+    (a1 + a2)/3.  species "C" or "BN" (odd layers B/N on the same lattice: strained
+    hBN, a test geometry).  periodic_z: the z edge is (xz, yz, nlayers * spacing) and
+    the stacking continues through it (each layer also slides by its height fraction of
+    (xz, yz)); otherwise z is not periodic, with ``vacuum`` A around the layers.
+    mol_mode "unique" (layer k has id k+1) or "alternate" (1, 2, 1, 2, ...)."""
+    a = math.sqrt(3.0) * A_CC_GRAPHENE
+    lx, ly, xy = m * a, n * a * math.sqrt(3.0) / 2.0, n * a / 2.0
+    if periodic_z:
+        zlo, lz = -spacing / 2.0, nlayers * spacing
+    else:
+        xz = yz = 0.0
+        zlo, lz = -vacuum / 2.0, (nlayers - 1) * spacing + vacuum
+    h = np.array([[lx, xy, xz], [0.0, ly, yz], [0.0, 0.0, lz]])
+    lo = np.array([0.0, 0.0, zlo])
+    xs, ts, ms = [], [], []
+    ii, jj = np.meshgrid(np.arange(m), np.arange(n), indexing="ij")
+    ii, jj = ii.ravel().astype(float), jj.ravel().astype(float)
+    for k in range(nlayers):
+        f0 = (k % 2) / 3.0
+        for b, f in enumerate((f0, f0 + 1.0 / 3.0)):
+            lam = np.stack([(ii + f) / m, (jj + f) / n, np.full(ii.shape, (k * spacing - zlo) / lz)], axis=1)
+            xs.append(lo + lam @ h.T)
+            t = 1 if species == "C" or k % 2 == 0 else 2 + b
+            ts.append(np.full(len(ii), t, dtype=np.int32))
+            ms.append(np.full(len(ii), (k + 1) if mol_mode == "unique" else 1 + k % 2, dtype=np.int64))
+    x = np.concatenate(xs)
+    tag = np.arange(1, len(x) + 1, dtype=np.int64)
+    return System(x, np.concatenate(ts), np.concatenate(ms), tag, lo, lo + np.array([lx, ly, lz]),
+                  np.array([True, True, periodic_z]), None,
+                  {"kind": "hex_layers", "m": m, "n": n, "nlayers": nlayers, "spacing": spacing},
+                  np.array([xy, xz, yz]))
 
 
 def flake_edges(nx: int = 4, ny: int = 3) -> System:
@@ -375,12 +419,13 @@ def read_lammps_data(path: str, periodic=(True, True, True)) -> System:
     and box, then sections.  Atoms lines are ``id mol type q x y z [ix iy iz]``
     (coordinates kept as written, image flags kept in meta["image"]); Masses and
     Velocities are read; other sections are skipped by their header counts.  Atoms are
-    returned in file order.  Tilted boxes are rejected.  ``periodic`` is the input
-    script's ``boundary`` (a data file does not carry it)."""
+    returned in file order; a tilted box's ``xy xz yz`` go to ``tilt``.  ``periodic`` is
+    the input script's ``boundary`` (a data file does not carry it)."""
     lines = open(path).read().split("\n")
     counts: Dict[str, int] = {}
     lo = np.zeros(3)
     hi = np.zeros(3)
+    tilt = None
     k = 1                                     # line 1 is a title
     while k < len(lines):
         raw = lines[k].split("#", 1)[0].strip()
@@ -394,8 +439,7 @@ def read_lammps_data(path: str, periodic=(True, True, True)) -> System:
             c = "xyz".index(w[-2][0])
             lo[c], hi[c] = float(w[0]), float(w[1])
         elif len(w) >= 6 and w[-3:] == ["xy", "xz", "yz"]:
-            if any(float(t) != 0.0 for t in w[:3]):
-                raise ValueError("tilted (triclinic) boxes are not supported")
+            tilt = np.array([float(t) for t in w[:3]])
         else:
             key = " ".join(w[1:])
             if key not in _HEADER_KEYS:
@@ -474,7 +518,7 @@ def read_lammps_data(path: str, periodic=(True, True, True)) -> System:
     meta = {"kind": "data_file", "path": os.path.basename(path), "ntypes": ntypes, "image": img}
     if np.all(tmass > 0):
         meta["type_masses"] = tmass
-    return System(x, typ, mol, tag, lo, hi, np.array(periodic, dtype=bool), v, meta)
+    return System(x, typ, mol, tag, lo, hi, np.array(periodic, dtype=bool), v, meta, tilt)
 
 
 # ------------------------------------------------------------------------- output
@@ -486,6 +530,8 @@ def write_lammps_data(s: System, path: str, ntypes: int = 3) -> None:
         fh.write(f"{s.n} atoms\n{ntypes} atom types\n\n")
         for c, nm in enumerate("xyz"):
             fh.write(f"{s.box_lo[c]:.17g} {s.box_hi[c]:.17g} {nm}lo {nm}hi\n")
+        if s.tilt is not None:
+            fh.write(f"{s.tilt[0]:.17g} {s.tilt[1]:.17g} {s.tilt[2]:.17g} xy xz yz\n")
         fh.write("\nMasses\n\n")
         for t in range(1, ntypes + 1):
             fh.write(f"{t} {MASSES[t]}\n")

@@ -126,6 +126,10 @@ int main(int argc, char **argv) {
   double box[6] = {lmp->domain->boxlo[0], lmp->domain->boxlo[1], lmp->domain->boxlo[2],
                    lmp->domain->boxhi[0], lmp->domain->boxhi[1], lmp->domain->boxhi[2]};
   rec("box", 'd', 6, box);
+  if (lmp->domain->triclinic) {
+    double tilt[3] = {lmp->domain->xy, lmp->domain->xz, lmp->domain->yz};
+    rec("tilt", 'd', 3, tilt);
+  }
 
   Pair *pair = lmp->force->pair;
   rec("virial", 'd', 6, pair->virial);

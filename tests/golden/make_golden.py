@@ -158,6 +158,8 @@ def pack(s: S.System, r, tap_flag, extra=None):
     for k in ("vatom_tersoff", "vatom_ilp"):
         if k in r:
             d[k] = r[k].reshape(n, 6)
+    if "tilt" in r:
+        d["tilt"] = r["tilt"]
     if "nlist" in r:
         nl = r["nlist"].reshape(-1, 3)
         nl = nl[np.lexsort((nl[:, 2], nl[:, 1], nl[:, 0]))]
@@ -203,6 +205,8 @@ def main():
         _cases_case5016()
     if want("kc_bilayer", "kc_bilayer_notaper", "kc_trilayer_t30"):
         _cases_kc()
+    if want("tri_bilayer", "tri_tilted_bn", "tri_small"):
+        _cases_triclinic()
 
 
 def _cases_bilayer_small():
@@ -281,6 +285,20 @@ def _cases_kc():
     save("kc_trilayer_t30", pack(k, r30, 1, {"interlayer": "kc", "x0": r0["x"].reshape(-1, 3),
                                              "v0": r0["v"].reshape(-1, 3), "f0": r0["f"].reshape(-1, 3),
                                              "e0": r0["e_ilp"][0]}))
+
+
+def _cases_triclinic():
+    # 16-18. triclinic (hexagonal) cells: an AB bilayer (xy tilt, z not periodic), four
+    #        alternating-id layers with B/N in a cell periodic in z with all three tilts
+    #        (the stacking continues through the tilted z edge), and a 24-atom bilayer
+    #        cell much smaller than the 18 A neighbour cutoff (many images per edge)
+    s = S.thermalize(S.displace(S.hex_layers(8, 6), 0.05, seed=81), 300.0, seed=82)
+    save("tri_bilayer", pack(s, run_reference(s), 1))
+    t = S.displace(S.hex_layers(7, 5, nlayers=4, spacing=3.35, species="BN", mol_mode="alternate", periodic_z=True,
+                                xz=0.37, yz=0.21), 0.03, seed=83)
+    save("tri_tilted_bn", pack(t, run_reference(t), 1))
+    u = S.displace(S.hex_layers(3, 2), 0.03, seed=84)
+    save("tri_small", pack(u, run_reference(u), 1))
 
 
 if __name__ == "__main__":

@@ -57,8 +57,14 @@ def test_reader_round_trip_and_errors(tmp_path):
     for k in ("x", "v", "type", "mol", "tag", "box_lo", "box_hi"):
         assert np.array_equal(getattr(r, k), getattr(s, k)), k
     txt = open(p).read()
-    bad = {"tilt": txt.replace("zlo zhi\n", "zlo zhi\n0.5 0 0 xy xz yz\n", 1),
-           "section": txt.replace("Atoms # full", "Ellipse"),
+    # a tilted box: its xy xz yz line round-trips through tilt
+    t = S.hex_layers(5, 3, nlayers=2, periodic_z=True, xz=0.3, yz=-0.2)
+    q = str(tmp_path / "t.data")
+    S.write_lammps_data(t, q)
+    rt = S.read_lammps_data(q)
+    assert np.array_equal(rt.tilt, t.tilt) and np.array_equal(rt.x, t.x)
+    assert r.tilt is None
+    bad = {"section": txt.replace("Atoms # full", "Ellipse"),
            "columns": txt.replace("Atoms # full\n\n1 ", "Atoms # full\n\n1 1 ", 1),
            "short": txt[:txt.index("Velocities")].rsplit("\n", 5)[0]}
     for name, t in bad.items():

@@ -235,7 +235,11 @@ int lmff_set_box(lmff_engine *e, const double lo[3], const double hi[3], double 
  * or 4 lanes per atom in the intralayer lists, 8 in the gather, one lane per bond in
  * Tersoff when it runs alone), 0 = the large-system kernels at every size; the lists and
  * results are the same to the bit either way, except Tersoff run alone, which agrees to
- * rounding.  "check_every" = how often
+ * rounding.  "pdl" = a mask of the step's dependent kernels launched with programmatic
+ * dependent launch up to 65,536 atoms (each scheduled before the previous one ends and
+ * waiting for it on the device): 1 the pair kernel, 2 the normal-derivative kernel, 4 the
+ * gather, 8 the intralayer lists in step graphs, +16 dependents scheduled as each kernel
+ * starts; 0 = ordinary launches; default 14.  The results do not depend on it.  "check_every" = how often
  * lmff_run_nve tests the pair list: 1 = every step, for displacement alone (LAMMPS's
  * neigh_modify every 1 delay 0 check yes); k > 1 = at steps whose index is a multiple
  * of k, rebuilding when an atom may move more than skin/2 before the next test (its

@@ -325,6 +325,46 @@ struct ForceArgs {
   // variants of the short lists, the gather and Tersoff are not used)
   int no_small;
   int kc;              // interlayer style is kolmogorov/crespi/full
+  // programmatic dependent launch (PDL) of the step's chain kernels, a PDL_* mask: which
+  // kernels are launched early behind the kernel before them on the stream (the pair
+  // kernel, the normal-derivative kernel, the gather, and inside a step graph the
+  // intralayer-list kernel after the previous step's gather), and whether the kernels
+  // let their dependents be scheduled as soon as they start (PDL_TRIGGER) or only as
+  // their blocks exit
+  int pdl;
 };
+
+enum : int { PDL_ILP = 1, PDL_NDERIV = 2, PDL_FINISH = 4, PDL_SHORT = 8, PDL_TRIGGER = 16 };
+
+// First statement of a kernel that may be launched early: wait until the kernels it
+// depends on have completed and their writes are visible (griddepcontrol.wait; a no-op
+// for an ordinary launch), then, with trigger, let its own dependents be scheduled.
+// Waiting before any load or store covers both orders of hazard with the previous kernel.
+__device__ __forceinline__ void pdl_enter(int pdl) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (pdl & PDL_TRIGGER) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// <<<grid, block, 0, s>>> with programmatic stream serialisation when pdl is set: the
+// kernel may be scheduled before the previous kernel on s completes and waits in
+// pdl_enter.  Only for launches whose predecessor on s is always a kernel.
+template <typename... KP, typename... A>
+inline void launch_pdl(bool pdl, void (*k)(KP...), int grid, int block, cudaStream_t s, A... args) {
+  if (!pdl) {
+    k<<<grid, block, 0, s>>>(args...);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
 
 }  // namespace lmff

@@ -81,6 +81,7 @@ constexpr int SHORT_SG16_MAX_ATOMS = 16384;
 constexpr int SHORT_SG_MAX_ATOMS = 65536;
 template <int SG>
 __global__ void k_short(ForceArgs<R> a, const double *cutILPsq64, double tcutmaxsq64) {
+  pdl_enter(a.pdl);
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gtid / SG;
   if (i >= a.n) return;   // whole groups: blockDim is a multiple of SG
@@ -1806,6 +1807,7 @@ constexpr int ilp_min_blocks() {
 // GH: subdomain mode (owned + ghost atoms, see ForceArgs::own_perm)
 template <int TPA, bool EV, bool EATOM, bool ONE, bool GH, bool KC, bool TWO>
 __global__ void __launch_bounds__(256, (ilp_min_blocks<TPA, EV, EATOM, ONE, GH, KC, TWO>())) k_ilp(ForceArgs<R> a) {
+  pdl_enter(a.pdl);
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gtid / TPA;
   const int lane = threadIdx.x & (TPA - 1);
@@ -2136,6 +2138,7 @@ __global__ void k_nframe(ForceArgs<R> a) {
 
 template <bool EV>
 __global__ void k_nderiv(ForceArgs<R> a) {
+  pdl_enter(a.pdl);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   NDeriv o;
@@ -2184,6 +2187,7 @@ __device__ __forceinline__ void kick_atom(const KickArgs &kick, const ForceArgs<
 // derivative forces from every j with a in N_ilp(j).  Fixed summation order.
 template <bool EATOM, bool KICK>
 __global__ void k_finish(ForceArgs<R> a, KickArgs kick) {
+  pdl_enter(a.pdl);
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   double Fx = 0, Fy = 0, Fz = 0, ea = 0;
@@ -2258,6 +2262,7 @@ constexpr int FINISH_ATOMS = 32;
 constexpr int FINISH_LANES_MAX_ATOMS = 65536;
 template <bool EATOM, bool KICK>
 __global__ void __launch_bounds__(FINISH_LANES * FINISH_ATOMS) k_finish_lanes(ForceArgs<R> a, KickArgs kick) {
+  pdl_enter(a.pdl);
   constexpr int L = FINISH_LANES, NA = FINISH_ATOMS, NV = EATOM ? 4 : 3;
   __shared__ double sv[NA][L][NV];
   __shared__ int sf[NA][L];
@@ -2725,12 +2730,14 @@ void upload_pot(const PotConst<R> &p, cudaStream_t s) {
 
 void launch_short(const ForceArgs<R> &a, const double *cutILPsq64, double tcutmaxsq64, cudaStream_t s) {
   if (a.n == 0) return;
+  const bool p = (a.pdl & PDL_SHORT) != 0;
   if (a.no_small)
-    k_short<1><<<(a.n + 127) / 128, 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
+    launch_pdl(p, k_short<1>, (a.n + 127) / 128, 128, s, a, cutILPsq64, tcutmaxsq64);
   else if (a.n <= SHORT_SG16_MAX_ATOMS)
-    k_short<16><<<(int)(((long long)a.n * 16 + 127) / 128), 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
-  else if (a.n <= SHORT_SG_MAX_ATOMS) k_short<4><<<(int)(((long long)a.n * 4 + 127) / 128), 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
-  else k_short<1><<<(a.n + 127) / 128, 128, 0, s>>>(a, cutILPsq64, tcutmaxsq64);
+    launch_pdl(p, k_short<16>, (int)(((long long)a.n * 16 + 127) / 128), 128, s, a, cutILPsq64, tcutmaxsq64);
+  else if (a.n <= SHORT_SG_MAX_ATOMS)
+    launch_pdl(p, k_short<4>, (int)(((long long)a.n * 4 + 127) / 128), 128, s, a, cutILPsq64, tcutmaxsq64);
+  else launch_pdl(p, k_short<1>, (a.n + 127) / 128, 128, s, a, cutILPsq64, tcutmaxsq64);
 }
 
 void launch_tersoff(const ForceArgs<R> &a, bool ev, bool eatom, cudaStream_t s) {
@@ -2754,17 +2761,18 @@ template <int TPA, bool ONE>
 static void launch_ilp_t(const ForceArgs<R> &a, bool ev, bool eatom, int block, cudaStream_t s) {
   long long threads = (long long)a.n * TPA;
   int g = (int)((threads + block - 1) / block);
+  const bool p = (a.pdl & PDL_ILP) != 0;
   if (a.kc) {
-    if (ev && eatom) k_ilp<TPA, true, true, ONE, false, true, false><<<g, block, 0, s>>>(a);
-    else if (ev) k_ilp<TPA, true, false, ONE, false, true, false><<<g, block, 0, s>>>(a);
-    else k_ilp<TPA, false, false, ONE, false, true, false><<<g, block, 0, s>>>(a);
+    if (ev && eatom) launch_pdl(p, k_ilp<TPA, true, true, ONE, false, true, false>, g, block, s, a);
+    else if (ev) launch_pdl(p, k_ilp<TPA, true, false, ONE, false, true, false>, g, block, s, a);
+    else launch_pdl(p, k_ilp<TPA, false, false, ONE, false, true, false>, g, block, s, a);
     return;
   }
-  if (ev && eatom) k_ilp<TPA, true, true, ONE, false, false, false><<<g, block, 0, s>>>(a);
-  else if (ev) k_ilp<TPA, true, false, ONE, false, false, false><<<g, block, 0, s>>>(a);
+  if (ev && eatom) launch_pdl(p, k_ilp<TPA, true, true, ONE, false, false, false>, g, block, s, a);
+  else if (ev) launch_pdl(p, k_ilp<TPA, true, false, ONE, false, false, false>, g, block, s, a);
   else if (TWO_PAIR_BODY && !a.list_full && a.pair_tile != 1 && (ONE ? h_two_one : h_two_multi))
-    k_ilp<TPA, false, false, ONE, false, false, TWO_PAIR_BODY><<<g, block, 0, s>>>(a);
-  else k_ilp<TPA, false, false, ONE, false, false, false><<<g, block, 0, s>>>(a);
+    launch_pdl(p, k_ilp<TPA, false, false, ONE, false, false, TWO_PAIR_BODY>, g, block, s, a);
+  else launch_pdl(p, k_ilp<TPA, false, false, ONE, false, false, false>, g, block, s, a);
 }
 
 template <bool ONE>
@@ -2817,8 +2825,9 @@ void launch_nderiv(const ForceArgs<R> &a, bool ev, cudaStream_t s) {
   if (a.n == 0) return;
   const int b = per_atom_block(a.n);
   const int g = (a.n + b - 1) / b;
-  if (ev) k_nderiv<true><<<g, b, 0, s>>>(a);
-  else k_nderiv<false><<<g, b, 0, s>>>(a);
+  const bool p = (a.pdl & PDL_NDERIV) != 0;
+  if (ev) launch_pdl(p, k_nderiv<true>, g, b, s, a);
+  else launch_pdl(p, k_nderiv<false>, g, b, s, a);
 }
 
 void launch_finish(const ForceArgs<R> &a, bool eatom, const KickArgs *kick, cudaStream_t s) {
@@ -2826,18 +2835,21 @@ void launch_finish(const ForceArgs<R> &a, bool eatom, const KickArgs *kick, cuda
   int g = (a.n + 127) / 128;
   KickArgs k{};
   if (kick) k = *kick;
+  // early launch only behind the normal-derivative kernel (an evaluation without ILP, or
+  // one that clears the Tersoff per-atom energies, puts a memset there)
+  const bool p = (a.pdl & PDL_FINISH) && a.do_ilp && !(eatom && !a.do_ters);
   if (a.n <= FINISH_LANES_MAX_ATOMS && !a.no_small) {
     const int gl = (a.n + FINISH_ATOMS - 1) / FINISH_ATOMS, bl = FINISH_LANES * FINISH_ATOMS;
-    if (kick && !eatom) k_finish_lanes<false, true><<<gl, bl, 0, s>>>(a, k);
-    else if (kick) k_finish_lanes<true, true><<<gl, bl, 0, s>>>(a, k);
-    else if (eatom) k_finish_lanes<true, false><<<gl, bl, 0, s>>>(a, k);
-    else k_finish_lanes<false, false><<<gl, bl, 0, s>>>(a, k);
+    if (kick && !eatom) launch_pdl(p, k_finish_lanes<false, true>, gl, bl, s, a, k);
+    else if (kick) launch_pdl(p, k_finish_lanes<true, true>, gl, bl, s, a, k);
+    else if (eatom) launch_pdl(p, k_finish_lanes<true, false>, gl, bl, s, a, k);
+    else launch_pdl(p, k_finish_lanes<false, false>, gl, bl, s, a, k);
     return;
   }
-  if (kick && !eatom) k_finish<false, true><<<g, 128, 0, s>>>(a, k);
-  else if (kick) k_finish<true, true><<<g, 128, 0, s>>>(a, k);
-  else if (eatom) k_finish<true, false><<<g, 128, 0, s>>>(a, k);
-  else k_finish<false, false><<<g, 128, 0, s>>>(a, k);
+  if (kick && !eatom) launch_pdl(p, k_finish<false, true>, g, 128, s, a, k);
+  else if (kick) launch_pdl(p, k_finish<true, true>, g, 128, s, a, k);
+  else if (eatom) launch_pdl(p, k_finish<true, false>, g, 128, s, a, k);
+  else launch_pdl(p, k_finish<false, false>, g, 128, s, a, k);
 }
 
 #ifndef LMFF_PACKED_X2

@@ -363,6 +363,33 @@ def test_step_graph_with_check_interval_bitwise_equals_host_loop(check_every):
     assert rel_max(fg, r["f"]) < 1e-10
 
 
+@pytest.mark.parametrize("prec", [capi.FP64, capi.MIXED])
+def test_programmatic_dependent_launch_changes_nothing(prec):
+    """The chain kernels launched with programmatic dependent launch (option pdl = 31:
+    every chain kernel early, dependents scheduled as each kernel starts, each waiting on
+    the device for the kernel before it) and with ordinary launches: the same trajectory, thermo output and rebuild count through
+    the step graphs (every 4th step a rebuild check), and the same single-point forces,
+    energies and per-atom energies, to the bit."""
+    s = S.thermalize(S.twisted_bilayer(8, 8, 3.0, top="hbn"), 1500.0, seed=11)
+    out = []
+    for pdl in (31, 0):
+        eng = capi.Engine(TERSOFF, ILP, precision=prec, skin=0.4)
+        eng.set_option("pdl", pdl)
+        eng.set_option("check_every", 4)
+        r = eng.compute_system(s, eatom=True)
+        eng.upload(s)
+        th = eng.run_nve(80, 0.001, thermo_every=20)
+        out.append((r, eng.download(), th, eng.stats()))
+        eng.close()
+    (r1, (x1, v1, f1), th1, s1), (r0, (x0, v0, f0), th0, s0) = out
+    assert np.array_equal(r1["f"], r0["f"]) and np.array_equal(r1["eatom"], r0["eatom"])
+    assert r1["e_tersoff"] == r0["e_tersoff"] and r1["e_ilp"] == r0["e_ilp"]
+    assert np.array_equal(r1["virial"], r0["virial"])
+    assert s1["graph_steps"] > 0 and s1["rebuilds"] == s0["rebuilds"] >= 2
+    assert np.array_equal(x1, x0) and np.array_equal(v1, v0) and np.array_equal(f1, f0)
+    assert [t["etotal"] for t in th1] == [t["etotal"] for t in th0]
+
+
 def test_step_graph_skin_trip_redo():
     """A check interval far too long for the motion (16 steps at 1500 K, skin 0.4 A):
     atoms move more than skin/2 between checks, the graph raises the trip and the chunk

@@ -45,7 +45,11 @@ namespace lmff {
 LMFF_FORCE_API(f64, double)
 LMFF_FORCE_API(f32, float)
 namespace f64 {
-void launch_vatom(const ForceArgs<double> &a, double *out, cudaStream_t s);
+void launch_vatom_terms(const ForceArgs<double> &a, bool ilp, cudaStream_t s);
+void launch_vatom_gather(const ForceArgs<double> &a, double *out, cudaStream_t s);
+}
+namespace f32 {
+void launch_vatom_ilp(const ForceArgs<float> &a, cudaStream_t s);
 }
 
 static const double LOG2E = 1.4426950408889634;
@@ -577,9 +581,10 @@ struct Engine {
   double **d_arrs = nullptr;
   double **d_karrs = nullptr;
   double *d_kout = nullptr;
-  // per-atom virial pass (lmff_compute_vatom): own shares, slots, the sorted result and
-  // the result in the caller's order, VA_DOUBLES per atom of capacity va_cap
-  static constexpr int VA_DOUBLES = 6 * (2 + MAXTERS + MAXILP + 2);
+  // per-atom virial pass (lmff_compute_vatom): own shares, slots, the sorted result, the
+  // result in the caller's order and the mixed pass's frame tensors (7 float4), VA_DOUBLES
+  // per atom of capacity va_cap
+  static constexpr int VA_DOUBLES = 6 * (2 + MAXTERS + MAXILP + 2) + 14;
   double *d_va = nullptr;
   int va_cap = 0;
   // device calls on this engine (counted by DeviceCall) and the one whose evaluation
@@ -2015,7 +2020,23 @@ struct Engine {
     a.va_is = a.va_ts + MAXTERS * c6;
     double *sorted = a.va_is + MAXILP * c6;
     double *inorder = sorted + c6;
-    f64::launch_vatom(a, sorted, stream);
+    a.va_tens = reinterpret_cast<float4 *>(inorder + c6);   // 16-byte aligned: 912 B per atom before it
+    // the interlayer shares in the precision of the evaluation: FP64, or the mixed
+    // engines' FP32 pair form with FP64 sums
+    const bool mixed_ilp = precision == LMFF_MIXED && a.do_ilp;
+    f64::launch_vatom_terms(a, !mixed_ilp, stream);
+    if (mixed_ilp) {
+      ForceArgs<float> b = args<float>();
+      b.do_ters = a.do_ters;
+      b.do_ilp = a.do_ilp;
+      b.va_t = a.va_t;
+      b.va_i = a.va_i;
+      b.va_ts = a.va_ts;
+      b.va_is = a.va_is;
+      b.va_tens = a.va_tens;
+      f32::launch_vatom_ilp(b, stream);
+    }
+    f64::launch_vatom_gather(a, sorted, stream);
     CK(cudaGetLastError());
     const bool overwrite = (which & LMFF_OVERWRITE) != 0;
     if (!overwrite) CK(cudaMemcpyAsync(inorder, out, sizeof(double) * 6 * (size_t)nn, cudaMemcpyHostToDevice, stream));

@@ -303,6 +303,7 @@ struct ForceArgs {
   // va_i: n entries) and the shares it leaves for its Tersoff bond partners (va_ts:
   // MAXTERS per atom, by short-list slot) and intralayer neighbours (va_is: MAXILP per atom)
   double *va_t, *va_i, *va_ts, *va_is;
+  float4 *va_tens;     // mixed pass: 7 per atom, the frame's partner-share tensors (k_va_tens)
   int *status;
   int do_ters, do_ilp;
   int list_full;       // the pair list also holds same-molecule / non-ILP pairs

@@ -2386,6 +2386,42 @@ __global__ void k_ters_eatom_own(ForceArgs<R> a) {
   a.eatom_ters[i] = (a.stat_ters[i] - bonds) + e;
 }
 
+// Per-atom virial pass, both precision modes: atom i's slots, the halves of its
+// normal-derivative tallies that its intralayer neighbours m receive,
+// 0.5 (v_m (x) c_m(g_i) + [c_m(G_i row p)]_pb), from its FP64 frame and the sums
+// g_i = sum_j c_ij del_ij, G_i = sum_j c_ij del_ij (x) del_ij of the terms it owns
+// (c_m(g) = -(dn_i/dx_m)^T g; zero slots when i owns none or has no frame).
+__device__ __forceinline__ void va_write_slots(const ForceArgs<R> &a, int i, bool on, const NFrame &fri, double gx,
+                                               double gy, double gz, const double G[6]) {
+  double s[MAXILP][6];
+#pragma unroll
+  for (int m = 0; m < MAXILP; m++)
+#pragma unroll
+    for (int k = 0; k < 6; k++) s[m][k] = 0.0;
+  if (on && fri.ok) {
+    NDeriv og, o0, o1, o2;
+    nderiv_apply<false>(fri, make_d4(gx, gy, gz, 0.0), og);
+    nderiv_apply<false>(fri, make_d4(G[0], G[3], G[4], 0.0), o0);   // row x of G
+    nderiv_apply<false>(fri, make_d4(G[3], G[1], G[5], 0.0), o1);   // row y
+    nderiv_apply<false>(fri, make_d4(G[4], G[5], G[2], 0.0), o2);   // row z
+#pragma unroll
+    for (int m = 0; m < MAXILP; m++) {
+      if (m >= fri.cont) break;
+      const double *v = fri.v[m];
+      s[m][0] = 0.5 * (v[0] * og.c[m][0] + o0.c[m][0]);
+      s[m][1] = 0.5 * (v[1] * og.c[m][1] + o1.c[m][1]);
+      s[m][2] = 0.5 * (v[2] * og.c[m][2] + o2.c[m][2]);
+      s[m][3] = 0.5 * (v[0] * og.c[m][1] + o0.c[m][1]);
+      s[m][4] = 0.5 * (v[0] * og.c[m][2] + o0.c[m][2]);
+      s[m][5] = 0.5 * (v[1] * og.c[m][2] + o1.c[m][2]);
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < MAXILP; m++)
+#pragma unroll
+    for (int k = 0; k < 6; k++) a.va_is[((size_t)i * MAXILP + m) * 6 + k] = s[m][k];
+}
+
 #ifndef LMFF_PACKED_X2
 // ===================================================== per-atom virial (FP64) =====
 // Pair::vatom as the reference's tallies split it (pair.cpp ev_tally :913, ev_tally_xyz
@@ -2562,35 +2598,7 @@ __global__ void __launch_bounds__(128) k_va_ilp(ForceArgs<R> a) {
   }
 #pragma unroll
   for (int k = 0; k < 6; k++) a.va_i[6 * (size_t)i + k] = w[k];
-  // ---- i's slots: the halves of its normal-derivative tallies that its intralayer
-  // neighbours receive
-  double s[MAXILP][6];
-#pragma unroll
-  for (int m = 0; m < MAXILP; m++)
-#pragma unroll
-    for (int k = 0; k < 6; k++) s[m][k] = 0.0;
-  if (ie >= 0 && iown && fri.ok) {
-    NDeriv og, o0, o1, o2;
-    nderiv_apply<false>(fri, make_d4(gx, gy, gz, 0.0), og);
-    nderiv_apply<false>(fri, make_d4(G[0], G[3], G[4], 0.0), o0);   // row x of G
-    nderiv_apply<false>(fri, make_d4(G[3], G[1], G[5], 0.0), o1);   // row y
-    nderiv_apply<false>(fri, make_d4(G[4], G[5], G[2], 0.0), o2);   // row z
-#pragma unroll
-    for (int m = 0; m < MAXILP; m++) {
-      if (m >= fri.cont) break;
-      const double *v = fri.v[m];
-      s[m][0] = 0.5 * (v[0] * og.c[m][0] + o0.c[m][0]);
-      s[m][1] = 0.5 * (v[1] * og.c[m][1] + o1.c[m][1]);
-      s[m][2] = 0.5 * (v[2] * og.c[m][2] + o2.c[m][2]);
-      s[m][3] = 0.5 * (v[0] * og.c[m][1] + o0.c[m][1]);
-      s[m][4] = 0.5 * (v[0] * og.c[m][2] + o0.c[m][2]);
-      s[m][5] = 0.5 * (v[1] * og.c[m][2] + o1.c[m][2]);
-    }
-  }
-#pragma unroll
-  for (int m = 0; m < MAXILP; m++)
-#pragma unroll
-    for (int k = 0; k < 6; k++) a.va_is[((size_t)i * MAXILP + m) * 6 + k] = s[m][k];
+  va_write_slots(a, i, ie >= 0 && iown, fri, gx, gy, gz, G);
 }
 
 // Per atom: its own shares plus the slots its Tersoff bond partners and the atoms whose
@@ -2646,7 +2654,147 @@ __global__ void __launch_bounds__(128) k_va_gather(ForceArgs<R> a, double *out) 
 #pragma unroll
   for (int k = 0; k < 6; k++) out[6 * (size_t)i + k] = w[k];
 }
-#endif  // !LMFF_PACKED_X2
+#else   // LMFF_PACKED_X2: the mixed engines' interlayer per-atom virial
+// The same split as k_va_ilp with the pair terms in the pair kernel's FP32 form:
+//  * the own share is half of del (x) f_ij over the atom's interlayer pairs, f_ij the
+//    per-pair force on i the pair kernel forms (vdW, both repulsion terms' pair forces;
+//    the three tallies of a pair sum to exactly this);
+//  * the partner j's normal-derivative share, W_j(g) + del_ji (x) sum_m c_m(g) for
+//    g = c_ji del_ji = Tap q fpair1(j) del, is linear in g: with the 27 numbers of
+//    k_va_tens per atom (A[k][a] = W_j(e_a)[k], B[a][b] = sum_m c_m(e_a)[b]) it is
+//    sum_a A[k][a] g_a - del_p(k) sum_a B[a][b(k)] g_a;
+//  * g_i, G_i and the shares are summed in FP64, and the slots come from the FP64 frame.
+
+// per atom: A (18, row-major k, a) then B (9, row-major a, b), from three applications
+// of the FP64 frame to the unit vectors, stored as FP32 in 7 float4
+__global__ void __launch_bounds__(128) k_va_tens(ForceArgs<R> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  NFrame fr;
+  nframe_eval(a, i, fr);
+  float t[28];
+#pragma unroll
+  for (int k = 0; k < 28; k++) t[k] = 0.f;
+  if (fr.ok) {
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+      NDeriv o;
+      nderiv_apply<true>(fr, make_d4(e == 0 ? 1.0 : 0.0, e == 1 ? 1.0 : 0.0, e == 2 ? 1.0 : 0.0, 0.0), o);
+#pragma unroll
+      for (int k = 0; k < 6; k++) t[3 * k + e] = (float)o.W[k];
+#pragma unroll
+      for (int b = 0; b < 3; b++) t[18 + 3 * e + b] = (float)(o.c[0][b] + o.c[1][b] + o.c[2][b]);
+    }
+  }
+  float4 *q = a.va_tens + 7 * (size_t)i;
+#pragma unroll
+  for (int k = 0; k < 7; k++) q[k] = make_float4(t[4 * k], t[4 * k + 1], t[4 * k + 2], t[4 * k + 3]);
+}
+
+template <bool GH, bool KC>
+__global__ void __launch_bounds__(128) k_va_ilp32(ForceArgs<R> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  double w[6] = {0, 0, 0, 0, 0, 0};
+  double gx = 0, gy = 0, gz = 0;
+  double G[6] = {0, 0, 0, 0, 0, 0};   // xx yy zz xy xz yz
+  AtomI<R> ai;
+  ai.load(a.A, i);
+  const int ie = c_pot.i_map[info_type(ai.info)];
+  const bool iown = !GH || owned(a, i);
+  if (ie >= 0) {
+    const SysDesc &sd = a.A.sys[a.A.sysid[i]];
+    const long long mi = info_mol(ai.info);
+    const long long itag = a.tag[i];
+    const float4 ni = a.nrm32[i];
+    const int64_t q1 = a.list_off[i + 1];
+    for (int64_t q = a.list_off[i]; q < q1; q++) {
+      int j, sx, sy, sz;
+      decode_entry(a.list[q], a.lc, j, sx, sy, sz);
+      R dx, dy, dz;
+      long long jinfo;
+      ai.disp(a.A, sd, j, sx, sy, sz, dx, dy, dz, jinfo);
+      if (info_mol(jinfo) == mi) continue;
+      const int je = c_pot.i_map[info_type(jinfo)];
+      if (je < 0) continue;
+      const R rsq = dx * dx + dy * dy + dz * dz;
+      if (!(rsq < c_pot.i_cutsq)) continue;
+      const R rinv = rsqrt_ftz(rsq), r = rsq * rinv;
+      R Tap = 1, dTap = 0;
+      if (c_pot.tap) {
+        const R x = r * c_pot.i_inv_rcut, x2 = x * x;
+        Tap = ((R(20) * x + R(-70)) * x + R(84)) * x + R(-35);
+        Tap = Tap * (x2 * x2) + R(1);
+        const R y = x2 - x;
+        dTap = (y * y) * (y * (R(140) * c_pot.i_inv_rcut));
+      }
+      const bool jown = !GH || owned(a, j);
+      const bool keep = GH ? keep_half_r(itag, a.tag[j], -dx, -dy, -dz)
+                           : (c_pot.vdw_sym || keep_half(itag, a.tag[j], sx, sy, sz));
+      const R wi = iown ? R(1) : R(0), wj = jown ? R(1) : R(0);
+      const R wv = GH ? ((keep ? iown : jown) ? R(1) : R(0)) : R(1);
+      const IlpP<R> &pij = c_pot.ilp[ie * MAXELEM + je];
+      const IlpP<R> &pji = c_pot.ilp[je * MAXELEM + ie];
+      const IlpP<R> &pv = (c_pot.vdw_sym || keep) ? pij : pji;
+      const R r2inv = rinv * rinv, r6inv = r2inv * r2inv * r2inv, r8inv = r6inv * r2inv;
+      R Vv, fpv;
+      if constexpr (KC) {
+        Vv = -pv.kc_Az06 * r6inv;
+        fpv = R(-6) * pv.kc_Az06 * r8inv;
+      } else {
+        const R TS = R(1) + Math<R>::exp_ts(pv, r), TSinv = Math<R>::rcp(TS);
+        Vv = -pv.C6 * r6inv * TSinv;
+        fpv = pv.C6 * r8inv * TSinv * (R(-6) + pv.d_over_seff * (TS - R(1)) * TSinv * r);
+      }
+      const R fsum_v = (fpv * Tap - Vv * dTap * rinv) * wv;
+      const float4 nj = a.nrm32[j];
+      const R p = ni.x * dx + ni.y * dy + ni.z * dz;
+      const R qq = nj.x * dx + nj.y * dy + nj.z * dz;
+      R V, fpair1, fsum, V2, fpair1b, fsum2;
+      const R exp0 = Math<R>::exp_rep0(pij, r);
+      rep_term<KC>(pij, exp0, Math<R>::exp_rep1(pij, rsq - p * p), rsq - p * p, rinv, V, fpair1, fsum);
+      const R exp0b = pji.same_as_swapped ? exp0 : Math<R>::exp_rep0(pji, r);
+      rep_term<KC>(pji, exp0b, Math<R>::exp_rep1(pji, rsq - qq * qq), rsq - qq * qq, rinv, V2, fpair1b, fsum2);
+      V *= wi; fpair1 *= wi; fsum *= wi;
+      V2 *= wj; fpair1b *= wj; fsum2 *= wj;
+      const R crad = fsum_v + (fsum + fsum2) * Tap - (V + V2) * dTap * rinv;
+      const R tp1 = Tap * p * fpair1, tq1 = Tap * qq * fpair1b;
+      const R fx = crad * dx - tp1 * ni.x - tq1 * nj.x;
+      const R fy = crad * dy - tp1 * ni.y - tq1 * nj.y;
+      const R fz = crad * dz - tp1 * ni.z - tq1 * nj.z;
+      w[0] += 0.5 * (double)(dx * fx); w[1] += 0.5 * (double)(dy * fy); w[2] += 0.5 * (double)(dz * fz);
+      w[3] += 0.5 * (double)(dx * fy); w[4] += 0.5 * (double)(dx * fz); w[5] += 0.5 * (double)(dy * fz);
+      gx += (double)(tp1 * dx); gy += (double)(tp1 * dy); gz += (double)(tp1 * dz);
+      G[0] += (double)(tp1 * (dx * dx)); G[1] += (double)(tp1 * (dy * dy)); G[2] += (double)(tp1 * (dz * dz));
+      G[3] += (double)(tp1 * (dx * dy)); G[4] += (double)(tp1 * (dx * dz)); G[5] += (double)(tp1 * (dy * dz));
+      if (tq1 != R(0)) {
+        // the partner's normal-derivative share, g = tq1 del
+        const R g0 = tq1 * dx, g1 = tq1 * dy, g2 = tq1 * dz;
+        const float4 *tt = a.va_tens + 7 * (size_t)j;
+        const float4 t0 = tt[0], t1 = tt[1], t2 = tt[2], t3 = tt[3], t4 = tt[4], t5 = tt[5], t6 = tt[6];
+        // A[k][e] = t[3k + e], B[e][b] = t[18 + 3e + b]
+        const R A0 = t0.x * g0 + t0.y * g1 + t0.z * g2;   // k = 0 (xx)
+        const R A1 = t0.w * g0 + t1.x * g1 + t1.y * g2;   // k = 1 (yy)
+        const R A2 = t1.z * g0 + t1.w * g1 + t2.x * g2;   // k = 2 (zz)
+        const R A3 = t2.y * g0 + t2.z * g1 + t2.w * g2;   // k = 3 (xy)
+        const R A4 = t3.x * g0 + t3.y * g1 + t3.z * g2;   // k = 4 (xz)
+        const R A5 = t3.w * g0 + t4.x * g1 + t4.y * g2;   // k = 5 (yz)
+        const R s0 = t4.z * g0 + t5.y * g1 + t6.x * g2;   // sum_e B[e][0] g_e
+        const R s1 = t4.w * g0 + t5.z * g1 + t6.y * g2;   // b = 1
+        const R s2 = t5.x * g0 + t5.w * g1 + t6.z * g2;   // b = 2
+        w[0] += 0.5 * (double)(A0 - dx * s0); w[1] += 0.5 * (double)(A1 - dy * s1);
+        w[2] += 0.5 * (double)(A2 - dz * s2); w[3] += 0.5 * (double)(A3 - dx * s1);
+        w[4] += 0.5 * (double)(A4 - dx * s2); w[5] += 0.5 * (double)(A5 - dy * s2);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 6; k++) a.va_i[6 * (size_t)i + k] = w[k];
+  NFrame fri;
+  nframe_eval(a, i, fri);
+  va_write_slots(a, i, ie >= 0 && iown, fri, gx, gy, gz, G);
+}
+#endif  // LMFF_PACKED_X2
 
 // ============================================================ host launchers ======
 
@@ -2857,7 +3005,9 @@ void launch_finish(const ForceArgs<R> &a, bool eatom, const KickArgs *kick, cuda
 // shares (the one-thread routine with VA; it also rewrites the force scratch arrays,
 // which the evaluation has already gathered), the FP64 normal frames, ILP's shares, and
 // the gather into out[6 n] (sorted order).  a.do_ters / a.do_ilp select the styles.
-void launch_vatom(const ForceArgs<R> &a, double *out, cudaStream_t s) {
+// ilp = false leaves the interlayer shares to the mixed pass (launch_vatom_ilp of the
+// FP32 unit), which runs between this and launch_vatom_gather.
+void launch_vatom_terms(const ForceArgs<R> &a, bool ilp, cudaStream_t s) {
   if (a.n == 0) return;
   const int g = (a.n + 127) / 128;
   const bool gh = a.own_perm != nullptr;
@@ -2865,14 +3015,31 @@ void launch_vatom(const ForceArgs<R> &a, double *out, cudaStream_t s) {
     if (gh) k_tersoff<false, false, true, true><<<g, 128, 0, s>>>(a);
     else k_tersoff<false, false, false, true><<<g, 128, 0, s>>>(a);
   }
-  if (a.do_ilp) {
+  if (a.do_ilp && ilp) {
     k_nframe<<<g, 128, 0, s>>>(a);
     if (gh && a.kc) k_va_ilp<true, true><<<g, 128, 0, s>>>(a);
     else if (gh) k_va_ilp<true, false><<<g, 128, 0, s>>>(a);
     else if (a.kc) k_va_ilp<false, true><<<g, 128, 0, s>>>(a);
     else k_va_ilp<false, false><<<g, 128, 0, s>>>(a);
   }
-  k_va_gather<<<g, 128, 0, s>>>(a, out);
+}
+
+void launch_vatom_gather(const ForceArgs<R> &a, double *out, cudaStream_t s) {
+  if (a.n == 0) return;
+  k_va_gather<<<(a.n + 127) / 128, 128, 0, s>>>(a, out);
+}
+#else
+// The mixed engines' interlayer per-atom virial: the per-atom frame tensors, then the
+// FP32 pass over the pair list.
+void launch_vatom_ilp(const ForceArgs<R> &a, cudaStream_t s) {
+  if (a.n == 0 || !a.do_ilp) return;
+  const int g = (a.n + 127) / 128;
+  const bool gh = a.own_perm != nullptr;
+  k_va_tens<<<g, 128, 0, s>>>(a);
+  if (gh && a.kc) k_va_ilp32<true, true><<<g, 128, 0, s>>>(a);
+  else if (gh) k_va_ilp32<true, false><<<g, 128, 0, s>>>(a);
+  else if (a.kc) k_va_ilp32<false, true><<<g, 128, 0, s>>>(a);
+  else k_va_ilp32<false, false><<<g, 128, 0, s>>>(a);
 }
 #endif
 

@@ -97,15 +97,21 @@ def test_mixed_matches_oracle_on_benchmark_workloads(name):
 @pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
 @pytest.mark.parametrize("name", sorted(_CASES))
 def test_vatom_matches_oracle_on_benchmark_workloads(name, precision):
-    """Per-atom virial (an FP64 pass in either mode) at 1e-10 per style; with three
-    intralayer neighbours for every atom each style's per-atom virials sum to its fdotr
-    virial (the reference leaves out only the dn_i/dx_i term of atoms with two)."""
+    """Per-atom virial at 1e-10 per style (Tersoff an FP64 pass in either mode; the
+    interlayer shares in the mixed mode at max |dW| <= 1e-4 eV); with three intralayer
+    neighbours for every atom each style's per-atom virials sum to its fdotr virial (the
+    reference leaves out only the dn_i/dx_i term of atoms with two): 1e-9, the mixed
+    interlayer sum at the mixed virial bar."""
     s, ref = _oracle(name)
     got = _engine(name, precision=precision).compute_system(s, vatom=True)
     assert rel_max(got["vatom_tersoff"], ref["vatom_tersoff"]) <= F64_TOL
-    assert rel_max(got["vatom_ilp"], ref["vatom_ilp"]) <= F64_TOL
     assert rel_max(got["vatom_tersoff"].sum(0), ref["virial_tersoff"]) <= 1e-9
-    assert rel_max(got["vatom_ilp"].sum(0), ref["virial_ilp"]) <= 1e-9
+    if precision == capi.FP64:
+        assert rel_max(got["vatom_ilp"], ref["vatom_ilp"]) <= F64_TOL
+        assert rel_max(got["vatom_ilp"].sum(0), ref["virial_ilp"]) <= 1e-9
+    else:
+        assert np.abs(got["vatom_ilp"] - ref["vatom_ilp"]).max() <= 1e-4
+        assert rel_max(got["vatom_ilp"].sum(0), ref["virial_ilp"]) <= MIX_W_REL
 
 
 @pytest.mark.parametrize("name", sorted(_CASES))

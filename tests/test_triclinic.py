@@ -6,8 +6,9 @@ through the subdomain form on the cell's atoms and their periodic images; the im
 shares of forces, per-atom energies and per-atom virials are folded into their owners.
 
 Bars as the orthogonal parity tests: FP64 1e-10 (max-norm relative), mixed max |dF| <=
-1e-5 eV/A, energies 1e-6 and virial 1e-5 relative; per-atom virial (an FP64 pass) 1e-10
-in both modes."""
+1e-5 eV/A, energies 1e-6 and virial 1e-5 relative; per-atom virial 1e-10 in the FP64
+mode, max |dW| <= 1e-4 eV in the mixed mode (its interlayer shares take the pair
+kernel's FP32 form)."""
 import numpy as np
 import pytest
 from conftest import ILP, TERSOFF, load_golden, rel_max, rel_rms
@@ -56,7 +57,7 @@ def test_mixed_triclinic_matches_reference(name):
     assert abs(r["e_tersoff"] - g["e_tersoff"]) <= MIX_E_REL * abs(g["e_tersoff"])
     assert abs(r["e_ilp"] - g["e_ilp"]) <= MIX_E_REL * abs(g["e_ilp"])
     assert rel_max(r["virial"], g["virial"]) <= MIX_W_REL
-    assert rel_max(r["vatom"], g["vatom_tersoff"] + g["vatom_ilp"]) <= F64_TOL
+    assert np.abs(r["vatom"] - (g["vatom_tersoff"] + g["vatom_ilp"])).max() <= 1e-4
 
 
 def test_triclinic_atoms_outside_the_cell_are_wrapped():

@@ -4,8 +4,11 @@ it (pair_tersoff.cpp:173, :223, :253; pair_ilp_graphene_hbn.cpp:536, :667, :671;
 pair_kolmogorov_crespi_full.cpp:536, :668, :675), from the reference harness's fixtures
 (tests/golden/*.npz, vatom_tersoff / vatom_ilp, ghost rows folded into their owners).
 
-The pass is FP64 in either precision mode, from the evaluated positions, so both modes
-are held to the FP64 bar: max-norm relative error <= 1e-10 per style."""
+Bars: Tersoff's shares come from an FP64 pass in either precision mode, max-norm relative
+error <= 1e-10; the interlayer shares are FP64 in the FP64 mode (1e-10) and in the mixed
+mode take the pair kernel's FP32 form with FP64 sums, max |dW| <= 1e-4 eV per component
+(the per-atom counterpart of the 1e-5 eV/A force bar: pair forces times separations of a
+few A)."""
 import os
 
 import numpy as np
@@ -17,6 +20,7 @@ from lmff_gb300 import build, capi
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-10
+MIX_VA_ABS = 1e-4
 KC = os.path.join(POT, "CC.KC-full")
 EINVAL = -1
 BOTH = capi.TERSOFF | capi.ILP
@@ -46,7 +50,10 @@ def test_vatom_matches_reference(name, precision):
     g = load_golden(name)
     r = _engine(g, precision).compute(g["x"], g["type"], g["mol"], g["tag"], vatom=True)
     assert rel_max(r["vatom_tersoff"], g["vatom_tersoff"]) <= TOL
-    assert rel_max(r["vatom_ilp"], g["vatom_ilp"]) <= TOL
+    if precision == capi.FP64:
+        assert rel_max(r["vatom_ilp"], g["vatom_ilp"]) <= TOL
+    else:
+        assert np.abs(r["vatom_ilp"] - g["vatom_ilp"]).max() <= MIX_VA_ABS
 
 
 @pytest.mark.parametrize("name", ["kc_bilayer", "kc_bilayer_notaper"])
@@ -67,10 +74,10 @@ def test_vatom_force_only_evaluation_and_overwrite():
     v = np.ones((len(perm), 6))
     capi._lib.lmff_compute_vatom(eng._h, BOTH, len(perm), capi._p(v))
     want = (g["vatom_tersoff"] + g["vatom_ilp"])[perm]
-    assert rel_max(v - 1.0, want) <= TOL
+    assert np.abs(v - 1.0 - want).max() <= MIX_VA_ABS
     eng.compute(g["x"][perm], g["type"][perm], g["mol"][perm], g["tag"][perm], same_atoms=True)
     rc = capi._lib.lmff_compute_vatom(eng._h, BOTH | capi.OVERWRITE, len(perm), capi._p(v))
-    assert rc == 0 and rel_max(v, want) <= TOL
+    assert rc == 0 and np.abs(v - want).max() <= MIX_VA_ABS
 
 
 def test_vatom_needs_a_directly_preceding_evaluation():

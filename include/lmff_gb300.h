@@ -290,8 +290,9 @@ int lmff_compute_ghost(lmff_engine *e, int nlocal, int nall, const double *x, co
  * vatom[natoms*6] in the evaluated call's atom order, rows xx yy zz xy xz yz (LAMMPS
  * order, energy units, not divided by a volume); natoms = that call's natoms (nall in
  * subdomain mode, where ghost rows carry the shares LAMMPS's reverse communication
- * folds into their owners).  Computed in FP64 by a separate pass in either precision
- * mode, from the evaluated positions; not for batches (LMFF_EUNSUPPORTED). */
+ * folds into their owners).  A separate pass on the evaluated positions: Tersoff's
+ * shares in FP64, the interlayer shares in the evaluation's precision (LMFF_MIXED: FP32
+ * pair terms, FP64 sums); not for batches (LMFF_EUNSUPPORTED). */
 int lmff_compute_vatom(lmff_engine *e, int which, int natoms, double *vatom);
 
 /* Same on device pointers (d_x[natoms*3] double, d_type int32, d_mol int64, d_tag int64

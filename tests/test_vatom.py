@@ -56,12 +56,16 @@ def test_vatom_matches_reference(name, precision):
         assert np.abs(r["vatom_ilp"] - g["vatom_ilp"]).max() <= MIX_VA_ABS
 
 
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
 @pytest.mark.parametrize("name", ["kc_bilayer", "kc_bilayer_notaper"])
-def test_vatom_kolmogorov_crespi_matches_reference(name):
+def test_vatom_kolmogorov_crespi_matches_reference(name, precision):
     g = load_golden(name)
-    r = _engine(g, capi.FP64, kc=True).compute(g["x"], g["type"], g["mol"], g["tag"], vatom=True)
+    r = _engine(g, precision, kc=True).compute(g["x"], g["type"], g["mol"], g["tag"], vatom=True)
     assert rel_max(r["vatom_tersoff"], g["vatom_tersoff"]) <= TOL
-    assert rel_max(r["vatom_ilp"], g["vatom_ilp"]) <= TOL
+    if precision == capi.FP64:
+        assert rel_max(r["vatom_ilp"], g["vatom_ilp"]) <= TOL
+    else:
+        assert np.abs(r["vatom_ilp"] - g["vatom_ilp"]).max() <= MIX_VA_ABS
 
 
 def test_vatom_force_only_evaluation_and_overwrite():
